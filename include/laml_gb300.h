@@ -1,0 +1,247 @@
+/*
+ * laml_gb300 -- C ABI of the GB300 (sm_103a) engine for LAML's PMM
+ * likelihood / EM path.
+ *
+ * Plain pointers and sizes only.  Host-side encoders run on the CPU and fill
+ * caller-allocated arrays; device entry points take a `laml_batch` whose
+ * pointers are device addresses and launch on the given CUDA stream
+ * (`stream` is a cudaStream_t passed as void*; NULL = legacy default stream).
+ *
+ * The reference surface each entry point replaces is cited beside it
+ * (paths are relative to the LAML repository).
+ *
+ * Return codes: LAML_OK (0) or a negative LAML_ERR_*; laml_last_error()
+ * returns a message for the calling thread's last failure.
+ */
+#ifndef LAML_GB300_H
+#define LAML_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define LAML_OK 0
+#define LAML_ERR_ARG -1        /* bad argument / size */
+#define LAML_ERR_CUDA -2       /* a CUDA runtime call failed */
+#define LAML_ERR_PARSE -3      /* malformed newick */
+#define LAML_ERR_PRIOR -4      /* an observed state has no prior (phylogeny.py:91-93) */
+#define LAML_ERR_TIMEOUT -5    /* a device-side grid barrier gave up waiting */
+#define LAML_ERR_NOT_BINARY -6 /* a node with more than two children */
+#define LAML_ERR_LEAF -7       /* a leaf label missing from the leaf order */
+
+/* Character codes of the encoded matrix (int32 input to laml_dataset_*). */
+#define LAML_CHAR_MISSING (-1)  /* '?' */
+#define LAML_CHAR_SILENCED (-2) /* an explicit -1 in the exact (EM_solver) model */
+
+/* ------------------------------------------------------------------------
+ * Host encoders (no GPU needed)
+ * --------------------------------------------------------------------- */
+
+/* Sizes of a newick tree as fastEM_solver.parse_tree numbers it
+ * (laml_libs/fastEM_solver.py:46-146): a unifurcating root is dropped.
+ * label_bytes counts the labels' bytes including one NUL each. */
+int laml_newick_size(const char* newick, int32_t* num_nodes, int32_t* num_leaves,
+                     int64_t* label_bytes);
+
+/* Encode a newick tree in the node order of fastEM_solver.parse_tree:
+ * leaves 0..n-1 in `leaf_order` order (or treeswift preorder when
+ * leaf_order == NULL), internal nodes n..N-1 in treeswift preorder, children
+ * in networkx successor order (child0, child1; -1 for leaves).  Missing edge
+ * lengths give has_length = 0 and branch_length = 0.  Labels are written
+ * NUL-terminated into `labels` with their start offsets in label_offsets[N];
+ * unlabelled nodes are named "node_<preorder index>" (fastEM_solver.py:65-67).
+ * Replaces: fastEM_solver.parse_tree + the networkx traversals of
+ * EMOptimizer.optimize (fast_em/laml.py:234-251). */
+int laml_newick_encode(const char* newick, const char* const* leaf_order, int32_t n_leaf_order,
+                       int32_t* parent, int32_t* child0, int32_t* child1,
+                       double* branch_length, uint8_t* has_length,
+                       char* labels, int64_t* label_offsets);
+
+/* Site layout of a character matrix for the device kernels.
+ * chars: n_leaves x n_sites int32 in leaf order (LAML_CHAR_* or >= 0 raw
+ * states); priors as CSR over sites: prior_ptr[n_sites+1], prior_state[],
+ * prior_prob[].  compat = 1 recodes as fast_em/phylogeny.py:62-94 (observed
+ * states only, raw float32 priors, '?' and -1 both missing); compat = 0 as
+ * ML_solver.py:69-74 (priors normalised over each site's dict, the mass of
+ * unobserved mutated states kept as one extra state, -1 = silenced).
+ * Sites are sorted by state count (descending) and packed into groups of
+ * `group_sites` (8, 16 or 32) sites; see laml_dataset_encode. */
+typedef struct laml_dataset_info {
+    int32_t n_leaves, n_sites, n_sites_pad, n_groups, group_sites;
+    int64_t row_len;     /* floats per node row (sum over groups of max_C * group_sites) */
+    int32_t max_states;  /* max over sites of (mutated states + 2) */
+    int64_t n_missing;   /* '?' entries */
+    int64_t n_silenced;  /* LAML_CHAR_SILENCED entries */
+} laml_dataset_info;
+
+int laml_dataset_measure(int32_t n_leaves, int32_t n_sites, const int32_t* chars,
+                         const int32_t* prior_ptr, const int32_t* prior_state,
+                         const double* prior_prob, int32_t compat, int32_t group_sites,
+                         laml_dataset_info* info);
+
+/* Fill the layout: codes[n_leaves * n_sites_pad] (int16, layout site order:
+ * 0 = unmutated, >= 2 = state slot, -1 missing, -2 silenced), q[row_len]
+ * (prior of slot j of layout site c at group_off[g] + j*group_sites + lane),
+ * site_perm[n_sites_pad] (original site of each layout site, -1 padding),
+ * site_C[n_sites_pad] (states incl. unmutated and silenced), site_sumq[],
+ * group_off[n_groups], group_C[n_groups], state_map[] (CSR by original site:
+ * the original state of slot 2+i; offsets in state_ptr[n_sites+1]).
+ * Returns LAML_ERR_PRIOR (with the site and state in laml_last_error) when an
+ * observed state has no prior. Replaces fast_em/phylogeny.py:48-114. */
+int laml_dataset_encode(int32_t n_leaves, int32_t n_sites, const int32_t* chars,
+                        const int32_t* prior_ptr, const int32_t* prior_state,
+                        const double* prior_prob, int32_t compat, int32_t group_sites,
+                        int16_t* codes, float* q, int32_t* site_perm, int32_t* site_C,
+                        float* site_sumq, int32_t* group_off, int32_t* group_C,
+                        int32_t* state_ptr, int32_t* state_map);
+
+/* Batch plan: the level schedule and buffer offsets of many trees.
+ * Trees are given in the laml_newick_encode numbering, concatenated. */
+typedef struct laml_plan_input {
+    int32_t n_trees;
+    const int32_t* tree_nodes;     /* [T] N_p */
+    const int32_t* tree_leaves;    /* [T] n_p */
+    const int32_t* tree_dataset;   /* [T] */
+    const int32_t* child0;         /* [sum N_p] local ids, -1 for leaves */
+    const int32_t* child1;
+    int32_t n_datasets;
+    const int32_t* ds_groups;      /* [D] */
+    const int32_t* ds_sites_pad;   /* [D] */
+    const int64_t* ds_row_len;     /* [D] */
+    const int32_t* ds_group_base;  /* [D] offset of the dataset's groups in group_C */
+    const int32_t* group_C;        /* [sum groups] */
+} laml_plan_input;
+
+typedef struct laml_plan_sizes {
+    int64_t n_nodes;
+    int64_t part_floats;   /* floats of one partial buffer (internal nodes only) */
+    int64_t scalar_len;    /* per-(internal node, site) scalars */
+    int64_t site_len;      /* per-(tree, site) slots */
+    int64_t count_floats;  /* count partials: 8 per (node, group) */
+    int64_t post_len;      /* per-(node, site) posterior slots */
+    int32_t n_in_levels, n_out_levels;
+    int64_t n_in_items, n_out_items, n_root_items;
+} laml_plan_sizes;
+
+typedef struct laml_plan_output {
+    /* trees [T] */
+    int32_t *tr_node_base, *tr_root, *tr_quirk;
+    int64_t *tr_site_base, *tr_cnt_base, *tr_post_base;
+    /* nodes [n_nodes] */
+    int32_t *nd_tree, *nd_c0, *nd_c1, *nd_parent, *nd_sib, *nd_leafrow;
+    int64_t *nd_prow, *nd_srow;
+    /* schedule */
+    int32_t* in_level_off;   /* [n_in_levels + 1] */
+    int32_t* in_items;       /* [2 * n_in_items] (node, group), inside by height */
+    int32_t* out_level_off;  /* [n_out_levels + 1] */
+    int32_t* out_items;      /* [2 * n_out_items], outside by depth >= 1 */
+    int32_t* root_items;     /* [2 * n_root_items] */
+} laml_plan_output;
+
+int laml_plan_measure(const laml_plan_input* in, laml_plan_sizes* sizes);
+int laml_plan_fill(const laml_plan_input* in, laml_plan_output* out);
+
+/* ------------------------------------------------------------------------
+ * Device batch: every pointer is a device address
+ * --------------------------------------------------------------------- */
+typedef struct laml_batch {
+    int32_t group_sites;     /* G: 8, 16 or 32 (must match the datasets) */
+    int32_t compat;          /* 1 fast_em semantics, 0 EM_solver semantics */
+    int32_t n_trees, n_datasets;
+    int64_t n_nodes;
+    int32_t n_in_levels, n_out_levels;
+    int64_t n_in_items, n_out_items, n_root_items;
+    /* datasets [D] */
+    const int32_t *ds_sites, *ds_sites_pad, *ds_groups, *ds_group_base, *ds_site_base;
+    const int64_t *ds_q_base, *ds_code_base;
+    const double *ds_missing, *ds_silenced;      /* counts over the real sites */
+    const int32_t *group_off, *group_C, *site_C;
+    const float *site_sumq, *q;
+    const int16_t* codes;
+    /* trees [T] */
+    const int32_t *tr_ds, *tr_node_base, *tr_nodes, *tr_leaves, *tr_root, *tr_quirk;
+    const int64_t *tr_site_base, *tr_cnt_base, *tr_post_base;
+    double *tr_nu, *tr_phi;
+    double* tr_prev;               /* [2T] nu, phi before the last M-step */
+    const uint8_t* tr_fix;         /* bit0: nu fixed, bit1: phi fixed */
+    double *tr_llh, *tr_llh_prev;
+    int32_t *tr_iter, *tr_status;  /* status: LAML_TREE_* */
+    /* nodes [n_nodes] */
+    const int32_t *nd_tree, *nd_c0, *nd_c1, *nd_parent, *nd_sib, *nd_leafrow;
+    const int64_t *nd_prow, *nd_srow;
+    double *nd_d, *nd_d_prev;
+    const uint8_t* nd_mask;        /* 1 = branch length is optimised */
+    float* nd_bt;                  /* [4 * n_nodes] P00, Pmut, Pstay, Psil */
+    double* nd_cnt;                /* [6 * n_nodes] expected counts summed over sites */
+    /* work buffers */
+    float *in_part, *out_part, *in_dot;
+    int32_t *in_x, *in_h, *out_x, *out_h;
+    double* llh_site;              /* [site_len] per (tree, layout site) */
+    float* root_lr;
+    int32_t* root_x;
+    float* cnt_part;               /* [count_floats] */
+    float *post0, *post1;          /* [post_len] or NULL */
+    /* schedule */
+    const int32_t *in_level_off, *in_items, *out_level_off, *out_items, *root_items;
+    /* control */
+    uint32_t* barrier;             /* 2 words, zeroed by the library before each persistent launch */
+    int32_t* error;                /* 1 word: 0 or a negative LAML_ERR_* set on the device */
+} laml_batch;
+
+#define LAML_TREE_ACTIVE 0
+#define LAML_TREE_CONVERGED 1
+#define LAML_TREE_NAN 2
+#define LAML_TREE_MAXITER 3
+
+/* Number of sites per group the kernels were built for (bit mask of 8|16|32). */
+int laml_supported_group_sites(void);
+
+/* Branch transition terms from nd_d, tr_nu (compat adds the EPS floors of
+ * fast_em/calculations.py:153-157).  Replaces the t1/t2/t3/alpha0 arrays. */
+int laml_branch_terms(const laml_batch* b, void* stream);
+
+/* Inside pass of every tree + per-site and per-tree log-likelihood (FP64 sum
+ * over sites); with `update_em` = 1 it also records llh_prev = llh.
+ * Replaces calc.compute_log_likelihood / jit_compute_log_likelihood
+ * (fast_em/calculations.py:456-504, fast_em/laml.py:80) and the inside half
+ * of EM_solver.Estep_in_llh / lineage_llh (laml_libs/EM_solver.py:91-141). */
+int laml_inside(const laml_batch* b, int32_t update_em, void* stream);
+
+/* Outside pass + expected transition counts (nd_cnt, 6 per branch) +
+ * per-leaf silenced posteriors; with `want_post` = 1 also the posteriors
+ * P(v = 0 | D), P(v = silenced | D) per (node, site) into post0/post1.
+ * Requires laml_inside first.  Replaces calc.compute_E_step
+ * (fast_em/calculations.py:506-577) and EM_solver.Estep_out_llh /
+ * Estep_posterior (laml_libs/EM_solver.py:143-300). */
+int laml_outside(const laml_batch* b, int32_t want_post, void* stream);
+
+/* M-step of every active tree: compat maximises the fastEM objective
+ * (fast_em/laml.py:62-78) by `rounds` coordinate-ascent rounds; exact follows
+ * EM_solver.Mstep (laml_libs/EM_solver.py:307-459) with bounded 1-D solves.
+ * Writes nd_d (old values to nd_d_prev), tr_nu, tr_phi and the branch terms. */
+int laml_mstep(const laml_batch* b, int32_t rounds, void* stream);
+
+/* `iters` fused EM iterations (outside+counts -> M-step -> inside ->
+ * convergence test per tree) in ONE persistent cooperative launch with a
+ * bounded grid barrier; trees whose status leaves ACTIVE stop changing.
+ * `rel_tol` is the stopping rule (1e-5 in fast_em/laml.py:183, 1e-8 in
+ * EM_solver.py:503); max_iters caps tr_iter.  Requires laml_inside(update_em=1)
+ * once before the first call.  Replaces the host EM loop of
+ * fast_em/laml.py:112-194 / EM_solver.EM_optimization. */
+int laml_em_run(const laml_batch* b, int32_t iters, int32_t rounds, double rel_tol,
+                int32_t max_iters, void* stream);
+
+/* Same iterations as laml_em_run, one kernel launch per tree level (no grid
+ * barrier); the reference-shaped "plain" path. */
+int laml_em_run_levels(const laml_batch* b, int32_t iters, int32_t rounds, double rel_tol,
+                       int32_t max_iters, void* stream);
+
+/* Message of the calling thread's last error ("" if none). */
+const char* laml_last_error(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* LAML_GB300_H */

@@ -1,0 +1,592 @@
+// Host encoders of the laml_gb300 C ABI: newick -> node table in the
+// reference's numbering, character matrix -> device site layout, and the
+// level schedule of a batch of trees.  Pure C++ (no CUDA), thread-safe.
+#include "laml_gb300.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <unordered_map>
+#include <vector>
+
+namespace laml {
+thread_local std::string g_last_error;
+void set_error(const std::string& s) { g_last_error = s; }
+}  // namespace laml
+
+extern "C" const char* laml_last_error(void) { return laml::g_last_error.c_str(); }
+
+namespace {
+
+using laml::set_error;
+
+// ---------------------------------------------------------------------------
+// newick
+// ---------------------------------------------------------------------------
+struct PNode {
+    std::string label;
+    bool has_label = false;
+    double length = 0.0;
+    bool has_length = false;
+    int parent = -1;
+    std::vector<int> children;  // newick order
+};
+
+bool parse_newick(const char* s, std::vector<PNode>& nodes) {
+    nodes.clear();
+    nodes.emplace_back();
+    int cur = 0;
+    std::vector<int> stack;
+    const size_t n = std::strlen(s);
+    size_t i = 0;
+    auto token_end = [&](size_t j) {
+        while (j < n && !std::strchr(",():;[", s[j])) ++j;
+        return j;
+    };
+    auto trim = [](const char* b, const char* e) {
+        while (b < e && std::isspace((unsigned char)*b)) ++b;
+        while (e > b && std::isspace((unsigned char)e[-1])) --e;
+        return std::string(b, e);
+    };
+    while (i < n) {
+        char ch = s[i];
+        if (ch == '(') {
+            int c = (int)nodes.size();
+            nodes.emplace_back();
+            nodes[c].parent = cur;
+            nodes[cur].children.push_back(c);
+            stack.push_back(cur);
+            cur = c;
+            ++i;
+        } else if (ch == ',') {
+            if (stack.empty()) { set_error("newick: ',' outside parentheses"); return false; }
+            int p = stack.back();
+            int c = (int)nodes.size();
+            nodes.emplace_back();
+            nodes[c].parent = p;
+            nodes[p].children.push_back(c);
+            cur = c;
+            ++i;
+        } else if (ch == ')') {
+            if (stack.empty()) { set_error("newick: unbalanced ')'"); return false; }
+            cur = stack.back();
+            stack.pop_back();
+            ++i;
+        } else if (ch == ':') {
+            size_t e = token_end(i + 1);
+            std::string tok = trim(s + i + 1, s + e);
+            char* endp = nullptr;
+            double v = std::strtod(tok.c_str(), &endp);
+            if (tok.empty() || endp == tok.c_str()) { set_error("newick: bad length '" + tok + "'"); return false; }
+            nodes[cur].length = v;
+            nodes[cur].has_length = true;
+            i = e;
+        } else if (ch == ';') {
+            break;
+        } else if (ch == '[') {
+            const char* e = std::strchr(s + i, ']');
+            if (!e) { set_error("newick: unterminated comment"); return false; }
+            i = (size_t)(e - s) + 1;
+        } else if (std::isspace((unsigned char)ch)) {
+            ++i;
+        } else {
+            size_t e = token_end(i);
+            std::string tok = trim(s + i, s + e);
+            if (!tok.empty()) { nodes[cur].label = tok; nodes[cur].has_label = true; }
+            i = e;
+        }
+    }
+    if (!stack.empty()) { set_error("newick: unbalanced '('"); return false; }
+    return true;
+}
+
+// treeswift preorder: stack, children pushed in newick order, popped last-first
+std::vector<int> ts_preorder(const std::vector<PNode>& nodes, int root) {
+    std::vector<int> out, st{root};
+    out.reserve(nodes.size());
+    while (!st.empty()) {
+        int v = st.back();
+        st.pop_back();
+        out.push_back(v);
+        for (int c : nodes[v].children) st.push_back(c);
+    }
+    return out;
+}
+
+struct Encoded {
+    int N = 0, n = 0;
+    std::vector<int> parent, c0, c1;
+    std::vector<double> bl;
+    std::vector<uint8_t> has;
+    std::vector<std::string> labels;
+};
+
+int encode_tree(const char* newick, const char* const* leaf_order, int n_order, Encoded& E) {
+    std::vector<PNode> nodes;
+    if (!parse_newick(newick, nodes)) return LAML_ERR_PARSE;
+    std::vector<int> pre = ts_preorder(nodes, 0);
+    // unnamed nodes: "node_<preorder index>" (fastEM_solver.py:65-67)
+    for (size_t k = 0; k < pre.size(); ++k) {
+        PNode& v = nodes[pre[k]];
+        if (!v.has_label) { v.label = "node_" + std::to_string(k); v.has_label = true; }
+    }
+    // graph order = preorder; a unifurcating root is removed (lines 77-80)
+    std::vector<int> order = pre;
+    int root = pre[0];
+    if (nodes[root].children.size() == 1) {
+        order.erase(order.begin());
+        root = nodes[root].children[0];
+    }
+    std::vector<int> leaves_pre;
+    for (int v : order)
+        if (nodes[v].children.empty()) leaves_pre.push_back(v);
+    std::vector<int> leaf_seq;
+    if (leaf_order) {
+        std::unordered_map<std::string, int> by_label;
+        for (int v : leaves_pre) by_label.emplace(nodes[v].label, v);
+        std::vector<uint8_t> used(nodes.size(), 0);
+        for (int k = 0; k < n_order; ++k) {
+            auto it = by_label.find(leaf_order[k]);
+            if (it != by_label.end() && !used[it->second]) {
+                leaf_seq.push_back(it->second);
+                used[it->second] = 1;
+            }
+        }
+        if (leaf_seq.size() != leaves_pre.size()) {
+            for (int v : leaves_pre)
+                if (!used[v]) { set_error("leaf '" + nodes[v].label + "' is not in the leaf order"); break; }
+            return LAML_ERR_LEAF;
+        }
+    } else {
+        leaf_seq = leaves_pre;
+    }
+    std::vector<int> id(nodes.size(), -1);
+    int next = 0;
+    for (int v : leaf_seq) id[v] = next++;
+    E.n = next;
+    for (int v : order)
+        if (!nodes[v].children.empty()) id[v] = next++;
+    E.N = next;
+    E.parent.assign(E.N, -1);
+    E.c0.assign(E.N, -1);
+    E.c1.assign(E.N, -1);
+    E.bl.assign(E.N, 0.0);
+    E.has.assign(E.N, 0);
+    E.labels.assign(E.N, std::string());
+    for (int v : order) {
+        int i = id[v];
+        E.labels[i] = nodes[v].label;
+        E.bl[i] = nodes[v].has_length ? nodes[v].length : 0.0;
+        E.has[i] = nodes[v].has_length ? 1 : 0;
+        const auto& ch = nodes[v].children;
+        if (ch.size() > 2 || (ch.size() == 1)) {
+            set_error("node '" + nodes[v].label + "' has " + std::to_string(ch.size()) +
+                      " children; the PMM kernels need a binary tree");
+            return LAML_ERR_NOT_BINARY;
+        }
+        if (ch.size() == 2) {
+            // networkx successor order: the preorder visit order = reversed newick order
+            E.c0[i] = id[ch[1]];
+            E.c1[i] = id[ch[0]];
+            E.parent[id[ch[0]]] = i;
+            E.parent[id[ch[1]]] = i;
+        }
+    }
+    (void)root;
+    return LAML_OK;
+}
+
+}  // namespace
+
+extern "C" int laml_newick_size(const char* newick, int32_t* num_nodes, int32_t* num_leaves,
+                                int64_t* label_bytes) {
+    if (!newick || !num_nodes || !num_leaves) { set_error("null argument"); return LAML_ERR_ARG; }
+    Encoded E;
+    int rc = encode_tree(newick, nullptr, 0, E);
+    if (rc != LAML_OK) return rc;
+    *num_nodes = E.N;
+    *num_leaves = E.n;
+    if (label_bytes) {
+        int64_t b = 0;
+        for (auto& s : E.labels) b += (int64_t)s.size() + 1;
+        *label_bytes = b;
+    }
+    return LAML_OK;
+}
+
+extern "C" int laml_newick_encode(const char* newick, const char* const* leaf_order,
+                                  int32_t n_leaf_order, int32_t* parent, int32_t* child0,
+                                  int32_t* child1, double* branch_length, uint8_t* has_length,
+                                  char* labels, int64_t* label_offsets) {
+    if (!newick || !parent || !child0 || !child1 || !branch_length || !has_length) {
+        set_error("null argument");
+        return LAML_ERR_ARG;
+    }
+    Encoded E;
+    int rc = encode_tree(newick, leaf_order, n_leaf_order, E);
+    if (rc != LAML_OK) return rc;
+    std::memcpy(parent, E.parent.data(), sizeof(int32_t) * E.N);
+    std::memcpy(child0, E.c0.data(), sizeof(int32_t) * E.N);
+    std::memcpy(child1, E.c1.data(), sizeof(int32_t) * E.N);
+    std::memcpy(branch_length, E.bl.data(), sizeof(double) * E.N);
+    std::memcpy(has_length, E.has.data(), E.N);
+    if (labels && label_offsets) {
+        int64_t off = 0;
+        for (int i = 0; i < E.N; ++i) {
+            label_offsets[i] = off;
+            std::memcpy(labels + off, E.labels[i].c_str(), E.labels[i].size() + 1);
+            off += (int64_t)E.labels[i].size() + 1;
+        }
+    }
+    return LAML_OK;
+}
+
+// ---------------------------------------------------------------------------
+// dataset layout
+// ---------------------------------------------------------------------------
+namespace {
+
+struct SiteEnc {
+    std::vector<int> states;     // sorted observed mutated states
+    std::vector<double> q;       // per slot 2.. (exact: + lumped state)
+    int C = 2;
+};
+
+int encode_sites(int n, int K, const int32_t* chars, const int32_t* pp, const int32_t* ps,
+                 const double* pq, int compat, std::vector<SiteEnc>& S, int64_t* nmiss,
+                 int64_t* nsil) {
+    S.assign(K, SiteEnc());
+    int64_t miss = 0, sil = 0;
+    std::vector<int> col(n);
+    for (int c = 0; c < K; ++c) {
+        for (int i = 0; i < n; ++i) {
+            int x = chars[(int64_t)i * K + c];
+            col[i] = x;
+            if (x < 0) {
+                if (!compat && x == LAML_CHAR_SILENCED) ++sil;
+                else ++miss;
+            }
+        }
+        std::vector<int> st;
+        for (int i = 0; i < n; ++i)
+            if (col[i] > 0) st.push_back(col[i]);
+        std::sort(st.begin(), st.end());
+        st.erase(std::unique(st.begin(), st.end()), st.end());
+        SiteEnc& E = S[c];
+        E.states = st;
+        double tot = 0.0;
+        for (int k = pp[c]; k < pp[c + 1]; ++k) tot += pq[k];
+        for (int o : st) {
+            int hit = -1;
+            for (int k = pp[c]; k < pp[c + 1]; ++k)
+                if (ps[k] == o) { hit = k; break; }
+            if (hit < 0) {
+                set_error("missing mutation prior for character " + std::to_string(c) + ", state " +
+                          std::to_string(o));
+                return LAML_ERR_PRIOR;
+            }
+            if (compat) E.q.push_back((double)(float)pq[hit]);
+            else E.q.push_back(tot > 0 ? pq[hit] / tot : 0.0);
+        }
+        if (!compat) {
+            double s = 0.0;
+            for (double v : E.q) s += v;
+            double other = 1.0 - s;
+            if (other > 0.0) E.q.push_back(other);   // mass of the unobserved mutated states
+        }
+        E.C = (int)E.q.size() + 2;
+    }
+    *nmiss = miss;
+    *nsil = sil;
+    return LAML_OK;
+}
+
+bool check_group(int G) { return G == 8 || G == 16 || G == 32; }
+
+}  // namespace
+
+extern "C" int laml_dataset_measure(int32_t n_leaves, int32_t n_sites, const int32_t* chars,
+                                    const int32_t* prior_ptr, const int32_t* prior_state,
+                                    const double* prior_prob, int32_t compat, int32_t G,
+                                    laml_dataset_info* info) {
+    if (!chars || !prior_ptr || !info || n_leaves <= 0 || n_sites <= 0 || !check_group(G)) {
+        set_error("laml_dataset_measure: bad argument");
+        return LAML_ERR_ARG;
+    }
+    std::vector<SiteEnc> S;
+    int64_t nm, ns;
+    int rc = encode_sites(n_leaves, n_sites, chars, prior_ptr, prior_state, prior_prob, compat, S, &nm, &ns);
+    if (rc) return rc;
+    std::vector<int> Cs;
+    for (auto& e : S) Cs.push_back(e.C);
+    std::sort(Cs.begin(), Cs.end(), std::greater<int>());
+    int Kpad = (n_sites + G - 1) / G * G;
+    Cs.resize(Kpad, 2);
+    int NG = Kpad / G;
+    int64_t row = 0;
+    for (int g = 0; g < NG; ++g) row += (int64_t)Cs[g * G] * G;
+    info->n_leaves = n_leaves;
+    info->n_sites = n_sites;
+    info->n_sites_pad = Kpad;
+    info->n_groups = NG;
+    info->group_sites = G;
+    info->row_len = row;
+    info->max_states = Cs[0];
+    info->n_missing = nm;
+    info->n_silenced = ns;
+    return LAML_OK;
+}
+
+extern "C" int laml_dataset_encode(int32_t n_leaves, int32_t n_sites, const int32_t* chars,
+                                   const int32_t* prior_ptr, const int32_t* prior_state,
+                                   const double* prior_prob, int32_t compat, int32_t G,
+                                   int16_t* codes, float* q, int32_t* site_perm, int32_t* site_C,
+                                   float* site_sumq, int32_t* group_off, int32_t* group_C,
+                                   int32_t* state_ptr, int32_t* state_map) {
+    laml_dataset_info info;
+    int rc = laml_dataset_measure(n_leaves, n_sites, chars, prior_ptr, prior_state, prior_prob,
+                                  compat, G, &info);
+    if (rc) return rc;
+    std::vector<SiteEnc> S;
+    int64_t nm, ns;
+    encode_sites(n_leaves, n_sites, chars, prior_ptr, prior_state, prior_prob, compat, S, &nm, &ns);
+    const int K = n_sites, Kpad = info.n_sites_pad, NG = info.n_groups;
+    std::vector<int> perm(K);
+    for (int c = 0; c < K; ++c) perm[c] = c;
+    std::stable_sort(perm.begin(), perm.end(), [&](int a, int b) { return S[a].C > S[b].C; });
+    perm.resize(Kpad, -1);
+    int64_t off = 0;
+    for (int g = 0; g < NG; ++g) {
+        int c0 = perm[g * G];
+        int Cg = c0 >= 0 ? S[c0].C : 2;
+        group_off[g] = (int32_t)off;
+        group_C[g] = Cg;
+        off += (int64_t)Cg * G;
+    }
+    std::memset(q, 0, sizeof(float) * info.row_len);
+    for (int c = 0; c < Kpad; ++c) {
+        int o = perm[c];
+        site_perm[c] = o;
+        int g = c / G, lane = c % G;
+        if (o < 0) {
+            site_C[c] = 2;
+            site_sumq[c] = 0.f;
+            continue;
+        }
+        site_C[c] = S[o].C;
+        double sq = 0.0;
+        for (size_t j = 0; j < S[o].q.size(); ++j) {
+            float v = (float)S[o].q[j];
+            q[group_off[g] + (int64_t)(j + 2) * G + lane] = v;
+            sq += (double)v;
+        }
+        site_sumq[c] = (float)sq;
+    }
+    // codes in layout site order
+    std::vector<std::unordered_map<int, int>> slot(K);
+    for (int c = 0; c < K; ++c)
+        for (size_t j = 0; j < S[c].states.size(); ++j) slot[c][S[c].states[j]] = (int)j + 2;
+    for (int i = 0; i < n_leaves; ++i) {
+        for (int c = 0; c < Kpad; ++c) {
+            int o = perm[c];
+            int16_t v = 0;
+            if (o >= 0) {
+                int x = chars[(int64_t)i * K + o];
+                if (x < 0) v = (!compat && x == LAML_CHAR_SILENCED) ? -2 : -1;
+                else if (x == 0) v = 0;
+                else v = (int16_t)slot[o][x];
+            }
+            codes[(int64_t)i * Kpad + c] = v;
+        }
+    }
+    if (state_ptr && state_map) {
+        int64_t p = 0;
+        for (int c = 0; c < K; ++c) {
+            state_ptr[c] = (int32_t)p;
+            for (int s : S[c].states) state_map[p++] = s;
+        }
+        state_ptr[K] = (int32_t)p;
+    }
+    return LAML_OK;
+}
+
+// ---------------------------------------------------------------------------
+// batch plan
+// ---------------------------------------------------------------------------
+namespace {
+
+struct TreeLevels {
+    std::vector<int> height, depth, parent;
+};
+
+int tree_levels(int N, int n, const int32_t* c0, const int32_t* c1, TreeLevels& L, int* root) {
+    L.height.assign(N, 0);
+    L.depth.assign(N, -1);
+    L.parent.assign(N, -1);
+    for (int u = 0; u < N; ++u) {
+        bool leaf = c0[u] < 0;
+        if (leaf != (u < n) || (c1[u] < 0) != leaf) {
+            set_error("plan: leaves must be 0..n-1 and internal nodes binary");
+            return LAML_ERR_ARG;
+        }
+        if (!leaf) {
+            if (c0[u] >= N || c1[u] >= N) { set_error("plan: child id out of range"); return LAML_ERR_ARG; }
+            L.parent[c0[u]] = u;
+            L.parent[c1[u]] = u;
+        }
+    }
+    int r = -1;
+    for (int u = 0; u < N; ++u)
+        if (L.parent[u] < 0) {
+            if (r >= 0) { set_error("plan: more than one root"); return LAML_ERR_ARG; }
+            r = u;
+        }
+    if (r < 0 || N < 3) { set_error("plan: a tree needs a root and at least two leaves"); return LAML_ERR_ARG; }
+    // heights: children have larger ids than their internal parent in the
+    // preorder numbering, but do not rely on it: iterate to a fixed point
+    std::vector<int> order;   // preorder from the root
+    order.reserve(N);
+    std::vector<int> st{r};
+    L.depth[r] = 0;
+    while (!st.empty()) {
+        int u = st.back();
+        st.pop_back();
+        order.push_back(u);
+        if (c0[u] >= 0) {
+            L.depth[c0[u]] = L.depth[u] + 1;
+            L.depth[c1[u]] = L.depth[u] + 1;
+            st.push_back(c1[u]);
+            st.push_back(c0[u]);
+        }
+    }
+    if ((int)order.size() != N) { set_error("plan: tree is not connected"); return LAML_ERR_ARG; }
+    for (int k = N - 1; k >= 0; --k) {
+        int u = order[k];
+        if (c0[u] >= 0) L.height[u] = 1 + std::max(L.height[c0[u]], L.height[c1[u]]);
+    }
+    *root = r;
+    return LAML_OK;
+}
+
+}  // namespace
+
+extern "C" int laml_plan_measure(const laml_plan_input* in, laml_plan_sizes* sz) {
+    if (!in || !sz || in->n_trees <= 0) { set_error("plan: bad argument"); return LAML_ERR_ARG; }
+    std::memset(sz, 0, sizeof(*sz));
+    int64_t nb = 0;
+    int hmax = 0, dmax = 0;
+    for (int p = 0; p < in->n_trees; ++p) {
+        int N = in->tree_nodes[p], n = in->tree_leaves[p], d = in->tree_dataset[p];
+        if (d < 0 || d >= in->n_datasets) { set_error("plan: bad dataset id"); return LAML_ERR_ARG; }
+        TreeLevels L;
+        int root;
+        int rc = tree_levels(N, n, in->child0 + nb, in->child1 + nb, L, &root);
+        if (rc) return rc;
+        int NG = in->ds_groups[d], Kp = in->ds_sites_pad[d];
+        for (int u = 0; u < N; ++u) {
+            hmax = std::max(hmax, L.height[u]);
+            dmax = std::max(dmax, L.depth[u]);
+        }
+        sz->n_nodes += N;
+        sz->part_floats += (int64_t)(N - n) * in->ds_row_len[d];
+        sz->scalar_len += (int64_t)(N - n) * Kp;
+        sz->site_len += Kp;
+        sz->count_floats += (int64_t)N * NG * 8;
+        sz->post_len += (int64_t)N * Kp;
+        sz->n_in_items += (int64_t)(N - n) * NG;
+        sz->n_out_items += (int64_t)(N - 1) * NG;
+        sz->n_root_items += NG;
+        nb += N;
+    }
+    sz->n_in_levels = hmax;
+    sz->n_out_levels = dmax;
+    return LAML_OK;
+}
+
+extern "C" int laml_plan_fill(const laml_plan_input* in, laml_plan_output* o) {
+    laml_plan_sizes sz;
+    int rc = laml_plan_measure(in, &sz);
+    if (rc) return rc;
+    const int T = in->n_trees;
+    const int H = sz.n_in_levels, D = sz.n_out_levels;
+    std::vector<std::vector<int>> in_lv(H + 1), out_lv(D + 1);
+    int64_t nb = 0, pb = 0, sb = 0, tb = 0, cb = 0, qb = 0;
+    int maxNG = 0;
+    for (int p = 0; p < T; ++p) {
+        int N = in->tree_nodes[p], n = in->tree_leaves[p], d = in->tree_dataset[p];
+        const int32_t* c0 = in->child0 + nb;
+        const int32_t* c1 = in->child1 + nb;
+        TreeLevels L;
+        int root;
+        tree_levels(N, n, c0, c1, L, &root);
+        int NG = in->ds_groups[d], Kp = in->ds_sites_pad[d];
+        int64_t R = in->ds_row_len[d];
+        maxNG = std::max(maxNG, NG);
+        o->tr_node_base[p] = (int32_t)nb;
+        o->tr_root[p] = (int32_t)(nb + root);
+        o->tr_quirk[p] = (int32_t)(nb + N - 1);   // parent_sibling[root] = (-1,-1) -> node N-1
+        o->tr_site_base[p] = tb;
+        o->tr_cnt_base[p] = cb;
+        o->tr_post_base[p] = qb;
+        for (int u = 0; u < N; ++u) {
+            int64_t g = nb + u;
+            o->nd_tree[g] = p;
+            o->nd_c0[g] = c0[u] >= 0 ? (int32_t)(nb + c0[u]) : -1;
+            o->nd_c1[g] = c1[u] >= 0 ? (int32_t)(nb + c1[u]) : -1;
+            int par = L.parent[u];
+            o->nd_parent[g] = par >= 0 ? (int32_t)(nb + par) : -1;
+            int sib = -1;
+            if (par >= 0) sib = (c0[par] == u) ? c1[par] : c0[par];
+            o->nd_sib[g] = sib >= 0 ? (int32_t)(nb + sib) : -1;
+            if (u < n) {
+                o->nd_leafrow[g] = u;
+                o->nd_prow[g] = -1;
+                o->nd_srow[g] = -1;
+            } else {
+                o->nd_leafrow[g] = -1;
+                o->nd_prow[g] = pb + (int64_t)(u - n) * R;
+                o->nd_srow[g] = sb + (int64_t)(u - n) * Kp;
+                in_lv[L.height[u]].push_back((int)g);
+            }
+            if (L.depth[u] >= 1) out_lv[L.depth[u]].push_back((int)g);
+        }
+        pb += (int64_t)(N - n) * R;
+        sb += (int64_t)(N - n) * Kp;
+        tb += Kp;
+        cb += (int64_t)N * NG * 8;
+        qb += (int64_t)N * Kp;
+        nb += N;
+    }
+    // items, group-major within a level (groups are sorted by state count)
+    auto emit = [&](const std::vector<std::vector<int>>& lv, int first, int last, int32_t* off,
+                    int32_t* items) {
+        int64_t k = 0;
+        for (int l = first; l <= last; ++l) {
+            off[l - first] = (int32_t)k;
+            for (int g = 0; g < maxNG; ++g)
+                for (int node : lv[l]) {
+                    int d = in->tree_dataset[o->nd_tree[node]];
+                    if (g < in->ds_groups[d]) {
+                        items[2 * k] = node;
+                        items[2 * k + 1] = g;
+                        ++k;
+                    }
+                }
+        }
+        off[last - first + 1] = (int32_t)k;
+    };
+    emit(in_lv, 1, H, o->in_level_off, o->in_items);
+    emit(out_lv, 1, D, o->out_level_off, o->out_items);
+    int64_t k = 0;
+    for (int g = 0; g < maxNG; ++g)
+        for (int p = 0; p < T; ++p) {
+            if (g < in->ds_groups[in->tree_dataset[p]]) {
+                o->root_items[2 * k] = o->tr_root[p];
+                o->root_items[2 * k + 1] = g;
+                ++k;
+            }
+        }
+    return LAML_OK;
+}

@@ -1,0 +1,910 @@
+// sm_103a kernels of the PMM inside / outside / E-step / M-step path.
+//
+// Layout (per dataset): sites are sorted by state count and packed in groups
+// of G sites; a node row holds, per group g, group_C[g] state slots x G
+// sites interleaved (slot j of the lane-th site of the group at
+// group_off[g] + j*G + lane).  Slot 0 = unmutated, slot 1 = silenced,
+// slots 2.. = the observed mutated states (+ one lumped state in the exact
+// model).  Only internal nodes own rows; a leaf's inside vector is a function
+// of its character code and phi and is never stored.
+//
+// Work item = (node, group); a thread owns one (node, site) and loops over
+// that site's states, so every per-site reduction (the prior-weighted sum for
+// the transition out of state 0, the max used for scaling) stays in
+// registers.  Values are FP32 in linear space with a power-of-two scale per
+// (node, site): a stored row S holds the product of normalised child
+// vectors; h = exponent of max(S) is stored beside it and readers use
+// S * 2^-h, with the cumulative exponent X kept as an int32.  Per-site
+// log-likelihoods are formed in FP64.
+//
+// Math restated from fast_em/calculations.py (edge products 11-91, leaf init
+// 278-334, inside 193-276, outside 135-191, responsibilities 373-454) in
+// linear space:
+//   E_v[0] = P00 in_v[0] + Pmut sum_a q_a in_v[a] + Psil in_v[s]
+//   E_v[a] = Pstay in_v[a] + Psil in_v[s],  E_v[s] = in_v[s]
+//   out_v[0] = P00 x0, out_v[a] = Pmut q_a x0 + Pstay x_a,
+//   out_v[s] = Psil (x0 + sum_a x_a) + x_s,  x = out_parent * E_sibling
+// with P00 = e^{-d(1+nu)}, Pmut = (1-e^{-d}) e^{-nu d}, Pstay = e^{-nu d},
+// Psil = 1-e^{-nu d}.
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <cmath>
+#include <cstdio>
+#include <string>
+#include <vector>
+
+#include "laml_gb300.h"
+
+namespace laml {
+void set_error(const std::string& s);
+}
+
+namespace {
+
+constexpr float kEPS = 1e-6f;          // fast_em/calculations.py:9
+constexpr double kEPSd = 1e-6;
+constexpr double kCalcEps = 1e-10;     // fast_em/laml.py:47
+constexpr double kDmin = 0.005, kDmax = 10.0;   // core_constants.py:7-8
+constexpr double kEpsS = 1e-6, kEpsNu = 1e-5;   // EM_solver.Mstep defaults (EM_solver.py:307)
+constexpr double kLn2 = 0.69314718055994530942;
+constexpr int kBlock = 256;
+constexpr unsigned kFull = 0xffffffffu;
+
+// ---------------------------------------------------------------------------
+// small helpers
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ float pow2i(int e) {   // 2^e for e in [-126, 127]
+    return __int_as_float((127 + e) << 23);
+}
+
+__device__ __forceinline__ int scale_exp(float m) {
+    // exponent h with m * 2^-h in [0.5, 1), clamped so 2^-h stays a normal float
+    if (!(m > 0.f)) return 0;
+    int h;
+    frexpf(m, &h);
+    return max(-125, min(125, h));
+}
+
+struct Leaf {
+    float e1, ephi, es;   // max(1-phi, eps), max(phi, eps), eps
+};
+
+__device__ __forceinline__ Leaf leaf_params(const laml_batch& b, int tree) {
+    double phi = __ldcg(b.tr_phi + tree);
+    Leaf L;
+    if (b.compat) {
+        L.e1 = fmaxf((float)(1.0 - phi), kEPS);
+        L.ephi = fmaxf((float)phi, kEPS);
+        L.es = kEPS;
+    } else {
+        L.e1 = (float)(1.0 - phi);
+        L.ephi = (float)phi;
+        L.es = 0.f;
+    }
+    return L;
+}
+
+// One child's inside vector at one site, normalised.
+struct Child {
+    const float* row;   // internal: &row[slot 0] of this site (stride G); null for a leaf
+    float f;            // 2^-h
+    int X;              // cumulative exponent of the normalised vector
+    float s0, ss, D;    // slot 0, silenced slot, sum_a q_a * value_a
+    int code;           // leaf character code
+    float e1, ephi;
+};
+
+template <int G>
+__device__ __forceinline__ float child_val(const Child& c, int j) {
+    if (c.row) return __ldcg(c.row + j * G) * c.f;
+    return c.code == j ? c.e1 : (c.code == -1 ? c.ephi : 0.f);
+}
+
+template <int G>
+__device__ __forceinline__ Child load_child(const laml_batch& b, int x, int ds, int site,
+                                            int goff, int lane, const float* qrow, float sumq,
+                                            const Leaf& L) {
+    Child c;
+    c.e1 = L.e1;
+    c.ephi = L.ephi;
+    if (__ldg(b.nd_c0 + x) < 0) {
+        int row = __ldg(b.nd_leafrow + x);
+        int code = __ldg(b.codes + __ldg(b.ds_code_base + ds) +
+                         (int64_t)row * __ldg(b.ds_sites_pad + ds) + site);
+        c.row = nullptr;
+        c.f = 1.f;
+        c.X = 0;
+        c.code = code;
+        c.s0 = code == 0 ? L.e1 : (code == -1 ? L.ephi : 0.f);
+        c.ss = code < 0 ? 1.f : L.es;
+        c.D = code >= 2 ? __ldg(qrow + code * G) * L.e1 : (code == -1 ? L.ephi * sumq : 0.f);
+    } else {
+        int64_t s = __ldg(b.nd_srow + x) + site;
+        int h = __ldcg(b.in_h + s);
+        c.f = pow2i(-h);
+        c.X = __ldcg(b.in_x + s);
+        c.D = __ldcg(b.in_dot + s);
+        c.row = b.in_part + __ldg(b.nd_prow + x) + goff + lane;
+        c.code = 0;
+        c.s0 = __ldcg(c.row) * c.f;
+        c.ss = __ldcg(c.row + G) * c.f;
+    }
+    return c;
+}
+
+__device__ __forceinline__ float4 load_bt(const laml_batch& b, int x) {
+    return __ldcg(reinterpret_cast<const float4*>(b.nd_bt) + x);
+}
+
+struct SiteCtx {
+    int tree, ds, site, goff, C;
+    const float* qrow;
+    float sumq;
+};
+
+template <int G>
+__device__ __forceinline__ bool site_ctx(const laml_batch& b, int node, int g, int lane,
+                                         bool respect_status, SiteCtx& s) {
+    s.tree = __ldg(b.nd_tree + node);
+    if (respect_status && __ldcg(b.tr_status + s.tree) != LAML_TREE_ACTIVE) return false;
+    s.ds = __ldg(b.tr_ds + s.tree);
+    s.site = g * G + lane;
+    if (s.site >= __ldg(b.ds_sites + s.ds)) return false;
+    int gb = __ldg(b.ds_group_base + s.ds) + g;
+    s.goff = __ldg(b.group_off + gb);
+    int sb = __ldg(b.ds_site_base + s.ds) + s.site;
+    s.C = __ldg(b.site_C + sb);
+    s.sumq = __ldg(b.site_sumq + sb);
+    s.qrow = b.q + __ldg(b.ds_q_base + s.ds) + s.goff + lane;
+    return true;
+}
+
+// ---------------------------------------------------------------------------
+// inside: one internal node, one site
+// ---------------------------------------------------------------------------
+template <int G>
+__device__ void inside_item(const laml_batch& b, int u, int g, int lane, bool respect_status) {
+    SiteCtx s;
+    if (!site_ctx<G>(b, u, g, lane, respect_status, s)) return;
+    const Leaf L = leaf_params(b, s.tree);
+    const int v = __ldg(b.nd_c0 + u), w = __ldg(b.nd_c1 + u);
+    const Child cv = load_child<G>(b, v, s.ds, s.site, s.goff, lane, s.qrow, s.sumq, L);
+    const Child cw = load_child<G>(b, w, s.ds, s.site, s.goff, lane, s.qrow, s.sumq, L);
+    const float4 bv = load_bt(b, v), bw = load_bt(b, w);   // P00, Pmut, Pstay, Psil
+    const float ev0 = bv.x * cv.s0 + bv.y * cv.D + bv.w * cv.ss;
+    const float ew0 = bw.x * cw.s0 + bw.y * cw.D + bw.w * cw.ss;
+    const float kv = bv.w * cv.ss, kw = bw.w * cw.ss;
+    float* row = b.in_part + __ldg(b.nd_prow + u) + s.goff + lane;
+    const float s0 = ev0 * ew0, ss = cv.ss * cw.ss;
+    __stcg(row, s0);
+    __stcg(row + G, ss);
+    float mx = fmaxf(s0, ss), dot = 0.f;
+#pragma unroll 4
+    for (int j = 2; j < s.C; ++j) {
+        const float av = child_val<G>(cv, j), aw = child_val<G>(cw, j);
+        const float x = fmaf(bv.z, av, kv) * fmaf(bw.z, aw, kw);
+        __stcg(row + j * G, x);
+        dot = fmaf(__ldg(s.qrow + j * G), x, dot);
+        mx = fmaxf(mx, x);
+    }
+    const int h = scale_exp(mx);
+    const float f = pow2i(-h);
+    const int X = cv.X + cw.X + h;
+    const int64_t sr = __ldg(b.nd_srow + u) + s.site;
+    __stcg(b.in_h + sr, h);
+    __stcg(b.in_x + sr, X);
+    __stcg(b.in_dot + sr, dot * f);
+    if (u == __ldg(b.tr_root + s.tree)) {
+        // the root edge from a progenitor in state 0 (calculations.py:270-276, 504)
+        const float4 br = load_bt(b, u);
+        const float lr = br.x * (s0 * f) + br.y * (dot * f) + br.w * (ss * f);
+        const int64_t t = __ldg(b.tr_site_base + s.tree) + s.site;
+        __stcg(b.root_lr + t, lr);
+        __stcg(b.root_x + t, X);
+        __stcg(b.llh_site + t, (double)logf(lr) + (double)X * kLn2);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// outside + counts: one node v (leaf or internal, not the root), one site.
+// mode 0: x = out[parent] * E[sibling]; mode 1: the root with
+// parent = sibling = node N-1 (fast_em/laml.py:244-246 + calculations.py:418);
+// mode 2: the root below a progenitor in state 0 (EM_solver.py:282-286).
+// ---------------------------------------------------------------------------
+template <int G>
+__device__ void outside_item(const laml_batch& b, int v, int g, int lane, bool act, int mode,
+                             bool want_post) {
+    float c00 = 0.f, c0a = 0.f, c0s = 0.f, caa = 0.f, cas = 0.f, css = 0.f, lr = 0.f;
+    SiteCtx s;
+    bool live = act && site_ctx<G>(b, v, g, lane, true, s);
+    const bool leaf_v = act && __ldg(b.nd_c0 + v) < 0;
+    if (live) {
+        const Leaf L = leaf_params(b, s.tree);
+        const Child cv = load_child<G>(b, v, s.ds, s.site, s.goff, lane, s.qrow, s.sumq, L);
+        const float4 bv = load_bt(b, v);
+        float x0, xs, sumx = 0.f, dotxv = 0.f, out0, outs;
+        int Xx;
+        float* orow = nullptr;
+        float mx = 0.f;
+        if (mode == 2) {
+            x0 = 1.f;
+            xs = 0.f;
+            Xx = 0;
+        } else {
+            const int u = mode == 0 ? __ldg(b.nd_parent + v) : __ldg(b.tr_quirk + s.tree);
+            const int w = mode == 0 ? __ldg(b.nd_sib + v) : u;
+            const Child cw = load_child<G>(b, w, s.ds, s.site, s.goff, lane, s.qrow, s.sumq, L);
+            const float4 bw = load_bt(b, w);
+            const int64_t su = __ldg(b.nd_srow + u) + s.site;
+            const float fo = pow2i(-__ldcg(b.out_h + su));
+            const int Xo = __ldcg(b.out_x + su);
+            const float* urow = b.out_part + __ldg(b.nd_prow + u) + s.goff + lane;
+            const float o0 = __ldcg(urow) * fo, os = __ldcg(urow + G) * fo;
+            x0 = o0 * (bw.x * cw.s0 + bw.y * cw.D + bw.w * cw.ss);
+            xs = os * cw.ss;
+            Xx = Xo + cw.X;
+            const float kw = bw.w * cw.ss;
+            const bool write = (mode == 0) && cv.row != nullptr;
+            if (write) orow = b.out_part + __ldg(b.nd_prow + v) + s.goff + lane;
+            const float px = bv.y * x0;
+#pragma unroll 4
+            for (int j = 2; j < s.C; ++j) {
+                const float ou = __ldcg(urow + j * G) * fo;
+                const float xa = ou * fmaf(bw.z, child_val<G>(cw, j), kw);
+                sumx += xa;
+                dotxv = fmaf(xa, child_val<G>(cv, j), dotxv);
+                if (write) {
+                    const float o = fmaf(px, __ldg(s.qrow + j * G), bv.z * xa);
+                    __stcg(orow + j * G, o);
+                    mx = fmaxf(mx, o);
+                }
+            }
+        }
+        out0 = bv.x * x0;
+        outs = bv.w * (x0 + sumx) + xs;
+        if (orow) {
+            __stcg(orow, out0);
+            __stcg(orow + G, outs);
+            const int h = scale_exp(fmaxf(mx, fmaxf(out0, outs)));
+            const int64_t sv = __ldg(b.nd_srow + v) + s.site;
+            __stcg(b.out_h + sv, h);
+            __stcg(b.out_x + sv, Xx + h);
+        }
+        // responsibilities (calculations.py:418-451), divided by the site likelihood
+        const int64_t t = __ldg(b.tr_site_base + s.tree) + s.site;
+        const float lroot = __ldcg(b.root_lr + t);
+        const int e = Xx + cv.X - __ldcg(b.root_x + t);
+        const float sc = (lroot > 0.f) ? ldexpf(1.f / lroot, e) : 0.f;
+        c00 = x0 * cv.s0 * bv.x * sc;
+        c0a = x0 * bv.y * cv.D * sc;
+        c0s = x0 * cv.ss * bv.w * sc;
+        caa = bv.z * dotxv * sc;
+        cas = bv.w * cv.ss * sumx * sc;
+        css = xs * cv.ss * sc;
+        if (leaf_v) lr = cv.ss * outs * sc;
+        if (want_post && b.post0 && mode == 0) {
+            const int64_t pb = __ldg(b.tr_post_base + s.tree) +
+                               (int64_t)(v - __ldg(b.tr_node_base + s.tree)) *
+                                   __ldg(b.ds_sites_pad + s.ds) + s.site;
+            __stcg(b.post0 + pb, cv.s0 * out0 * sc);
+            __stcg(b.post1 + pb, cv.ss * outs * sc);
+        }
+    }
+    // sum over the G sites of the group
+#pragma unroll
+    for (int off = G / 2; off > 0; off >>= 1) {
+        c00 += __shfl_xor_sync(kFull, c00, off);
+        c0a += __shfl_xor_sync(kFull, c0a, off);
+        c0s += __shfl_xor_sync(kFull, c0s, off);
+        caa += __shfl_xor_sync(kFull, caa, off);
+        cas += __shfl_xor_sync(kFull, cas, off);
+        css += __shfl_xor_sync(kFull, css, off);
+        lr += __shfl_xor_sync(kFull, lr, off);
+    }
+    if (act && lane == 0) {
+        const int tree = __ldg(b.nd_tree + v);
+        if (__ldcg(b.tr_status + tree) == LAML_TREE_ACTIVE) {
+            const int ds = __ldg(b.tr_ds + tree);
+            const int NG = __ldg(b.ds_groups + ds);
+            float4* dst = reinterpret_cast<float4*>(
+                b.cnt_part + __ldg(b.tr_cnt_base + tree) +
+                ((int64_t)(v - __ldg(b.tr_node_base + tree)) * NG + g) * 8);
+            __stcg(dst, make_float4(c00, c0a, c0s, caa));
+            __stcg(dst + 1, make_float4(cas, css, lr, 0.f));
+        }
+    }
+}
+
+// outside row of a root (calculations.py:172-175) + the root's posteriors
+template <int G>
+__device__ void root_init_item(const laml_batch& b, int r, int g, int lane, bool want_post) {
+    SiteCtx s;
+    if (!site_ctx<G>(b, r, g, lane, true, s)) return;
+    const float4 br = load_bt(b, r);
+    float* row = b.out_part + __ldg(b.nd_prow + r) + s.goff + lane;
+    float mx = fmaxf(br.x, br.w);
+    __stcg(row, br.x);
+    __stcg(row + G, br.w);
+    for (int j = 2; j < s.C; ++j) {
+        const float o = br.y * __ldg(s.qrow + j * G);
+        __stcg(row + j * G, o);
+        mx = fmaxf(mx, o);
+    }
+    const int h = scale_exp(mx);
+    const int64_t sr = __ldg(b.nd_srow + r) + s.site;
+    __stcg(b.out_h + sr, h);
+    __stcg(b.out_x + sr, h);
+    if (want_post && b.post0) {
+        const Leaf L = leaf_params(b, s.tree);
+        const Child cr = load_child<G>(b, r, s.ds, s.site, s.goff, lane, s.qrow, s.sumq, L);
+        const int64_t t = __ldg(b.tr_site_base + s.tree) + s.site;
+        const float lroot = __ldcg(b.root_lr + t);
+        const float sc = lroot > 0.f ? ldexpf(1.f / lroot, cr.X - __ldcg(b.root_x + t)) : 0.f;
+        const int64_t pb = __ldg(b.tr_post_base + s.tree) +
+                           (int64_t)(r - __ldg(b.tr_node_base + s.tree)) *
+                               __ldg(b.ds_sites_pad + s.ds) + s.site;
+        __stcg(b.post0 + pb, cr.s0 * br.x * sc);
+        __stcg(b.post1 + pb, cr.ss * br.w * sc);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// block-level helpers (FP64)
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ double2 block_sum2(double a, double c, double2* sh) {
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+        a += __shfl_xor_sync(kFull, a, off);
+        c += __shfl_xor_sync(kFull, c, off);
+    }
+    const int wid = threadIdx.x >> 5, ln = threadIdx.x & 31;
+    __syncthreads();
+    if (ln == 0) sh[wid] = make_double2(a, c);
+    __syncthreads();
+    double2 r = make_double2(0.0, 0.0);
+    for (int k = 0; k < (int)(blockDim.x >> 5); ++k) {
+        r.x += sh[k].x;
+        r.y += sh[k].y;
+    }
+    return r;
+}
+
+__device__ __forceinline__ double inv_expm1(double x) {   // 1/(e^x - 1), x > 0
+    return 1.0 / expm1(x);
+}
+
+__device__ float4 branch_terms_of(double d, double nu, int compat) {
+    const double nd = d * nu;
+    const double p00 = exp(-d * (1.0 + nu));
+    const double e1md = (compat && d < kEPSd) ? kEPSd : -expm1(-d);
+    const double e1mnd = (compat && nd < kEPSd) ? kEPSd : -expm1(-nd);
+    const double pst = exp(-nd);
+    return make_float4((float)p00, (float)(e1md * pst), (float)pst, (float)e1mnd);
+}
+
+// d-stationarity of  -a d + b log(1-e^{-d}) + c log(1-e^{-nu d})  on [lo, hi]
+// (a decreasing function of d): safeguarded Newton in log d.
+__device__ double solve_branch(double a, double bb, double c, double nu, double d0, double lo,
+                               double hi) {
+    auto F = [&](double d, double* dF) {
+        const double em = expm1(d);
+        double f = -a, g = 0.0;
+        if (bb > 0.0) {
+            f += bb / em;
+            g -= bb * (em + 1.0) / (em * em);
+        }
+        if (c > 0.0) {
+            const double en = expm1(nu * d);
+            f += c * nu / en;
+            g -= c * nu * nu * (en + 1.0) / (en * en);
+        }
+        *dF = g * d;   // derivative in log d
+        return f;
+    };
+    double t;
+    if (F(lo, &t) <= 0.0) return lo;
+    if (F(hi, &t) >= 0.0) return hi;
+    double ulo = log(lo), uhi = log(hi);
+    double u = log(fmin(fmax(d0, lo), hi));
+    for (int it = 0; it < 100; ++it) {
+        double dF;
+        const double f = F(exp(u), &dF);
+        if (f > 0.0) ulo = u; else uhi = u;
+        double un = u - f / dF;
+        if (!(un > ulo && un < uhi)) un = 0.5 * (ulo + uhi);
+        if (fabs(un - u) <= 1e-14 * fmax(1.0, fabs(u)) || uhi - ulo < 1e-14) {
+            u = un;
+            break;
+        }
+        u = un;
+    }
+    return exp(u);
+}
+
+// ---------------------------------------------------------------------------
+// M-step of one tree (one thread block)
+// ---------------------------------------------------------------------------
+__device__ void mstep_tree(const laml_batch& b, int p, int rounds, double2* sh) {
+    if (__ldcg(b.tr_status + p) != LAML_TREE_ACTIVE) return;
+    const int N = __ldg(b.tr_nodes + p), n = __ldg(b.tr_leaves + p), base = __ldg(b.tr_node_base + p);
+    const int ds = __ldg(b.tr_ds + p), NG = __ldg(b.ds_groups + ds), K = __ldg(b.ds_sites + ds);
+    const int64_t cb = __ldg(b.tr_cnt_base + p);
+    const bool compat = b.compat != 0;
+    const uint8_t fix = __ldg(b.tr_fix + p);
+    double nu = __ldcg(b.tr_nu + p), phi = __ldcg(b.tr_phi + p);
+    // 1. counts summed over site groups, d saved
+    double lr = 0.0;
+    for (int v = threadIdx.x; v < N; v += blockDim.x) {
+        double c[7] = {0, 0, 0, 0, 0, 0, 0};
+        const float* src = b.cnt_part + cb + (int64_t)v * NG * 8;
+        for (int g = 0; g < NG; ++g) {
+            const float4 a = __ldcg(reinterpret_cast<const float4*>(src + g * 8));
+            const float4 z = __ldcg(reinterpret_cast<const float4*>(src + g * 8) + 1);
+            c[0] += a.x; c[1] += a.y; c[2] += a.z; c[3] += a.w;
+            c[4] += z.x; c[5] += z.y; c[6] += z.z;
+        }
+        if (!compat) {   // EM_solver.py:342-345: floor at eps_s, normalise to numsites
+            double t = 0.0;
+            for (int k = 0; k < 5; ++k) { c[k] = fmax(c[k], kEpsS); t += c[k]; }
+            for (int k = 0; k < 5; ++k) c[k] = c[k] / t * K;
+        }
+        double* dst = b.nd_cnt + (int64_t)(base + v) * 6;
+        for (int k = 0; k < 6; ++k) dst[k] = c[k];
+        lr += c[6];
+        b.nd_d_prev[base + v] = __ldcg(b.nd_d + base + v);
+    }
+    const double LR = block_sum2(lr, 0.0, sh).x;
+    if (threadIdx.x == 0) {
+        b.tr_prev[2 * p] = nu;
+        b.tr_prev[2 * p + 1] = phi;
+    }
+    // 2. phi (fast_em/laml.py:77 stationary point; EM_solver.py:318-326)
+    if (!(fix & 2)) {
+        const double M = __ldg(b.ds_missing + ds), total = (double)n * K;
+        if (compat) {
+            const double Bm = M - LR, R = total - M;
+            phi = (R + Bm) > 0.0 ? Bm / (R + Bm) : phi;
+            phi = fmin(fmax(phi, kCalcEps), 1.0 - kCalcEps);
+        } else {
+            const double sil = __ldg(b.ds_silenced + ds);
+            const double Rt = M - (LR - sil), R = total - M;
+            phi = (R + Rt) > 0.0 ? Rt / (R + Rt) : 0.0;
+            if (fabs(phi) < 1.0 / total) phi = 0.0;
+        }
+    }
+    __syncthreads();
+    // 3. coordinate rounds: d | nu, then nu | d
+    const int R = compat ? rounds : 1;
+    const double dlo = compat ? kCalcEps : kDmin, dhi = compat ? 1.0 / kCalcEps : kDmax;
+    for (int r = 0; r < R; ++r) {
+        const bool use_s = compat || nu > kEpsNu;
+        for (int v = threadIdx.x; v < N; v += blockDim.x) {
+            if (!__ldg(b.nd_mask + base + v)) continue;
+            const double* c = b.nd_cnt + (int64_t)(base + v) * 6;
+            const double c0 = __ldcg(c), c1 = __ldcg(c + 1), c2 = __ldcg(c + 2),
+                         c3 = __ldcg(c + 3), c4 = __ldcg(c + 4);
+            const double a = c0 * (1.0 + nu) + (c1 + c3) * nu;
+            const double cs = use_s ? c2 + c4 : 0.0;
+            const double d0 = __ldcg(b.nd_d + base + v);
+            b.nd_d[base + v] = solve_branch(a, c1, cs, nu, d0, dlo, dhi);
+        }
+        __syncthreads();
+        if (!(fix & 1)) {
+            // -A nu + sum_v c_v log(1 - e^{-nu d_v}); compat: every branch,
+            // exact: the optimised branches (EM_solver.py:392-407)
+            double A = 0.0, Cs = 0.0;
+            for (int v = threadIdx.x; v < N; v += blockDim.x) {
+                if (!compat && !__ldg(b.nd_mask + base + v)) continue;
+                const double* c = b.nd_cnt + (int64_t)(base + v) * 6;
+                const double d = __ldcg(b.nd_d + base + v);
+                A += (__ldcg(c) + __ldcg(c + 1) + __ldcg(c + 3)) * d;
+                Cs += __ldcg(c + 2) + __ldcg(c + 4);
+            }
+            double2 ac = block_sum2(A, Cs, sh);
+            A = ac.x;
+            const double nlo = compat ? kCalcEps : 0.0, nhi = compat ? 1.0 - kCalcEps : 1.0;
+            auto G1 = [&](double x, double* g2) {
+                double f = 0.0, s2 = 0.0;
+                for (int v = threadIdx.x; v < N; v += blockDim.x) {
+                    if (!compat && !__ldg(b.nd_mask + base + v)) continue;
+                    const double* c = b.nd_cnt + (int64_t)(base + v) * 6;
+                    const double cc = __ldcg(c + 2) + __ldcg(c + 4);
+                    if (cc <= 0.0) continue;
+                    const double d = __ldcg(b.nd_d + base + v);
+                    const double en = expm1(x * d);
+                    f += cc * d / en;
+                    s2 -= cc * d * d * (en + 1.0) / (en * en);
+                }
+                double2 t = block_sum2(f, s2, sh);
+                *g2 = t.y;
+                return t.x - A;
+            };
+            double g2;
+            if (ac.y <= 0.0) {
+                nu = nlo;
+            } else if (G1(nhi, &g2) >= 0.0) {
+                nu = nhi;
+            } else if (compat && G1(nlo, &g2) <= 0.0) {
+                nu = nlo;
+            } else {
+                double a = compat ? nlo : 1e-300, c = nhi;
+                double x = fmin(fmax(nu, compat ? nlo : 1e-12), nhi);
+                for (int it = 0; it < 200; ++it) {
+                    const double f = G1(x, &g2);
+                    if (f > 0.0) a = x; else c = x;
+                    double xn = x - f / g2;
+                    if (!(xn > a && xn < c)) xn = (a > 0.0 && c / a > 4.0) ? sqrt(a * c) : 0.5 * (a + c);
+                    if (fabs(xn - x) <= 1e-15 * x || c - a <= 1e-15 * c) { x = xn; break; }
+                    x = xn;
+                }
+                nu = x;
+            }
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        b.tr_nu[p] = nu;
+        b.tr_phi[p] = phi;
+    }
+    for (int v = threadIdx.x; v < N; v += blockDim.x) {
+        const double d = __ldcg(b.nd_d + base + v);
+        reinterpret_cast<float4*>(b.nd_bt)[base + v] = branch_terms_of(d, nu, b.compat);
+    }
+}
+
+// per-tree log-likelihood (FP64 sum over sites) and the EM stopping rule
+__device__ void tree_llh_item(const laml_batch& b, int p, int mode, double rel_tol, int max_iters) {
+    // mode 0: plain sum; 1: init (llh_prev = llh); 2: EM update
+    if (mode == 2 && __ldcg(b.tr_status + p) != LAML_TREE_ACTIVE) return;
+    const int ds = __ldg(b.tr_ds + p), K = __ldg(b.ds_sites + ds);
+    const int64_t t = __ldg(b.tr_site_base + p);
+    double s = 0.0;
+    for (int c = 0; c < K; ++c) s += __ldcg(b.llh_site + t + c);
+    if (mode == 0) { b.tr_llh[p] = s; return; }
+    if (mode == 1) {
+        b.tr_llh[p] = s;
+        b.tr_llh_prev[p] = s;
+        b.tr_iter[p] = 0;
+        b.tr_status[p] = LAML_TREE_ACTIVE;
+        return;
+    }
+    const double prev = b.tr_llh_prev[p];
+    const int it = b.tr_iter[p] + 1;
+    b.tr_iter[p] = it;
+    if (fabs(s - prev) / fabs(prev) < rel_tol) {
+        b.tr_llh[p] = s;
+        b.tr_status[p] = LAML_TREE_CONVERGED;
+    } else if (isnan(s)) {
+        b.tr_llh[p] = prev;
+        b.tr_status[p] = LAML_TREE_NAN;
+    } else {
+        b.tr_llh[p] = s;
+        b.tr_llh_prev[p] = s;
+        if (it >= max_iters) b.tr_status[p] = LAML_TREE_MAXITER;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// grid barrier with a bounded wait (no trap: on timeout the error word is set
+// and every block returns)
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ unsigned long long gtimer() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+__device__ bool grid_barrier(const laml_batch& b, unsigned& gen) {
+    __syncthreads();
+    __shared__ int s_ok;
+    if (threadIdx.x == 0) {
+        int ok = 1;
+        __threadfence();
+        const unsigned arrived = atomicAdd(b.barrier, 1u);
+        if (arrived == gen * gridDim.x + gridDim.x - 1) {
+            atomicExch(b.barrier + 1, gen + 1);
+        } else {
+            const unsigned long long t0 = gtimer();
+            while (atomicAdd(b.barrier + 1, 0u) <= gen) {
+                if (*(volatile int*)b.error != 0) { ok = 0; break; }
+                if (gtimer() - t0 > 2000000000ull) {   // 2 s
+                    atomicCAS(b.error, 0, LAML_ERR_TIMEOUT);
+                    ok = 0;
+                    break;
+                }
+                __nanosleep(100);
+            }
+        }
+        __threadfence();
+        if (*(volatile int*)b.error != 0) ok = 0;
+        s_ok = ok;
+    }
+    __syncthreads();
+    ++gen;
+    return s_ok != 0;
+}
+
+// ---------------------------------------------------------------------------
+// kernels
+// ---------------------------------------------------------------------------
+template <int G>
+__device__ __forceinline__ void for_items(const laml_batch& b, const int32_t* items, int64_t n,
+                                          int gwarp, int nwarps, int kind, bool want_post,
+                                          bool respect_status) {
+    constexpr int IPW = 32 / G;
+    const int lane32 = threadIdx.x & 31, lane = lane32 % G, sub = lane32 / G;
+    const int64_t nw = (n + IPW - 1) / IPW;
+    for (int64_t wi = gwarp; wi < nw; wi += nwarps) {
+        const int64_t it = wi * IPW + sub;
+        const bool act = it < n;
+        const int node = act ? __ldg(items + 2 * it) : 0;
+        const int g = act ? __ldg(items + 2 * it + 1) : 0;
+        if (kind == 0) {
+            if (act) inside_item<G>(b, node, g, lane, respect_status);
+        } else if (kind == 1) {
+            outside_item<G>(b, node, g, lane, act, 0, want_post);
+        } else if (kind == 2) {
+            if (act) root_init_item<G>(b, node, g, lane, want_post);
+        } else {
+            outside_item<G>(b, node, g, lane, act, b.compat ? 1 : 2, false);
+        }
+    }
+}
+
+template <int G>
+__global__ void __launch_bounds__(kBlock) k_items(laml_batch b, const int32_t* items, int64_t n,
+                                                   int kind, int want_post, int respect_status) {
+    const int gwarp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int nwarps = (gridDim.x * blockDim.x) >> 5;
+    for_items<G>(b, items, n, gwarp, nwarps, kind, want_post != 0, respect_status != 0);
+}
+
+__global__ void __launch_bounds__(kBlock) k_mstep(laml_batch b, int rounds) {
+    __shared__ double2 sh[kBlock / 32];
+    for (int p = blockIdx.x; p < b.n_trees; p += gridDim.x) mstep_tree(b, p, rounds, sh);
+}
+
+__global__ void k_tree_llh(laml_batch b, int mode, double rel_tol, int max_iters) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p < b.n_trees) tree_llh_item(b, p, mode, rel_tol, max_iters);
+}
+
+__global__ void k_branch_terms(laml_batch b) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < b.n_nodes) {
+        const int p = b.nd_tree[i];
+        reinterpret_cast<float4*>(b.nd_bt)[i] = branch_terms_of(b.nd_d[i], b.tr_nu[p], b.compat);
+    }
+}
+
+template <int G>
+__global__ void __launch_bounds__(kBlock) k_em_persistent(laml_batch b, int iters, int rounds,
+                                                           double rel_tol, int max_iters) {
+    __shared__ double2 sh[kBlock / 32];
+    const int gwarp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int nwarps = (gridDim.x * blockDim.x) >> 5;
+    unsigned gen = 0;
+    for (int it = 0; it < iters; ++it) {
+        for_items<G>(b, b.root_items, b.n_root_items, gwarp, nwarps, 2, false, true);
+        if (!grid_barrier(b, gen)) return;
+        for (int l = 0; l < b.n_out_levels; ++l) {
+            const int64_t o = b.out_level_off[l], e = b.out_level_off[l + 1];
+            for_items<G>(b, b.out_items + 2 * o, e - o, gwarp, nwarps, 1, false, true);
+            if (!grid_barrier(b, gen)) return;
+        }
+        for_items<G>(b, b.root_items, b.n_root_items, gwarp, nwarps, 3, false, true);
+        if (!grid_barrier(b, gen)) return;
+        for (int p = blockIdx.x; p < b.n_trees; p += gridDim.x) mstep_tree(b, p, rounds, sh);
+        if (!grid_barrier(b, gen)) return;
+        for (int l = 0; l < b.n_in_levels; ++l) {
+            const int64_t o = b.in_level_off[l], e = b.in_level_off[l + 1];
+            for_items<G>(b, b.in_items + 2 * o, e - o, gwarp, nwarps, 0, false, true);
+            if (!grid_barrier(b, gen)) return;
+        }
+        for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < b.n_trees;
+             p += gridDim.x * blockDim.x)
+            tree_llh_item(b, p, 2, rel_tol, max_iters);
+        if (!grid_barrier(b, gen)) return;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// host launchers
+// ---------------------------------------------------------------------------
+int g_num_sms = 0;
+
+int num_sms() {
+    if (g_num_sms == 0) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&g_num_sms, cudaDevAttrMultiProcessorCount, dev);
+        if (g_num_sms <= 0) g_num_sms = 1;
+    }
+    return g_num_sms;
+}
+
+int check(cudaError_t e, const char* what) {
+    if (e != cudaSuccess) {
+        laml::set_error(std::string(what) + ": " + cudaGetErrorString(e));
+        return LAML_ERR_CUDA;
+    }
+    return LAML_OK;
+}
+
+int validate(const laml_batch* b) {
+    if (!b || b->n_trees <= 0 || b->n_nodes <= 0) {
+        laml::set_error("laml_batch: empty or null batch");
+        return LAML_ERR_ARG;
+    }
+    if (b->group_sites != 8 && b->group_sites != 16 && b->group_sites != 32) {
+        laml::set_error("laml_batch: group_sites must be 8, 16 or 32");
+        return LAML_ERR_ARG;
+    }
+    return LAML_OK;
+}
+
+template <int G>
+int launch_items(const laml_batch& b, const int32_t* items, int64_t n, int kind, int want_post,
+                 int respect_status, cudaStream_t st) {
+    if (n <= 0) return LAML_OK;
+    const int ipb = (kBlock / 32) * (32 / G);
+    int64_t blocks = (n + ipb - 1) / ipb;
+    const int64_t cap = (int64_t)num_sms() * 16;
+    if (blocks > cap) blocks = cap;
+    k_items<G><<<(unsigned)blocks, kBlock, 0, st>>>(b, items, n, kind, want_post, respect_status);
+    return check(cudaGetLastError(), "k_items launch");
+}
+
+// host copies of the level offsets (tiny) are needed to launch per level
+struct Levels {
+    std::vector<int32_t> in, out;
+};
+
+int fetch_levels(const laml_batch& b, Levels& L, cudaStream_t st) {
+    L.in.resize(b.n_in_levels + 1);
+    L.out.resize(b.n_out_levels + 1);
+    int rc = check(cudaMemcpyAsync(L.in.data(), b.in_level_off, sizeof(int32_t) * L.in.size(),
+                                   cudaMemcpyDeviceToHost, st), "level offsets");
+    if (rc) return rc;
+    rc = check(cudaMemcpyAsync(L.out.data(), b.out_level_off, sizeof(int32_t) * L.out.size(),
+                               cudaMemcpyDeviceToHost, st), "level offsets");
+    if (rc) return rc;
+    return check(cudaStreamSynchronize(st), "level offsets");
+}
+
+template <int G>
+int inside_t(const laml_batch& b, int update_em, cudaStream_t st, const Levels& L,
+             int respect_status) {
+    for (int l = 0; l < b.n_in_levels; ++l) {
+        int rc = launch_items<G>(b, b.in_items + 2 * (int64_t)L.in[l], L.in[l + 1] - L.in[l], 0, 0,
+                                 respect_status, st);
+        if (rc) return rc;
+    }
+    return LAML_OK;
+}
+
+template <int G>
+int outside_t(const laml_batch& b, int want_post, cudaStream_t st, const Levels& L) {
+    int rc = launch_items<G>(b, b.root_items, b.n_root_items, 2, want_post, 1, st);
+    if (rc) return rc;
+    for (int l = 0; l < b.n_out_levels; ++l) {
+        rc = launch_items<G>(b, b.out_items + 2 * (int64_t)L.out[l], L.out[l + 1] - L.out[l], 1,
+                             want_post, 1, st);
+        if (rc) return rc;
+    }
+    return launch_items<G>(b, b.root_items, b.n_root_items, 3, 0, 1, st);
+}
+
+template <int G>
+int em_levels_t(const laml_batch& b, int iters, int rounds, double tol, int max_iters,
+                cudaStream_t st) {
+    Levels L;
+    int rc = fetch_levels(b, L, st);
+    if (rc) return rc;
+    const int tb = (b.n_trees + 127) / 128;
+    for (int it = 0; it < iters; ++it) {
+        if ((rc = outside_t<G>(b, 0, st, L))) return rc;
+        k_mstep<<<b.n_trees, kBlock, 0, st>>>(b, rounds);
+        if ((rc = check(cudaGetLastError(), "k_mstep"))) return rc;
+        if ((rc = inside_t<G>(b, 0, st, L, 1))) return rc;
+        k_tree_llh<<<tb, 128, 0, st>>>(b, 2, tol, max_iters);
+        if ((rc = check(cudaGetLastError(), "k_tree_llh"))) return rc;
+    }
+    return LAML_OK;
+}
+
+template <int G>
+int em_persistent_t(const laml_batch& b, int iters, int rounds, double tol, int max_iters,
+                    cudaStream_t st) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    int coop = 0;
+    cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev);
+    int per_sm = 0;
+    int rc = check(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_em_persistent<G>,
+                                                                 kBlock, 0), "occupancy");
+    if (rc) return rc;
+    if (!coop || per_sm <= 0) {
+        laml::set_error("cooperative launch unavailable for the persistent EM kernel");
+        return LAML_ERR_CUDA;
+    }
+    const int grid = per_sm * num_sms();
+    if ((rc = check(cudaMemsetAsync(b.barrier, 0, 2 * sizeof(uint32_t), st), "barrier reset")))
+        return rc;
+    laml_batch bb = b;
+    void* args[] = {&bb, &iters, &rounds, &tol, &max_iters};
+    return check(cudaLaunchCooperativeKernel((const void*)k_em_persistent<G>, dim3(grid),
+                                             dim3(kBlock), args, 0, st),
+                 "k_em_persistent launch");
+}
+
+#define DISPATCH_G(b, call)                                   \
+    switch ((b).group_sites) {                                \
+        case 8: { constexpr int GG = 8; return call; }        \
+        case 16: { constexpr int GG = 16; return call; }      \
+        default: { constexpr int GG = 32; return call; }      \
+    }
+
+}  // namespace
+
+extern "C" int laml_supported_group_sites(void) { return 8 | 16 | 32; }
+
+extern "C" int laml_branch_terms(const laml_batch* b, void* stream) {
+    int rc = validate(b);
+    if (rc) return rc;
+    cudaStream_t st = (cudaStream_t)stream;
+    const int64_t blocks = (b->n_nodes + kBlock - 1) / kBlock;
+    k_branch_terms<<<(unsigned)blocks, kBlock, 0, st>>>(*b);
+    return check(cudaGetLastError(), "k_branch_terms");
+}
+
+extern "C" int laml_inside(const laml_batch* b, int32_t update_em, void* stream) {
+    int rc = validate(b);
+    if (rc) return rc;
+    cudaStream_t st = (cudaStream_t)stream;
+    Levels L;
+    if ((rc = fetch_levels(*b, L, st))) return rc;
+    auto run = [&]() -> int { DISPATCH_G(*b, (inside_t<GG>(*b, update_em, st, L, 0))); };
+    if ((rc = run())) return rc;
+    const int tb = (b->n_trees + 127) / 128;
+    k_tree_llh<<<tb, 128, 0, st>>>(*b, update_em ? 1 : 0, 0.0, 0);
+    return check(cudaGetLastError(), "k_tree_llh");
+}
+
+extern "C" int laml_outside(const laml_batch* b, int32_t want_post, void* stream) {
+    int rc = validate(b);
+    if (rc) return rc;
+    if (want_post && (!b->post0 || !b->post1)) {
+        laml::set_error("laml_outside: want_post needs post0/post1 buffers");
+        return LAML_ERR_ARG;
+    }
+    cudaStream_t st = (cudaStream_t)stream;
+    Levels L;
+    if ((rc = fetch_levels(*b, L, st))) return rc;
+    DISPATCH_G(*b, (outside_t<GG>(*b, want_post, st, L)));
+}
+
+extern "C" int laml_mstep(const laml_batch* b, int32_t rounds, void* stream) {
+    int rc = validate(b);
+    if (rc) return rc;
+    k_mstep<<<b->n_trees, kBlock, 0, (cudaStream_t)stream>>>(*b, rounds);
+    return check(cudaGetLastError(), "k_mstep");
+}
+
+extern "C" int laml_em_run(const laml_batch* b, int32_t iters, int32_t rounds, double rel_tol,
+                           int32_t max_iters, void* stream) {
+    int rc = validate(b);
+    if (rc) return rc;
+    if (iters <= 0) return LAML_OK;
+    DISPATCH_G(*b, (em_persistent_t<GG>(*b, iters, rounds, rel_tol, max_iters,
+                                        (cudaStream_t)stream)));
+}
+
+extern "C" int laml_em_run_levels(const laml_batch* b, int32_t iters, int32_t rounds,
+                                  double rel_tol, int32_t max_iters, void* stream) {
+    int rc = validate(b);
+    if (rc) return rc;
+    if (iters <= 0) return LAML_OK;
+    DISPATCH_G(*b, (em_levels_t<GG>(*b, iters, rounds, rel_tol, max_iters, (cudaStream_t)stream)));
+}

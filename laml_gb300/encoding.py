@@ -1,0 +1,201 @@
+"""Host-side encoders: newick trees, character matrices and batch plans.
+
+Thin wrappers over the C++ encoders of liblaml_gb300.so (laml_newick_*,
+laml_dataset_*, laml_plan_*); all arrays are numpy.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass
+from typing import Dict, List, Optional, Sequence
+
+import numpy as np
+
+from . import _native as N
+
+MISSING = -1
+SILENCED = -2
+
+
+@dataclass
+class EncodedTree:
+    """A tree in fastEM_solver.parse_tree numbering (fastEM_solver.py:46-146):
+    leaves 0..n-1, internal nodes n..N-1 in treeswift preorder, children in
+    networkx successor order."""
+    num_nodes: int
+    num_leaves: int
+    parent: np.ndarray          # int32[N], -1 at the root
+    child0: np.ndarray          # int32[N], -1 at leaves
+    child1: np.ndarray
+    branch_length: np.ndarray   # float64[N] (0 where absent)
+    has_length: np.ndarray      # bool[N]
+    labels: List[str]
+
+    @property
+    def root(self) -> int:
+        return int(np.flatnonzero(self.parent < 0)[0])
+
+
+def encode_newick(newick: str, leaf_order: Optional[Sequence[str]] = None) -> EncodedTree:
+    L = N.lib()
+    nn, nl, lb = N.i32(), N.i32(), N.i64()
+    s = newick.encode()
+    N.check(L.laml_newick_size(s, C.byref(nn), C.byref(nl), C.byref(lb)))
+    n_nodes = nn.value
+    par = np.empty(n_nodes, np.int32)
+    c0 = np.empty(n_nodes, np.int32)
+    c1 = np.empty(n_nodes, np.int32)
+    bl = np.empty(n_nodes, np.float64)
+    has = np.empty(n_nodes, np.uint8)
+    labels = C.create_string_buffer(int(lb.value) + 1)
+    offs = np.empty(n_nodes, np.int64)
+    if leaf_order is not None:
+        arr = (C.c_char_p * len(leaf_order))(*[str(x).encode() for x in leaf_order])
+        lo, nlo = arr, len(leaf_order)
+    else:
+        lo, nlo = None, 0
+    N.check(L.laml_newick_encode(s, lo, nlo, N.ptr(par), N.ptr(c0), N.ptr(c1), N.ptr(bl),
+                                 N.ptr(has), labels, N.ptr(offs)))
+    raw = labels.raw
+    labs = []
+    for k in range(n_nodes):
+        o = int(offs[k])
+        e = raw.index(b"\0", o)
+        labs.append(raw[o:e].decode())
+    return EncodedTree(n_nodes, nl.value, par, c0, c1, bl, has.astype(bool), labs)
+
+
+def char_matrix(rows: Sequence[Sequence], exact: bool = False) -> np.ndarray:
+    """Rows of {int, '?'} -> int32 codes: '?' (and anything non-numeric or
+    negative) -> MISSING; an explicit -1 -> SILENCED when ``exact`` (EM_solver
+    treats -1 as observed silencing, EM_solver.py:104-110), else MISSING
+    (fastEM replaces '?' by -1, fastEM_solver.py:29)."""
+    n = len(rows)
+    K = len(rows[0]) if n else 0
+    out = np.empty((n, K), np.int32)
+    for i, r in enumerate(rows):
+        for c, x in enumerate(r):
+            if isinstance(x, str):
+                try:
+                    v = int(x)
+                except ValueError:
+                    out[i, c] = MISSING
+                    continue
+            else:
+                v = int(x)
+            out[i, c] = v if v >= 0 else (SILENCED if (exact and v == -1) else MISSING)
+    return out
+
+
+def priors_csr(Q: Sequence[Dict], n_sites: int):
+    """list of {state: prob} per site -> CSR (ptr, state, prob)."""
+    if len(Q) != n_sites:
+        raise ValueError(f"priors cover {len(Q)} sites, the matrix has {n_sites}")
+    ptr = np.zeros(n_sites + 1, np.int32)
+    st, pr = [], []
+    for c, q in enumerate(Q):
+        for k, v in q.items():
+            st.append(int(k))
+            pr.append(float(v))
+        ptr[c + 1] = len(st)
+    return ptr, np.asarray(st, np.int32), np.asarray(pr, np.float64)
+
+
+@dataclass
+class EncodedDataset:
+    """Device site layout of one character matrix + priors (see
+    laml_dataset_encode).  ``codes`` rows follow the tree's leaf order."""
+    n_leaves: int
+    n_sites: int
+    n_sites_pad: int
+    n_groups: int
+    group_sites: int
+    row_len: int
+    max_states: int
+    n_missing: int
+    n_silenced: int
+    codes: np.ndarray       # int16[n, Kpad]
+    q: np.ndarray           # float32[row_len]
+    site_perm: np.ndarray   # int32[Kpad]
+    site_C: np.ndarray      # int32[Kpad]
+    site_sumq: np.ndarray   # float32[Kpad]
+    group_off: np.ndarray   # int32[NG]
+    group_C: np.ndarray     # int32[NG]
+    state_ptr: np.ndarray   # int32[K+1]
+    state_map: np.ndarray   # int32[...]
+    compat: bool
+
+
+def encode_dataset(chars: np.ndarray, Q, compat: bool = True, group_sites: int = 8) -> EncodedDataset:
+    """chars: int32[n, K] from char_matrix (leaf order); Q: per-site prior
+    dicts or a (ptr, state, prob) CSR triple."""
+    L = N.lib()
+    chars = np.ascontiguousarray(chars, dtype=np.int32)
+    n, K = chars.shape
+    pp, ps, pq = Q if isinstance(Q, tuple) else priors_csr(Q, K)
+    pp = np.ascontiguousarray(pp, np.int32)
+    ps = np.ascontiguousarray(ps, np.int32)
+    pq = np.ascontiguousarray(pq, np.float64)
+    info = N.DatasetInfo()
+    N.check(L.laml_dataset_measure(n, K, N.ptr(chars), N.ptr(pp), N.ptr(ps), N.ptr(pq),
+                                   int(compat), group_sites, C.byref(info)))
+    Kp, NG, R = info.n_sites_pad, info.n_groups, info.row_len
+    codes = np.empty((n, Kp), np.int16)
+    q = np.empty(R, np.float32)
+    perm = np.empty(Kp, np.int32)
+    sC = np.empty(Kp, np.int32)
+    sq = np.empty(Kp, np.float32)
+    goff = np.empty(NG, np.int32)
+    gC = np.empty(NG, np.int32)
+    sptr = np.empty(K + 1, np.int32)
+    smap = np.empty(max(1, int(np.sum(chars > 0)) + K), np.int32)
+    N.check(L.laml_dataset_encode(n, K, N.ptr(chars), N.ptr(pp), N.ptr(ps), N.ptr(pq),
+                                  int(compat), group_sites, N.ptr(codes), N.ptr(q), N.ptr(perm),
+                                  N.ptr(sC), N.ptr(sq), N.ptr(goff), N.ptr(gC), N.ptr(sptr),
+                                  N.ptr(smap)))
+    return EncodedDataset(n, K, Kp, NG, group_sites, R, info.max_states, info.n_missing,
+                          info.n_silenced, codes, q, perm, sC, sq, goff, gC, sptr,
+                          smap[:sptr[-1]].copy(), compat)
+
+
+def plan_batch(trees: Sequence[EncodedTree], tree_ds: Sequence[int],
+               datasets: Sequence[EncodedDataset]):
+    """Level schedule + buffer offsets of a batch (laml_plan_*).  Returns
+    (sizes: dict, arrays: dict of numpy arrays)."""
+    L = N.lib()
+    T = len(trees)
+    tn = np.asarray([t.num_nodes for t in trees], np.int32)
+    tl = np.asarray([t.num_leaves for t in trees], np.int32)
+    td = np.asarray(tree_ds, np.int32)
+    c0 = np.concatenate([t.child0 for t in trees]).astype(np.int32)
+    c1 = np.concatenate([t.child1 for t in trees]).astype(np.int32)
+    dg = np.asarray([d.n_groups for d in datasets], np.int32)
+    dk = np.asarray([d.n_sites_pad for d in datasets], np.int32)
+    dr = np.asarray([d.row_len for d in datasets], np.int64)
+    gbase = np.zeros(len(datasets), np.int32)
+    gbase[1:] = np.cumsum(dg)[:-1]
+    gC = np.concatenate([d.group_C for d in datasets]).astype(np.int32)
+    pin = N.PlanInput(T, N.ptr(tn), N.ptr(tl), N.ptr(td), N.ptr(c0), N.ptr(c1), len(datasets),
+                      N.ptr(dg), N.ptr(dk), N.ptr(dr), N.ptr(gbase), N.ptr(gC))
+    sz = N.PlanSizes()
+    N.check(L.laml_plan_measure(C.byref(pin), C.byref(sz)))
+    nn = sz.n_nodes
+    arr = {
+        "tr_node_base": np.empty(T, np.int32), "tr_root": np.empty(T, np.int32),
+        "tr_quirk": np.empty(T, np.int32), "tr_site_base": np.empty(T, np.int64),
+        "tr_cnt_base": np.empty(T, np.int64), "tr_post_base": np.empty(T, np.int64),
+        "nd_tree": np.empty(nn, np.int32), "nd_c0": np.empty(nn, np.int32),
+        "nd_c1": np.empty(nn, np.int32), "nd_parent": np.empty(nn, np.int32),
+        "nd_sib": np.empty(nn, np.int32), "nd_leafrow": np.empty(nn, np.int32),
+        "nd_prow": np.empty(nn, np.int64), "nd_srow": np.empty(nn, np.int64),
+        "in_level_off": np.empty(sz.n_in_levels + 1, np.int32),
+        "in_items": np.empty(2 * max(1, sz.n_in_items), np.int32),
+        "out_level_off": np.empty(sz.n_out_levels + 1, np.int32),
+        "out_items": np.empty(2 * max(1, sz.n_out_items), np.int32),
+        "root_items": np.empty(2 * max(1, sz.n_root_items), np.int32),
+    }
+    pout = N.PlanOutput(*[N.ptr(arr[k]) for k in N.PLAN_OUT_FIELDS])
+    N.check(L.laml_plan_fill(C.byref(pin), C.byref(pout)))
+    sizes = {k: getattr(sz, k) for k, _ in N.PlanSizes._fields_}
+    arr["group_base"] = gbase
+    return sizes, arr

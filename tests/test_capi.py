@@ -1,0 +1,145 @@
+"""CPU checks of the C ABI: the library loads, exports every symbol declared
+in include/laml_gb300.h, and its host encoders agree with the oracle
+bit-for-bit (node numbering, recoding, priors)."""
+import os
+import re
+
+import numpy as np
+import pytest
+
+from laml_gb300 import _native as N
+from laml_gb300 import encoding as E
+from laml_gb300 import synth
+from oracle import pmm_oracle as O
+from tests.helpers import golden_path, read_char_matrix, read_prior_csv, rows_in_leaf_order
+
+HEADER = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "include",
+                      "laml_gb300.h")
+
+
+def declared_symbols():
+    src = open(HEADER).read()
+    return sorted(set(re.findall(r"^\s*(?:const\s+)?\w+\*?\s+\*?(laml_\w+)\s*\(", src, re.M)))
+
+
+def test_library_exports_every_declared_symbol():
+    import ctypes
+    lib = ctypes.CDLL(N.LIB_PATH)
+    syms = declared_symbols()
+    assert len(syms) >= 14
+    for s in syms:
+        assert hasattr(lib, s), s
+    assert set(syms) <= set(N.EXPORTS), set(syms) - set(N.EXPORTS)
+
+
+def test_batch_struct_matches_header():
+    """Field order of laml_batch in the ctypes mirror equals the header."""
+    src = open(HEADER).read()
+    body = src[src.index("typedef struct laml_batch {"):src.index("} laml_batch;")]
+    names = []
+    for line in body.splitlines()[1:]:
+        line = line.split("/*")[0].strip()
+        if not line:
+            continue
+        decl = line.rstrip(";")
+        parts = decl.split(None, 1) if not decl.startswith("const") else decl.split(None, 2)[1:]
+        rest = parts[-1] if len(parts) > 1 else parts[0]
+        rest = re.sub(r"^(int32_t|int64_t|uint8_t|uint32_t|int16_t|double|float)\s*", "", rest)
+        for n in rest.split(","):
+            names.append(n.strip().lstrip("*").strip())
+    assert names == [n for n, _ in N.BATCH_FIELDS]
+
+
+@pytest.mark.parametrize("seed", [0, 1, 2])
+def test_newick_order_matches_parse_tree(seed):
+    rng = np.random.default_rng(seed)
+    t = synth.yule_tree(40 + seed, rng)
+    nw = t.newick()
+    order = list(rng.permutation([t.labels[u] for u in t.leaves()]))
+    for lo in (None, order):
+        et = E.encode_newick(nw, lo)
+        ot = O.parse_tree(nw, ordered_leaf_labels=lo)
+        assert et.labels == ot.labels
+        assert et.num_leaves == ot.num_leaves
+        np.testing.assert_array_equal(et.parent, ot.parent)
+        for u in range(et.num_nodes):
+            ch = ot.children[u]
+            assert [et.child0[u], et.child1[u]] == (list(ch) if ch else [-1, -1])
+        np.testing.assert_array_equal(et.branch_length, ot.branch_lengths)
+
+
+def test_newick_unifurcating_root_and_unnamed_nodes():
+    nw = "(((a:1,b:2):0.5,c:3):0.25);"
+    et = E.encode_newick(nw)
+    ot = O.parse_tree(nw)
+    assert et.labels == ot.labels
+    assert et.num_nodes == 5 and et.num_leaves == 3
+    assert et.labels[3] == "node_1"      # preorder index 1 after the dropped root
+
+
+def test_newick_errors():
+    with pytest.raises(N.LamlError):
+        E.encode_newick("((a:1,b:1):1,c:1")
+    with pytest.raises(N.LamlError) as e:
+        E.encode_newick("(a:1,b:1,c:1):1;")
+    assert e.value.code == -6
+    with pytest.raises(N.LamlError) as e:
+        E.encode_newick("((a:1,b:1):1,c:1):1;", ["a", "b"])
+    assert e.value.code == -7
+
+
+@pytest.mark.parametrize("compat", [True, False])
+@pytest.mark.parametrize("G", [8, 16, 32])
+def test_dataset_recode_matches_oracle(compat, G):
+    T = open(golden_path("test4.tre")).read().strip()
+    msa, _ = read_char_matrix(golden_path("test4_charMtrx.txt"))
+    Q = read_prior_csv(golden_path("test4_prior.csv"), with_zero_key=not compat)
+    tr = O.parse_tree(T)
+    rows = rows_in_leaf_order(tr, msa)
+    enc = O.recode(rows, Q, compat=compat)
+    ds = E.encode_dataset(E.char_matrix(rows, exact=not compat), Q, compat=compat, group_sites=G)
+    K = len(Q)
+    assert ds.n_sites == K and ds.n_sites_pad % G == 0
+    for c in range(ds.n_sites_pad):
+        o = ds.site_perm[c]
+        if o < 0:
+            continue
+        k = int(enc.k[o])
+        assert ds.site_C[c] == k + 2
+        g, lane = c // G, c % G
+        qv = np.array([ds.q[ds.group_off[g] + j * G + lane] for j in range(2, k + 2)])
+        np.testing.assert_array_equal(qv, enc.q[o, :k].astype(np.float32))
+        # codes: slot j <-> recoded state j-1
+        oc = enc.chars[:, o]
+        gc = ds.codes[:, c].astype(np.int64)
+        np.testing.assert_array_equal(np.where(gc >= 2, gc - 1, gc), oc)
+    assert ds.n_missing == int(np.sum(enc.chars == O.MISSING))
+
+
+def test_dataset_missing_prior_is_an_error():
+    mat = np.array([[1, 2], [0, 3]], np.int32)
+    with pytest.raises(N.LamlError) as e:
+        E.encode_dataset(mat, [{1: 0.5}, {2: 1.0}], compat=True)
+    assert e.value.code == -4
+
+
+def test_plan_levels():
+    rng = np.random.default_rng(5)
+    trees = [E.encode_newick(synth.yule_tree(n, rng).newick()) for n in (7, 30, 3)]
+    mat = np.zeros((30, 5), np.int32)
+    ds = E.encode_dataset(mat, [{1: 1.0}] * 5, compat=True, group_sites=8)
+    sizes, arr = E.plan_batch(trees, [0, 0, 0], [ds])
+    assert sizes["n_nodes"] == sum(t.num_nodes for t in trees)
+    # every internal node appears once per group among the inside items, after its children
+    items = arr["in_items"][:2 * sizes["n_in_items"]].reshape(-1, 2)
+    lvl = np.empty(sizes["n_nodes"], int)
+    off = arr["in_level_off"]
+    for l in range(sizes["n_in_levels"]):
+        for node, g in items[off[l]:off[l + 1]]:
+            lvl[node] = l
+    for u in range(sizes["n_nodes"]):
+        c0, c1 = arr["nd_c0"][u], arr["nd_c1"][u]
+        if c0 >= 0:
+            for c in (c0, c1):
+                if arr["nd_c0"][c] >= 0:
+                    assert lvl[c] < lvl[u]

@@ -1,0 +1,155 @@
+"""GPU parity: the CUDA path (through the C ABI) against the FP64 oracle.
+
+Tolerances (FP32 kernels vs FP64 oracle): per-site and total log-likelihood
+1e-6 relative; expected counts and leaf posteriors 1e-4 relative (+1e-5
+absolute); posteriors 1e-4 absolute; EM fixed points 1e-6 relative in logL.
+"""
+import math
+
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+from laml_gb300 import problem as PB  # noqa: E402
+from laml_gb300 import synth  # noqa: E402
+from laml_gb300 import _native as N  # noqa: E402
+from oracle import pmm_oracle as O  # noqa: E402
+from tests.helpers import (golden_path, known_answers, read_char_matrix,  # noqa: E402
+                           read_prior_csv)
+
+LLH_RTOL = 1e-6
+
+
+def _oracle(w, t, compat):
+    tr = O.parse_tree(w.newicks[t], w.leaf_order)
+    enc = O.recode([w.rows[c] for c in w.leaf_order], w.Q, compat=compat)
+    return O.Problem(tr, enc, compat)
+
+
+def _wl(seed=3, n=40, K=13, T=3):
+    return synth.pmm_workload(n, K, 3, 12, 0.5, 0.1, 0.15, seed=seed, n_trees=T)
+
+
+@pytest.mark.parametrize("compat", [True, False])
+@pytest.mark.parametrize("G", [8, 16, 32])
+def test_estep_parity(compat, G):
+    w = _wl()
+    nu, phi = 0.13, 0.21
+    b = PB.make_batch(w.newicks, w.rows, w.Q, w.leaf_order, compat=compat, group_sites=G,
+                      nu=nu, phi=phi, want_post=True, clamp=False)
+    b.e_step(want_post=True)
+    torch.cuda.synchronize()
+    cnt, lr = b.counts_from_partials()
+    nb = b.v["tr_node_base"].cpu().numpy()
+    llh = b.work["tr_llh"].cpu().numpy()
+    for t in range(len(w.newicks)):
+        prob = _oracle(w, t, compat)
+        es = O.e_step(prob, prob.tree.branch_lengths, nu, phi)
+        np.testing.assert_allclose(b.site_llh(t), es.llh_site, rtol=LLH_RTOL)
+        assert llh[t] == pytest.approx(es.llh, rel=LLH_RTOL)
+        Nn = prob.tree.parent.shape[0]
+        np.testing.assert_allclose(cnt[nb[t]:nb[t] + Nn], es.counts, rtol=1e-4, atol=1e-5)
+        np.testing.assert_allclose(lr[t][:prob.tree.num_leaves], es.leaf_resp, rtol=1e-4,
+                                   atol=1e-5)
+        p0, p1 = b.posteriors(t)
+        np.testing.assert_allclose(p0, np.exp(es.post0), atol=1e-4)
+        np.testing.assert_allclose(p1, np.exp(es.post1), atol=1e-4)
+
+
+def test_known_answers_on_gpu():
+    """Every 3-leaf known answer of unit_tests_EMSolver/MLSolver, exact model."""
+    cases, _ = known_answers()
+    for case in cases:
+        leaves = sorted(case["msa"])
+        b = PB.make_batch([case["T"]], case["msa"], case["Q"], leaves, compat=False,
+                          nu=case["nu"], phi=case["phi"], clamp=False)
+        llh = b.log_likelihood()[0]
+        assert -llh == pytest.approx(case["true_nllh"], abs=1e-5), case["name"]
+
+
+@pytest.mark.parametrize("compat", [True, False])
+def test_em_parity_with_oracle(compat):
+    w = _wl(seed=11, n=48, K=12, T=2)
+    rounds = 4
+    b = PB.make_batch(w.newicks, w.rows, w.Q, w.leaf_order, compat=compat, nu=0.5, phi=0.5,
+                      clamp=compat)
+    res = b.run_em(rounds=rounds, max_iters=200)
+    for t in range(2):
+        prob = _oracle(w, t, compat)
+        if compat:
+            ref = O.em_compat(prob, prob.tree.branch_lengths, 0.5, 0.5, rounds=rounds)
+        else:
+            ref = O.em_exact(prob, prob.tree.branch_lengths, 0.5, 0.5)
+        r = res[t]
+        assert r.llh == pytest.approx(ref.llh, rel=1e-6)
+        assert abs(r.iterations - ref.iterations) <= 1
+        assert r.nu == pytest.approx(ref.nu, rel=1e-3, abs=1e-6)
+        assert r.phi == pytest.approx(ref.phi, rel=1e-3, abs=1e-6)
+        if r.iterations == ref.iterations:
+            np.testing.assert_allclose(r.branch_lengths, ref.d, rtol=1e-3, atol=1e-5)
+
+
+def test_exact_em_test4_fixed_point():
+    """unit_tests_EMSolver.py test_47 through the GPU exact-model EM."""
+    import random
+    T = open(golden_path("test4.tre")).read().strip()
+    msa, _ = read_char_matrix(golden_path("test4_charMtrx.txt"))
+    Q = read_prior_csv(golden_path("test4_prior.csv"), with_zero_key=True)
+    tr = O.parse_tree(T)
+    post = O.treeswift_postorder_ids(tr)
+    lens = [tr.branch_lengths[i] for i in post]
+    rs = random.Random(1221)
+    x, nu, phi = O.exact_initials(tr, lens, int(rs.random() * 10000))
+    d = np.empty(len(post))
+    d[post] = x
+    b = PB.make_batch([T], msa, Q, tr.labels[:tr.num_leaves], compat=False, nu=nu, phi=phi,
+                      d=[d], clamp=False)
+    r = b.run_em(max_iters=1000)[0]
+    assert abs(1007.009158767873 + r.llh) / 1007.009158767873 < 1e-4
+    assert r.phi == pytest.approx(0, abs=1e-4)
+    assert r.nu == pytest.approx(0, abs=1e-4)
+
+
+def test_compat_em_test4():
+    """unit_tests_fastEMSolver.py test_1: |nllh - 1007.009...| < 10, phi, nu ~ 0."""
+    T = open(golden_path("test4.tre")).read().strip()
+    msa, _ = read_char_matrix(golden_path("test4_charMtrx.txt"))
+    Q = read_prior_csv(golden_path("test4_prior.csv"))
+    tr = O.parse_tree(T)
+    b = PB.make_batch([T], msa, Q, tr.labels[:tr.num_leaves], compat=True, nu=0.5, phi=0.5)
+    r = b.run_em()[0]
+    assert abs(1007.009158767873 + r.llh) < 10
+    assert r.phi == pytest.approx(0, abs=1e-4)
+    assert r.nu == pytest.approx(0, abs=1e-4)
+
+
+def test_persistent_equals_per_level_launches():
+    w = _wl(seed=5, n=60, K=20, T=4)
+    out = []
+    for persistent in (True, False):
+        b = PB.make_batch(w.newicks, w.rows, w.Q, w.leaf_order, compat=True)
+        out.append(b.run_em(persistent=persistent, max_iters=50))
+    for a, c in zip(*out):
+        assert a.llh == c.llh and a.iterations == c.iterations
+        np.testing.assert_array_equal(a.branch_lengths, c.branch_lengths)
+
+
+def test_batched_equals_alone():
+    """Each tree's result is the same alone and in a batch (bitwise)."""
+    w = _wl(seed=8, n=50, K=17, T=5)
+    both = PB.make_batch(w.newicks, w.rows, w.Q, w.leaf_order, compat=True).run_em(max_iters=60)
+    for t in range(5):
+        alone = PB.make_batch([w.newicks[t]], w.rows, w.Q, w.leaf_order,
+                              compat=True).run_em(max_iters=60)[0]
+        assert alone.llh == both[t].llh
+        assert alone.iterations == both[t].iterations
+        np.testing.assert_array_equal(alone.branch_lengths, both[t].branch_lengths)
+
+
+def test_device_error_word_is_clear():
+    w = _wl(seed=9, n=30, K=9, T=2)
+    b = PB.make_batch(w.newicks, w.rows, w.Q, w.leaf_order, compat=True)
+    b.run_em(max_iters=20)
+    assert int(b.work["error"].item()) == 0
