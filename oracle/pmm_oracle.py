@@ -568,7 +568,7 @@ def _bisect_decreasing(fprime, lo, hi, iters=200):
     return x
 
 
-MSTEP_ROUNDS = 8
+MSTEP_ROUNDS = 4
 
 
 def mstep_compat(counts, leaf_resp_total, R, M, d, nu, phi, branch_mask, fix_nu, fix_phi,
