@@ -173,6 +173,8 @@ def main():
     ap.add_argument("--ref-trees", type=int, default=16)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--trees", type=int, default=512,
+                    help="use the first N candidates (smaller cases for profiling)")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
@@ -192,6 +194,7 @@ def main():
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
     w = synth.workload_config(WORKLOAD, seed=args.seed + rank)
+    w.newicks = w.newicks[:args.trees]
     G = args.group_sites or tune.pick_group_sites(w)
     stream = torch.cuda.Stream(dev)
     with torch.cuda.stream(stream):
