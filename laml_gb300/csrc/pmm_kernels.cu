@@ -370,10 +370,6 @@ __device__ __forceinline__ double2 block_sum2(double a, double c, double2* sh) {
     return r;
 }
 
-__device__ __forceinline__ double inv_expm1(double x) {   // 1/(e^x - 1), x > 0
-    return 1.0 / expm1(x);
-}
-
 __device__ float4 branch_terms_of(double d, double nu, int compat) {
     const double nd = d * nu;
     const double p00 = exp(-d * (1.0 + nu));
@@ -383,43 +379,61 @@ __device__ float4 branch_terms_of(double d, double nu, int compat) {
     return make_float4((float)p00, (float)(e1md * pst), (float)pst, (float)e1mnd);
 }
 
-// d-stationarity of  -a d + b log(1-e^{-d}) + c log(1-e^{-nu d})  on [lo, hi]
-// (a decreasing function of d): safeguarded Newton in log d.
-__device__ double solve_branch(double a, double bb, double c, double nu, double d0, double lo,
-                               double hi) {
-    auto F = [&](double d, double* dF) {
-        const double em = expm1(d);
-        double f = -a, g = 0.0;
-        if (bb > 0.0) {
-            f += bb / em;
-            g -= bb * (em + 1.0) / (em * em);
-        }
-        if (c > 0.0) {
-            const double en = expm1(nu * d);
-            f += c * nu / en;
-            g -= c * nu * nu * (en + 1.0) / (en * en);
-        }
-        *dF = g * d;   // derivative in log d
-        return f;
-    };
-    double t;
-    if (F(lo, &t) <= 0.0) return lo;
-    if (F(hi, &t) >= 0.0) return hi;
-    double ulo = log(lo), uhi = log(hi);
-    double u = log(fmin(fmax(d0, lo), hi));
-    for (int it = 0; it < 100; ++it) {
-        double dF;
-        const double f = F(exp(u), &dF);
-        if (f > 0.0) ulo = u; else uhi = u;
-        double un = u - f / dF;
-        if (!(un > ulo && un < uhi)) un = 0.5 * (ulo + uhi);
-        if (fabs(un - u) <= 1e-14 * fmax(1.0, fabs(u)) || uhi - ulo < 1e-14) {
-            u = un;
-            break;
-        }
-        u = un;
+// Stationarity in d of  -a d + b log(1-e^{-d}) + c log(1-e^{-nu d})  (a
+// decreasing function of d).  With h(x) = x / (e^x - 1) and
+// k(x) = x / (1 - e^{-x}) (both finite on (0, inf)):
+//   F(d) = -a + (b h(d) + c h(nu d)) / d,
+//   dF/dlog d = -(b h(d) k(d) + c h(nu d) k(nu d)) / d.
+template <typename T>
+__device__ __forceinline__ T branch_F(T a, T b, T c, T nu, T d, T* dFdu) {
+    T s = T(0), ds = T(0);
+    if (b > T(0)) {
+        const T h = d / expm1(d), k = d / (-expm1(-d));
+        s += b * h;
+        ds += b * h * k;
     }
-    return exp(u);
+    if (c > T(0)) {
+        const T x = nu * d;
+        const T h = x / expm1(x), k = x / (-expm1(-x));
+        s += c * h;
+        ds += c * h * k;
+    }
+    *dFdu = -ds / d;
+    return -a + s / d;
+}
+
+// Safeguarded Newton in log d on [lo, hi]: FP32 iterations from the previous
+// value, then (``polish``) FP64 Newton steps inside the FP32 bracket.
+__device__ double solve_branch(double a, double bb, double c, double nu, double d0, double lo,
+                               double hi, bool polish) {
+    float t;
+    const float af = (float)a, bf = (float)bb, cf = (float)c, nf = (float)nu;
+    if (branch_F<float>(af, bf, cf, nf, (float)lo, &t) <= 0.f) return lo;
+    if (branch_F<float>(af, bf, cf, nf, (float)hi, &t) >= 0.f) return hi;
+    float ulo = logf((float)lo), uhi = logf((float)hi);
+    float u = logf((float)fmin(fmax(d0, lo), hi));
+    for (int it = 0; it < 60; ++it) {
+        float dF;
+        const float f = branch_F<float>(af, bf, cf, nf, expf(u), &dF);
+        if (f > 0.f) ulo = u; else uhi = u;
+        float un = u - f / dF;
+        if (!(un > ulo && un < uhi)) un = 0.5f * (ulo + uhi);
+        const bool done = fabsf(un - u) <= 2e-6f * fmaxf(1.f, fabsf(u)) || uhi - ulo < 1e-6f;
+        u = un;
+        if (done) break;
+    }
+    double ud = (double)u;
+    if (polish) {
+        const double dl = log(lo), dh = log(hi);
+        for (int it = 0; it < 2; ++it) {
+            double dF;
+            const double f = branch_F<double>(a, bb, c, nu, exp(ud), &dF);
+            const double un = ud - f / dF;
+            if (!(un > dl && un < dh) || !(fabs(un - ud) < 1e-4 * fmax(1.0, fabs(ud)))) break;
+            ud = un;
+        }
+    }
+    return fmin(fmax(exp(ud), lo), hi);
 }
 
 // ---------------------------------------------------------------------------
@@ -487,7 +501,7 @@ __device__ void mstep_tree(const laml_batch& b, int p, int rounds, double2* sh) 
             const double a = c0 * (1.0 + nu) + (c1 + c3) * nu;
             const double cs = use_s ? c2 + c4 : 0.0;
             const double d0 = __ldcg(b.nd_d + base + v);
-            b.nd_d[base + v] = solve_branch(a, c1, cs, nu, d0, dlo, dhi);
+            b.nd_d[base + v] = solve_branch(a, c1, cs, nu, d0, dlo, dhi, r == R - 1);
         }
         __syncthreads();
         if (!(fix & 1)) {
@@ -503,42 +517,59 @@ __device__ void mstep_tree(const laml_batch& b, int p, int rounds, double2* sh) 
             }
             double2 ac = block_sum2(A, Cs, sh);
             A = ac.x;
-            const double nlo = compat ? kCalcEps : 0.0, nhi = compat ? 1.0 - kCalcEps : 1.0;
-            auto G1 = [&](double x, double* g2) {
-                double f = 0.0, s2 = 0.0;
+            const double nlo = compat ? kCalcEps : 1e-30, nhi = compat ? 1.0 - kCalcEps : 1.0;
+            // G(nu) = -A + S1 / nu,  dG/dlog nu = -S2 / nu,  S1 = sum c h(nu d),
+            // S2 = sum c h k  (h, k as in branch_F)
+            auto sums = [&](double x, bool fp64) {
+                double s1 = 0.0, s2 = 0.0;
                 for (int v = threadIdx.x; v < N; v += blockDim.x) {
                     if (!compat && !__ldg(b.nd_mask + base + v)) continue;
                     const double* c = b.nd_cnt + (int64_t)(base + v) * 6;
                     const double cc = __ldcg(c + 2) + __ldcg(c + 4);
                     if (cc <= 0.0) continue;
                     const double d = __ldcg(b.nd_d + base + v);
-                    const double en = expm1(x * d);
-                    f += cc * d / en;
-                    s2 -= cc * d * d * (en + 1.0) / (en * en);
+                    if (fp64) {
+                        const double y = x * d, h = y / expm1(y), k = y / (-expm1(-y));
+                        s1 += cc * h;
+                        s2 += cc * h * k;
+                    } else {
+                        const float y = (float)(x * d), h = y / expm1f(y), k = y / (-expm1f(-y));
+                        s1 += cc * (double)h;
+                        s2 += cc * (double)(h * k);
+                    }
                 }
-                double2 t = block_sum2(f, s2, sh);
-                *g2 = t.y;
-                return t.x - A;
+                return block_sum2(s1, s2, sh);
             };
-            double g2;
             if (ac.y <= 0.0) {
-                nu = nlo;
-            } else if (G1(nhi, &g2) >= 0.0) {
+                nu = compat ? nlo : 0.0;
+            } else if (-A * nhi + sums(nhi, false).x >= 0.0) {
                 nu = nhi;
-            } else if (compat && G1(nlo, &g2) <= 0.0) {
+            } else if (-A * nlo + sums(nlo, false).x <= 0.0) {
                 nu = nlo;
             } else {
-                double a = compat ? nlo : 1e-300, c = nhi;
-                double x = fmin(fmax(nu, compat ? nlo : 1e-12), nhi);
-                for (int it = 0; it < 200; ++it) {
-                    const double f = G1(x, &g2);
-                    if (f > 0.0) a = x; else c = x;
-                    double xn = x - f / g2;
-                    if (!(xn > a && xn < c)) xn = (a > 0.0 && c / a > 4.0) ? sqrt(a * c) : 0.5 * (a + c);
-                    if (fabs(xn - x) <= 1e-15 * x || c - a <= 1e-15 * c) { x = xn; break; }
-                    x = xn;
+                double wlo = log(nlo), whi = log(nhi);
+                double w = log(fmin(fmax(nu, nlo), nhi));
+                for (int it = 0; it < 100; ++it) {
+                    const double x = exp(w);
+                    const double2 S = sums(x, false);
+                    const double H = -A * x + S.x;      // same sign as G
+                    if (H > 0.0) wlo = w; else whi = w;
+                    double wn = w + H / S.y;
+                    if (!(wn > wlo && wn < whi)) wn = 0.5 * (wlo + whi);
+                    const bool done = fabs(wn - w) <= 1e-6 * fmax(1.0, fabs(w)) || whi - wlo < 1e-6;
+                    w = wn;
+                    if (done) break;
                 }
-                nu = x;
+                if (r == R - 1) {   // FP64 Newton polish
+                    for (int it = 0; it < 2; ++it) {
+                        const double x = exp(w);
+                        const double2 S = sums(x, true);
+                        const double wn = w + (-A * x + S.x) / S.y;
+                        if (!(wn > log(nlo) && wn < log(nhi)) || !(fabs(wn - w) < 1e-3)) break;
+                        w = wn;
+                    }
+                }
+                nu = exp(w);
             }
         }
         __syncthreads();
@@ -679,7 +710,7 @@ __global__ void k_branch_terms(laml_batch b) {
 }
 
 template <int G>
-__global__ void __launch_bounds__(kBlock) k_em_persistent(laml_batch b, int iters, int rounds,
+__global__ void __launch_bounds__(kBlock, 3) k_em_persistent(laml_batch b, int iters, int rounds,
                                                            double rel_tol, int max_iters) {
     __shared__ double2 sh[kBlock / 32];
     const int gwarp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
