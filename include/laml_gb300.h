@@ -175,6 +175,7 @@ typedef struct laml_batch {
     const uint8_t* nd_mask;        /* 1 = branch length is optimised */
     float* nd_bt;                  /* [4 * n_nodes] P00, Pmut, Pstay, Psil */
     double* nd_cnt;                /* [6 * n_nodes] expected counts summed over sites */
+    float* nd_stage;               /* [5 * n_nodes] M-step scratch (trees over 2048 nodes) */
     /* work buffers */
     float *in_part, *out_part, *in_dot;
     int32_t *in_x, *in_h, *out_x, *out_h;

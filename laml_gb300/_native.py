@@ -7,7 +7,8 @@ import ctypes as C
 import os
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-LIB_PATH = os.path.join(HERE, "_lib", "liblaml_gb300.so")
+# LAML_GB300_LIB selects another build of the library (tile-setting variants)
+LIB_PATH = os.environ.get("LAML_GB300_LIB") or os.path.join(HERE, "_lib", "liblaml_gb300.so")
 
 i32, i64, u8, u32, f32, f64 = C.c_int32, C.c_int64, C.c_uint8, C.c_uint32, C.c_float, C.c_double
 P = C.POINTER
@@ -69,7 +70,7 @@ BATCH_FIELDS = [
     ("tr_llh_prev", vp), ("tr_iter", vp), ("tr_status", vp),
     ("nd_tree", vp), ("nd_c0", vp), ("nd_c1", vp), ("nd_parent", vp), ("nd_sib", vp),
     ("nd_leafrow", vp), ("nd_prow", vp), ("nd_srow", vp), ("nd_d", vp), ("nd_d_prev", vp),
-    ("nd_mask", vp), ("nd_bt", vp), ("nd_cnt", vp),
+    ("nd_mask", vp), ("nd_bt", vp), ("nd_cnt", vp), ("nd_stage", vp),
     ("in_part", vp), ("out_part", vp), ("in_dot", vp), ("in_x", vp), ("in_h", vp),
     ("out_x", vp), ("out_h", vp), ("llh_site", vp), ("root_lr", vp), ("root_x", vp),
     ("cnt_part", vp), ("post0", vp), ("post1", vp),

@@ -36,23 +36,34 @@ def _compile(src, obj, extra):
     return obj
 
 
-def build(verbose=False, extra=()):
-    os.makedirs(OUT_DIR, exist_ok=True)
-    objs = [os.path.join(OUT_DIR, os.path.splitext(s)[0] + ".o") for s in SOURCES]
+def build(verbose=False, extra=(), out=None):
+    """Compile and link; ``extra`` are additional nvcc flags (e.g. -D tile
+    settings) and ``out`` an alternative library path for such variants."""
+    lib = out or LIB
+    os.makedirs(os.path.dirname(lib), exist_ok=True)
+    tag = os.path.splitext(os.path.basename(lib))[0]
+    objs = [os.path.join(os.path.dirname(lib), f"{tag}_{os.path.splitext(s)[0]}.o")
+            for s in SOURCES]
     with cf.ThreadPoolExecutor(max_workers=len(SOURCES)) as ex:
         list(ex.map(lambda a: _compile(a[0], a[1], list(extra)), zip(SOURCES, objs)))
-    tmp = LIB + ".tmp"
+    tmp = lib + ".tmp"
     cmd = [nvcc(), "-shared", *ARCH, "-o", tmp, *objs, "-lcudart"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
-    os.replace(tmp, LIB)
+    os.replace(tmp, lib)
     for o in objs:
         os.remove(o)
     if verbose:
-        print("built", LIB)
-    return LIB
+        print("built", lib)
+    return lib
 
 
 if __name__ == "__main__":
-    build(verbose=True, extra=sys.argv[1:])
+    args = sys.argv[1:]
+    out = None
+    if "-o" in args:
+        i = args.index("-o")
+        out = args[i + 1]
+        args = args[:i] + args[i + 2:]
+    build(verbose=True, extra=args, out=out)

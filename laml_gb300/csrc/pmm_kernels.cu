@@ -50,6 +50,14 @@ constexpr double kEpsS = 1e-6, kEpsNu = 1e-5;   // EM_solver.Mstep defaults (EM_
 constexpr double kLn2 = 0.69314718055994530942;
 constexpr int kBlock = 256;
 constexpr unsigned kFull = 0xffffffffu;
+#ifndef LAML_CHUNK
+#define LAML_CHUNK 4
+#endif
+constexpr int kChunk = LAML_CHUNK;   // states loaded ahead per step of a state loop
+#ifndef LAML_MINB
+#define LAML_MINB 3
+#endif
+constexpr int kMstepStage = 2048;    // branches of a tree staged in shared memory by the M-step
 
 // ---------------------------------------------------------------------------
 // small helpers
@@ -180,8 +188,25 @@ __device__ void inside_item(const laml_batch& b, int u, int g, int lane, bool re
     __stcg(row, s0);
     __stcg(row + G, ss);
     float mx = fmaxf(s0, ss), dot = 0.f;
-#pragma unroll 4
-    for (int j = 2; j < s.C; ++j) {
+    int j = 2;
+    // CH states per step: every load of a step is issued before its stores
+    for (; j + kChunk <= s.C; j += kChunk) {
+        float av[kChunk], aw[kChunk], qv[kChunk];
+#pragma unroll
+        for (int k = 0; k < kChunk; ++k) {
+            av[k] = child_val<G>(cv, j + k);
+            aw[k] = child_val<G>(cw, j + k);
+            qv[k] = __ldg(s.qrow + (j + k) * G);
+        }
+#pragma unroll
+        for (int k = 0; k < kChunk; ++k) {
+            const float x = fmaf(bv.z, av[k], kv) * fmaf(bw.z, aw[k], kw);
+            __stcg(row + (j + k) * G, x);
+            dot = fmaf(qv[k], x, dot);
+            mx = fmaxf(mx, x);
+        }
+    }
+    for (; j < s.C; ++j) {
         const float av = child_val<G>(cv, j), aw = child_val<G>(cw, j);
         const float x = fmaf(bv.z, av, kv) * fmaf(bw.z, aw, kw);
         __stcg(row + j * G, x);
@@ -248,8 +273,29 @@ __device__ void outside_item(const laml_batch& b, int v, int g, int lane, bool a
             const bool write = (mode == 0) && cv.row != nullptr;
             if (write) orow = b.out_part + __ldg(b.nd_prow + v) + s.goff + lane;
             const float px = bv.y * x0;
-#pragma unroll 4
-            for (int j = 2; j < s.C; ++j) {
+            int j = 2;
+            for (; j + kChunk <= s.C; j += kChunk) {
+                float ou[kChunk], aw[kChunk], av[kChunk], qv[kChunk];
+#pragma unroll
+                for (int k = 0; k < kChunk; ++k) {
+                    ou[k] = __ldcg(urow + (j + k) * G);
+                    aw[k] = child_val<G>(cw, j + k);
+                    av[k] = child_val<G>(cv, j + k);
+                    qv[k] = __ldg(s.qrow + (j + k) * G);
+                }
+#pragma unroll
+                for (int k = 0; k < kChunk; ++k) {
+                    const float xa = ou[k] * fo * fmaf(bw.z, aw[k], kw);
+                    sumx += xa;
+                    dotxv = fmaf(xa, av[k], dotxv);
+                    if (write) {
+                        const float o = fmaf(px, qv[k], bv.z * xa);
+                        __stcg(orow + (j + k) * G, o);
+                        mx = fmaxf(mx, o);
+                    }
+                }
+            }
+            for (; j < s.C; ++j) {
                 const float ou = __ldcg(urow + j * G) * fo;
                 const float xa = ou * fmaf(bw.z, child_val<G>(cw, j), kw);
                 sumx += xa;
@@ -371,12 +417,13 @@ __device__ __forceinline__ double2 block_sum2(double a, double c, double2* sh) {
 }
 
 __device__ float4 branch_terms_of(double d, double nu, int compat) {
-    const double nd = d * nu;
-    const double p00 = exp(-d * (1.0 + nu));
-    const double e1md = (compat && d < kEPSd) ? kEPSd : -expm1(-d);
-    const double e1mnd = (compat && nd < kEPSd) ? kEPSd : -expm1(-nd);
-    const double pst = exp(-nd);
-    return make_float4((float)p00, (float)(e1md * pst), (float)pst, (float)e1mnd);
+    // FP32 is the storage precision of the terms: compute them in FP32
+    const float df = (float)d, nf = (float)nu, nd = df * nf;
+    const float p00 = expf(-df * (1.f + nf));
+    const float e1md = (compat && d < kEPSd) ? kEPS : -expm1f(-df);
+    const float e1mnd = (compat && (double)d * nu < kEPSd) ? kEPS : -expm1f(-nd);
+    const float pst = expf(-nd);
+    return make_float4(p00, e1md * pst, pst, e1mnd);
 }
 
 // Stationarity in d of  -a d + b log(1-e^{-d}) + c log(1-e^{-nu d})  (a
@@ -386,17 +433,18 @@ __device__ float4 branch_terms_of(double d, double nu, int compat) {
 //   dF/dlog d = -(b h(d) k(d) + c h(nu d) k(nu d)) / d.
 template <typename T>
 __device__ __forceinline__ T branch_F(T a, T b, T c, T nu, T d, T* dFdu) {
+    // k(x) = x e^x / (e^x - 1) = h(x) + x
     T s = T(0), ds = T(0);
     if (b > T(0)) {
-        const T h = d / expm1(d), k = d / (-expm1(-d));
+        const T h = d / expm1(d);
         s += b * h;
-        ds += b * h * k;
+        ds += b * h * (h + d);
     }
     if (c > T(0)) {
         const T x = nu * d;
-        const T h = x / expm1(x), k = x / (-expm1(-x));
+        const T h = x / expm1(x);
         s += c * h;
-        ds += c * h * k;
+        ds += c * h * (h + x);
     }
     *dFdu = -ds / d;
     return -a + s / d;
@@ -437,9 +485,13 @@ __device__ double solve_branch(double a, double bb, double c, double nu, double 
 }
 
 // ---------------------------------------------------------------------------
-// M-step of one tree (one thread block)
+// M-step of one tree (one thread block).  Per-branch data used by every
+// round -- {C00, C00+C0a+Caa, C0a, C0s+Cas} and d -- is staged in shared
+// memory (global scratch for trees above kMstepStage nodes); the final round
+// polishes d and nu with FP64 Newton steps on the FP64 counts.
 // ---------------------------------------------------------------------------
-__device__ void mstep_tree(const laml_batch& b, int p, int rounds, double2* sh) {
+__device__ void mstep_tree(const laml_batch& b, int p, int rounds, double2* sh, float4* s_cnt,
+                           float* s_d) {
     if (__ldcg(b.tr_status + p) != LAML_TREE_ACTIVE) return;
     const int N = __ldg(b.tr_nodes + p), n = __ldg(b.tr_leaves + p), base = __ldg(b.tr_node_base + p);
     const int ds = __ldg(b.tr_ds + p), NG = __ldg(b.ds_groups + ds), K = __ldg(b.ds_sites + ds);
@@ -447,28 +499,41 @@ __device__ void mstep_tree(const laml_batch& b, int p, int rounds, double2* sh) 
     const bool compat = b.compat != 0;
     const uint8_t fix = __ldg(b.tr_fix + p);
     double nu = __ldcg(b.tr_nu + p), phi = __ldcg(b.tr_phi + p);
-    // 1. counts summed over site groups, d saved
+    float4* C4 = s_cnt;
+    float* Dd = s_d;
+    if (N > kMstepStage) {
+        C4 = reinterpret_cast<float4*>(b.nd_stage) + base;
+        Dd = b.nd_stage + 4 * b.n_nodes + base;
+    }
+    // 1. counts summed over site groups (EM_solver.py:342-345 normalisation in
+    //    the exact model), d saved
     double lr = 0.0;
     for (int v = threadIdx.x; v < N; v += blockDim.x) {
         double c[7] = {0, 0, 0, 0, 0, 0, 0};
-        const float* src = b.cnt_part + cb + (int64_t)v * NG * 8;
+        const float4* src = reinterpret_cast<const float4*>(b.cnt_part + cb + (int64_t)v * NG * 8);
         for (int g = 0; g < NG; ++g) {
-            const float4 a = __ldcg(reinterpret_cast<const float4*>(src + g * 8));
-            const float4 z = __ldcg(reinterpret_cast<const float4*>(src + g * 8) + 1);
-            c[0] += a.x; c[1] += a.y; c[2] += a.z; c[3] += a.w;
+            const float4 x = __ldcg(src + 2 * g), z = __ldcg(src + 2 * g + 1);
+            c[0] += x.x; c[1] += x.y; c[2] += x.z; c[3] += x.w;
             c[4] += z.x; c[5] += z.y; c[6] += z.z;
         }
-        if (!compat) {   // EM_solver.py:342-345: floor at eps_s, normalise to numsites
+        if (!compat) {
             double t = 0.0;
+#pragma unroll
             for (int k = 0; k < 5; ++k) { c[k] = fmax(c[k], kEpsS); t += c[k]; }
+#pragma unroll
             for (int k = 0; k < 5; ++k) c[k] = c[k] / t * K;
         }
         double* dst = b.nd_cnt + (int64_t)(base + v) * 6;
-        for (int k = 0; k < 6; ++k) dst[k] = c[k];
+#pragma unroll
+        for (int k = 0; k < 6; ++k) __stcg(dst + k, c[k]);
+        C4[v] = make_float4((float)c[0], (float)(c[0] + c[1] + c[3]), (float)c[1],
+                            (float)(c[2] + c[4]));
+        const double d = __ldcg(b.nd_d + base + v);
+        __stcg(b.nd_d_prev + base + v, d);
+        Dd[v] = (float)d;
         lr += c[6];
-        b.nd_d_prev[base + v] = __ldcg(b.nd_d + base + v);
     }
-    const double LR = block_sum2(lr, 0.0, sh).x;
+    const double LR = block_sum2(lr, 0.0, sh).x;   // also orders the staging writes
     if (threadIdx.x == 0) {
         b.tr_prev[2 * p] = nu;
         b.tr_prev[2 * p + 1] = phi;
@@ -487,21 +552,31 @@ __device__ void mstep_tree(const laml_batch& b, int p, int rounds, double2* sh) 
             if (fabs(phi) < 1.0 / total) phi = 0.0;
         }
     }
-    __syncthreads();
-    // 3. coordinate rounds: d | nu, then nu | d
+    // 3. coordinate rounds: d | nu (per branch), then nu | d
     const int R = compat ? rounds : 1;
     const double dlo = compat ? kCalcEps : kDmin, dhi = compat ? 1.0 / kCalcEps : kDmax;
     for (int r = 0; r < R; ++r) {
+        const bool last = r == R - 1;
         const bool use_s = compat || nu > kEpsNu;
         for (int v = threadIdx.x; v < N; v += blockDim.x) {
             if (!__ldg(b.nd_mask + base + v)) continue;
-            const double* c = b.nd_cnt + (int64_t)(base + v) * 6;
-            const double c0 = __ldcg(c), c1 = __ldcg(c + 1), c2 = __ldcg(c + 2),
-                         c3 = __ldcg(c + 3), c4 = __ldcg(c + 4);
-            const double a = c0 * (1.0 + nu) + (c1 + c3) * nu;
-            const double cs = use_s ? c2 + c4 : 0.0;
-            const double d0 = __ldcg(b.nd_d + base + v);
-            b.nd_d[base + v] = solve_branch(a, c1, cs, nu, d0, dlo, dhi, r == R - 1);
+            double a, bb, cs;
+            if (last) {   // the FP64 counts for the polished solve
+                const double* c = b.nd_cnt + (int64_t)(base + v) * 6;
+                const double c0 = __ldcg(c), c1 = __ldcg(c + 1), c2 = __ldcg(c + 2),
+                             c3 = __ldcg(c + 3), c4 = __ldcg(c + 4);
+                a = c0 + nu * (c0 + c1 + c3);
+                bb = c1;
+                cs = use_s ? c2 + c4 : 0.0;
+            } else {
+                const float4 q = C4[v];
+                a = (double)q.x + nu * (double)q.y;
+                bb = q.z;
+                cs = use_s ? (double)q.w : 0.0;
+            }
+            const double dn = solve_branch(a, bb, cs, nu, (double)Dd[v], dlo, dhi, last);
+            Dd[v] = (float)dn;
+            if (last) __stcg(b.nd_d + base + v, dn);
         }
         __syncthreads();
         if (!(fix & 1)) {
@@ -510,12 +585,11 @@ __device__ void mstep_tree(const laml_batch& b, int p, int rounds, double2* sh) 
             double A = 0.0, Cs = 0.0;
             for (int v = threadIdx.x; v < N; v += blockDim.x) {
                 if (!compat && !__ldg(b.nd_mask + base + v)) continue;
-                const double* c = b.nd_cnt + (int64_t)(base + v) * 6;
-                const double d = __ldcg(b.nd_d + base + v);
-                A += (__ldcg(c) + __ldcg(c + 1) + __ldcg(c + 3)) * d;
-                Cs += __ldcg(c + 2) + __ldcg(c + 4);
+                const float4 q = C4[v];
+                A += (double)q.y * (double)Dd[v];
+                Cs += q.w;
             }
-            double2 ac = block_sum2(A, Cs, sh);
+            const double2 ac = block_sum2(A, Cs, sh);
             A = ac.x;
             const double nlo = compat ? kCalcEps : 1e-30, nhi = compat ? 1.0 - kCalcEps : 1.0;
             // G(nu) = -A + S1 / nu,  dG/dlog nu = -S2 / nu,  S1 = sum c h(nu d),
@@ -524,18 +598,19 @@ __device__ void mstep_tree(const laml_batch& b, int p, int rounds, double2* sh) 
                 double s1 = 0.0, s2 = 0.0;
                 for (int v = threadIdx.x; v < N; v += blockDim.x) {
                     if (!compat && !__ldg(b.nd_mask + base + v)) continue;
-                    const double* c = b.nd_cnt + (int64_t)(base + v) * 6;
-                    const double cc = __ldcg(c + 2) + __ldcg(c + 4);
-                    if (cc <= 0.0) continue;
-                    const double d = __ldcg(b.nd_d + base + v);
                     if (fp64) {
-                        const double y = x * d, h = y / expm1(y), k = y / (-expm1(-y));
+                        const double* c = b.nd_cnt + (int64_t)(base + v) * 6;
+                        const double cc = __ldcg(c + 2) + __ldcg(c + 4);
+                        if (cc <= 0.0) continue;
+                        const double y = x * __ldcg(b.nd_d + base + v), h = y / expm1(y);
                         s1 += cc * h;
-                        s2 += cc * h * k;
+                        s2 += cc * h * (h + y);
                     } else {
-                        const float y = (float)(x * d), h = y / expm1f(y), k = y / (-expm1f(-y));
-                        s1 += cc * (double)h;
-                        s2 += cc * (double)(h * k);
+                        const float cc = C4[v].w;
+                        if (cc <= 0.f) continue;
+                        const float y = (float)x * Dd[v], h = y / expm1f(y);
+                        s1 += (double)(cc * h);
+                        s2 += (double)(cc * h * (h + y));
                     }
                 }
                 return block_sum2(s1, s2, sh);
@@ -560,11 +635,18 @@ __device__ void mstep_tree(const laml_batch& b, int p, int rounds, double2* sh) 
                     w = wn;
                     if (done) break;
                 }
-                if (r == R - 1) {   // FP64 Newton polish
+                if (last) {   // FP64 Newton polish
+                    double A64 = 0.0;
+                    for (int v = threadIdx.x; v < N; v += blockDim.x) {
+                        if (!compat && !__ldg(b.nd_mask + base + v)) continue;
+                        const double* c = b.nd_cnt + (int64_t)(base + v) * 6;
+                        A64 += (__ldcg(c) + __ldcg(c + 1) + __ldcg(c + 3)) * __ldcg(b.nd_d + base + v);
+                    }
+                    A64 = block_sum2(A64, 0.0, sh).x;
                     for (int it = 0; it < 2; ++it) {
                         const double x = exp(w);
                         const double2 S = sums(x, true);
-                        const double wn = w + (-A * x + S.x) / S.y;
+                        const double wn = w + (-A64 * x + S.x) / S.y;
                         if (!(wn > log(nlo) && wn < log(nhi)) || !(fabs(wn - w) < 1e-3)) break;
                         w = wn;
                     }
@@ -684,7 +766,7 @@ __device__ __forceinline__ void for_items(const laml_batch& b, const int32_t* it
 }
 
 template <int G>
-__global__ void __launch_bounds__(kBlock) k_items(laml_batch b, const int32_t* items, int64_t n,
+__global__ void __launch_bounds__(kBlock, LAML_MINB) k_items(laml_batch b, const int32_t* items, int64_t n,
                                                    int kind, int want_post, int respect_status) {
     const int gwarp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int nwarps = (gridDim.x * blockDim.x) >> 5;
@@ -693,7 +775,9 @@ __global__ void __launch_bounds__(kBlock) k_items(laml_batch b, const int32_t* i
 
 __global__ void __launch_bounds__(kBlock) k_mstep(laml_batch b, int rounds) {
     __shared__ double2 sh[kBlock / 32];
-    for (int p = blockIdx.x; p < b.n_trees; p += gridDim.x) mstep_tree(b, p, rounds, sh);
+    __shared__ float4 s_cnt[kMstepStage];
+    __shared__ float s_d[kMstepStage];
+    for (int p = blockIdx.x; p < b.n_trees; p += gridDim.x) mstep_tree(b, p, rounds, sh, s_cnt, s_d);
 }
 
 __global__ void k_tree_llh(laml_batch b, int mode, double rel_tol, int max_iters) {
@@ -710,9 +794,11 @@ __global__ void k_branch_terms(laml_batch b) {
 }
 
 template <int G>
-__global__ void __launch_bounds__(kBlock, 3) k_em_persistent(laml_batch b, int iters, int rounds,
+__global__ void __launch_bounds__(kBlock, LAML_MINB) k_em_persistent(laml_batch b, int iters, int rounds,
                                                            double rel_tol, int max_iters) {
     __shared__ double2 sh[kBlock / 32];
+    __shared__ float4 s_cnt[kMstepStage];
+    __shared__ float s_d[kMstepStage];
     const int gwarp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int nwarps = (gridDim.x * blockDim.x) >> 5;
     unsigned gen = 0;
@@ -726,7 +812,7 @@ __global__ void __launch_bounds__(kBlock, 3) k_em_persistent(laml_batch b, int i
         }
         for_items<G>(b, b.root_items, b.n_root_items, gwarp, nwarps, 3, false, true);
         if (!grid_barrier(b, gen)) return;
-        for (int p = blockIdx.x; p < b.n_trees; p += gridDim.x) mstep_tree(b, p, rounds, sh);
+        for (int p = blockIdx.x; p < b.n_trees; p += gridDim.x) mstep_tree(b, p, rounds, sh, s_cnt, s_d);
         if (!grid_barrier(b, gen)) return;
         for (int l = 0; l < b.n_in_levels; ++l) {
             const int64_t o = b.in_level_off[l], e = b.in_level_off[l + 1];

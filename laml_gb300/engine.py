@@ -153,6 +153,7 @@ class DeviceBatch:
             "tr_iter": torch.zeros(T, dtype=i32, device=dev),
             "tr_status": torch.zeros(T, dtype=i32, device=dev),
             "nd_d_prev": e(nn, f64), "nd_bt": e(4 * nn, f32), "nd_cnt": e(6 * nn, f64),
+            "nd_stage": e(5 * nn, f32),
             "in_part": e(sizes["part_floats"], f32), "out_part": e(sizes["part_floats"], f32),
             "in_dot": e(sizes["scalar_len"], f32), "in_x": e(sizes["scalar_len"], i32),
             "in_h": e(sizes["scalar_len"], i32), "out_x": e(sizes["scalar_len"], i32),
