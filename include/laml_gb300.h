@@ -218,11 +218,15 @@ int laml_inside(const laml_batch* b, int32_t update_em, void* stream);
  * Estep_posterior (laml_libs/EM_solver.py:143-300). */
 int laml_outside(const laml_batch* b, int32_t want_post, void* stream);
 
+/* M-step flags: FP64 Newton polish of the final branch-length and nu solves
+ * (the solves otherwise run FP32 Newton iterations with FP64 accumulation). */
+#define LAML_MSTEP_FP64_POLISH 1
+
 /* M-step of every active tree: compat maximises the fastEM objective
  * (fast_em/laml.py:62-78) by `rounds` coordinate-ascent rounds; exact follows
  * EM_solver.Mstep (laml_libs/EM_solver.py:307-459) with bounded 1-D solves.
  * Writes nd_d (old values to nd_d_prev), tr_nu, tr_phi and the branch terms. */
-int laml_mstep(const laml_batch* b, int32_t rounds, void* stream);
+int laml_mstep(const laml_batch* b, int32_t rounds, int32_t flags, void* stream);
 
 /* `iters` fused EM iterations (outside+counts -> M-step -> inside ->
  * convergence test per tree) in ONE persistent cooperative launch with a
@@ -232,12 +236,12 @@ int laml_mstep(const laml_batch* b, int32_t rounds, void* stream);
  * once before the first call.  Replaces the host EM loop of
  * fast_em/laml.py:112-194 / EM_solver.EM_optimization. */
 int laml_em_run(const laml_batch* b, int32_t iters, int32_t rounds, double rel_tol,
-                int32_t max_iters, void* stream);
+                int32_t max_iters, int32_t flags, void* stream);
 
 /* Same iterations as laml_em_run, one kernel launch per tree level (no grid
  * barrier); the reference-shaped "plain" path. */
 int laml_em_run_levels(const laml_batch* b, int32_t iters, int32_t rounds, double rel_tol,
-                       int32_t max_iters, void* stream);
+                       int32_t max_iters, int32_t flags, void* stream);
 
 /* Message of the calling thread's last error ("" if none). */
 const char* laml_last_error(void);

@@ -18,6 +18,7 @@ LAML_OK = 0
 ERRORS = {-1: "LAML_ERR_ARG", -2: "LAML_ERR_CUDA", -3: "LAML_ERR_PARSE", -4: "LAML_ERR_PRIOR",
           -5: "LAML_ERR_TIMEOUT", -6: "LAML_ERR_NOT_BINARY", -7: "LAML_ERR_LEAF"}
 TREE_ACTIVE, TREE_CONVERGED, TREE_NAN, TREE_MAXITER = 0, 1, 2, 3
+MSTEP_FP64_POLISH = 1
 
 
 class LamlError(RuntimeError):
@@ -95,9 +96,9 @@ EXPORTS = {
     "laml_branch_terms": (i32, [P(Batch), vp]),
     "laml_inside": (i32, [P(Batch), i32, vp]),
     "laml_outside": (i32, [P(Batch), i32, vp]),
-    "laml_mstep": (i32, [P(Batch), i32, vp]),
-    "laml_em_run": (i32, [P(Batch), i32, i32, f64, i32, vp]),
-    "laml_em_run_levels": (i32, [P(Batch), i32, i32, f64, i32, vp]),
+    "laml_mstep": (i32, [P(Batch), i32, i32, vp]),
+    "laml_em_run": (i32, [P(Batch), i32, i32, f64, i32, i32, vp]),
+    "laml_em_run_levels": (i32, [P(Batch), i32, i32, f64, i32, i32, vp]),
     "laml_last_error": (C.c_char_p, []),
 }
 

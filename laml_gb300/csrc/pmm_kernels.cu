@@ -55,7 +55,7 @@ constexpr unsigned kFull = 0xffffffffu;
 #endif
 constexpr int kChunk = LAML_CHUNK;   // states loaded ahead per step of a state loop
 #ifndef LAML_MINB
-#define LAML_MINB 3
+#define LAML_MINB 4
 #endif
 constexpr int kMstepStage = 2048;    // branches of a tree staged in shared memory by the M-step
 
@@ -470,8 +470,9 @@ __device__ double solve_branch(double a, double bb, double c, double nu, double 
         u = un;
         if (done) break;
     }
+    if (!polish) return fmin(fmax((double)expf(u), lo), hi);
     double ud = (double)u;
-    if (polish) {
+    {
         const double dl = log(lo), dh = log(hi);
         for (int it = 0; it < 2; ++it) {
             double dF;
@@ -491,7 +492,7 @@ __device__ double solve_branch(double a, double bb, double c, double nu, double 
 // polishes d and nu with FP64 Newton steps on the FP64 counts.
 // ---------------------------------------------------------------------------
 __device__ void mstep_tree(const laml_batch& b, int p, int rounds, double2* sh, float4* s_cnt,
-                           float* s_d) {
+                           float* s_d, bool polish) {
     if (__ldcg(b.tr_status + p) != LAML_TREE_ACTIVE) return;
     const int N = __ldg(b.tr_nodes + p), n = __ldg(b.tr_leaves + p), base = __ldg(b.tr_node_base + p);
     const int ds = __ldg(b.tr_ds + p), NG = __ldg(b.ds_groups + ds), K = __ldg(b.ds_sites + ds);
@@ -561,7 +562,7 @@ __device__ void mstep_tree(const laml_batch& b, int p, int rounds, double2* sh, 
         for (int v = threadIdx.x; v < N; v += blockDim.x) {
             if (!__ldg(b.nd_mask + base + v)) continue;
             double a, bb, cs;
-            if (last) {   // the FP64 counts for the polished solve
+            if (last && polish) {   // the FP64 counts for the polished solve
                 const double* c = b.nd_cnt + (int64_t)(base + v) * 6;
                 const double c0 = __ldcg(c), c1 = __ldcg(c + 1), c2 = __ldcg(c + 2),
                              c3 = __ldcg(c + 3), c4 = __ldcg(c + 4);
@@ -574,7 +575,7 @@ __device__ void mstep_tree(const laml_batch& b, int p, int rounds, double2* sh, 
                 bb = q.z;
                 cs = use_s ? (double)q.w : 0.0;
             }
-            const double dn = solve_branch(a, bb, cs, nu, (double)Dd[v], dlo, dhi, last);
+            const double dn = solve_branch(a, bb, cs, nu, (double)Dd[v], dlo, dhi, last && polish);
             Dd[v] = (float)dn;
             if (last) __stcg(b.nd_d + base + v, dn);
         }
@@ -622,20 +623,21 @@ __device__ void mstep_tree(const laml_batch& b, int p, int rounds, double2* sh, 
             } else if (-A * nlo + sums(nlo, false).x <= 0.0) {
                 nu = nlo;
             } else {
-                double wlo = log(nlo), whi = log(nhi);
-                double w = log(fmin(fmax(nu, nlo), nhi));
+                float wlo = logf((float)nlo), whi = logf((float)nhi);
+                float w = logf((float)fmin(fmax(nu, nlo), nhi));
                 for (int it = 0; it < 100; ++it) {
-                    const double x = exp(w);
+                    const float x = expf(w);
                     const double2 S = sums(x, false);
-                    const double H = -A * x + S.x;      // same sign as G
-                    if (H > 0.0) wlo = w; else whi = w;
-                    double wn = w + H / S.y;
-                    if (!(wn > wlo && wn < whi)) wn = 0.5 * (wlo + whi);
-                    const bool done = fabs(wn - w) <= 1e-6 * fmax(1.0, fabs(w)) || whi - wlo < 1e-6;
+                    const float H = (float)(-A * x + S.x);   // same sign as G
+                    if (H > 0.f) wlo = w; else whi = w;
+                    float wn = w + H / (float)S.y;
+                    if (!(wn > wlo && wn < whi)) wn = 0.5f * (wlo + whi);
+                    const bool done = fabsf(wn - w) <= 1e-6f * fmaxf(1.f, fabsf(w)) || whi - wlo < 1e-6f;
                     w = wn;
                     if (done) break;
                 }
-                if (last) {   // FP64 Newton polish
+                double wd = (double)w;
+                if (last && polish) {   // FP64 Newton polish
                     double A64 = 0.0;
                     for (int v = threadIdx.x; v < N; v += blockDim.x) {
                         if (!compat && !__ldg(b.nd_mask + base + v)) continue;
@@ -644,14 +646,14 @@ __device__ void mstep_tree(const laml_batch& b, int p, int rounds, double2* sh, 
                     }
                     A64 = block_sum2(A64, 0.0, sh).x;
                     for (int it = 0; it < 2; ++it) {
-                        const double x = exp(w);
+                        const double x = exp(wd);
                         const double2 S = sums(x, true);
-                        const double wn = w + (-A64 * x + S.x) / S.y;
-                        if (!(wn > log(nlo) && wn < log(nhi)) || !(fabs(wn - w) < 1e-3)) break;
-                        w = wn;
+                        const double wn = wd + (-A64 * x + S.x) / S.y;
+                        if (!(wn > log(nlo) && wn < log(nhi)) || !(fabs(wn - wd) < 1e-3)) break;
+                        wd = wn;
                     }
                 }
-                nu = exp(w);
+                nu = fmin(fmax(polish ? exp(wd) : (double)expf(w), nlo), nhi);
             }
         }
         __syncthreads();
@@ -708,6 +710,12 @@ __device__ __forceinline__ unsigned long long gtimer() {
     return t;
 }
 
+__device__ __forceinline__ unsigned ld_acquire(const uint32_t* p) {
+    unsigned v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
 __device__ bool grid_barrier(const laml_batch& b, unsigned& gen) {
     __syncthreads();
     __shared__ int s_ok;
@@ -719,7 +727,7 @@ __device__ bool grid_barrier(const laml_batch& b, unsigned& gen) {
             atomicExch(b.barrier + 1, gen + 1);
         } else {
             const unsigned long long t0 = gtimer();
-            while (atomicAdd(b.barrier + 1, 0u) <= gen) {
+            while (ld_acquire(b.barrier + 1) <= gen) {
                 if (*(volatile int*)b.error != 0) { ok = 0; break; }
                 if (gtimer() - t0 > 2000000000ull) {   // 2 s
                     atomicCAS(b.error, 0, LAML_ERR_TIMEOUT);
@@ -773,11 +781,12 @@ __global__ void __launch_bounds__(kBlock, LAML_MINB) k_items(laml_batch b, const
     for_items<G>(b, items, n, gwarp, nwarps, kind, want_post != 0, respect_status != 0);
 }
 
-__global__ void __launch_bounds__(kBlock) k_mstep(laml_batch b, int rounds) {
+__global__ void __launch_bounds__(kBlock) k_mstep(laml_batch b, int rounds, int flags) {
     __shared__ double2 sh[kBlock / 32];
     __shared__ float4 s_cnt[kMstepStage];
     __shared__ float s_d[kMstepStage];
-    for (int p = blockIdx.x; p < b.n_trees; p += gridDim.x) mstep_tree(b, p, rounds, sh, s_cnt, s_d);
+    for (int p = blockIdx.x; p < b.n_trees; p += gridDim.x)
+        mstep_tree(b, p, rounds, sh, s_cnt, s_d, (flags & LAML_MSTEP_FP64_POLISH) != 0);
 }
 
 __global__ void k_tree_llh(laml_batch b, int mode, double rel_tol, int max_iters) {
@@ -795,7 +804,7 @@ __global__ void k_branch_terms(laml_batch b) {
 
 template <int G>
 __global__ void __launch_bounds__(kBlock, LAML_MINB) k_em_persistent(laml_batch b, int iters, int rounds,
-                                                           double rel_tol, int max_iters) {
+                                                           double rel_tol, int max_iters, int flags) {
     __shared__ double2 sh[kBlock / 32];
     __shared__ float4 s_cnt[kMstepStage];
     __shared__ float s_d[kMstepStage];
@@ -812,7 +821,8 @@ __global__ void __launch_bounds__(kBlock, LAML_MINB) k_em_persistent(laml_batch 
         }
         for_items<G>(b, b.root_items, b.n_root_items, gwarp, nwarps, 3, false, true);
         if (!grid_barrier(b, gen)) return;
-        for (int p = blockIdx.x; p < b.n_trees; p += gridDim.x) mstep_tree(b, p, rounds, sh, s_cnt, s_d);
+        for (int p = blockIdx.x; p < b.n_trees; p += gridDim.x)
+            mstep_tree(b, p, rounds, sh, s_cnt, s_d, (flags & LAML_MSTEP_FP64_POLISH) != 0);
         if (!grid_barrier(b, gen)) return;
         for (int l = 0; l < b.n_in_levels; ++l) {
             const int64_t o = b.in_level_off[l], e = b.in_level_off[l + 1];
@@ -915,14 +925,14 @@ int outside_t(const laml_batch& b, int want_post, cudaStream_t st, const Levels&
 
 template <int G>
 int em_levels_t(const laml_batch& b, int iters, int rounds, double tol, int max_iters,
-                cudaStream_t st) {
+                int flags, cudaStream_t st) {
     Levels L;
     int rc = fetch_levels(b, L, st);
     if (rc) return rc;
     const int tb = (b.n_trees + 127) / 128;
     for (int it = 0; it < iters; ++it) {
         if ((rc = outside_t<G>(b, 0, st, L))) return rc;
-        k_mstep<<<b.n_trees, kBlock, 0, st>>>(b, rounds);
+        k_mstep<<<b.n_trees, kBlock, 0, st>>>(b, rounds, flags);
         if ((rc = check(cudaGetLastError(), "k_mstep"))) return rc;
         if ((rc = inside_t<G>(b, 0, st, L, 1))) return rc;
         k_tree_llh<<<tb, 128, 0, st>>>(b, 2, tol, max_iters);
@@ -933,7 +943,7 @@ int em_levels_t(const laml_batch& b, int iters, int rounds, double tol, int max_
 
 template <int G>
 int em_persistent_t(const laml_batch& b, int iters, int rounds, double tol, int max_iters,
-                    cudaStream_t st) {
+                    int flags, cudaStream_t st) {
     int dev = 0;
     cudaGetDevice(&dev);
     int coop = 0;
@@ -950,7 +960,7 @@ int em_persistent_t(const laml_batch& b, int iters, int rounds, double tol, int 
     if ((rc = check(cudaMemsetAsync(b.barrier, 0, 2 * sizeof(uint32_t), st), "barrier reset")))
         return rc;
     laml_batch bb = b;
-    void* args[] = {&bb, &iters, &rounds, &tol, &max_iters};
+    void* args[] = {&bb, &iters, &rounds, &tol, &max_iters, &flags};
     return check(cudaLaunchCooperativeKernel((const void*)k_em_persistent<G>, dim3(grid),
                                              dim3(kBlock), args, 0, st),
                  "k_em_persistent launch");
@@ -1002,26 +1012,27 @@ extern "C" int laml_outside(const laml_batch* b, int32_t want_post, void* stream
     DISPATCH_G(*b, (outside_t<GG>(*b, want_post, st, L)));
 }
 
-extern "C" int laml_mstep(const laml_batch* b, int32_t rounds, void* stream) {
+extern "C" int laml_mstep(const laml_batch* b, int32_t rounds, int32_t flags, void* stream) {
     int rc = validate(b);
     if (rc) return rc;
-    k_mstep<<<b->n_trees, kBlock, 0, (cudaStream_t)stream>>>(*b, rounds);
+    k_mstep<<<b->n_trees, kBlock, 0, (cudaStream_t)stream>>>(*b, rounds, flags);
     return check(cudaGetLastError(), "k_mstep");
 }
 
 extern "C" int laml_em_run(const laml_batch* b, int32_t iters, int32_t rounds, double rel_tol,
-                           int32_t max_iters, void* stream) {
+                           int32_t max_iters, int32_t flags, void* stream) {
     int rc = validate(b);
     if (rc) return rc;
     if (iters <= 0) return LAML_OK;
-    DISPATCH_G(*b, (em_persistent_t<GG>(*b, iters, rounds, rel_tol, max_iters,
+    DISPATCH_G(*b, (em_persistent_t<GG>(*b, iters, rounds, rel_tol, max_iters, flags,
                                         (cudaStream_t)stream)));
 }
 
 extern "C" int laml_em_run_levels(const laml_batch* b, int32_t iters, int32_t rounds,
-                                  double rel_tol, int32_t max_iters, void* stream) {
+                                  double rel_tol, int32_t max_iters, int32_t flags, void* stream) {
     int rc = validate(b);
     if (rc) return rc;
     if (iters <= 0) return LAML_OK;
-    DISPATCH_G(*b, (em_levels_t<GG>(*b, iters, rounds, rel_tol, max_iters, (cudaStream_t)stream)));
+    DISPATCH_G(*b, (em_levels_t<GG>(*b, iters, rounds, rel_tol, max_iters, flags,
+                                    (cudaStream_t)stream)));
 }

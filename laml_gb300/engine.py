@@ -197,14 +197,16 @@ class DeviceBatch:
     def outside(self, want_post=False):
         N.check(N.lib().laml_outside(C.byref(self.b), int(want_post), self._s()))
 
-    def mstep(self, rounds=MSTEP_ROUNDS):
-        N.check(N.lib().laml_mstep(C.byref(self.b), rounds, self._s()))
+    def mstep(self, rounds=MSTEP_ROUNDS, polish=False):
+        N.check(N.lib().laml_mstep(C.byref(self.b), rounds,
+                                   N.MSTEP_FP64_POLISH if polish else 0, self._s()))
 
     def em_iterations(self, iters, rounds=MSTEP_ROUNDS, rel_tol=None, max_iters=100000,
-                      persistent=True):
+                      persistent=True, polish=False):
         tol = rel_tol if rel_tol is not None else (EM_STOP_COMPAT if self.compat else EM_STOP_EXACT)
         f = N.lib().laml_em_run if persistent else N.lib().laml_em_run_levels
-        N.check(f(C.byref(self.b), iters, rounds, tol, max_iters, self._s()))
+        N.check(f(C.byref(self.b), iters, rounds, tol, max_iters,
+                  N.MSTEP_FP64_POLISH if polish else 0, self._s()))
 
     def check_device_error(self):
         err = int(self.work["error"].item())
@@ -245,7 +247,7 @@ class DeviceBatch:
         return out, lr
 
     def run_em(self, rounds=MSTEP_ROUNDS, rel_tol=None, max_iters=100000, chunk=4,
-               persistent=True):
+               persistent=True, polish=False):
         """EM to convergence for every tree: inside at the start parameters,
         then chunks of fused iterations until no tree is ACTIVE."""
         self.branch_terms()
@@ -253,7 +255,7 @@ class DeviceBatch:
         done = 0
         while True:
             self.em_iterations(chunk, rounds=rounds, rel_tol=rel_tol, max_iters=max_iters,
-                               persistent=persistent)
+                               persistent=persistent, polish=polish)
             done += chunk
             st = self.work["tr_status"]
             if not bool((st == N.TREE_ACTIVE).any()):

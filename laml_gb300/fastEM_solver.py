@@ -1,0 +1,290 @@
+"""Drop-in mirror of laml_libs/fastEM_solver.py on the GB300 engine.
+
+Same constructor and methods as the reference solver (Virtual_solver /
+ML_solver / EM_solver / fastEM_solver, laml_libs/*.py):
+
+* ``fastEM_solver(treeList, data, prior, params)`` -- ``treeList`` newick
+  strings; ``data = {'charMtrx': {cell: [int|'?']}, 'ordered_leaf_labels':
+  [[...]], ...}``; ``prior = {'Q': [{state: prob}], ...}``.
+* ``score_tree(strategy) -> (score, status)``: the fastEM path
+  (fastEM_solver.py:283-353): each tree runs fastEM's EM from nu = phi = 0.5
+  (or the fixed values given), branch lengths written back; with
+  ``'final_optimization'`` in the strategy the exact EM (EM_solver) runs
+  instead (fastEM_solver.py:295-297).
+* ``negative_llh()``: the exact-model log-likelihood (ML_solver.py:252-254,
+  EM_solver.py:135-141).
+* ``optimize(initials, fixed_phi, fixed_nu, fixed_brlen, verbose, max_trials,
+  random_seeds, ultra_constr)``: the exact EM with EM_solver's initial points
+  (ML_solver.py:256-336, EM_solver.py:514-527).
+* ``get_params()``, ``get_tree_newick()``, ``params.nu`` / ``params.phi``.
+
+Every likelihood, E-step and M-step runs on the GPU; there is no CPU path.
+Only binary trees are supported (a polytomy raises ValueError) and the
+ultrametric equality constraints of EM_solver.Mstep (EM_solver.py:53-89,
+358-361) are not implemented (``ultra_constr=True`` raises
+NotImplementedError).
+"""
+from __future__ import annotations
+
+import random as _random
+from typing import List, Optional
+
+import numpy as np
+
+from .encoding import EncodedTree, char_matrix, encode_dataset, encode_newick
+from .engine import MSTEP_ROUNDS, DeviceBatch
+from .fast_em.phylogeny import Phylogeny, build_phylogeny, tree_to_networkx
+
+EPS_PARAM = 1e-10          # laml_libs/core_constants.py:4 (eps)
+DMIN, DMAX = 0.005, 10.0   # laml_libs/core_constants.py:7-8
+
+
+class Params:
+    def __init__(self, nu, phi):
+        self.nu = nu
+        self.phi = phi
+
+
+def write_newick(et: EncodedTree, d: Optional[np.ndarray] = None) -> str:
+    """Newick of an encoded tree (children in their newick order, every node
+    labelled, lengths from ``d`` or the tree)."""
+    d = et.branch_length if d is None else d
+    root = et.root
+    out = []
+    st = [(root, 0)]
+    while st:
+        u, k = st.pop()
+        if et.child0[u] < 0:
+            out.append(f"{et.labels[u]}:{float(d[u])!r}")
+            continue
+        ch = (int(et.child1[u]), int(et.child0[u]))   # newick order
+        if k == 0:
+            out.append("(")
+        if k < 2:
+            if k > 0:
+                out.append(",")
+            st.append((u, k + 1))
+            st.append((ch[k], 0))
+        else:
+            out.append(f"){et.labels[u]}:{float(d[u])!r}")
+    return "".join(out) + ";"
+
+
+def parse_tree(tree, has_branch_mask=False, ordered_leaf_labels=None, fixed=None,
+               rng=None) -> dict:
+    """fastEM_solver.parse_tree (fastEM_solver.py:46-146) for a newick string
+    (or an object with ``.newick()``): the networkx tree, branch lengths
+    (U(0.01, 0.5) where missing, leaves first), the branch mask (True = free;
+    ``fixed`` is the set of labels marked fixed) and the relabeling vector."""
+    nw = tree if isinstance(tree, str) else tree.newick()
+    et = encode_newick(nw, ordered_leaf_labels)
+    rng = rng if rng is not None else _random
+    bl = et.branch_length.copy()
+    for i in range(et.num_nodes):
+        if not et.has_length[i]:
+            bl[i] = rng.uniform(0.01, 0.5)
+    if has_branch_mask:
+        fixed = fixed or set()
+        mask = np.array([lab not in fixed for lab in et.labels])
+    else:
+        mask = np.ones(et.num_nodes, bool)
+    return {"nxtree": tree_to_networkx(et), "num_leaves": et.num_leaves, "branch_lengths": bl,
+            "branch_mask": mask, "relabeling_vector": list(et.labels), "encoded": et}
+
+
+def parse_data(parser_tree_out, data, prior) -> Phylogeny:
+    """fastEM_solver.parse_data (fastEM_solver.py:17-44)."""
+    order = parser_tree_out["relabeling_vector"][:parser_tree_out["num_leaves"]]
+    rows = {c: data["charMtrx"][c] for c in order}
+    pri = {}
+    for c, q in enumerate(prior["Q"]):
+        for s, p in q.items():
+            pri[(c, int(s))] = float(p)
+    return build_phylogeny(parser_tree_out["nxtree"], parser_tree_out["num_leaves"], rows, pri)
+
+
+def _lca(et: EncodedTree, a: int, b: int) -> int:
+    seen = set()
+    x = a
+    while x >= 0:
+        seen.add(x)
+        x = int(et.parent[x])
+    x = b
+    while x not in seen:
+        x = int(et.parent[x])
+    return x
+
+
+class fastEM_solver:
+    """The reference solver's interface, every computation on the GPU."""
+
+    def __init__(self, treeList, data, prior, params={'nu': 0, 'phi': 0, 'sigma': 0},
+                 group_sites: int = 8, device="cuda"):
+        self.solver_name = "fastEM_solver"
+        self.data, self.prior = data, prior
+        self.charMtrx = data["charMtrx"]
+        self.Q = prior["Q"]
+        self.treeList = [t if isinstance(t, str) else t.newick() for t in treeList]
+        # fastEM_solver passes nu = phi = 0 to its parents (fastEM_solver.py:152)
+        self.params = Params(0, 0)
+        self.numsites = len(next(iter(self.charMtrx.values())))
+        self.G, self.device = group_sites, device
+        order = data.get("ordered_leaf_labels")
+        self.ordered_leaf_labels = []
+        self.trees: List[EncodedTree] = []
+        for i, nw in enumerate(self.treeList):
+            lo = order[i] if order is not None else None
+            et = encode_newick(nw, lo)
+            if lo is None:
+                lo = et.labels[:et.num_leaves]
+            self.ordered_leaf_labels.append(list(lo))
+            self.trees.append(et)
+        self._d = [t.branch_length.copy() for t in self.trees]
+        for t, d in zip(self.trees, self._d):
+            for i in np.flatnonzero(~t.has_length):
+                d[i] = _random.uniform(0.01, 0.5)
+        self._ds_cache = {}
+
+    # -- helpers --------------------------------------------------------
+    def _dataset(self, tidx, compat):
+        key = (tidx, compat)
+        if key not in self._ds_cache:
+            lo = self.ordered_leaf_labels[tidx]
+            mat = char_matrix([self.charMtrx[c] for c in lo], exact=not compat)
+            self._ds_cache[key] = encode_dataset(mat, self.Q, compat=compat, group_sites=self.G)
+        return self._ds_cache[key]
+
+    def _fixed_mask(self, tidx, fixed_brlen):
+        """Branches fixed by ``fixed_brlen[tidx]``: {(leafA, leafB): length}
+        fixes the edge above LCA(leafA, leafB) (ML_solver.py:296-305)."""
+        et = self.trees[tidx]
+        mask = np.ones(et.num_nodes, bool)
+        d = self._d[tidx]
+        if fixed_brlen is None:
+            return mask
+        lab = {l: i for i, l in enumerate(et.labels)}
+        for (a, b), L in fixed_brlen[tidx].items():
+            u = _lca(et, lab[a], lab[b])
+            mask[u] = False
+            d[u] = L
+        return mask
+
+    # -- Virtual_solver / ML_solver surface -------------------------------
+    def get_tree_newick(self):
+        return [write_newick(t, d) for t, d in zip(self.trees, self._d)]
+
+    def get_params(self):
+        return {'phi': self.params.phi, 'nu': self.params.nu}
+
+    def negative_llh(self):
+        """EM_solver.lineage_llh at the current parameters (exact model)."""
+        total = 0.0
+        for i, t in enumerate(self.trees):
+            b = DeviceBatch([self._dataset(i, False)], [t], [0], [self._d[i]],
+                            [self.params.nu], [self.params.phi], compat=False,
+                            device=self.device)
+            total += float(b.log_likelihood()[0])
+        return -total
+
+    def score_tree(self, strategy={'ultra_constr': False, 'fixed_phi': None, 'fixed_nu': None,
+                                   'fixed_brlen': None, 'nodes_to_recompute': None}):
+        if 'final_optimization' in strategy:
+            return self.score_tree_oldEM(strategy)
+        fixed_phi, fixed_nu = strategy.get('fixed_phi'), strategy.get('fixed_nu')
+        has_mask = strategy.get('fixed_brlen') is not None
+        score = None
+        for i, t in enumerate(self.trees):
+            # fastEM_solver.py:310-316: every node is marked fixed and the
+            # recompute test compares a label with node objects, so with
+            # fixed_brlen given no branch length is freed
+            mask = np.zeros(t.num_nodes, bool) if has_mask else np.ones(t.num_nodes, bool)
+            nu = fixed_nu if fixed_nu else 0.5
+            phi = fixed_phi if fixed_phi else 0.5
+            b = DeviceBatch([self._dataset(i, True)], [t], [0],
+                            [np.maximum(self._d[i], 1e-6)],
+                            [min(max(nu, 1e-6), 1 - 1e-6)], [min(max(phi, 1e-6), 1 - 1e-6)],
+                            compat=True, mask=[mask], device=self.device)
+            r = b.run_em(rounds=MSTEP_ROUNDS)[0]
+            self.params.nu, self.params.phi = r.nu, r.phi
+            self._d[i] = r.branch_lengths
+            score = r.llh
+        return score, "optimal"
+
+    def score_tree_oldEM(self, strategy):
+        nllh, status = self.optimize(initials=1, verbose=-1,
+                                     ultra_constr=strategy.get('ultra_constr', False),
+                                     fixed_phi=strategy.get('fixed_phi'),
+                                     fixed_nu=strategy.get('fixed_nu'),
+                                     fixed_brlen=strategy.get('fixed_brlen'))
+        return (None if nllh is None else -nllh), status
+
+    def optimize(self, initials=20, fixed_phi=None, fixed_nu=None, fixed_brlen=None, verbose=1,
+                 max_trials=100, random_seeds=None, ultra_constr=False):
+        """EM_solver.optimize_one from ``initials`` starting points (the best
+        nllh wins), seeds as ML_solver.optimize (ML_solver.py:263-282)."""
+        if ultra_constr:
+            raise NotImplementedError("ultrametric-constrained M-step is not implemented; "
+                                      "call with ultra_constr=False")
+        if random_seeds is None:
+            rseeds = [int(_random.random() * 10000) for _ in range(initials)]
+        elif isinstance(random_seeds, int):
+            _random.seed(a=random_seeds)
+            rseeds = [int(_random.random() * 10000) for _ in range(initials)]
+        else:
+            rseeds = list(random_seeds)[:initials]
+        best = None
+        for rep in range(initials):
+            res = self._optimize_one(rseeds[rep], fixed_phi, fixed_nu, fixed_brlen)
+            if best is None or res[0] < best[0]:
+                best = res
+        nllh, nu, phi, ds = best
+        self.params = Params(nu, phi)
+        self._d = ds
+        return nllh, "optimal"
+
+    def _optimize_one(self, randseed, fixed_phi, fixed_nu, fixed_brlen):
+        rs = _random.Random(randseed)
+        ds, masks = [], []
+        for i, t in enumerate(self.trees):
+            masks.append(self._fixed_mask(i, fixed_brlen))
+        # ML_solver.ini_all: one draw per edge (treeswift postorder), then nu, phi
+        post = []
+        for t in self.trees:
+            post.append(_ts_postorder(t))
+        ne = sum(len(p) for p in post)
+        x = [rs.random() * (DMAX / 2 - 2 * DMIN) + 2 * DMIN for _ in range(ne)]
+        nu = rs.random() * 0.99 if fixed_nu is None else fixed_nu
+        phi = rs.random() * 0.99 if fixed_phi is None else fixed_phi
+        k = 0
+        for i, t in enumerate(self.trees):
+            d = np.empty(t.num_nodes)
+            for u in post[i]:
+                has = t.has_length[u] or not masks[i][u]
+                d[u] = max(2 * DMIN, self._d[i][u]) if has else x[k]
+                k += 1
+            ds.append(d)
+        total, out_d = 0.0, []
+        for i, t in enumerate(self.trees):
+            b = DeviceBatch([self._dataset(i, False)], [t], [0], [ds[i]], [nu], [phi],
+                            compat=False, mask=[masks[i]], fix_nu=fixed_nu is not None,
+                            fix_phi=fixed_phi is not None, device=self.device)
+            r = b.run_em(max_iters=1000)[0]
+            total += r.llh
+            out_d.append(r.branch_lengths)
+            nu, phi = r.nu, r.phi
+        return -total, nu, phi, out_d
+
+
+def _ts_postorder(t: EncodedTree):
+    """Node ids in treeswift postorder (children in newick order)."""
+    out, st = [], [(t.root, False)]
+    while st:
+        u, done = st.pop()
+        if done:
+            out.append(u)
+            continue
+        st.append((u, True))
+        if t.child0[u] >= 0:
+            st.append((int(t.child0[u]), False))
+            st.append((int(t.child1[u]), False))
+    return out
