@@ -173,6 +173,8 @@ def main():
     ap.add_argument("--ref-trees", type=int, default=16)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--levels", action="store_true",
+                    help="one launch per tree level instead of the persistent kernel")
     ap.add_argument("--trees", type=int, default=512,
                     help="use the first N candidates (smaller cases for profiling)")
     args = ap.parse_args()
@@ -207,7 +209,7 @@ def main():
     K = b.datasets[0].n_sites
 
     def step():
-        b.em_iterations(1, rel_tol=-1.0, max_iters=1 << 30)
+        b.em_iterations(1, rel_tol=-1.0, max_iters=1 << 30, persistent=not args.levels)
 
     for _ in range(args.warmup):
         step()
@@ -283,12 +285,14 @@ def main():
             "node_site_updates_per_s": nsu,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": None,
-                         "kernel": "k_em_persistent", "bytes_per_launch": bytes_it,
+                         "kernel": "k_items (per level)" if args.levels else "k_em_persistent",
+                         "bytes_per_launch": bytes_it,
                          "peak_kind": peak_kind},
             "e2e": e2e,
             "cpu_baseline": cpu,
             "clocks": clk.summary(),
-            "gpu_launches": args.steps,
+            "gpu_launches": args.steps * (1 if not args.levels else
+                                          b.sizes["n_in_levels"] + b.sizes["n_out_levels"] + 4),
             "wall_s_timed": t1 - t0,
             "llh_mean": float(np.mean(llh_now)),
         }

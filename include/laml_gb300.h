@@ -59,6 +59,20 @@ int laml_newick_encode(const char* newick, const char* const* leaf_order, int32_
                        double* branch_length, uint8_t* has_length,
                        char* labels, int64_t* label_offsets);
 
+/* Batch form of laml_newick_encode for many trees over one leaf set (the
+ * candidates of a topology search): every tree must have exactly the leaves
+ * of `leaf_order`, which numbers them 0..n-1.  laml_newick_batch_measure gives
+ * an upper bound of the total node count to size the outputs; node_offsets
+ * [n_trees + 1] receives the compacted start of each tree.  Parses once per
+ * tree on `n_threads` host threads (0 = all); no labels are produced. */
+int laml_newick_batch_measure(int32_t n_trees, const char* const* newicks,
+                              int64_t* raw_nodes_total);
+int laml_newick_encode_batch(int32_t n_trees, const char* const* newicks,
+                             const char* const* leaf_order, int32_t n_leaf_order,
+                             int32_t n_threads, int64_t* node_offsets, int32_t* num_leaves,
+                             int32_t* parent, int32_t* child0, int32_t* child1,
+                             double* branch_length, uint8_t* has_length);
+
 /* Site layout of a character matrix for the device kernels.
  * chars: n_leaves x n_sites int32 in leaf order (LAML_CHAR_* or >= 0 raw
  * states); priors as CSR over sites: prior_ptr[n_sites+1], prior_state[],
@@ -210,13 +224,26 @@ int laml_branch_terms(const laml_batch* b, void* stream);
  * of EM_solver.Estep_in_llh / lineage_llh (laml_libs/EM_solver.py:91-141). */
 int laml_inside(const laml_batch* b, int32_t update_em, void* stream);
 
-/* Outside pass + expected transition counts (nd_cnt, 6 per branch) +
- * per-leaf silenced posteriors; with `want_post` = 1 also the posteriors
- * P(v = 0 | D), P(v = silenced | D) per (node, site) into post0/post1.
- * Requires laml_inside first.  Replaces calc.compute_E_step
+/* laml_outside flags */
+#define LAML_OUT_POSTERIORS 1  /* also P(v = 0 | D), P(v = silenced | D) into post0/post1 */
+#define LAML_OUT_TRUE_ROOT 2   /* root counts from the progenitor in state 0 even in compat */
+
+/* Outside pass + expected transition counts per (node, site group) in
+ * cnt_part (C00, C0a, C0s, Caa, Cas, Css, P(silenced|D) at '?' leaf entries,
+ * at observed leaf entries).  Requires laml_inside first.  In compat mode the
+ * root's row follows parent_sibling[root] = (-1, -1) -> node N-1 unless
+ * LAML_OUT_TRUE_ROOT.  Replaces calc.compute_E_step
  * (fast_em/calculations.py:506-577) and EM_solver.Estep_out_llh /
  * Estep_posterior (laml_libs/EM_solver.py:143-300). */
-int laml_outside(const laml_batch* b, int32_t want_post, void* stream);
+int laml_outside(const laml_batch* b, int32_t flags, void* stream);
+
+/* d logL / d branch length (grad_d[n_nodes], device) and d logL / d(nu, phi)
+ * per tree (grad_nu_phi[2T], device) from the counts of
+ * laml_outside(LAML_OUT_TRUE_ROOT).  No reference counterpart computes the
+ * exact gradient; it is the adjoint of the inside pass (the outside pass
+ * reused as the backward) and equals the gradient of the M-step objective
+ * (fast_em/laml.py:62-78) at the current parameters with true root counts. */
+int laml_gradient(const laml_batch* b, double* grad_d, double* grad_nu_phi, void* stream);
 
 /* M-step flags: FP64 Newton polish of the final branch-length and nu solves
  * (the solves otherwise run FP32 Newton iterations with FP64 accumulation). */

@@ -19,6 +19,7 @@ ERRORS = {-1: "LAML_ERR_ARG", -2: "LAML_ERR_CUDA", -3: "LAML_ERR_PARSE", -4: "LA
           -5: "LAML_ERR_TIMEOUT", -6: "LAML_ERR_NOT_BINARY", -7: "LAML_ERR_LEAF"}
 TREE_ACTIVE, TREE_CONVERGED, TREE_NAN, TREE_MAXITER = 0, 1, 2, 3
 MSTEP_FP64_POLISH = 1
+OUT_POSTERIORS, OUT_TRUE_ROOT = 1, 2
 
 
 class LamlError(RuntimeError):
@@ -87,6 +88,9 @@ class Batch(C.Structure):
 EXPORTS = {
     "laml_newick_size": (i32, [C.c_char_p, P(i32), P(i32), P(i64)]),
     "laml_newick_encode": (i32, [C.c_char_p, P(C.c_char_p), i32, vp, vp, vp, vp, vp, vp, vp]),
+    "laml_newick_batch_measure": (i32, [i32, P(C.c_char_p), P(i64)]),
+    "laml_newick_encode_batch": (i32, [i32, P(C.c_char_p), P(C.c_char_p), i32, i32, vp, vp, vp,
+                                       vp, vp, vp, vp]),
     "laml_dataset_measure": (i32, [i32, i32, vp, vp, vp, vp, i32, i32, P(DatasetInfo)]),
     "laml_dataset_encode": (i32, [i32, i32, vp, vp, vp, vp, i32, i32, vp, vp, vp, vp, vp, vp, vp,
                                   vp, vp]),
@@ -97,6 +101,7 @@ EXPORTS = {
     "laml_inside": (i32, [P(Batch), i32, vp]),
     "laml_outside": (i32, [P(Batch), i32, vp]),
     "laml_mstep": (i32, [P(Batch), i32, i32, vp]),
+    "laml_gradient": (i32, [P(Batch), vp, vp, vp]),
     "laml_em_run": (i32, [P(Batch), i32, i32, f64, i32, i32, vp]),
     "laml_em_run_levels": (i32, [P(Batch), i32, i32, f64, i32, i32, vp]),
     "laml_last_error": (C.c_char_p, []),

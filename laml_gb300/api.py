@@ -19,13 +19,13 @@ import numpy as np
 import torch
 
 from .engine import MSTEP_ROUNDS, TreeResult
-from .problem import dataset_from_rows, encode_trees, make_batch
+from .encoding import encode_newick_batch
+from .problem import dataset_from_rows, make_batch
 
 
 @dataclass
 class ScoreResult:
     results: List[TreeResult]
-    labels: List[List[str]]      # relabeling vectors (node order of each result)
     h2d_bytes: int
     d2h_bytes: int
 
@@ -40,7 +40,7 @@ def score_candidates(newicks: Sequence[str], rows: dict, Q, leaf_order: Sequence
                      fix_nu=None, fix_phi=None, masks=None, device="cuda", chunk: int = 4,
                      rng: Optional[random.Random] = None) -> ScoreResult:
     ds = dataset_from_rows(rows, Q, leaf_order, compat, group_sites)
-    trees = encode_trees(newicks, leaf_order)
+    trees = encode_newick_batch(newicks, leaf_order)
     rng = rng if rng is not None else random
     d = []
     for t in trees:
@@ -54,5 +54,5 @@ def score_candidates(newicks: Sequence[str], rows: dict, Q, leaf_order: Sequence
                    phi=phi, d=d, mask=masks, fix_nu=fix_nu, fix_phi=fix_phi, device=device,
                    trees=trees, dataset=ds)
     res = b.run_em(rounds=rounds, max_iters=max_iters, chunk=chunk)
-    d2h = sum(8 * (r.branch_lengths.size + 4) for r in res)
-    return ScoreResult(res, [t.labels for t in trees], b.h2d_bytes, d2h)
+    d2h = b.last_d2h_bytes
+    return ScoreResult(res, b.h2d_bytes, d2h)

@@ -8,6 +8,8 @@
 #include <cstdio>
 #include <cstring>
 #include <string>
+#include <atomic>
+#include <thread>
 #include <unordered_map>
 #include <vector>
 
@@ -240,6 +242,149 @@ extern "C" int laml_newick_encode(const char* newick, const char* const* leaf_or
             off += (int64_t)E.labels[i].size() + 1;
         }
     }
+    return LAML_OK;
+}
+
+// ---------------------------------------------------------------------------
+// batch newick encoding: many trees over one leaf set, one parse each,
+// parallel over trees
+// ---------------------------------------------------------------------------
+namespace {
+
+int64_t raw_node_count(const char* s) {
+    int64_t n = 1;
+    for (const char* p = s; *p && *p != ';'; ++p) {
+        if (*p == '(' || *p == ',') ++n;
+        else if (*p == '[') {
+            while (*p && *p != ']') ++p;
+            if (!*p) break;
+        }
+    }
+    return n;
+}
+
+}  // namespace
+
+extern "C" int laml_newick_batch_measure(int32_t n_trees, const char* const* newicks,
+                                         int64_t* raw_nodes_total) {
+    if (n_trees < 0 || (n_trees > 0 && !newicks) || !raw_nodes_total) {
+        set_error("laml_newick_batch_measure: bad argument");
+        return LAML_ERR_ARG;
+    }
+    int64_t t = 0;
+    for (int i = 0; i < n_trees; ++i) t += raw_node_count(newicks[i]);
+    *raw_nodes_total = t;
+    return LAML_OK;
+}
+
+extern "C" int laml_newick_encode_batch(int32_t n_trees, const char* const* newicks,
+                                        const char* const* leaf_order, int32_t n_leaf_order,
+                                        int32_t n_threads, int64_t* node_offsets,
+                                        int32_t* num_leaves, int32_t* parent, int32_t* child0,
+                                        int32_t* child1, double* branch_length,
+                                        uint8_t* has_length) {
+    if (n_trees <= 0 || !newicks || !leaf_order || !node_offsets || !num_leaves) {
+        set_error("laml_newick_encode_batch: bad argument");
+        return LAML_ERR_ARG;
+    }
+    // raw offsets (upper bounds); compacted offsets are written afterwards
+    std::vector<int64_t> raw(n_trees + 1, 0);
+    for (int i = 0; i < n_trees; ++i) raw[i + 1] = raw[i] + raw_node_count(newicks[i]);
+    std::unordered_map<std::string, int> order;
+    order.reserve((size_t)n_leaf_order * 2);
+    for (int k = 0; k < n_leaf_order; ++k) order.emplace(leaf_order[k], k);
+    std::vector<int64_t> used(n_trees, 0);
+    std::vector<int> rc(n_trees, LAML_OK);
+    std::vector<std::string> msg(n_trees);
+    std::atomic<int> next{0};
+    auto work = [&]() {
+        std::vector<PNode> nodes;
+        for (;;) {
+            const int i = next.fetch_add(1);
+            if (i >= n_trees) break;
+            if (!parse_newick(newicks[i], nodes)) { rc[i] = LAML_ERR_PARSE; msg[i] = laml::g_last_error; continue; }
+            std::vector<int> pre = ts_preorder(nodes, 0);
+            int root = pre[0];
+            size_t first = 0;
+            if (nodes[root].children.size() == 1) { first = 1; root = nodes[root].children[0]; }
+            // leaves take their leaf-order position; internal nodes follow in preorder
+            std::vector<int> id(nodes.size(), -1);
+            int nl = 0, ni = 0;
+            for (size_t k = first; k < pre.size(); ++k) {
+                const PNode& v = nodes[pre[k]];
+                if (v.children.empty()) {
+                    auto it = v.has_label ? order.find(v.label) : order.end();
+                    if (it == order.end()) {
+                        rc[i] = LAML_ERR_LEAF;
+                        msg[i] = "leaf '" + v.label + "' is not in the leaf order";
+                        break;
+                    }
+                    id[pre[k]] = it->second;
+                    ++nl;
+                } else {
+                    ++ni;
+                }
+            }
+            if (rc[i]) continue;
+            if (nl != n_leaf_order) {
+                rc[i] = LAML_ERR_LEAF;
+                msg[i] = "tree " + std::to_string(i) + " does not have every leaf of the leaf order";
+                continue;
+            }
+            int nxt = nl;
+            for (size_t k = first; k < pre.size(); ++k)
+                if (!nodes[pre[k]].children.empty()) id[pre[k]] = nxt++;
+            const int64_t o = raw[i];
+            int32_t* P = parent + o; int32_t* A = child0 + o; int32_t* B = child1 + o;
+            double* D = branch_length + o; uint8_t* H = has_length + o;
+            for (size_t k = first; k < pre.size(); ++k) {
+                const PNode& v = nodes[pre[k]];
+                const int u = id[pre[k]];
+                D[u] = v.has_length ? v.length : 0.0;
+                H[u] = v.has_length ? 1 : 0;
+                if (pre[k] == root) P[u] = -1;
+                if (v.children.size() == 2) {
+                    A[u] = id[v.children[1]];
+                    B[u] = id[v.children[0]];
+                    P[id[v.children[0]]] = u;
+                    P[id[v.children[1]]] = u;
+                } else if (!v.children.empty()) {
+                    rc[i] = LAML_ERR_NOT_BINARY;
+                    msg[i] = "tree " + std::to_string(i) + ": a node with " +
+                             std::to_string(v.children.size()) + " children";
+                    break;
+                } else {
+                    A[u] = -1;
+                    B[u] = -1;
+                }
+            }
+            used[i] = nl + ni;
+            num_leaves[i] = nl;
+        }
+    };
+    int nt = n_threads > 0 ? n_threads : (int)std::thread::hardware_concurrency();
+    nt = std::max(1, std::min(nt, std::min(n_trees, 64)));
+    std::vector<std::thread> th;
+    for (int t = 1; t < nt; ++t) th.emplace_back(work);
+    work();
+    for (auto& t : th) t.join();
+    for (int i = 0; i < n_trees; ++i)
+        if (rc[i]) { set_error(msg[i]); return rc[i]; }
+    // compact in place (outputs move towards lower offsets only)
+    int64_t w = 0;
+    for (int i = 0; i < n_trees; ++i) {
+        node_offsets[i] = w;
+        const int64_t o = raw[i], n = used[i];
+        if (w != o) {
+            std::memmove(parent + w, parent + o, sizeof(int32_t) * n);
+            std::memmove(child0 + w, child0 + o, sizeof(int32_t) * n);
+            std::memmove(child1 + w, child1 + o, sizeof(int32_t) * n);
+            std::memmove(branch_length + w, branch_length + o, sizeof(double) * n);
+            std::memmove(has_length + w, has_length + o, n);
+        }
+        w += n;
+    }
+    node_offsets[n_trees] = w;
     return LAML_OK;
 }
 

@@ -240,7 +240,7 @@ __device__ void inside_item(const laml_batch& b, int u, int g, int lane, bool re
 template <int G>
 __device__ void outside_item(const laml_batch& b, int v, int g, int lane, bool act, int mode,
                              bool want_post) {
-    float c00 = 0.f, c0a = 0.f, c0s = 0.f, caa = 0.f, cas = 0.f, css = 0.f, lr = 0.f;
+    float c00 = 0.f, c0a = 0.f, c0s = 0.f, caa = 0.f, cas = 0.f, css = 0.f, lr = 0.f, lro = 0.f;
     SiteCtx s;
     bool live = act && site_ctx<G>(b, v, g, lane, true, s);
     const bool leaf_v = act && __ldg(b.nd_c0 + v) < 0;
@@ -328,7 +328,10 @@ __device__ void outside_item(const laml_batch& b, int v, int g, int lane, bool a
         caa = bv.z * dotxv * sc;
         cas = bv.w * cv.ss * sumx * sc;
         css = xs * cv.ss * sc;
-        if (leaf_v) lr = cv.ss * outs * sc;
+        if (leaf_v) {   // P(leaf silenced | D): '?' entries and observed entries apart
+            const float pl = cv.ss * outs * sc;
+            if (cv.code == -1) lr = pl; else lro = pl;
+        }
         if (want_post && b.post0 && mode == 0) {
             const int64_t pb = __ldg(b.tr_post_base + s.tree) +
                                (int64_t)(v - __ldg(b.tr_node_base + s.tree)) *
@@ -347,6 +350,7 @@ __device__ void outside_item(const laml_batch& b, int v, int g, int lane, bool a
         cas += __shfl_xor_sync(kFull, cas, off);
         css += __shfl_xor_sync(kFull, css, off);
         lr += __shfl_xor_sync(kFull, lr, off);
+        lro += __shfl_xor_sync(kFull, lro, off);
     }
     if (act && lane == 0) {
         const int tree = __ldg(b.nd_tree + v);
@@ -357,7 +361,7 @@ __device__ void outside_item(const laml_batch& b, int v, int g, int lane, bool a
                 b.cnt_part + __ldg(b.tr_cnt_base + tree) +
                 ((int64_t)(v - __ldg(b.tr_node_base + tree)) * NG + g) * 8);
             __stcg(dst, make_float4(c00, c0a, c0s, caa));
-            __stcg(dst + 1, make_float4(cas, css, lr, 0.f));
+            __stcg(dst + 1, make_float4(cas, css, lr, lro));
         }
     }
 }
@@ -508,14 +512,14 @@ __device__ void mstep_tree(const laml_batch& b, int p, int rounds, double2* sh, 
     }
     // 1. counts summed over site groups (EM_solver.py:342-345 normalisation in
     //    the exact model), d saved
-    double lr = 0.0;
+    double lr = 0.0, lro = 0.0;
     for (int v = threadIdx.x; v < N; v += blockDim.x) {
-        double c[7] = {0, 0, 0, 0, 0, 0, 0};
+        double c[8] = {0, 0, 0, 0, 0, 0, 0, 0};
         const float4* src = reinterpret_cast<const float4*>(b.cnt_part + cb + (int64_t)v * NG * 8);
         for (int g = 0; g < NG; ++g) {
             const float4 x = __ldcg(src + 2 * g), z = __ldcg(src + 2 * g + 1);
             c[0] += x.x; c[1] += x.y; c[2] += x.z; c[3] += x.w;
-            c[4] += z.x; c[5] += z.y; c[6] += z.z;
+            c[4] += z.x; c[5] += z.y; c[6] += z.z; c[7] += z.w;
         }
         if (!compat) {
             double t = 0.0;
@@ -533,8 +537,10 @@ __device__ void mstep_tree(const laml_batch& b, int p, int rounds, double2* sh, 
         __stcg(b.nd_d_prev + base + v, d);
         Dd[v] = (float)d;
         lr += c[6];
+        lro += c[7];
     }
-    const double LR = block_sum2(lr, 0.0, sh).x;   // also orders the staging writes
+    const double2 LRs = block_sum2(lr, lro, sh);   // also orders the staging writes
+    const double LR = LRs.x + LRs.y;
     if (threadIdx.x == 0) {
         b.tr_prev[2 * p] = nu;
         b.tr_prev[2 * p + 1] = phi;
@@ -547,8 +553,7 @@ __device__ void mstep_tree(const laml_batch& b, int p, int rounds, double2* sh, 
             phi = (R + Bm) > 0.0 ? Bm / (R + Bm) : phi;
             phi = fmin(fmax(phi, kCalcEps), 1.0 - kCalcEps);
         } else {
-            const double sil = __ldg(b.ds_silenced + ds);
-            const double Rt = M - (LR - sil), R = total - M;
+            const double Rt = M - LRs.x, R = total - M;   // '?' entries only
             phi = (R + Rt) > 0.0 ? Rt / (R + Rt) : 0.0;
             if (fabs(phi) < 1.0 / total) phi = 0.0;
         }
@@ -768,7 +773,7 @@ __device__ __forceinline__ void for_items(const laml_batch& b, const int32_t* it
         } else if (kind == 2) {
             if (act) root_init_item<G>(b, node, g, lane, want_post);
         } else {
-            outside_item<G>(b, node, g, lane, act, b.compat ? 1 : 2, false);
+            outside_item<G>(b, node, g, lane, act, (b.compat && kind == 3) ? 1 : 2, false);
         }
     }
 }
@@ -787,6 +792,51 @@ __global__ void __launch_bounds__(kBlock) k_mstep(laml_batch b, int rounds, int 
     __shared__ float s_d[kMstepStage];
     for (int p = blockIdx.x; p < b.n_trees; p += gridDim.x)
         mstep_tree(b, p, rounds, sh, s_cnt, s_d, (flags & LAML_MSTEP_FP64_POLISH) != 0);
+}
+
+// d logL / d(d_v, nu, phi) from the expected counts (Fisher's identity: the
+// gradient of the expected complete-data log-likelihood at the current
+// parameters); with the compat EPS floors a floored term has zero derivative.
+__global__ void __launch_bounds__(kBlock) k_gradient(laml_batch b, double* grad_d,
+                                                     double* grad_np) {
+    __shared__ double2 sh[kBlock / 32];
+    for (int p = blockIdx.x; p < b.n_trees; p += gridDim.x) {
+        const int N = b.tr_nodes[p], n = b.tr_leaves[p], base = b.tr_node_base[p];
+        const int ds = b.tr_ds[p], NG = b.ds_groups[ds], K = b.ds_sites[ds];
+        const int64_t cb = b.tr_cnt_base[p];
+        const bool compat = b.compat != 0;
+        const double nu = b.tr_nu[p], phi = b.tr_phi[p];
+        double gnu = 0.0, lrm = 0.0, lro = 0.0;
+        for (int v = threadIdx.x; v < N; v += blockDim.x) {
+            double c[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+            const float4* src = reinterpret_cast<const float4*>(b.cnt_part + cb + (int64_t)v * NG * 8);
+            for (int g = 0; g < NG; ++g) {
+                const float4 x = src[2 * g], z = src[2 * g + 1];
+                c[0] += x.x; c[1] += x.y; c[2] += x.z; c[3] += x.w;
+                c[4] += z.x; c[5] += z.y; c[6] += z.z; c[7] += z.w;
+            }
+            const double d = b.nd_d[base + v], nd = d * nu;
+            const double dt3 = (compat && d < kEPSd) ? 0.0 : 1.0 / expm1(d);   // d/dd log(1-e^-d)
+            const bool fl2 = (compat && nd < kEPSd) || nu <= 0.0;
+            const double en = expm1(nd);
+            const double dt2_dd = fl2 ? 0.0 : nu / en, dt2_dnu = fl2 ? 0.0 : d / en;
+            const double cs = c[2] + c[4];
+            grad_d[base + v] = -c[0] * (1.0 + nu) + c[1] * (dt3 - nu) + cs * dt2_dd - c[3] * nu;
+            gnu += -(c[0] + c[1] + c[3]) * d + cs * dt2_dnu;
+            lrm += c[6];
+            lro += c[7];
+        }
+        const double gsum = block_sum2(gnu, 0.0, sh).x;
+        const double2 L = block_sum2(lrm, lro, sh);
+        if (threadIdx.x == 0) {
+            const double M = b.ds_missing[ds], R = (double)n * K - M;
+            const double de1 = (compat && 1.0 - phi <= kEPSd) ? 0.0 : -1.0 / (1.0 - phi);
+            const double dep = (compat && phi <= kEPSd) ? 0.0 : 1.0 / phi;
+            grad_np[2 * p] = gsum;
+            grad_np[2 * p + 1] = (R - L.y) * de1 + (M - L.x) * dep;
+        }
+        __syncthreads();
+    }
 }
 
 __global__ void k_tree_llh(laml_batch b, int mode, double rel_tol, int max_iters) {
@@ -912,7 +962,8 @@ int inside_t(const laml_batch& b, int update_em, cudaStream_t st, const Levels& 
 }
 
 template <int G>
-int outside_t(const laml_batch& b, int want_post, cudaStream_t st, const Levels& L) {
+int outside_t(const laml_batch& b, int flags, cudaStream_t st, const Levels& L) {
+    const int want_post = flags & LAML_OUT_POSTERIORS;
     int rc = launch_items<G>(b, b.root_items, b.n_root_items, 2, want_post, 1, st);
     if (rc) return rc;
     for (int l = 0; l < b.n_out_levels; ++l) {
@@ -920,7 +971,10 @@ int outside_t(const laml_batch& b, int want_post, cudaStream_t st, const Levels&
                              want_post, 1, st);
         if (rc) return rc;
     }
-    return launch_items<G>(b, b.root_items, b.n_root_items, 3, 0, 1, st);
+    // kind 3: the E-step row of the root (compat: from node N-1); kind 4: from
+    // the progenitor in state 0 (the true posterior counts, for gradients)
+    return launch_items<G>(b, b.root_items, b.n_root_items,
+                           (flags & LAML_OUT_TRUE_ROOT) ? 4 : 3, 0, 1, st);
 }
 
 template <int G>
@@ -977,6 +1031,18 @@ int em_persistent_t(const laml_batch& b, int iters, int rounds, double tol, int 
 
 extern "C" int laml_supported_group_sites(void) { return 8 | 16 | 32; }
 
+extern "C" int laml_gradient(const laml_batch* b, double* grad_d, double* grad_nu_phi,
+                             void* stream) {
+    int rc = validate(b);
+    if (rc) return rc;
+    if (!grad_d || !grad_nu_phi) {
+        laml::set_error("laml_gradient: null output");
+        return LAML_ERR_ARG;
+    }
+    k_gradient<<<b->n_trees, kBlock, 0, (cudaStream_t)stream>>>(*b, grad_d, grad_nu_phi);
+    return check(cudaGetLastError(), "k_gradient");
+}
+
 extern "C" int laml_branch_terms(const laml_batch* b, void* stream) {
     int rc = validate(b);
     if (rc) return rc;
@@ -999,17 +1065,17 @@ extern "C" int laml_inside(const laml_batch* b, int32_t update_em, void* stream)
     return check(cudaGetLastError(), "k_tree_llh");
 }
 
-extern "C" int laml_outside(const laml_batch* b, int32_t want_post, void* stream) {
+extern "C" int laml_outside(const laml_batch* b, int32_t flags, void* stream) {
     int rc = validate(b);
     if (rc) return rc;
-    if (want_post && (!b->post0 || !b->post1)) {
+    if ((flags & LAML_OUT_POSTERIORS) && (!b->post0 || !b->post1)) {
         laml::set_error("laml_outside: want_post needs post0/post1 buffers");
         return LAML_ERR_ARG;
     }
     cudaStream_t st = (cudaStream_t)stream;
     Levels L;
     if ((rc = fetch_levels(*b, L, st))) return rc;
-    DISPATCH_G(*b, (outside_t<GG>(*b, want_post, st, L)));
+    DISPATCH_G(*b, (outside_t<GG>(*b, flags, st, L)));
 }
 
 extern "C" int laml_mstep(const laml_batch* b, int32_t rounds, int32_t flags, void* stream) {

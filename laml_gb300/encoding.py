@@ -29,7 +29,7 @@ class EncodedTree:
     child1: np.ndarray
     branch_length: np.ndarray   # float64[N] (0 where absent)
     has_length: np.ndarray      # bool[N]
-    labels: List[str]
+    labels: Optional[List[str]]
 
     @property
     def root(self) -> int:
@@ -63,6 +63,36 @@ def encode_newick(newick: str, leaf_order: Optional[Sequence[str]] = None) -> En
         e = raw.index(b"\0", o)
         labs.append(raw[o:e].decode())
     return EncodedTree(n_nodes, nl.value, par, c0, c1, bl, has.astype(bool), labs)
+
+
+def encode_newick_batch(newicks: Sequence[str], leaf_order: Sequence[str],
+                        n_threads: int = 0) -> List[EncodedTree]:
+    """Many trees over one leaf set in one C call (laml_newick_encode_batch);
+    the trees carry no labels (``labels`` is None)."""
+    L = N.lib()
+    T = len(newicks)
+    arr = (C.c_char_p * T)(*[s.encode() for s in newicks])
+    lo = (C.c_char_p * len(leaf_order))(*[str(x).encode() for x in leaf_order])
+    tot = N.i64()
+    N.check(L.laml_newick_batch_measure(T, arr, C.byref(tot)))
+    m = tot.value
+    par = np.empty(m, np.int32)
+    c0 = np.empty(m, np.int32)
+    c1 = np.empty(m, np.int32)
+    bl = np.empty(m, np.float64)
+    has = np.empty(m, np.uint8)
+    off = np.empty(T + 1, np.int64)
+    nl = np.empty(T, np.int32)
+    N.check(L.laml_newick_encode_batch(T, arr, lo, len(leaf_order), n_threads, N.ptr(off),
+                                       N.ptr(nl), N.ptr(par), N.ptr(c0), N.ptr(c1), N.ptr(bl),
+                                       N.ptr(has)))
+    out = []
+    hb = has.astype(bool)
+    for i in range(T):
+        a, b = int(off[i]), int(off[i + 1])
+        out.append(EncodedTree(b - a, int(nl[i]), par[a:b], c0[a:b], c1[a:b], bl[a:b], hb[a:b],
+                               None))
+    return out
 
 
 def char_matrix(rows: Sequence[Sequence], exact: bool = False) -> np.ndarray:

@@ -90,6 +90,8 @@ class DeviceBatch:
         self.datasets = list(datasets)
         sizes, plan = plan_batch(trees, tree_ds, datasets)
         self.sizes = sizes
+        self._node_base = plan["tr_node_base"].astype(np.int64)
+        self.last_d2h_bytes = 0
         nn = sizes["n_nodes"]
         nu = np.broadcast_to(np.asarray(nu, np.float64), (T,)).copy()
         phi = np.broadcast_to(np.asarray(phi, np.float64), (T,)).copy()
@@ -194,19 +196,43 @@ class DeviceBatch:
     def inside(self, update_em=False):
         N.check(N.lib().laml_inside(C.byref(self.b), int(update_em), self._s()))
 
-    def outside(self, want_post=False):
-        N.check(N.lib().laml_outside(C.byref(self.b), int(want_post), self._s()))
+    def outside(self, want_post=False, true_root=False):
+        flags = (N.OUT_POSTERIORS if want_post else 0) | (N.OUT_TRUE_ROOT if true_root else 0)
+        N.check(N.lib().laml_outside(C.byref(self.b), flags, self._s()))
 
-    def mstep(self, rounds=MSTEP_ROUNDS, polish=False):
+    def gradient(self):
+        """(grad_d [n_nodes], grad_nu [T], grad_phi [T]) as float64 device
+        tensors, from the counts of outside(true_root=True)."""
+        gd = torch.empty(self.sizes["n_nodes"], dtype=torch.float64, device=self.device)
+        gp = torch.empty(2 * self.T, dtype=torch.float64, device=self.device)
+        N.check(N.lib().laml_gradient(C.byref(self.b), gd.data_ptr(), gp.data_ptr(), self._s()))
+        return gd, gp[0::2], gp[1::2]
+
+    def set_params(self, d=None, nu=None, phi=None):
+        """Overwrite branch lengths (float64 [n_nodes]) / nu / phi ([T]) from
+        device or host tensors."""
+        if d is not None:
+            self.v["nd_d"].copy_(torch.as_tensor(d, dtype=torch.float64).reshape(-1))
+        if nu is not None:
+            self.v["tr_nu"].copy_(torch.as_tensor(nu, dtype=torch.float64).reshape(-1))
+        if phi is not None:
+            self.v["tr_phi"].copy_(torch.as_tensor(phi, dtype=torch.float64).reshape(-1))
+
+    def _polish(self, polish):
+        # the exact (EM_solver) model polishes its solves in FP64 by default
+        return (not self.compat) if polish is None else bool(polish)
+
+    def mstep(self, rounds=MSTEP_ROUNDS, polish=None):
         N.check(N.lib().laml_mstep(C.byref(self.b), rounds,
-                                   N.MSTEP_FP64_POLISH if polish else 0, self._s()))
+                                   N.MSTEP_FP64_POLISH if self._polish(polish) else 0,
+                                   self._s()))
 
     def em_iterations(self, iters, rounds=MSTEP_ROUNDS, rel_tol=None, max_iters=100000,
-                      persistent=True, polish=False):
+                      persistent=True, polish=None):
         tol = rel_tol if rel_tol is not None else (EM_STOP_COMPAT if self.compat else EM_STOP_EXACT)
         f = N.lib().laml_em_run if persistent else N.lib().laml_em_run_levels
         N.check(f(C.byref(self.b), iters, rounds, tol, max_iters,
-                  N.MSTEP_FP64_POLISH if polish else 0, self._s()))
+                  N.MSTEP_FP64_POLISH if self._polish(polish) else 0, self._s()))
 
     def check_device_error(self):
         err = int(self.work["error"].item())
@@ -241,13 +267,13 @@ class DeviceBatch:
             blk = cnt[base[p]:base[p] + t.num_nodes * ng * 8].reshape(t.num_nodes, ng, 8)
             s = blk.astype(np.float64).sum(axis=1)
             out[nb[p]:nb[p] + t.num_nodes] = s[:, :6]
-            lr.append(s[:, 6])
+            lr.append(s[:, 6] + s[:, 7])
         self._counts = out
         self._leaf_resp = lr
         return out, lr
 
     def run_em(self, rounds=MSTEP_ROUNDS, rel_tol=None, max_iters=100000, chunk=4,
-               persistent=True, polish=False):
+               persistent=True, polish=None):
         """EM to convergence for every tree: inside at the start parameters,
         then chunks of fused iterations until no tree is ACTIVE."""
         self.branch_terms()
@@ -267,15 +293,24 @@ class DeviceBatch:
         return self.results()
 
     def results(self) -> List[TreeResult]:
-        llh = self.work["tr_llh"].cpu().numpy()
-        it = self.work["tr_iter"].cpu().numpy()
-        st = self.work["tr_status"].cpu().numpy()
-        nu = self.v["tr_nu"].cpu().numpy()
-        phi = self.v["tr_phi"].cpu().numpy()
-        prev = self.work["tr_prev"].cpu().numpy().reshape(-1, 2)
-        d = self.v["nd_d"].cpu().numpy()
-        dprev = self.work["nd_d_prev"].cpu().numpy()
-        nb = self.v["tr_node_base"].cpu().numpy()
+        """Per-tree results, fetched with one device->host copy."""
+        T, nn = self.T, self.sizes["n_nodes"]
+        w, v = self.work, self.v
+        dev = torch.cat([w["tr_llh"].view(-1), v["tr_nu"].view(-1), v["tr_phi"].view(-1),
+                         w["tr_prev"].view(-1), v["nd_d"].view(-1), w["nd_d_prev"].view(-1),
+                         w["tr_iter"].to(torch.float64), w["tr_status"].to(torch.float64)])
+        host = dev.cpu().numpy()
+        self.last_d2h_bytes = host.nbytes
+        o = 0
+        llh = host[o:o + T]; o += T
+        nu = host[o:o + T]; o += T
+        phi = host[o:o + T]; o += T
+        prev = host[o:o + 2 * T].reshape(-1, 2); o += 2 * T
+        d = host[o:o + nn]; o += nn
+        dprev = host[o:o + nn]; o += nn
+        it = host[o:o + T].astype(np.int64); o += T
+        st = host[o:o + T].astype(np.int64)
+        nb = self._node_base
         out = []
         for p, t in enumerate(self.trees):
             sl = slice(nb[p], nb[p] + t.num_nodes)
