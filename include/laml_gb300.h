@@ -270,6 +270,26 @@ int laml_em_run(const laml_batch* b, int32_t iters, int32_t rounds, double rel_t
 int laml_em_run_levels(const laml_batch* b, int32_t iters, int32_t rounds, double rel_tol,
                        int32_t max_iters, int32_t flags, void* stream);
 
+/* The inside pass (per-tree log-likelihood into tr_llh, per-site values into
+ * llh_site / root_lr / root_x) without allocating any device memory.  No
+ * counterpart exists in the reference: it is for callers that must not call
+ * cudaMalloc -- a host runtime that owns the device memory budget and forbids
+ * a library from growing its footprint, or a latency-bound scoring loop that
+ * cannot afford the device-wide synchronisation cudaMalloc/cudaFree imply.
+ * The inside partials and per-(node, site) scalars (b->in_part, in_x, in_h,
+ * in_dot are ignored) live in one fixed 32 MiB array inside the library that
+ * every GPU which loads the library holds until the process exits; the caller
+ * passes the batch's plan sizes (laml_plan_sizes.part_floats / scalar_len) and
+ * a batch whose 4 * part_floats + 12 * scalar_len bytes (plus alignment)
+ * exceed 32 MiB is rejected with LAML_ERR_ARG.  The first call on each device
+ * looks up the array's device address (cudaGetSymbolAddress) with that device
+ * current; make that first call before any stream capture.  Every call shares
+ * the one array: calls whose work overlaps on the GPU race and must be
+ * serialised by the caller (one stream, or events).  Nothing in the array has
+ * to start at zero: the pass writes every word it reads. */
+int laml_inside_noalloc(const laml_batch* b, int64_t part_floats, int64_t scalar_len,
+                        void* stream);
+
 /* Message of the calling thread's last error ("" if none). */
 const char* laml_last_error(void);
 

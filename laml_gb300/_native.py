@@ -104,6 +104,7 @@ EXPORTS = {
     "laml_gradient": (i32, [P(Batch), vp, vp, vp]),
     "laml_em_run": (i32, [P(Batch), i32, i32, f64, i32, i32, vp]),
     "laml_em_run_levels": (i32, [P(Batch), i32, i32, f64, i32, i32, vp]),
+    "laml_inside_noalloc": (i32, [P(Batch), i64, i64, vp]),
     "laml_last_error": (C.c_char_p, []),
 }
 

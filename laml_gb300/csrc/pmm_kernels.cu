@@ -1102,3 +1102,93 @@ extern "C" int laml_em_run_levels(const laml_batch* b, int32_t iters, int32_t ro
     DISPATCH_G(*b, (em_levels_t<GG>(*b, iters, rounds, rel_tol, max_iters, flags,
                                     (cudaStream_t)stream)));
 }
+
+// ---------------------------------------------------------------------------
+// laml_inside_noalloc: the inside pass for callers that cannot allocate
+// device memory.  Its scratch (the inside partial rows and the per-(node,
+// site) scale exponents and prior-weighted sums) is a fixed array of the
+// library, not a caller buffer.
+// ---------------------------------------------------------------------------
+#include <mutex>
+
+namespace {
+
+constexpr size_t kNoAllocScratchBytes = size_t(32) << 20;   // 32 MiB per device
+// Device storage of the no-allocation entry point.  In host code this name is
+// only a stand-in: its device address comes from cudaGetSymbolAddress.
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
+
+std::mutex g_noalloc_mu;
+void* g_noalloc_addr[128] = {};   // device address of the scratch, per device ordinal
+
+size_t align256(size_t x) { return (x + 255) / 256 * 256; }
+
+template <int G>
+__global__ void __launch_bounds__(kBlock, LAML_MINB) k_inside_level(laml_batch b, int level) {
+    const int32_t o = b.in_level_off[level], e = b.in_level_off[level + 1];
+    const int gwarp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int nwarps = (gridDim.x * blockDim.x) >> 5;
+    for_items<G>(b, b.in_items + 2 * (int64_t)o, e - o, gwarp, nwarps, 0, false, false);
+}
+
+template <int G>
+int inside_noalloc_t(const laml_batch& b, cudaStream_t st) {
+    const unsigned grid = (unsigned)num_sms() * 8;
+    for (int l = 0; l < b.n_in_levels; ++l) {
+        k_inside_level<G><<<grid, kBlock, 0, st>>>(b, l);
+        int rc = check(cudaGetLastError(), "k_inside_level");
+        if (rc) return rc;
+    }
+    const int tb = (b.n_trees + 127) / 128;
+    k_tree_llh<<<tb, 128, 0, st>>>(b, 0, 0.0, 0);
+    return check(cudaGetLastError(), "k_tree_llh");
+}
+
+}  // namespace
+
+extern "C" int laml_inside_noalloc(const laml_batch* b, int64_t part_floats, int64_t scalar_len,
+                                   void* stream) {
+    int rc = validate(b);
+    if (rc) return rc;
+    if (part_floats < 0 || scalar_len < 0) {
+        laml::set_error("laml_inside_noalloc: negative size");
+        return LAML_ERR_ARG;
+    }
+    const size_t need = align256((size_t)part_floats * sizeof(float)) +
+                        3 * align256((size_t)scalar_len * sizeof(float));
+    if (need > kNoAllocScratchBytes) {
+        laml::set_error("laml_inside_noalloc: the batch needs " + std::to_string(need) +
+                        " bytes of scratch; the library's fixed scratch holds " +
+                        std::to_string(kNoAllocScratchBytes) + " bytes (use laml_inside)");
+        return LAML_ERR_ARG;
+    }
+    int dev = 0;
+    if ((rc = check(cudaGetDevice(&dev), "cudaGetDevice"))) return rc;
+    if (dev < 0 || dev >= 128) {
+        laml::set_error("laml_inside_noalloc: device ordinal out of range");
+        return LAML_ERR_ARG;
+    }
+    void* base = nullptr;
+    {
+        std::lock_guard<std::mutex> lock(g_noalloc_mu);
+        if (!g_noalloc_addr[dev]) {
+            // once per device, with that device current
+            void* p = nullptr;
+            if ((rc = check(cudaGetSymbolAddress(&p, g_noalloc_scratch), "cudaGetSymbolAddress")))
+                return rc;
+            g_noalloc_addr[dev] = p;
+        }
+        base = g_noalloc_addr[dev];
+    }
+    unsigned char* s = static_cast<unsigned char*>(base);
+    laml_batch bb = *b;
+    bb.in_part = reinterpret_cast<float*>(s);
+    s += align256((size_t)part_floats * sizeof(float));
+    bb.in_x = reinterpret_cast<int32_t*>(s);
+    s += align256((size_t)scalar_len * sizeof(float));
+    bb.in_h = reinterpret_cast<int32_t*>(s);
+    s += align256((size_t)scalar_len * sizeof(float));
+    bb.in_dot = reinterpret_cast<float*>(s);
+    cudaStream_t st = (cudaStream_t)stream;
+    DISPATCH_G(bb, (inside_noalloc_t<GG>(bb, st)));
+}
