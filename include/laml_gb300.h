@@ -150,7 +150,7 @@ typedef struct laml_plan_output {
     int32_t* in_level_off;   /* [n_in_levels + 1] */
     int32_t* in_items;       /* [2 * n_in_items] (node, group), inside by height */
     int32_t* out_level_off;  /* [n_out_levels + 1] */
-    int32_t* out_items;      /* [2 * n_out_items], outside by depth >= 1 */
+    int32_t* out_items;      /* [2 * n_out_items] (internal parent, group), by parent depth */
     int32_t* root_items;     /* [2 * n_root_items] */
 } laml_plan_output;
 

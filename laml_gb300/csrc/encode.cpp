@@ -627,12 +627,13 @@ extern "C" int laml_plan_measure(const laml_plan_input* in, laml_plan_sizes* sz)
         if (d < 0 || d >= in->n_datasets) { set_error("plan: bad dataset id"); return LAML_ERR_ARG; }
         TreeLevels L;
         int root;
-        int rc = tree_levels(N, n, in->child0 + nb, in->child1 + nb, L, &root);
+        const int32_t* c0 = in->child0 + nb;
+        int rc = tree_levels(N, n, c0, in->child1 + nb, L, &root);
         if (rc) return rc;
         int NG = in->ds_groups[d], Kp = in->ds_sites_pad[d];
         for (int u = 0; u < N; ++u) {
             hmax = std::max(hmax, L.height[u]);
-            dmax = std::max(dmax, L.depth[u]);
+            if (c0[u] >= 0) dmax = std::max(dmax, L.depth[u] + 1);   // levels of internal parents
         }
         sz->n_nodes += N;
         sz->part_floats += (int64_t)(N - n) * in->ds_row_len[d];
@@ -641,7 +642,7 @@ extern "C" int laml_plan_measure(const laml_plan_input* in, laml_plan_sizes* sz)
         sz->count_floats += (int64_t)N * NG * 8;
         sz->post_len += (int64_t)N * Kp;
         sz->n_in_items += (int64_t)(N - n) * NG;
-        sz->n_out_items += (int64_t)(N - 1) * NG;
+        sz->n_out_items += (int64_t)(N - n) * NG;
         sz->n_root_items += NG;
         nb += N;
     }
@@ -695,7 +696,7 @@ extern "C" int laml_plan_fill(const laml_plan_input* in, laml_plan_output* o) {
                 o->nd_srow[g] = sb + (int64_t)(u - n) * Kp;
                 in_lv[L.height[u]].push_back((int)g);
             }
-            if (L.depth[u] >= 1) out_lv[L.depth[u]].push_back((int)g);
+            if (u >= n) out_lv[L.depth[u] + 1].push_back((int)g);   // outside by parent depth
         }
         pb += (int64_t)(N - n) * R;
         sb += (int64_t)(N - n) * Kp;

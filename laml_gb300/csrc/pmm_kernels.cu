@@ -366,6 +366,170 @@ __device__ void outside_item(const laml_batch& b, int v, int g, int lane, bool a
     }
 }
 
+// ---------------------------------------------------------------------------
+// outside by parent: one internal node u, one site -> the outside rows and
+// the expected counts of BOTH children v, w.  For child v the input is
+// x^v = out[u] * E[w] (E = edge-inside), for w it is x^w = out[u] * E[v], so
+// out[u] and each child's inside row are read once for the pair.
+// ---------------------------------------------------------------------------
+struct ChildOut {
+    float x0, xs, sumx, dot, mx;
+    int X;
+    float* orow;
+};
+
+template <int G>
+__device__ __forceinline__ void child_finish(const laml_batch& b, const SiteCtx& s, int v,
+                                             const Child& cv, const float4& bv, ChildOut& o,
+                                             bool want_post, float lroot, int xroot, float* cnt) {
+    const float out0 = bv.x * o.x0;
+    const float outs = bv.w * (o.x0 + o.sumx) + o.xs;
+    if (o.orow) {
+        __stcg(o.orow, out0);
+        __stcg(o.orow + G, outs);
+        const int h = scale_exp(fmaxf(o.mx, fmaxf(out0, outs)));
+        const int64_t sv = __ldg(b.nd_srow + v) + s.site;
+        __stcg(b.out_h + sv, h);
+        __stcg(b.out_x + sv, o.X + h);
+    }
+    const int e = o.X + cv.X - xroot;
+    const float sc = (lroot > 0.f) ? ldexpf(1.f / lroot, e) : 0.f;
+    cnt[0] = o.x0 * cv.s0 * bv.x * sc;
+    cnt[1] = o.x0 * bv.y * cv.D * sc;
+    cnt[2] = o.x0 * cv.ss * bv.w * sc;
+    cnt[3] = bv.z * o.dot * sc;
+    cnt[4] = bv.w * cv.ss * o.sumx * sc;
+    cnt[5] = o.xs * cv.ss * sc;
+    cnt[6] = 0.f;
+    cnt[7] = 0.f;
+    if (cv.row == nullptr) {   // P(leaf silenced | D): '?' entries and observed entries apart
+        const float pl = cv.ss * outs * sc;
+        if (cv.code == -1) cnt[6] = pl; else cnt[7] = pl;
+    }
+    if (want_post && b.post0) {
+        const int64_t pb = __ldg(b.tr_post_base + s.tree) +
+                           (int64_t)(v - __ldg(b.tr_node_base + s.tree)) *
+                               __ldg(b.ds_sites_pad + s.ds) + s.site;
+        __stcg(b.post0 + pb, cv.s0 * out0 * sc);
+        __stcg(b.post1 + pb, cv.ss * outs * sc);
+    }
+}
+
+template <int G>
+__device__ __forceinline__ void write_counts(const laml_batch& b, int tree, int v, int g,
+                                             const float* c) {
+    const int ds = __ldg(b.tr_ds + tree);
+    const int NG = __ldg(b.ds_groups + ds);
+    float4* dst = reinterpret_cast<float4*>(
+        b.cnt_part + __ldg(b.tr_cnt_base + tree) +
+        ((int64_t)(v - __ldg(b.tr_node_base + tree)) * NG + g) * 8);
+    __stcg(dst, make_float4(c[0], c[1], c[2], c[3]));
+    __stcg(dst + 1, make_float4(c[4], c[5], c[6], c[7]));
+}
+
+template <int G>
+__device__ void outside_parent_item(const laml_batch& b, int u, int g, int lane, bool act,
+                                    bool want_post) {
+    float cv_[8] = {0, 0, 0, 0, 0, 0, 0, 0}, cw_[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    SiteCtx s;
+    const bool live = act && site_ctx<G>(b, u, g, lane, true, s);
+    const int v = act ? __ldg(b.nd_c0 + u) : 0, w = act ? __ldg(b.nd_c1 + u) : 0;
+    if (live) {
+        const Leaf L = leaf_params(b, s.tree);
+        const Child cv = load_child<G>(b, v, s.ds, s.site, s.goff, lane, s.qrow, s.sumq, L);
+        const Child cw = load_child<G>(b, w, s.ds, s.site, s.goff, lane, s.qrow, s.sumq, L);
+        const float4 bv = load_bt(b, v), bw = load_bt(b, w);
+        const int64_t su = __ldg(b.nd_srow + u) + s.site;
+        const float fo = pow2i(-__ldcg(b.out_h + su));
+        const int Xo = __ldcg(b.out_x + su);
+        const float* urow = b.out_part + __ldg(b.nd_prow + u) + s.goff + lane;
+        const float o0 = __ldcg(urow) * fo, os = __ldcg(urow + G) * fo;
+        const float ev0 = bv.x * cv.s0 + bv.y * cv.D + bv.w * cv.ss;
+        const float ew0 = bw.x * cw.s0 + bw.y * cw.D + bw.w * cw.ss;
+        ChildOut A, B;   // A: child v (uses E[w]), B: child w (uses E[v])
+        A.x0 = o0 * ew0; A.xs = os * cw.ss; A.X = Xo + cw.X;
+        B.x0 = o0 * ev0; B.xs = os * cv.ss; B.X = Xo + cv.X;
+        A.sumx = A.dot = A.mx = 0.f;
+        B.sumx = B.dot = B.mx = 0.f;
+        A.orow = cv.row ? b.out_part + __ldg(b.nd_prow + v) + s.goff + lane : nullptr;
+        B.orow = cw.row ? b.out_part + __ldg(b.nd_prow + w) + s.goff + lane : nullptr;
+        const float kv = bv.w * cv.ss, kw = bw.w * cw.ss;
+        const float pxa = bv.y * A.x0, pxb = bw.y * B.x0;
+        int j = 2;
+        for (; j + kChunk <= s.C; j += kChunk) {
+            float ou[kChunk], av[kChunk], aw[kChunk], qv[kChunk];
+#pragma unroll
+            for (int k = 0; k < kChunk; ++k) {
+                ou[k] = __ldcg(urow + (j + k) * G);
+                av[k] = child_val<G>(cv, j + k);
+                aw[k] = child_val<G>(cw, j + k);
+                qv[k] = __ldg(s.qrow + (j + k) * G);
+            }
+#pragma unroll
+            for (int k = 0; k < kChunk; ++k) {
+                const float o = ou[k] * fo;
+                const float xa = o * fmaf(bw.z, aw[k], kw);   // into v
+                const float xb = o * fmaf(bv.z, av[k], kv);   // into w
+                A.sumx += xa;
+                A.dot = fmaf(xa, av[k], A.dot);
+                B.sumx += xb;
+                B.dot = fmaf(xb, aw[k], B.dot);
+                if (A.orow) {
+                    const float r = fmaf(pxa, qv[k], bv.z * xa);
+                    __stcg(A.orow + (j + k) * G, r);
+                    A.mx = fmaxf(A.mx, r);
+                }
+                if (B.orow) {
+                    const float r = fmaf(pxb, qv[k], bw.z * xb);
+                    __stcg(B.orow + (j + k) * G, r);
+                    B.mx = fmaxf(B.mx, r);
+                }
+            }
+        }
+        for (; j < s.C; ++j) {
+            const float o = __ldcg(urow + j * G) * fo;
+            const float av = child_val<G>(cv, j), aw = child_val<G>(cw, j);
+            const float qj = __ldg(s.qrow + j * G);
+            const float xa = o * fmaf(bw.z, aw, kw);
+            const float xb = o * fmaf(bv.z, av, kv);
+            A.sumx += xa;
+            A.dot = fmaf(xa, av, A.dot);
+            B.sumx += xb;
+            B.dot = fmaf(xb, aw, B.dot);
+            if (A.orow) {
+                const float r = fmaf(pxa, qj, bv.z * xa);
+                __stcg(A.orow + j * G, r);
+                A.mx = fmaxf(A.mx, r);
+            }
+            if (B.orow) {
+                const float r = fmaf(pxb, qj, bw.z * xb);
+                __stcg(B.orow + j * G, r);
+                B.mx = fmaxf(B.mx, r);
+            }
+        }
+        const int64_t t = __ldg(b.tr_site_base + s.tree) + s.site;
+        const float lroot = __ldcg(b.root_lr + t);
+        const int xroot = __ldcg(b.root_x + t);
+        child_finish<G>(b, s, v, cv, bv, A, want_post, lroot, xroot, cv_);
+        child_finish<G>(b, s, w, cw, bw, B, want_post, lroot, xroot, cw_);
+    }
+#pragma unroll
+    for (int off = G / 2; off > 0; off >>= 1) {
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+            cv_[k] += __shfl_xor_sync(kFull, cv_[k], off);
+            cw_[k] += __shfl_xor_sync(kFull, cw_[k], off);
+        }
+    }
+    if (act && lane == 0) {
+        const int tree = __ldg(b.nd_tree + u);
+        if (__ldcg(b.tr_status + tree) == LAML_TREE_ACTIVE) {
+            write_counts<G>(b, tree, v, g, cv_);
+            write_counts<G>(b, tree, w, g, cw_);
+        }
+    }
+}
+
 // outside row of a root (calculations.py:172-175) + the root's posteriors
 template <int G>
 __device__ void root_init_item(const laml_batch& b, int r, int g, int lane, bool want_post) {
@@ -464,7 +628,9 @@ __device__ double solve_branch(double a, double bb, double c, double nu, double 
     if (branch_F<float>(af, bf, cf, nf, (float)hi, &t) >= 0.f) return hi;
     float ulo = logf((float)lo), uhi = logf((float)hi);
     float u = logf((float)fmin(fmax(d0, lo), hi));
-    for (int it = 0; it < 60; ++it) {
+    // warm-started from the previous d: a few Newton steps; the cap stops
+    // oscillation at the FP32 noise floor
+    for (int it = 0; it < 24; ++it) {
         float dF;
         const float f = branch_F<float>(af, bf, cf, nf, expf(u), &dF);
         if (f > 0.f) ulo = u; else uhi = u;
@@ -630,7 +796,7 @@ __device__ void mstep_tree(const laml_batch& b, int p, int rounds, double2* sh, 
             } else {
                 float wlo = logf((float)nlo), whi = logf((float)nhi);
                 float w = logf((float)fmin(fmax(nu, nlo), nhi));
-                for (int it = 0; it < 100; ++it) {
+                for (int it = 0; it < 20; ++it) {
                     const float x = expf(w);
                     const double2 S = sums(x, false);
                     const float H = (float)(-A * x + S.x);   // same sign as G
@@ -769,7 +935,7 @@ __device__ __forceinline__ void for_items(const laml_batch& b, const int32_t* it
         if (kind == 0) {
             if (act) inside_item<G>(b, node, g, lane, respect_status);
         } else if (kind == 1) {
-            outside_item<G>(b, node, g, lane, act, 0, want_post);
+            outside_parent_item<G>(b, node, g, lane, act, want_post);
         } else if (kind == 2) {
             if (act) root_init_item<G>(b, node, g, lane, want_post);
         } else {

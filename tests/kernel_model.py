@@ -276,7 +276,10 @@ class Model:
 
         for l in range(s["n_out_levels"]):
             for k in range(p["out_level_off"][l], p["out_level_off"][l + 1]):
-                acc(int(items[2 * k]), int(items[2 * k + 1]), 0)
+                # one item per internal parent: both children (outside_parent_item)
+                u, g = int(items[2 * k]), int(items[2 * k + 1])
+                acc(int(p["nd_c0"][u]), g, 0)
+                acc(int(p["nd_c1"][u]), g, 0)
         for k in range(s["n_root_items"]):
             acc(int(p["root_items"][2 * k]), int(p["root_items"][2 * k + 1]),
                 1 if self.compat else 2)
