@@ -161,6 +161,73 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def run_serving(args):
+    """Poisson stream of PMM requests (leaves log-uniform 200-10,000, sites
+    U(30, 300), M_k ~ U{5..100}, nu ~ U(0, 0.2), phi ~ U(0, 0.3), Yule trees)
+    through the continuous-batching server; half log-likelihood requests,
+    half EM-to-convergence requests.  A pool of seeded problems is drawn once
+    (generation is not timed); arrivals are replayed in real time."""
+    import numpy as np
+    import torch
+
+    from laml_gb300 import serving as S
+    from laml_gb300 import synth
+
+    rng = np.random.default_rng(args.seed + 7)
+    pool = []
+    for i in range(args.serve_pool):
+        n = int(round(math.exp(rng.uniform(math.log(200), math.log(10000)))))
+        K = int(rng.integers(30, 301))
+        nu, phi = float(rng.uniform(0, 0.2)), float(rng.uniform(0, 0.3))
+        w = synth.pmm_workload(n, K, 5, 100, 0.5, nu, phi, seed=args.seed + 1000 + i)
+        pool.append(w)
+    rate, dur = args.serve_rate, args.serve_seconds
+    t, arrivals = 0.0, []
+    while True:
+        t += rng.exponential(1.0 / rate)
+        if t > dur:
+            break
+        arrivals.append((t, int(rng.integers(len(pool))), "llh" if rng.random() < 0.5 else "em"))
+    srv = S.PMMServer(hbm_budget=args.serve_budget << 30)
+    # warm the kernels and the allocator with one small request of each kind
+    for kind in ("llh", "em"):
+        w = pool[0]
+        srv.submit(S.Request(w.newicks[0], w.rows, w.Q, w.leaf_order, kind=kind)).result()
+    futs = []
+    t0 = time.perf_counter()
+    with Clocks(0) as clk:
+        for (ta, k, kind) in arrivals:
+            now = time.perf_counter() - t0
+            if ta > now:
+                time.sleep(ta - now)
+            w = pool[k]
+            futs.append((kind, srv.submit(S.Request(w.newicks[0], w.rows, w.Q, w.leaf_order,
+                                                    kind=kind))))
+        replies = [(kind, f.result()) for kind, f in futs]
+        t_end = time.perf_counter()
+    srv.close()
+    lat = np.array([r.latency for _, r in replies])
+    lat_em = np.array([r.latency for k, r in replies if k == "em"])
+    lat_llh = np.array([r.latency for k, r in replies if k == "llh"])
+    iters = sum(r.result.iterations for _, r in replies)
+    span = t_end - t0
+    line = {"metric": METRIC, "mode": "serving", "value": iters / span, "unit": UNIT,
+            "n_gpus": 1, "requests": len(replies), "offered_rate_per_s": rate,
+            "completed_per_s": len(replies) / span,
+            "p50_latency_s": float(np.percentile(lat, 50)),
+            "p99_latency_s": float(np.percentile(lat, 99)),
+            "p50_latency_em_s": float(np.percentile(lat_em, 50)) if len(lat_em) else None,
+            "p99_latency_em_s": float(np.percentile(lat_em, 99)) if len(lat_em) else None,
+            "p50_latency_llh_s": float(np.percentile(lat_llh, 50)) if len(lat_llh) else None,
+            "p99_latency_llh_s": float(np.percentile(lat_llh, 99)) if len(lat_llh) else None,
+            "higher_is_better": True, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": "Poisson requests, leaves log-U(200,10000), sites U(30,300), "
+                                   "M_k U{5..100}, nu U(0,0.2), phi U(0,0.3); half llh, half EM",
+                       "pool": len(pool), "seconds": dur, "hbm_budget_gb": args.serve_budget},
+            "clocks": clk.summary()}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -173,13 +240,23 @@ def main():
     ap.add_argument("--ref-trees", type=int, default=16)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
-    ap.add_argument("--levels", action="store_true",
-                    help="one launch per tree level instead of the persistent kernel")
+    ap.add_argument("--path", default="graph", choices=["graph", "persistent", "levels"],
+                    help="graph: a CUDA graph of the per-level launches of one EM iteration "
+                         "(one graph launch per step); persistent: one cooperative launch "
+                         "per step; levels: the per-level launches issued directly")
     ap.add_argument("--trees", type=int, default=512,
                     help="use the first N candidates (smaller cases for profiling)")
+    ap.add_argument("--serving", action="store_true",
+                    help="Poisson request stream through the continuous-batching server")
+    ap.add_argument("--serve-rate", type=float, default=200.0)
+    ap.add_argument("--serve-seconds", type=float, default=5.0)
+    ap.add_argument("--serve-pool", type=int, default=16)
+    ap.add_argument("--serve-budget", type=int, default=64, help="HBM budget in GiB")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
+    if args.serving:
+        return run_serving(args)
 
     import numpy as np
     import torch
@@ -208,8 +285,16 @@ def main():
     nodes = b.sizes["n_nodes"]
     K = b.datasets[0].n_sites
 
-    def step():
-        b.em_iterations(1, rel_tol=-1.0, max_iters=1 << 30, persistent=not args.levels)
+    if args.path == "graph":
+        with torch.cuda.stream(stream):
+            graph = b.em_graph(1, rel_tol=-1.0, max_iters=1 << 30, persistent=False)
+
+        def step():
+            b.launch_graph(graph)
+    else:
+        def step():
+            b.em_iterations(1, rel_tol=-1.0, max_iters=1 << 30,
+                            persistent=args.path == "persistent")
 
     for _ in range(args.warmup):
         step()
@@ -285,14 +370,17 @@ def main():
             "node_site_updates_per_s": nsu,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": None,
-                         "kernel": "k_items (per level)" if args.levels else "k_em_persistent",
+                         "kernel": {"graph": "EM-iteration graph (k_items per level, k_mstep)",
+                                    "persistent": "k_em_persistent",
+                                    "levels": "k_items per level, k_mstep"}[args.path],
                          "bytes_per_launch": bytes_it,
                          "peak_kind": peak_kind},
             "e2e": e2e,
             "cpu_baseline": cpu,
             "clocks": clk.summary(),
-            "gpu_launches": args.steps * (1 if not args.levels else
+            "gpu_launches": args.steps * (1 if args.path == "persistent" else
                                           b.sizes["n_in_levels"] + b.sizes["n_out_levels"] + 4),
+            "path": args.path,
             "wall_s_timed": t1 - t0,
             "llh_mean": float(np.mean(llh_now)),
         }

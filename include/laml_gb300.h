@@ -200,6 +200,10 @@ typedef struct laml_batch {
     float *post0, *post1;          /* [post_len] or NULL */
     /* schedule */
     const int32_t *in_level_off, *in_items, *out_level_off, *out_items, *root_items;
+    /* optional HOST copies of in_level_off / out_level_off: when set, the
+     * per-level entry points launch without reading the offsets back from the
+     * device (no stream synchronisation) */
+    const int32_t *h_in_level_off, *h_out_level_off;
     /* control */
     uint32_t* barrier;             /* 2 words, zeroed by the library before each persistent launch */
     int32_t* error;                /* 1 word: 0 or a negative LAML_ERR_* set on the device */
@@ -289,6 +293,17 @@ int laml_em_run_levels(const laml_batch* b, int32_t iters, int32_t rounds, doubl
  * to start at zero: the pass writes every word it reads. */
 int laml_inside_noalloc(const laml_batch* b, int64_t part_floats, int64_t scalar_len,
                         void* stream);
+
+/* Capture `iters` EM iterations (as laml_em_run, or as laml_em_run_levels when
+ * `persistent` = 0, which needs h_in_level_off / h_out_level_off) into a CUDA
+ * graph bound to the buffers of `b`; laml_graph_launch replays it on a stream
+ * (one graph launch per call).  The graph must be destroyed before the
+ * batch's buffers are freed.  Replaces the per-iteration dispatch of the
+ * reference's host EM loop (fast_em/laml.py:153-192). */
+int laml_em_graph_create(const laml_batch* b, int32_t iters, int32_t rounds, double rel_tol,
+                         int32_t max_iters, int32_t flags, int32_t persistent, void** graph);
+int laml_graph_launch(void* graph, void* stream);
+void laml_graph_destroy(void* graph);
 
 /* Message of the calling thread's last error ("" if none). */
 const char* laml_last_error(void);

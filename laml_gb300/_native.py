@@ -77,7 +77,8 @@ BATCH_FIELDS = [
     ("out_x", vp), ("out_h", vp), ("llh_site", vp), ("root_lr", vp), ("root_x", vp),
     ("cnt_part", vp), ("post0", vp), ("post1", vp),
     ("in_level_off", vp), ("in_items", vp), ("out_level_off", vp), ("out_items", vp),
-    ("root_items", vp), ("barrier", vp), ("error", vp),
+    ("root_items", vp), ("h_in_level_off", vp), ("h_out_level_off", vp),
+    ("barrier", vp), ("error", vp),
 ]
 
 
@@ -105,6 +106,9 @@ EXPORTS = {
     "laml_em_run": (i32, [P(Batch), i32, i32, f64, i32, i32, vp]),
     "laml_em_run_levels": (i32, [P(Batch), i32, i32, f64, i32, i32, vp]),
     "laml_inside_noalloc": (i32, [P(Batch), i64, i64, vp]),
+    "laml_em_graph_create": (i32, [P(Batch), i32, i32, f64, i32, i32, i32, P(vp)]),
+    "laml_graph_launch": (i32, [vp, vp]),
+    "laml_graph_destroy": (None, [vp]),
     "laml_last_error": (C.c_char_p, []),
 }
 

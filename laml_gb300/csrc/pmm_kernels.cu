@@ -29,6 +29,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <string>
@@ -584,6 +585,25 @@ __device__ __forceinline__ double2 block_sum2(double a, double c, double2* sh) {
     return r;
 }
 
+__device__ __forceinline__ float2 block_sum2f(float a, float c, double2* shd) {
+    float2* sh = reinterpret_cast<float2*>(shd);
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+        a += __shfl_xor_sync(kFull, a, off);
+        c += __shfl_xor_sync(kFull, c, off);
+    }
+    const int wid = threadIdx.x >> 5, ln = threadIdx.x & 31;
+    __syncthreads();
+    if (ln == 0) sh[wid] = make_float2(a, c);
+    __syncthreads();
+    float2 r = make_float2(0.f, 0.f);
+    for (int k = 0; k < (int)(blockDim.x >> 5); ++k) {
+        r.x += sh[k].x;
+        r.y += sh[k].y;
+    }
+    return r;
+}
+
 __device__ float4 branch_terms_of(double d, double nu, int compat) {
     // FP32 is the storage precision of the terms: compute them in FP32
     const float df = (float)d, nf = (float)nu, nd = df * nf;
@@ -616,6 +636,27 @@ __device__ __forceinline__ T branch_F(T a, T b, T c, T nu, T d, T* dFdu) {
     }
     *dFdu = -ds / d;
     return -a + s / d;
+}
+
+// FP32 safeguarded Newton in log d on [lo, hi] from the previous value.
+__device__ float solve_branch_f(float a, float bb, float c, float nu, float d0, float lo,
+                                float hi) {
+    float t;
+    if (branch_F<float>(a, bb, c, nu, lo, &t) <= 0.f) return lo;
+    if (branch_F<float>(a, bb, c, nu, hi, &t) >= 0.f) return hi;
+    float ulo = logf(lo), uhi = logf(hi);
+    float u = logf(fminf(fmaxf(d0, lo), hi));
+    for (int it = 0; it < 24; ++it) {
+        float dF;
+        const float f = branch_F<float>(a, bb, c, nu, expf(u), &dF);
+        if (f > 0.f) ulo = u; else uhi = u;
+        float un = u - f / dF;
+        if (!(un > ulo && un < uhi)) un = 0.5f * (ulo + uhi);
+        const bool done = fabsf(un - u) <= 2e-6f * fmaxf(1.f, fabsf(u)) || uhi - ulo < 1e-6f;
+        u = un;
+        if (done) break;
+    }
+    return fminf(fmaxf(expf(u), lo), hi);
 }
 
 // Safeguarded Newton in log d on [lo, hi]: FP32 iterations from the previous
@@ -678,34 +719,41 @@ __device__ void mstep_tree(const laml_batch& b, int p, int rounds, double2* sh, 
     }
     // 1. counts summed over site groups (EM_solver.py:342-345 normalisation in
     //    the exact model), d saved
-    double lr = 0.0, lro = 0.0;
+    // (FP32 accumulation: the FP64 pipe of this part is narrow)
+    float lr = 0.f, lro = 0.f;
     for (int v = threadIdx.x; v < N; v += blockDim.x) {
-        double c[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+        float c[8] = {0, 0, 0, 0, 0, 0, 0, 0};
         const float4* src = reinterpret_cast<const float4*>(b.cnt_part + cb + (int64_t)v * NG * 8);
         for (int g = 0; g < NG; ++g) {
             const float4 x = __ldcg(src + 2 * g), z = __ldcg(src + 2 * g + 1);
             c[0] += x.x; c[1] += x.y; c[2] += x.z; c[3] += x.w;
             c[4] += z.x; c[5] += z.y; c[6] += z.z; c[7] += z.w;
         }
-        if (!compat) {
-            double t = 0.0;
-#pragma unroll
-            for (int k = 0; k < 5; ++k) { c[k] = fmax(c[k], kEpsS); t += c[k]; }
-#pragma unroll
-            for (int k = 0; k < 5; ++k) c[k] = c[k] / t * K;
-        }
         double* dst = b.nd_cnt + (int64_t)(base + v) * 6;
+        if (!compat) {
+            double cd[5], t = 0.0;
 #pragma unroll
-        for (int k = 0; k < 6; ++k) __stcg(dst + k, c[k]);
-        C4[v] = make_float4((float)c[0], (float)(c[0] + c[1] + c[3]), (float)c[1],
-                            (float)(c[2] + c[4]));
+            for (int k = 0; k < 5; ++k) { cd[k] = fmax((double)c[k], kEpsS); t += cd[k]; }
+#pragma unroll
+            for (int k = 0; k < 5; ++k) {
+                cd[k] = cd[k] / t * K;
+                __stcg(dst + k, cd[k]);
+                c[k] = (float)cd[k];
+            }
+            __stcg(dst + 5, (double)c[5]);
+        } else {
+#pragma unroll
+            for (int k = 0; k < 6; ++k) __stcg(dst + k, (double)c[k]);
+        }
+        C4[v] = make_float4(c[0], c[0] + c[1] + c[3], c[1], c[2] + c[4]);
         const double d = __ldcg(b.nd_d + base + v);
         __stcg(b.nd_d_prev + base + v, d);
         Dd[v] = (float)d;
         lr += c[6];
         lro += c[7];
     }
-    const double2 LRs = block_sum2(lr, lro, sh);   // also orders the staging writes
+    const float2 LRf = block_sum2f(lr, lro, sh);   // also orders the staging writes
+    const double2 LRs = make_double2((double)LRf.x, (double)LRf.y);
     const double LR = LRs.x + LRs.y;
     if (threadIdx.x == 0) {
         b.tr_prev[2 * p] = nu;
@@ -730,62 +778,69 @@ __device__ void mstep_tree(const laml_batch& b, int p, int rounds, double2* sh, 
     for (int r = 0; r < R; ++r) {
         const bool last = r == R - 1;
         const bool use_s = compat || nu > kEpsNu;
+        const float nuf = (float)nu;
         for (int v = threadIdx.x; v < N; v += blockDim.x) {
             if (!__ldg(b.nd_mask + base + v)) continue;
-            double a, bb, cs;
             if (last && polish) {   // the FP64 counts for the polished solve
                 const double* c = b.nd_cnt + (int64_t)(base + v) * 6;
                 const double c0 = __ldcg(c), c1 = __ldcg(c + 1), c2 = __ldcg(c + 2),
                              c3 = __ldcg(c + 3), c4 = __ldcg(c + 4);
-                a = c0 + nu * (c0 + c1 + c3);
-                bb = c1;
-                cs = use_s ? c2 + c4 : 0.0;
+                const double dn = solve_branch(c0 + nu * (c0 + c1 + c3), c1,
+                                               use_s ? c2 + c4 : 0.0, nu, (double)Dd[v], dlo,
+                                               dhi, true);
+                Dd[v] = (float)dn;
+                __stcg(b.nd_d + base + v, dn);
             } else {
                 const float4 q = C4[v];
-                a = (double)q.x + nu * (double)q.y;
-                bb = q.z;
-                cs = use_s ? (double)q.w : 0.0;
+                const float dn = solve_branch_f(q.x + nuf * q.y, q.z, use_s ? q.w : 0.f, nuf,
+                                                Dd[v], (float)dlo, (float)dhi);
+                Dd[v] = dn;
+                if (last) __stcg(b.nd_d + base + v, (double)dn);
             }
-            const double dn = solve_branch(a, bb, cs, nu, (double)Dd[v], dlo, dhi, last && polish);
-            Dd[v] = (float)dn;
-            if (last) __stcg(b.nd_d + base + v, dn);
         }
         __syncthreads();
         if (!(fix & 1)) {
             // -A nu + sum_v c_v log(1 - e^{-nu d_v}); compat: every branch,
             // exact: the optimised branches (EM_solver.py:392-407)
-            double A = 0.0, Cs = 0.0;
+            float Af = 0.f, Csf = 0.f;
             for (int v = threadIdx.x; v < N; v += blockDim.x) {
                 if (!compat && !__ldg(b.nd_mask + base + v)) continue;
                 const float4 q = C4[v];
-                A += (double)q.y * (double)Dd[v];
-                Cs += q.w;
+                Af += q.y * Dd[v];
+                Csf += q.w;
             }
-            const double2 ac = block_sum2(A, Cs, sh);
-            A = ac.x;
+            const float2 acf = block_sum2f(Af, Csf, sh);
+            const double2 ac = make_double2((double)acf.x, (double)acf.y);
+            double A = ac.x;
             const double nlo = compat ? kCalcEps : 1e-30, nhi = compat ? 1.0 - kCalcEps : 1.0;
             // G(nu) = -A + S1 / nu,  dG/dlog nu = -S2 / nu,  S1 = sum c h(nu d),
             // S2 = sum c h k  (h, k as in branch_F)
             auto sums = [&](double x, bool fp64) {
-                double s1 = 0.0, s2 = 0.0;
-                for (int v = threadIdx.x; v < N; v += blockDim.x) {
-                    if (!compat && !__ldg(b.nd_mask + base + v)) continue;
-                    if (fp64) {
+                if (fp64) {
+                    double s1 = 0.0, s2 = 0.0;
+                    for (int v = threadIdx.x; v < N; v += blockDim.x) {
+                        if (!compat && !__ldg(b.nd_mask + base + v)) continue;
                         const double* c = b.nd_cnt + (int64_t)(base + v) * 6;
                         const double cc = __ldcg(c + 2) + __ldcg(c + 4);
                         if (cc <= 0.0) continue;
                         const double y = x * __ldcg(b.nd_d + base + v), h = y / expm1(y);
                         s1 += cc * h;
                         s2 += cc * h * (h + y);
-                    } else {
-                        const float cc = C4[v].w;
-                        if (cc <= 0.f) continue;
-                        const float y = (float)x * Dd[v], h = y / expm1f(y);
-                        s1 += (double)(cc * h);
-                        s2 += (double)(cc * h * (h + y));
                     }
+                    return block_sum2(s1, s2, sh);
                 }
-                return block_sum2(s1, s2, sh);
+                float s1 = 0.f, s2 = 0.f;
+                const float xf = (float)x;
+                for (int v = threadIdx.x; v < N; v += blockDim.x) {
+                    if (!compat && !__ldg(b.nd_mask + base + v)) continue;
+                    const float cc = C4[v].w;
+                    if (cc <= 0.f) continue;
+                    const float y = xf * Dd[v], h = y / expm1f(y);
+                    s1 += cc * h;
+                    s2 += cc * h * (h + y);
+                }
+                const float2 r = block_sum2f(s1, s2, sh);
+                return make_double2((double)r.x, (double)r.y);
             };
             if (ac.y <= 0.0) {
                 nu = compat ? nlo : 0.0;
@@ -833,10 +888,8 @@ __device__ void mstep_tree(const laml_batch& b, int p, int rounds, double2* sh, 
         b.tr_nu[p] = nu;
         b.tr_phi[p] = phi;
     }
-    for (int v = threadIdx.x; v < N; v += blockDim.x) {
-        const double d = __ldcg(b.nd_d + base + v);
-        reinterpret_cast<float4*>(b.nd_bt)[base + v] = branch_terms_of(d, nu, b.compat);
-    }
+    for (int v = threadIdx.x; v < N; v += blockDim.x)
+        reinterpret_cast<float4*>(b.nd_bt)[base + v] = branch_terms_of((double)Dd[v], nu, b.compat);
 }
 
 // per-tree log-likelihood (FP64 sum over sites) and the EM stopping rule
@@ -952,7 +1005,7 @@ __global__ void __launch_bounds__(kBlock, LAML_MINB) k_items(laml_batch b, const
     for_items<G>(b, items, n, gwarp, nwarps, kind, want_post != 0, respect_status != 0);
 }
 
-__global__ void __launch_bounds__(kBlock) k_mstep(laml_batch b, int rounds, int flags) {
+__global__ void __launch_bounds__(kBlock, 4) k_mstep(laml_batch b, int rounds, int flags) {
     __shared__ double2 sh[kBlock / 32];
     __shared__ float4 s_cnt[kMstepStage];
     __shared__ float s_d[kMstepStage];
@@ -1107,6 +1160,11 @@ struct Levels {
 int fetch_levels(const laml_batch& b, Levels& L, cudaStream_t st) {
     L.in.resize(b.n_in_levels + 1);
     L.out.resize(b.n_out_levels + 1);
+    if (b.h_in_level_off && b.h_out_level_off) {
+        std::copy(b.h_in_level_off, b.h_in_level_off + L.in.size(), L.in.begin());
+        std::copy(b.h_out_level_off, b.h_out_level_off + L.out.size(), L.out.begin());
+        return LAML_OK;
+    }
     int rc = check(cudaMemcpyAsync(L.in.data(), b.in_level_off, sizeof(int32_t) * L.in.size(),
                                    cudaMemcpyDeviceToHost, st), "level offsets");
     if (rc) return rc;
@@ -1186,6 +1244,11 @@ int em_persistent_t(const laml_batch& b, int iters, int rounds, double tol, int 
                  "k_em_persistent launch");
 }
 
+struct GraphHolder {
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+};
+
 #define DISPATCH_G(b, call)                                   \
     switch ((b).group_sites) {                                \
         case 8: { constexpr int GG = 8; return call; }        \
@@ -1258,6 +1321,65 @@ extern "C" int laml_em_run(const laml_batch* b, int32_t iters, int32_t rounds, d
     if (iters <= 0) return LAML_OK;
     DISPATCH_G(*b, (em_persistent_t<GG>(*b, iters, rounds, rel_tol, max_iters, flags,
                                         (cudaStream_t)stream)));
+}
+
+extern "C" int laml_em_graph_create(const laml_batch* b, int32_t iters, int32_t rounds,
+                                    double rel_tol, int32_t max_iters, int32_t flags,
+                                    int32_t persistent, void** graph) {
+    int rc = validate(b);
+    if (rc) return rc;
+    if (!graph || iters <= 0) {
+        laml::set_error("laml_em_graph_create: bad argument");
+        return LAML_ERR_ARG;
+    }
+    if (!persistent && (!b->h_in_level_off || !b->h_out_level_off)) {
+        laml::set_error("laml_em_graph_create: per-level capture needs the host level offsets");
+        return LAML_ERR_ARG;
+    }
+    cudaStream_t st;
+    if ((rc = check(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking), "stream"))) return rc;
+    GraphHolder* g = new GraphHolder();
+    rc = check(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal), "begin capture");
+    if (!rc) {
+        auto body = [&]() -> int {
+            if (persistent) {
+                DISPATCH_G(*b, (em_persistent_t<GG>(*b, iters, rounds, rel_tol, max_iters, flags, st)));
+            }
+            DISPATCH_G(*b, (em_levels_t<GG>(*b, iters, rounds, rel_tol, max_iters, flags, st)));
+        };
+        int brc = body();
+        cudaGraph_t gr = nullptr;
+        int erc = check(cudaStreamEndCapture(st, &gr), "end capture");
+        rc = brc ? brc : erc;
+        g->graph = gr;
+        if (!rc) rc = check(cudaGraphInstantiate(&g->exec, gr, 0), "graph instantiate");
+    }
+    cudaStreamDestroy(st);
+    if (rc) {
+        if (g->exec) cudaGraphExecDestroy(g->exec);
+        if (g->graph) cudaGraphDestroy(g->graph);
+        delete g;
+        return rc;
+    }
+    *graph = g;
+    return LAML_OK;
+}
+
+extern "C" int laml_graph_launch(void* graph, void* stream) {
+    if (!graph) {
+        laml::set_error("laml_graph_launch: null graph");
+        return LAML_ERR_ARG;
+    }
+    GraphHolder* g = static_cast<GraphHolder*>(graph);
+    return check(cudaGraphLaunch(g->exec, (cudaStream_t)stream), "graph launch");
+}
+
+extern "C" void laml_graph_destroy(void* graph) {
+    if (!graph) return;
+    GraphHolder* g = static_cast<GraphHolder*>(graph);
+    if (g->exec) cudaGraphExecDestroy(g->exec);
+    if (g->graph) cudaGraphDestroy(g->graph);
+    delete g;
 }
 
 extern "C" int laml_em_run_levels(const laml_batch* b, int32_t iters, int32_t rounds,

@@ -183,6 +183,11 @@ class DeviceBatch:
         if not want_post:
             b.post0 = None
             b.post1 = None
+        # host copies of the level offsets: per-level launches need no read-back
+        self._h_in_off = np.ascontiguousarray(plan["in_level_off"], np.int32)
+        self._h_out_off = np.ascontiguousarray(plan["out_level_off"], np.int32)
+        b.h_in_level_off = self._h_in_off.ctypes.data
+        b.h_out_level_off = self._h_out_off.ctypes.data
         self._stream_ptr = (stream.cuda_stream if stream is not None
                             else torch.cuda.current_stream(self.device).cuda_stream)
 
@@ -233,6 +238,32 @@ class DeviceBatch:
         f = N.lib().laml_em_run if persistent else N.lib().laml_em_run_levels
         N.check(f(C.byref(self.b), iters, rounds, tol, max_iters,
                   N.MSTEP_FP64_POLISH if self._polish(polish) else 0, self._s()))
+
+    def em_graph(self, iters=1, rounds=MSTEP_ROUNDS, rel_tol=None, max_iters=100000,
+                 persistent=False, polish=None):
+        """A CUDA graph of ``iters`` EM iterations on this batch (replay with
+        ``launch_graph``); cached per argument set."""
+        tol = rel_tol if rel_tol is not None else (EM_STOP_COMPAT if self.compat else EM_STOP_EXACT)
+        key = (iters, rounds, tol, max_iters, bool(persistent), self._polish(polish))
+        if not hasattr(self, "_graphs"):
+            self._graphs = {}
+        if key not in self._graphs:
+            h = C.c_void_p()
+            N.check(N.lib().laml_em_graph_create(
+                C.byref(self.b), iters, rounds, tol, max_iters,
+                N.MSTEP_FP64_POLISH if key[5] else 0, int(persistent), C.byref(h)))
+            self._graphs[key] = h
+        return self._graphs[key]
+
+    def launch_graph(self, g):
+        N.check(N.lib().laml_graph_launch(g, self._s()))
+
+    def __del__(self):
+        for g in getattr(self, "_graphs", {}).values():
+            try:
+                N.lib().laml_graph_destroy(g)
+            except Exception:
+                pass
 
     def check_device_error(self):
         err = int(self.work["error"].item())

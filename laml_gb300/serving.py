@@ -1,0 +1,272 @@
+"""Continuous-batching server for PMM likelihood / EM requests.
+
+Requests (a tree, its character matrix and priors, a kind -- "llh" for one
+log-likelihood, "em" for fastEM's EM to convergence -- and starting nu, phi)
+are encoded on the submitting thread (C++ encoders) and queued.  A scheduler
+thread admits queued requests into *cohorts* whenever cohort slots and HBM
+budget are free: a cohort is one DeviceBatch (any mix of tree sizes and
+site counts) on its own CUDA stream, driven in chunks of fused EM iterations
+with per-level launches, so cohorts admitted at different times run
+concurrently on the device.  Encoded inputs, partials and EM state stay on
+the GPU for the life of the cohort; a request's future resolves as soon as
+its own tree leaves the ACTIVE state (other trees of its cohort keep
+iterating), and a cohort's memory returns to the budget when all its trees
+are done.
+
+Each tree's arithmetic does not depend on what else is in its batch, so a
+request's result is bitwise the same alone or in any mix.
+"""
+from __future__ import annotations
+
+import collections
+import threading
+import time
+from concurrent.futures import Future
+from dataclasses import dataclass, field
+from typing import Dict, List, Optional
+
+import numpy as np
+import torch
+
+from . import _native as N
+from .encoding import EncodedDataset, EncodedTree, char_matrix, encode_dataset, encode_newick
+from .encoding import plan_batch
+from .engine import MSTEP_ROUNDS, DeviceBatch, TreeResult
+
+EPS = 1e-6
+
+
+@dataclass
+class Request:
+    newick: str
+    rows: Dict[str, list]
+    Q: List[dict]
+    leaf_order: Optional[List[str]] = None
+    kind: str = "em"              # "llh" or "em"
+    nu: float = 0.5
+    phi: float = 0.5
+
+
+@dataclass
+class Reply:
+    result: TreeResult
+    t_submit: float
+    t_admit: float
+    t_done: float
+
+    @property
+    def latency(self):
+        return self.t_done - self.t_submit
+
+
+@dataclass
+class _Job:
+    req: Request
+    tree: EncodedTree
+    ds: EncodedDataset
+    footprint: int
+    future: Future
+    t_submit: float
+    t_admit: float = 0.0
+
+
+@dataclass
+class _Cohort:
+    jobs: List[_Job]
+    batch: DeviceBatch
+    stream: torch.cuda.Stream
+    kind: str
+    footprint: int
+    event: torch.cuda.Event
+    done: np.ndarray = None
+    host_status: torch.Tensor = None
+
+
+def footprint_bytes(tree: EncodedTree, ds: EncodedDataset) -> int:
+    """Device bytes a single-tree batch of this request holds."""
+    sizes, _ = plan_batch([tree], [0], [ds])
+    nn = sizes["n_nodes"]
+    return int(8 * sizes["part_floats"] + 20 * sizes["scalar_len"] + 4 * sizes["count_floats"]
+               + 200 * nn + ds.codes.nbytes + 4 * ds.row_len + 64 * ds.n_sites_pad
+               + 16 * sizes["n_in_items"] + 16 * sizes["n_out_items"])
+
+
+class PMMServer:
+    def __init__(self, device="cuda", hbm_budget: int = 64 << 30, max_cohort: int = 256,
+                 max_cohorts: int = 4, group_sites: int = 8, rounds: int = MSTEP_ROUNDS,
+                 chunk: int = 2, max_iters: int = 100000):
+        self.device = torch.device(device)
+        self.budget = hbm_budget
+        self.max_cohort = max_cohort
+        self.max_cohorts = max_cohorts
+        self.G = group_sites
+        self.rounds = rounds
+        self.chunk = chunk
+        self.max_iters = max_iters
+        self._pending: collections.deque = collections.deque()
+        self._lock = threading.Lock()
+        self._wake = threading.Event()
+        self._active: List[_Cohort] = []
+        self._used = 0
+        self._closing = False
+        self._streams = [torch.cuda.Stream(self.device) for _ in range(max_cohorts)]
+        self._free_streams = list(self._streams)
+        self.error: Optional[BaseException] = None
+        self._thread = threading.Thread(target=self._run, daemon=True)
+        self._thread.start()
+
+    # -- client side ------------------------------------------------------
+    def submit(self, req: Request) -> Future:
+        t0 = time.perf_counter()
+        lo = req.leaf_order
+        tree = encode_newick(req.newick, lo)
+        order = lo if lo is not None else tree.labels[:tree.num_leaves]
+        ds = encode_dataset(char_matrix([req.rows[c] for c in order]), req.Q, compat=True,
+                            group_sites=self.G)
+        fp = footprint_bytes(tree, ds)
+        if fp > self.budget:
+            raise ValueError(f"request needs {fp} bytes of HBM, the budget is {self.budget}")
+        fut: Future = Future()
+        with self._lock:
+            self._pending.append(_Job(req, tree, ds, fp, fut, t0))
+        self._wake.set()
+        return fut
+
+    def close(self, wait: bool = True):
+        self._closing = True
+        self._wake.set()
+        if wait:
+            self._thread.join()
+        if self.error is not None:
+            raise self.error
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+        return False
+
+    # -- scheduler ----------------------------------------------------------
+    def _admit(self):
+        while self._free_streams:
+            with self._lock:
+                if not self._pending:
+                    return
+                kind = self._pending[0].req.kind
+                jobs, used = [], 0
+                rest = collections.deque()
+                while self._pending and len(jobs) < self.max_cohort:
+                    j = self._pending.popleft()
+                    if j.req.kind == kind and self._used + used + j.footprint <= self.budget:
+                        jobs.append(j)
+                        used += j.footprint
+                    else:
+                        rest.append(j)
+                        if j.req.kind == kind:
+                            break          # FIFO within a kind: wait for memory
+                rest.extend(self._pending)
+                self._pending = rest
+            if not jobs:
+                return
+            self._used += used
+            self._launch(jobs, kind, used)
+
+    def _launch(self, jobs: List[_Job], kind: str, used: int):
+        stream = self._free_streams.pop()
+        now = time.perf_counter()
+        for j in jobs:
+            j.t_admit = now
+        with torch.cuda.stream(stream):
+            nu = np.clip([j.req.nu for j in jobs], EPS, 1 - EPS)
+            phi = np.clip([j.req.phi for j in jobs], EPS, 1 - EPS)
+            d = [np.maximum(j.tree.branch_length, EPS) for j in jobs]
+            b = DeviceBatch([j.ds for j in jobs], [j.tree for j in jobs], list(range(len(jobs))),
+                            d, nu, phi, compat=True, device=self.device, stream=stream)
+            b.branch_terms()
+            b.inside(update_em=True)
+            if kind == "em":
+                b.em_iterations(self.chunk, rounds=self.rounds, max_iters=self.max_iters,
+                                persistent=False)
+            host = torch.empty(len(jobs), dtype=torch.int32, pin_memory=True)
+            host.copy_(b.work["tr_status"], non_blocking=True)
+            ev = torch.cuda.Event()
+            ev.record(stream)
+        c = _Cohort(jobs, b, stream, kind, used, ev, np.zeros(len(jobs), bool), host)
+        self._active.append(c)
+
+    def _progress(self, c: _Cohort) -> bool:
+        """Returns True when the cohort is finished."""
+        if not c.event.query():
+            return False
+        b = c.batch
+        now = time.perf_counter()
+        if c.kind == "llh":
+            with torch.cuda.stream(c.stream):
+                llh = b.work["tr_llh"].cpu().numpy()
+            for i, j in enumerate(c.jobs):
+                r = TreeResult(float(llh[i]), float(j.req.nu), float(j.req.phi), 0,
+                               N.TREE_CONVERGED, j.tree.branch_length.copy())
+                j.future.set_result(Reply(r, j.t_submit, j.t_admit, now))
+            return True
+        st = c.host_status.numpy()
+        newly = (~c.done) & (st != N.TREE_ACTIVE)
+        if newly.any():
+            with torch.cuda.stream(c.stream):
+                res = b.results()
+            for i in np.flatnonzero(newly):
+                j = c.jobs[i]
+                j.future.set_result(Reply(res[i], j.t_submit, j.t_admit, now))
+            c.done |= newly
+        if c.done.all():
+            return True
+        with torch.cuda.stream(c.stream):
+            b.em_iterations(self.chunk, rounds=self.rounds, max_iters=self.max_iters,
+                            persistent=False)
+            c.host_status.copy_(b.work["tr_status"], non_blocking=True)
+            c.event.record(c.stream)
+        return False
+
+    def _run(self):
+        try:
+            while True:
+                self._admit()
+                finished = [c for c in self._active if self._progress(c)]
+                for c in finished:
+                    self._active.remove(c)
+                    self._used -= c.footprint
+                    self._free_streams.append(c.stream)
+                    c.batch = None
+                with self._lock:
+                    idle = not self._pending and not self._active
+                if idle and self._closing:
+                    return
+                if not finished:
+                    self._wake.wait(0.0002)
+                    self._wake.clear()
+        except BaseException as ex:   # surface to every waiter
+            self.error = ex
+            with self._lock:
+                for j in self._pending:
+                    j.future.set_exception(ex)
+            for c in self._active:
+                for j in c.jobs:
+                    if not j.future.done():
+                        j.future.set_exception(ex)
+
+
+def run_alone(req: Request, group_sites: int = 8, rounds: int = MSTEP_ROUNDS,
+              device="cuda") -> TreeResult:
+    """The same request outside the server (for mix-vs-alone checks)."""
+    lo = req.leaf_order
+    tree = encode_newick(req.newick, lo)
+    order = lo if lo is not None else tree.labels[:tree.num_leaves]
+    ds = encode_dataset(char_matrix([req.rows[c] for c in order]), req.Q, compat=True,
+                        group_sites=group_sites)
+    b = DeviceBatch([ds], [tree], [0], [np.maximum(tree.branch_length, EPS)],
+                    [min(max(req.nu, EPS), 1 - EPS)], [min(max(req.phi, EPS), 1 - EPS)],
+                    compat=True, device=device)
+    if req.kind == "llh":
+        llh = float(b.log_likelihood()[0])
+        return TreeResult(llh, req.nu, req.phi, 0, N.TREE_CONVERGED, tree.branch_length.copy())
+    return b.run_em(rounds=rounds, persistent=False)[0]

@@ -36,9 +36,10 @@ def test_batch_struct_matches_header():
     """Field order of laml_batch in the ctypes mirror equals the header."""
     src = open(HEADER).read()
     body = src[src.index("typedef struct laml_batch {"):src.index("} laml_batch;")]
+    body = re.sub(r"/\*.*?\*/", "", body, flags=re.S)
     names = []
     for line in body.splitlines()[1:]:
-        line = line.split("/*")[0].strip()
+        line = line.strip()
         if not line:
             continue
         decl = line.rstrip(";")

@@ -161,3 +161,20 @@ def test_device_error_word_is_clear():
     b = PB.make_batch(w.newicks, w.rows, w.Q, w.leaf_order, compat=True)
     b.run_em(max_iters=20)
     assert int(b.work["error"].item()) == 0
+
+
+def test_graph_replay_equals_direct_launches():
+    w = _wl(seed=6, n=60, K=20, T=4)
+    a = PB.make_batch(w.newicks, w.rows, w.Q, w.leaf_order, compat=True)
+    c = PB.make_batch(w.newicks, w.rows, w.Q, w.leaf_order, compat=True)
+    for x in (a, c):
+        x.branch_terms()
+        x.inside(update_em=True)
+    g = a.em_graph(1, persistent=False)
+    for _ in range(6):
+        a.launch_graph(g)
+        c.em_iterations(1, persistent=False)
+    torch.cuda.synchronize()
+    for ra, rc in zip(a.results(), c.results()):
+        assert ra.llh == rc.llh and ra.iterations == rc.iterations
+        np.testing.assert_array_equal(ra.branch_lengths, rc.branch_lengths)
