@@ -126,6 +126,9 @@ typedef struct laml_plan_input {
     const int64_t* ds_row_len;     /* [D] */
     const int32_t* ds_group_base;  /* [D] offset of the dataset's groups in group_C */
     const int32_t* group_C;        /* [sum groups] */
+    const int32_t* ds_sites;       /* [D] real sites */
+    const int32_t* ds_leaves;      /* [D] rows of the dataset's code matrix */
+    const int32_t* group_off;      /* [sum groups] offset of each group in a row */
 } laml_plan_input;
 
 typedef struct laml_plan_sizes {
@@ -137,6 +140,7 @@ typedef struct laml_plan_sizes {
     int64_t post_len;      /* per-(node, site) posterior slots */
     int32_t n_in_levels, n_out_levels;
     int64_t n_in_items, n_out_items, n_root_items;
+    int64_t n_groups_total;
 } laml_plan_sizes;
 
 typedef struct laml_plan_output {
@@ -152,6 +156,16 @@ typedef struct laml_plan_output {
     int32_t* out_level_off;  /* [n_out_levels + 1] */
     int32_t* out_items;      /* [2 * n_out_items] (internal parent, group), by parent depth */
     int32_t* root_items;     /* [2 * n_root_items] */
+    /* item descriptors, 12 int32 per item, parallel to in_items / out_items:
+     * {u, v, w, tree | flags << 24}, {group, global group, srow(u), prow(u)/8},
+     * {ref(v), ref(w), srow(v), srow(w)} with ref = prow/8 for an internal
+     * child and the leaf row for a leaf; flags: 1 v is a leaf, 2 w is a leaf,
+     * 4 u is the root */
+    int32_t* in_desc;
+    int32_t* out_desc;
+    /* per global group, 8 int32: {group_off, first site (global), q offset,
+     * dataset}, {code offset, sites_pad, real sites, 0} */
+    int32_t* grp_desc;
 } laml_plan_output;
 
 int laml_plan_measure(const laml_plan_input* in, laml_plan_sizes* sizes);
@@ -200,6 +214,7 @@ typedef struct laml_batch {
     float *post0, *post1;          /* [post_len] or NULL */
     /* schedule */
     const int32_t *in_level_off, *in_items, *out_level_off, *out_items, *root_items;
+    const int32_t *in_desc, *out_desc, *grp_desc;   /* laml_plan_output's descriptors */
     /* optional HOST copies of in_level_off / out_level_off: when set, the
      * per-level entry points launch without reading the offsets back from the
      * device (no stream synchronisation) */

@@ -37,20 +37,22 @@ class DatasetInfo(C.Structure):
 class PlanInput(C.Structure):
     _fields_ = [("n_trees", i32), ("tree_nodes", vp), ("tree_leaves", vp), ("tree_dataset", vp),
                 ("child0", vp), ("child1", vp), ("n_datasets", i32), ("ds_groups", vp),
-                ("ds_sites_pad", vp), ("ds_row_len", vp), ("ds_group_base", vp), ("group_C", vp)]
+                ("ds_sites_pad", vp), ("ds_row_len", vp), ("ds_group_base", vp), ("group_C", vp),
+                ("ds_sites", vp), ("ds_leaves", vp), ("group_off", vp)]
 
 
 class PlanSizes(C.Structure):
     _fields_ = [("n_nodes", i64), ("part_floats", i64), ("scalar_len", i64), ("site_len", i64),
                 ("count_floats", i64), ("post_len", i64), ("n_in_levels", i32),
                 ("n_out_levels", i32), ("n_in_items", i64), ("n_out_items", i64),
-                ("n_root_items", i64)]
+                ("n_root_items", i64), ("n_groups_total", i64)]
 
 
 PLAN_OUT_FIELDS = ["tr_node_base", "tr_root", "tr_quirk", "tr_site_base", "tr_cnt_base",
                    "tr_post_base", "nd_tree", "nd_c0", "nd_c1", "nd_parent", "nd_sib",
                    "nd_leafrow", "nd_prow", "nd_srow", "in_level_off", "in_items",
-                   "out_level_off", "out_items", "root_items"]
+                   "out_level_off", "out_items", "root_items", "in_desc", "out_desc",
+                   "grp_desc"]
 
 
 class PlanOutput(C.Structure):
@@ -77,7 +79,8 @@ BATCH_FIELDS = [
     ("out_x", vp), ("out_h", vp), ("llh_site", vp), ("root_lr", vp), ("root_x", vp),
     ("cnt_part", vp), ("post0", vp), ("post1", vp),
     ("in_level_off", vp), ("in_items", vp), ("out_level_off", vp), ("out_items", vp),
-    ("root_items", vp), ("h_in_level_off", vp), ("h_out_level_off", vp),
+    ("root_items", vp), ("in_desc", vp), ("out_desc", vp), ("grp_desc", vp),
+    ("h_in_level_off", vp), ("h_out_level_off", vp),
     ("barrier", vp), ("error", vp),
 ]
 

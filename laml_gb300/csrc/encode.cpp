@@ -9,6 +9,8 @@
 #include <cstring>
 #include <string>
 #include <atomic>
+#include <climits>
+#include <cstdint>
 #include <thread>
 #include <unordered_map>
 #include <vector>
@@ -618,7 +620,10 @@ int tree_levels(int N, int n, const int32_t* c0, const int32_t* c1, TreeLevels& 
 }  // namespace
 
 extern "C" int laml_plan_measure(const laml_plan_input* in, laml_plan_sizes* sz) {
-    if (!in || !sz || in->n_trees <= 0) { set_error("plan: bad argument"); return LAML_ERR_ARG; }
+    if (!in || !sz || in->n_trees <= 0 || in->n_trees >= (1 << 24)) {
+        set_error("plan: bad argument (1 <= n_trees < 2^24)");
+        return LAML_ERR_ARG;
+    }
     std::memset(sz, 0, sizeof(*sz));
     int64_t nb = 0;
     int hmax = 0, dmax = 0;
@@ -648,6 +653,7 @@ extern "C" int laml_plan_measure(const laml_plan_input* in, laml_plan_sizes* sz)
     }
     sz->n_in_levels = hmax;
     sz->n_out_levels = dmax;
+    for (int d = 0; d < in->n_datasets; ++d) sz->n_groups_total += in->ds_groups[d];
     return LAML_OK;
 }
 
@@ -725,6 +731,66 @@ extern "C" int laml_plan_fill(const laml_plan_input* in, laml_plan_output* o) {
     };
     emit(in_lv, 1, H, o->in_level_off, o->in_items);
     emit(out_lv, 1, D, o->out_level_off, o->out_items);
+    // global group table and item descriptors
+    if (o->grp_desc || o->in_desc || o->out_desc) {
+        if (!in->ds_sites || !in->ds_leaves || !in->group_off) {
+            set_error("plan: descriptors need ds_sites, ds_leaves and group_off");
+            return LAML_ERR_ARG;
+        }
+        std::vector<int64_t> site_base(in->n_datasets), q_base(in->n_datasets),
+            code_base(in->n_datasets);
+        int64_t sb = 0, qb2 = 0, cb2 = 0;
+        for (int d = 0; d < in->n_datasets; ++d) {
+            site_base[d] = sb;
+            q_base[d] = qb2;
+            code_base[d] = cb2;
+            sb += in->ds_sites_pad[d];
+            qb2 += in->ds_row_len[d];
+            cb2 += (int64_t)in->ds_leaves[d] * in->ds_sites_pad[d];
+        }
+        if (qb2 >= INT32_MAX || cb2 >= INT32_MAX || sz.part_floats / 8 >= INT32_MAX ||
+            sz.scalar_len >= INT32_MAX) {
+            set_error("plan: batch too large for 32-bit descriptors");
+            return LAML_ERR_ARG;
+        }
+        if (o->grp_desc) {
+            for (int d = 0; d < in->n_datasets; ++d)
+                for (int g = 0; g < in->ds_groups[d]; ++g) {
+                    const int gi = in->ds_group_base[d] + g;
+                    const int G = in->ds_sites_pad[d] / in->ds_groups[d];
+                    int32_t* e = o->grp_desc + 8 * (int64_t)gi;
+                    e[0] = in->group_off[gi];
+                    e[1] = (int32_t)(site_base[d] + (int64_t)g * G);
+                    e[2] = (int32_t)(q_base[d] + in->group_off[gi]);
+                    e[3] = d;
+                    e[4] = (int32_t)code_base[d];
+                    e[5] = in->ds_sites_pad[d];
+                    e[6] = in->ds_sites[d];
+                    e[7] = 0;
+                }
+        }
+        auto ref = [&](int x) -> int32_t {
+            return o->nd_c0[x] < 0 ? o->nd_leafrow[x] : (int32_t)(o->nd_prow[x] / 8);
+        };
+        auto fill = [&](const int32_t* items, int64_t n_items, int32_t* desc) {
+            for (int64_t k = 0; k < n_items; ++k) {
+                const int u = items[2 * k], g = items[2 * k + 1];
+                const int tree = o->nd_tree[u];
+                const int d = in->tree_dataset[tree];
+                const int v = o->nd_c0[u], w = o->nd_c1[u];
+                int flags = (o->nd_c0[v] < 0 ? 1 : 0) | (o->nd_c0[w] < 0 ? 2 : 0) |
+                            (o->tr_root[tree] == u ? 4 : 0);
+                int32_t* e = desc + 12 * k;
+                e[0] = u; e[1] = v; e[2] = w; e[3] = tree | (flags << 24);
+                e[4] = g; e[5] = in->ds_group_base[d] + g;
+                e[6] = (int32_t)o->nd_srow[u]; e[7] = (int32_t)(o->nd_prow[u] / 8);
+                e[8] = ref(v); e[9] = ref(w);
+                e[10] = (int32_t)o->nd_srow[v]; e[11] = (int32_t)o->nd_srow[w];
+            }
+        };
+        if (o->in_desc) fill(o->in_items, sz.n_in_items, o->in_desc);
+        if (o->out_desc) fill(o->out_items, sz.n_out_items, o->out_desc);
+    }
     int64_t k = 0;
     for (int g = 0; g < maxNG; ++g)
         for (int p = 0; p < T; ++p) {

@@ -58,6 +58,9 @@ constexpr int kChunk = LAML_CHUNK;   // states loaded ahead per step of a state 
 #ifndef LAML_MINB
 #define LAML_MINB 4
 #endif
+#ifndef LAML_MINB_OUT
+#define LAML_MINB_OUT LAML_MINB   // resident blocks per SM asked of the outside kernel
+#endif
 constexpr int kMstepStage = 2048;    // branches of a tree staged in shared memory by the M-step
 
 // ---------------------------------------------------------------------------
@@ -531,6 +534,243 @@ __device__ void outside_parent_item(const laml_batch& b, int u, int g, int lane,
     }
 }
 
+// ---------------------------------------------------------------------------
+// Descriptor-driven items: every address an item needs comes from its 48-byte
+// descriptor and the per-group table, so the loads of an item form a chain of
+// three (descriptor -> scalars/rows/codes -> state loop) instead of six.
+// ---------------------------------------------------------------------------
+struct ItemDesc {
+    int u, v, w, tree, flags, g, gd, u_srow, u_prow8, v_ref, w_ref, v_srow, w_srow;
+};
+
+__device__ __forceinline__ ItemDesc load_desc(const int32_t* base, int64_t it) {
+    const int4* p = reinterpret_cast<const int4*>(base) + 3 * it;
+    const int4 A = __ldg(p), B = __ldg(p + 1), C = __ldg(p + 2);
+    ItemDesc d;
+    d.u = A.x; d.v = A.y; d.w = A.z;
+    d.tree = A.w & 0xffffff;
+    d.flags = (int)((unsigned)A.w >> 24);
+    d.g = B.x; d.gd = B.y; d.u_srow = B.z; d.u_prow8 = B.w;
+    d.v_ref = C.x; d.w_ref = C.y; d.v_srow = C.z; d.w_srow = C.w;
+    return d;
+}
+
+struct GroupCtx {
+    int code_base, kpad;
+};
+
+template <int G>
+__device__ __forceinline__ bool site_ctx_d(const laml_batch& b, const ItemDesc& d, int lane,
+                                           bool respect_status, SiteCtx& s, GroupCtx& gc) {
+    s.tree = d.tree;
+    if (respect_status && __ldcg(b.tr_status + s.tree) != LAML_TREE_ACTIVE) return false;
+    const int4* gp = reinterpret_cast<const int4*>(b.grp_desc) + 2 * d.gd;
+    const int4 G1 = __ldg(gp), G2 = __ldg(gp + 1);
+    s.site = d.g * G + lane;
+    if (s.site >= G2.z) return false;
+    s.goff = G1.x;
+    s.ds = G1.w;
+    const int sb = G1.y + lane;
+    s.C = __ldg(b.site_C + sb);
+    s.sumq = __ldg(b.site_sumq + sb);
+    s.qrow = b.q + G1.z + lane;
+    gc.code_base = G2.x;
+    gc.kpad = G2.y;
+    return true;
+}
+
+template <int G>
+__device__ __forceinline__ Child load_child_d(const laml_batch& b, bool leaf, int ref, int srow,
+                                              const SiteCtx& s, const GroupCtx& gc, int lane,
+                                              const Leaf& L) {
+    Child c;
+    c.e1 = L.e1;
+    c.ephi = L.ephi;
+    if (leaf) {
+        const int code = __ldg(b.codes + gc.code_base + (int64_t)ref * gc.kpad + s.site);
+        c.row = nullptr;
+        c.f = 1.f;
+        c.X = 0;
+        c.code = code;
+        c.s0 = code == 0 ? L.e1 : (code == -1 ? L.ephi : 0.f);
+        c.ss = code < 0 ? 1.f : L.es;
+        c.D = code >= 2 ? __ldg(s.qrow + code * G) * L.e1 : (code == -1 ? L.ephi * s.sumq : 0.f);
+    } else {
+        const int64_t si = (int64_t)srow + s.site;
+        c.row = b.in_part + (int64_t)ref * 8 + s.goff + lane;
+        const float r0 = __ldcg(c.row), r1 = __ldcg(c.row + G);   // rows before scalars: both in flight
+        const int h = __ldcg(b.in_h + si);
+        c.f = pow2i(-h);
+        c.X = __ldcg(b.in_x + si);
+        c.D = __ldcg(b.in_dot + si);
+        c.code = 0;
+        c.s0 = r0 * c.f;
+        c.ss = r1 * c.f;
+    }
+    return c;
+}
+
+template <int G>
+__device__ void inside_item_d(const laml_batch& b, const ItemDesc& d, int lane,
+                              bool respect_status) {
+    SiteCtx s;
+    GroupCtx gc;
+    if (!site_ctx_d<G>(b, d, lane, respect_status, s, gc)) return;
+    const Leaf L = leaf_params(b, s.tree);
+    const Child cv = load_child_d<G>(b, d.flags & 1, d.v_ref, d.v_srow, s, gc, lane, L);
+    const Child cw = load_child_d<G>(b, d.flags & 2, d.w_ref, d.w_srow, s, gc, lane, L);
+    const float4 bv = load_bt(b, d.v), bw = load_bt(b, d.w);
+    const float ev0 = bv.x * cv.s0 + bv.y * cv.D + bv.w * cv.ss;
+    const float ew0 = bw.x * cw.s0 + bw.y * cw.D + bw.w * cw.ss;
+    const float kv = bv.w * cv.ss, kw = bw.w * cw.ss;
+    float* row = b.in_part + (int64_t)d.u_prow8 * 8 + s.goff + lane;
+    const float s0 = ev0 * ew0, ss = cv.ss * cw.ss;
+    __stcg(row, s0);
+    __stcg(row + G, ss);
+    float mx = fmaxf(s0, ss), dot = 0.f;
+    int j = 2;
+    for (; j + kChunk <= s.C; j += kChunk) {
+        float av[kChunk], aw[kChunk], qv[kChunk];
+#pragma unroll
+        for (int k = 0; k < kChunk; ++k) {
+            av[k] = child_val<G>(cv, j + k);
+            aw[k] = child_val<G>(cw, j + k);
+            qv[k] = __ldg(s.qrow + (j + k) * G);
+        }
+#pragma unroll
+        for (int k = 0; k < kChunk; ++k) {
+            const float x = fmaf(bv.z, av[k], kv) * fmaf(bw.z, aw[k], kw);
+            __stcg(row + (j + k) * G, x);
+            dot = fmaf(qv[k], x, dot);
+            mx = fmaxf(mx, x);
+        }
+    }
+    for (; j < s.C; ++j) {
+        const float av = child_val<G>(cv, j), aw = child_val<G>(cw, j);
+        const float x = fmaf(bv.z, av, kv) * fmaf(bw.z, aw, kw);
+        __stcg(row + j * G, x);
+        dot = fmaf(__ldg(s.qrow + j * G), x, dot);
+        mx = fmaxf(mx, x);
+    }
+    const int h = scale_exp(mx);
+    const float f = pow2i(-h);
+    const int X = cv.X + cw.X + h;
+    const int64_t sr = (int64_t)d.u_srow + s.site;
+    __stcg(b.in_h + sr, h);
+    __stcg(b.in_x + sr, X);
+    __stcg(b.in_dot + sr, dot * f);
+    if (d.flags & 4) {
+        // the root edge from a progenitor in state 0 (calculations.py:270-276, 504)
+        const float4 br = load_bt(b, d.u);
+        const float lr = br.x * (s0 * f) + br.y * (dot * f) + br.w * (ss * f);
+        const int64_t t = __ldg(b.tr_site_base + s.tree) + s.site;
+        __stcg(b.root_lr + t, lr);
+        __stcg(b.root_x + t, X);
+        __stcg(b.llh_site + t, (double)logf(lr) + (double)X * kLn2);
+    }
+}
+
+template <int G>
+__device__ void outside_item_d(const laml_batch& b, const ItemDesc& d, int lane, bool act,
+                               bool want_post) {
+    float cv_[8] = {0, 0, 0, 0, 0, 0, 0, 0}, cw_[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    SiteCtx s;
+    GroupCtx gc;
+    const bool live = act && site_ctx_d<G>(b, d, lane, true, s, gc);
+    if (live) {
+        const Leaf L = leaf_params(b, s.tree);
+        const Child cv = load_child_d<G>(b, d.flags & 1, d.v_ref, d.v_srow, s, gc, lane, L);
+        const Child cw = load_child_d<G>(b, d.flags & 2, d.w_ref, d.w_srow, s, gc, lane, L);
+        const float4 bv = load_bt(b, d.v), bw = load_bt(b, d.w);
+        const int64_t su = (int64_t)d.u_srow + s.site;
+        const float* urow = b.out_part + (int64_t)d.u_prow8 * 8 + s.goff + lane;
+        const float u0 = __ldcg(urow), u1 = __ldcg(urow + G);
+        const float fo = pow2i(-__ldcg(b.out_h + su));
+        const int Xo = __ldcg(b.out_x + su);
+        const float o0 = u0 * fo, os = u1 * fo;
+        const float ev0 = bv.x * cv.s0 + bv.y * cv.D + bv.w * cv.ss;
+        const float ew0 = bw.x * cw.s0 + bw.y * cw.D + bw.w * cw.ss;
+        ChildOut A, B;   // A: child v (uses E[w]), B: child w (uses E[v])
+        A.x0 = o0 * ew0; A.xs = os * cw.ss; A.X = Xo + cw.X;
+        B.x0 = o0 * ev0; B.xs = os * cv.ss; B.X = Xo + cv.X;
+        A.sumx = A.dot = A.mx = 0.f;
+        B.sumx = B.dot = B.mx = 0.f;
+        A.orow = cv.row ? b.out_part + (int64_t)d.v_ref * 8 + s.goff + lane : nullptr;
+        B.orow = cw.row ? b.out_part + (int64_t)d.w_ref * 8 + s.goff + lane : nullptr;
+        const float kv = bv.w * cv.ss, kw = bw.w * cw.ss;
+        const float pxa = bv.y * A.x0, pxb = bw.y * B.x0;
+        int j = 2;
+        for (; j + kChunk <= s.C; j += kChunk) {
+            float ou[kChunk], av[kChunk], aw[kChunk], qv[kChunk];
+#pragma unroll
+            for (int k = 0; k < kChunk; ++k) {
+                ou[k] = __ldcg(urow + (j + k) * G);
+                av[k] = child_val<G>(cv, j + k);
+                aw[k] = child_val<G>(cw, j + k);
+                qv[k] = __ldg(s.qrow + (j + k) * G);
+            }
+#pragma unroll
+            for (int k = 0; k < kChunk; ++k) {
+                const float o = ou[k] * fo;
+                const float xa = o * fmaf(bw.z, aw[k], kw);
+                const float xb = o * fmaf(bv.z, av[k], kv);
+                A.sumx += xa;
+                A.dot = fmaf(xa, av[k], A.dot);
+                B.sumx += xb;
+                B.dot = fmaf(xb, aw[k], B.dot);
+                if (A.orow) {
+                    const float r = fmaf(pxa, qv[k], bv.z * xa);
+                    __stcg(A.orow + (j + k) * G, r);
+                    A.mx = fmaxf(A.mx, r);
+                }
+                if (B.orow) {
+                    const float r = fmaf(pxb, qv[k], bw.z * xb);
+                    __stcg(B.orow + (j + k) * G, r);
+                    B.mx = fmaxf(B.mx, r);
+                }
+            }
+        }
+        for (; j < s.C; ++j) {
+            const float o = __ldcg(urow + j * G) * fo;
+            const float av = child_val<G>(cv, j), aw = child_val<G>(cw, j);
+            const float qj = __ldg(s.qrow + j * G);
+            const float xa = o * fmaf(bw.z, aw, kw);
+            const float xb = o * fmaf(bv.z, av, kv);
+            A.sumx += xa;
+            A.dot = fmaf(xa, av, A.dot);
+            B.sumx += xb;
+            B.dot = fmaf(xb, aw, B.dot);
+            if (A.orow) {
+                const float r = fmaf(pxa, qj, bv.z * xa);
+                __stcg(A.orow + j * G, r);
+                A.mx = fmaxf(A.mx, r);
+            }
+            if (B.orow) {
+                const float r = fmaf(pxb, qj, bw.z * xb);
+                __stcg(B.orow + j * G, r);
+                B.mx = fmaxf(B.mx, r);
+            }
+        }
+        const int64_t t = __ldg(b.tr_site_base + s.tree) + s.site;
+        const float lroot = __ldcg(b.root_lr + t);
+        const int xroot = __ldcg(b.root_x + t);
+        child_finish<G>(b, s, d.v, cv, bv, A, want_post, lroot, xroot, cv_);
+        child_finish<G>(b, s, d.w, cw, bw, B, want_post, lroot, xroot, cw_);
+    }
+#pragma unroll
+    for (int off = G / 2; off > 0; off >>= 1) {
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+            cv_[k] += __shfl_xor_sync(kFull, cv_[k], off);
+            cw_[k] += __shfl_xor_sync(kFull, cw_[k], off);
+        }
+    }
+    if (act && lane == 0 && __ldcg(b.tr_status + d.tree) == LAML_TREE_ACTIVE) {
+        write_counts<G>(b, d.tree, d.v, d.g, cv_);
+        write_counts<G>(b, d.tree, d.w, d.g, cw_);
+    }
+}
+
 // outside row of a root (calculations.py:172-175) + the root's posteriors
 template <int G>
 __device__ void root_init_item(const laml_batch& b, int r, int g, int lane, bool want_post) {
@@ -973,36 +1213,43 @@ __device__ bool grid_barrier(const laml_batch& b, unsigned& gen) {
 // ---------------------------------------------------------------------------
 // kernels
 // ---------------------------------------------------------------------------
-template <int G>
+template <int G, int KIND>
 __device__ __forceinline__ void for_items(const laml_batch& b, const int32_t* items, int64_t n,
-                                          int gwarp, int nwarps, int kind, bool want_post,
-                                          bool respect_status) {
+                                          int gwarp, int nwarps, bool want_post,
+                                          bool respect_status, const int32_t* desc = nullptr) {
+    constexpr int kind = KIND;
     constexpr int IPW = 32 / G;
     const int lane32 = threadIdx.x & 31, lane = lane32 % G, sub = lane32 / G;
     const int64_t nw = (n + IPW - 1) / IPW;
     for (int64_t wi = gwarp; wi < nw; wi += nwarps) {
         const int64_t it = wi * IPW + sub;
         const bool act = it < n;
-        const int node = act ? __ldg(items + 2 * it) : 0;
-        const int g = act ? __ldg(items + 2 * it + 1) : 0;
-        if (kind == 0) {
-            if (act) inside_item<G>(b, node, g, lane, respect_status);
-        } else if (kind == 1) {
-            outside_parent_item<G>(b, node, g, lane, act, want_post);
-        } else if (kind == 2) {
-            if (act) root_init_item<G>(b, node, g, lane, want_post);
+        if constexpr (KIND <= 1) {   // descriptor-driven inside / outside
+            const ItemDesc d = load_desc(desc, act ? it : 0);
+            if (kind == 0) {
+                if (act) inside_item_d<G>(b, d, lane, respect_status);
+            } else {
+                outside_item_d<G>(b, d, lane, act, want_post);
+            }
         } else {
-            outside_item<G>(b, node, g, lane, act, (b.compat && kind == 3) ? 1 : 2, false);
+            const int node = act ? __ldg(items + 2 * it) : 0;
+            const int g = act ? __ldg(items + 2 * it + 1) : 0;
+            if constexpr (KIND == 2) {
+                if (act) root_init_item<G>(b, node, g, lane, want_post);
+            } else {
+                outside_item<G>(b, node, g, lane, act, (b.compat && kind == 3) ? 1 : 2, false);
+            }
         }
     }
 }
 
-template <int G>
-__global__ void __launch_bounds__(kBlock, LAML_MINB) k_items(laml_batch b, const int32_t* items, int64_t n,
-                                                   int kind, int want_post, int respect_status) {
+template <int G, int KIND>
+__global__ void __launch_bounds__(kBlock, KIND == 1 ? LAML_MINB_OUT : LAML_MINB) k_items(laml_batch b, const int32_t* items, int64_t n,
+                                                   int want_post, int respect_status,
+                                                   const int32_t* desc) {
     const int gwarp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int nwarps = (gridDim.x * blockDim.x) >> 5;
-    for_items<G>(b, items, n, gwarp, nwarps, kind, want_post != 0, respect_status != 0);
+    for_items<G, KIND>(b, items, n, gwarp, nwarps, want_post != 0, respect_status != 0, desc);
 }
 
 __global__ void __launch_bounds__(kBlock, 4) k_mstep(laml_batch b, int rounds, int flags) {
@@ -1081,21 +1328,23 @@ __global__ void __launch_bounds__(kBlock, LAML_MINB) k_em_persistent(laml_batch 
     const int nwarps = (gridDim.x * blockDim.x) >> 5;
     unsigned gen = 0;
     for (int it = 0; it < iters; ++it) {
-        for_items<G>(b, b.root_items, b.n_root_items, gwarp, nwarps, 2, false, true);
+        for_items<G, 2>(b, b.root_items, b.n_root_items, gwarp, nwarps, false, true);
         if (!grid_barrier(b, gen)) return;
         for (int l = 0; l < b.n_out_levels; ++l) {
             const int64_t o = b.out_level_off[l], e = b.out_level_off[l + 1];
-            for_items<G>(b, b.out_items + 2 * o, e - o, gwarp, nwarps, 1, false, true);
+            for_items<G, 1>(b, b.out_items + 2 * o, e - o, gwarp, nwarps, false, true,
+                            b.out_desc + 12 * o);
             if (!grid_barrier(b, gen)) return;
         }
-        for_items<G>(b, b.root_items, b.n_root_items, gwarp, nwarps, 3, false, true);
+        for_items<G, 3>(b, b.root_items, b.n_root_items, gwarp, nwarps, false, true);
         if (!grid_barrier(b, gen)) return;
         for (int p = blockIdx.x; p < b.n_trees; p += gridDim.x)
             mstep_tree(b, p, rounds, sh, s_cnt, s_d, (flags & LAML_MSTEP_FP64_POLISH) != 0);
         if (!grid_barrier(b, gen)) return;
         for (int l = 0; l < b.n_in_levels; ++l) {
             const int64_t o = b.in_level_off[l], e = b.in_level_off[l + 1];
-            for_items<G>(b, b.in_items + 2 * o, e - o, gwarp, nwarps, 0, false, true);
+            for_items<G, 0>(b, b.in_items + 2 * o, e - o, gwarp, nwarps, false, true,
+                            b.in_desc + 12 * o);
             if (!grid_barrier(b, gen)) return;
         }
         for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < b.n_trees;
@@ -1137,18 +1386,28 @@ int validate(const laml_batch* b) {
         laml::set_error("laml_batch: group_sites must be 8, 16 or 32");
         return LAML_ERR_ARG;
     }
+    if (!b->in_desc || !b->out_desc || !b->grp_desc) {
+        laml::set_error("laml_batch: in_desc, out_desc and grp_desc (laml_plan_fill) are required");
+        return LAML_ERR_ARG;
+    }
     return LAML_OK;
 }
 
 template <int G>
 int launch_items(const laml_batch& b, const int32_t* items, int64_t n, int kind, int want_post,
-                 int respect_status, cudaStream_t st) {
+                 int respect_status, cudaStream_t st, const int32_t* desc = nullptr) {
     if (n <= 0) return LAML_OK;
     const int ipb = (kBlock / 32) * (32 / G);
     int64_t blocks = (n + ipb - 1) / ipb;
     const int64_t cap = (int64_t)num_sms() * 16;
     if (blocks > cap) blocks = cap;
-    k_items<G><<<(unsigned)blocks, kBlock, 0, st>>>(b, items, n, kind, want_post, respect_status);
+    switch (kind) {
+        case 0: k_items<G, 0><<<(unsigned)blocks, kBlock, 0, st>>>(b, items, n, want_post, respect_status, desc); break;
+        case 1: k_items<G, 1><<<(unsigned)blocks, kBlock, 0, st>>>(b, items, n, want_post, respect_status, desc); break;
+        case 2: k_items<G, 2><<<(unsigned)blocks, kBlock, 0, st>>>(b, items, n, want_post, respect_status, desc); break;
+        case 3: k_items<G, 3><<<(unsigned)blocks, kBlock, 0, st>>>(b, items, n, want_post, respect_status, desc); break;
+        default: k_items<G, 4><<<(unsigned)blocks, kBlock, 0, st>>>(b, items, n, want_post, respect_status, desc); break;
+    }
     return check(cudaGetLastError(), "k_items launch");
 }
 
@@ -1179,7 +1438,8 @@ int inside_t(const laml_batch& b, int update_em, cudaStream_t st, const Levels& 
              int respect_status) {
     for (int l = 0; l < b.n_in_levels; ++l) {
         int rc = launch_items<G>(b, b.in_items + 2 * (int64_t)L.in[l], L.in[l + 1] - L.in[l], 0, 0,
-                                 respect_status, st);
+                                 respect_status, st,
+                                 b.in_desc + 12 * (int64_t)L.in[l]);
         if (rc) return rc;
     }
     return LAML_OK;
@@ -1192,7 +1452,8 @@ int outside_t(const laml_batch& b, int flags, cudaStream_t st, const Levels& L) 
     if (rc) return rc;
     for (int l = 0; l < b.n_out_levels; ++l) {
         rc = launch_items<G>(b, b.out_items + 2 * (int64_t)L.out[l], L.out[l + 1] - L.out[l], 1,
-                             want_post, 1, st);
+                             want_post, 1, st,
+                             b.out_desc + 12 * (int64_t)L.out[l]);
         if (rc) return rc;
     }
     // kind 3: the E-step row of the root (compat: from node N-1); kind 4: from
@@ -1416,7 +1677,8 @@ __global__ void __launch_bounds__(kBlock, LAML_MINB) k_inside_level(laml_batch b
     const int32_t o = b.in_level_off[level], e = b.in_level_off[level + 1];
     const int gwarp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int nwarps = (gridDim.x * blockDim.x) >> 5;
-    for_items<G>(b, b.in_items + 2 * (int64_t)o, e - o, gwarp, nwarps, 0, false, false);
+    for_items<G, 0>(b, b.in_items + 2 * (int64_t)o, e - o, gwarp, nwarps, false, false,
+                    b.in_desc + 12 * (int64_t)o);
 }
 
 template <int G>

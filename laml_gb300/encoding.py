@@ -205,8 +205,12 @@ def plan_batch(trees: Sequence[EncodedTree], tree_ds: Sequence[int],
     gbase = np.zeros(len(datasets), np.int32)
     gbase[1:] = np.cumsum(dg)[:-1]
     gC = np.concatenate([d.group_C for d in datasets]).astype(np.int32)
+    dK = np.asarray([d.n_sites for d in datasets], np.int32)
+    dn = np.asarray([d.n_leaves for d in datasets], np.int32)
+    goff = np.concatenate([d.group_off for d in datasets]).astype(np.int32)
     pin = N.PlanInput(T, N.ptr(tn), N.ptr(tl), N.ptr(td), N.ptr(c0), N.ptr(c1), len(datasets),
-                      N.ptr(dg), N.ptr(dk), N.ptr(dr), N.ptr(gbase), N.ptr(gC))
+                      N.ptr(dg), N.ptr(dk), N.ptr(dr), N.ptr(gbase), N.ptr(gC), N.ptr(dK),
+                      N.ptr(dn), N.ptr(goff))
     sz = N.PlanSizes()
     N.check(L.laml_plan_measure(C.byref(pin), C.byref(sz)))
     nn = sz.n_nodes
@@ -223,6 +227,9 @@ def plan_batch(trees: Sequence[EncodedTree], tree_ds: Sequence[int],
         "out_level_off": np.empty(sz.n_out_levels + 1, np.int32),
         "out_items": np.empty(2 * max(1, sz.n_out_items), np.int32),
         "root_items": np.empty(2 * max(1, sz.n_root_items), np.int32),
+        "in_desc": np.empty(12 * max(1, sz.n_in_items), np.int32),
+        "out_desc": np.empty(12 * max(1, sz.n_out_items), np.int32),
+        "grp_desc": np.empty(8 * max(1, sz.n_groups_total), np.int32),
     }
     pout = N.PlanOutput(*[N.ptr(arr[k]) for k in N.PLAN_OUT_FIELDS])
     N.check(L.laml_plan_fill(C.byref(pin), C.byref(pout)))

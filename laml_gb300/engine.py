@@ -140,7 +140,8 @@ class DeviceBatch:
         for k in ("tr_node_base", "tr_root", "tr_quirk", "tr_site_base", "tr_cnt_base",
                   "tr_post_base", "nd_tree", "nd_c0", "nd_c1", "nd_parent", "nd_sib",
                   "nd_leafrow", "nd_prow", "nd_srow", "in_level_off", "in_items",
-                  "out_level_off", "out_items", "root_items"):
+                  "out_level_off", "out_items", "root_items", "in_desc", "out_desc",
+                  "grp_desc"):
             pk.add(k, plan[k])
         self._h2d_bytes = pk.size
         ctx = torch.cuda.stream(stream) if stream is not None else _nullctx()

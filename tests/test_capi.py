@@ -144,3 +144,40 @@ def test_plan_levels():
             for c in (c0, c1):
                 if arr["nd_c0"][c] >= 0:
                     assert lvl[c] < lvl[u]
+
+
+def test_item_descriptors_match_plan():
+    rng = np.random.default_rng(9)
+    trees = [E.encode_newick(synth.yule_tree(n, rng).newick()) for n in (9, 31, 4)]
+    mats = [np.zeros((31, 21), np.int32), np.zeros((31, 5), np.int32)]
+    dss = [E.encode_dataset(m, [{1: 1.0}] * m.shape[1], compat=True, group_sites=8) for m in mats]
+    tree_ds = [0, 1, 0]
+    sizes, a = E.plan_batch(trees, tree_ds, dss)
+    gbase = a["group_base"]
+    for kind in ("in", "out"):
+        items = a[f"{kind}_items"][:2 * sizes[f"n_{kind}_items"]].reshape(-1, 2)
+        desc = a[f"{kind}_desc"][:12 * len(items)].reshape(-1, 12)
+        for (u, g), e in zip(items, desc):
+            t = a["nd_tree"][u]
+            v, w = a["nd_c0"][u], a["nd_c1"][u]
+            assert list(e[:3]) == [u, v, w]
+            assert e[3] & 0xffffff == t
+            fl = e[3] >> 24
+            assert bool(fl & 1) == (a["nd_c0"][v] < 0) and bool(fl & 2) == (a["nd_c0"][w] < 0)
+            assert bool(fl & 4) == (a["tr_root"][t] == u)
+            assert e[4] == g and e[5] == gbase[tree_ds[t]] + g
+            assert e[6] == a["nd_srow"][u] and e[7] * 8 == a["nd_prow"][u]
+            for x, ref, sr in ((v, e[8], e[10]), (w, e[9], e[11])):
+                if a["nd_c0"][x] < 0:
+                    assert ref == a["nd_leafrow"][x]
+                else:
+                    assert ref * 8 == a["nd_prow"][x] and sr == a["nd_srow"][x]
+    gd = a["grp_desc"][:8 * sizes["n_groups_total"]].reshape(-1, 8)
+    kp = [d.n_sites_pad for d in dss]
+    for d, ds in enumerate(dss):
+        for g in range(ds.n_groups):
+            e = gd[gbase[d] + g]
+            assert e[0] == ds.group_off[g] and e[3] == d and e[5] == ds.n_sites_pad
+            assert e[1] == sum(kp[:d]) + g * 8
+            assert e[2] == sum(x.row_len for x in dss[:d]) + ds.group_off[g]
+            assert e[4] == sum(x.codes.size for x in dss[:d]) and e[6] == ds.n_sites

@@ -178,3 +178,14 @@ def test_graph_replay_equals_direct_launches():
     for ra, rc in zip(a.results(), c.results()):
         assert ra.llh == rc.llh and ra.iterations == rc.iterations
         np.testing.assert_array_equal(ra.branch_lengths, rc.branch_lengths)
+
+
+def test_em_large_tree_uses_global_mstep_staging():
+    """A tree above the 2048-node shared-memory staging of the M-step."""
+    w = synth.pmm_workload(1500, 8, 3, 10, 0.5, 0.1, 0.15, seed=31)
+    b = PB.make_batch(w.newicks, w.rows, w.Q, w.leaf_order, compat=True)
+    r = b.run_em(max_iters=6)[0]
+    prob = _oracle(w, 0, True)
+    ref = O.em_compat(prob, prob.tree.branch_lengths, 0.5, 0.5, max_iters=6)
+    assert r.iterations == ref.iterations
+    assert r.llh == pytest.approx(ref.llh, rel=1e-6)
