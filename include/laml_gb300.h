@@ -232,6 +232,18 @@ typedef struct laml_batch {
 /* Number of sites per group the kernels were built for (bit mask of 8|16|32). */
 int laml_supported_group_sites(void);
 
+/* Builds in_desc / out_desc / grp_desc (laml_plan_output's layout, byte for
+ * byte) on the device from the batch's node arrays, items and dataset
+ * tables, so a caller uploads the node arrays only (the descriptors are 48
+ * bytes per item, most of a batch's host->device bytes otherwise).  Outputs
+ * are device buffers of 12 * n_in_items, 12 * n_out_items and
+ * 8 * (total groups) int32, 16-byte aligned; the batch's own descriptor
+ * pointers are not read.  laml_plan_fill must have accepted the batch (its
+ * 32-bit range check covers these descriptors).  No reference counterpart:
+ * the reference walks the tree objects on the host for every pass. */
+int laml_plan_descriptors(const laml_batch* b, int32_t* in_desc, int32_t* out_desc,
+                          int32_t* grp_desc, void* stream);
+
 /* Branch transition terms from nd_d, tr_nu (compat adds the EPS floors of
  * fast_em/calculations.py:153-157).  Replaces the t1/t2/t3/alpha0 arrays. */
 int laml_branch_terms(const laml_batch* b, void* stream);

@@ -101,6 +101,7 @@ EXPORTS = {
     "laml_plan_measure": (i32, [P(PlanInput), P(PlanSizes)]),
     "laml_plan_fill": (i32, [P(PlanInput), P(PlanOutput)]),
     "laml_supported_group_sites": (i32, []),
+    "laml_plan_descriptors": (i32, [P(Batch), vp, vp, vp, vp]),
     "laml_branch_terms": (i32, [P(Batch), vp]),
     "laml_inside": (i32, [P(Batch), i32, vp]),
     "laml_outside": (i32, [P(Batch), i32, vp]),

@@ -619,27 +619,68 @@ int tree_levels(int N, int n, const int32_t* c0, const int32_t* c1, TreeLevels& 
 
 }  // namespace
 
-extern "C" int laml_plan_measure(const laml_plan_input* in, laml_plan_sizes* sz) {
+namespace {
+
+template <class F>
+void parallel_for(int64_t n, F f) {
+    int nt = (int)std::min<unsigned>(std::max(1u, std::thread::hardware_concurrency()), 16u);
+    if (n < 4096 || nt <= 1) {
+        f((int64_t)0, n);
+        return;
+    }
+    std::vector<std::thread> th;
+    const int64_t chunk = (n + nt - 1) / nt;
+    for (int t = 0; t < nt; ++t) {
+        const int64_t a = t * chunk, e = std::min(n, a + chunk);
+        if (a >= e) break;
+        th.emplace_back([&f, a, e]() { f(a, e); });
+    }
+    for (auto& x : th) x.join();
+}
+
+struct PlanScratch {
+    std::vector<TreeLevels> lv;
+    std::vector<int> root;
+    std::vector<int64_t> node_base;
+};
+
+int plan_levels(const laml_plan_input* in, PlanScratch& S, laml_plan_sizes* sz) {
     if (!in || !sz || in->n_trees <= 0 || in->n_trees >= (1 << 24)) {
         set_error("plan: bad argument (1 <= n_trees < 2^24)");
         return LAML_ERR_ARG;
     }
+    const int T = in->n_trees;
     std::memset(sz, 0, sizeof(*sz));
-    int64_t nb = 0;
-    int hmax = 0, dmax = 0;
-    for (int p = 0; p < in->n_trees; ++p) {
-        int N = in->tree_nodes[p], n = in->tree_leaves[p], d = in->tree_dataset[p];
+    S.lv.assign(T, TreeLevels());
+    S.root.assign(T, -1);
+    S.node_base.assign(T + 1, 0);
+    for (int p = 0; p < T; ++p) {
+        const int d = in->tree_dataset[p];
         if (d < 0 || d >= in->n_datasets) { set_error("plan: bad dataset id"); return LAML_ERR_ARG; }
-        TreeLevels L;
-        int root;
-        const int32_t* c0 = in->child0 + nb;
-        int rc = tree_levels(N, n, c0, in->child1 + nb, L, &root);
-        if (rc) return rc;
-        int NG = in->ds_groups[d], Kp = in->ds_sites_pad[d];
+        S.node_base[p + 1] = S.node_base[p] + in->tree_nodes[p];
+    }
+    std::vector<int> rcs(T, LAML_OK);
+    std::vector<std::string> msgs(T);
+    parallel_for(T, [&](int64_t a, int64_t e) {
+        for (int64_t p = a; p < e; ++p) {
+            const int64_t nb = S.node_base[p];
+            rcs[p] = tree_levels(in->tree_nodes[p], in->tree_leaves[p], in->child0 + nb,
+                                 in->child1 + nb, S.lv[p], &S.root[p]);
+            if (rcs[p]) msgs[p] = laml::g_last_error;
+        }
+    });
+    for (int p = 0; p < T; ++p)
+        if (rcs[p]) { set_error(msgs[p]); return rcs[p]; }
+    int hmax = 0, dmax = 0;
+    for (int p = 0; p < T; ++p) {
+        const int N = in->tree_nodes[p], n = in->tree_leaves[p], d = in->tree_dataset[p];
+        const int32_t* c0 = in->child0 + S.node_base[p];
+        const TreeLevels& L = S.lv[p];
         for (int u = 0; u < N; ++u) {
             hmax = std::max(hmax, L.height[u]);
             if (c0[u] >= 0) dmax = std::max(dmax, L.depth[u] + 1);   // levels of internal parents
         }
+        const int NG = in->ds_groups[d], Kp = in->ds_sites_pad[d];
         sz->n_nodes += N;
         sz->part_floats += (int64_t)(N - n) * in->ds_row_len[d];
         sz->scalar_len += (int64_t)(N - n) * Kp;
@@ -649,7 +690,6 @@ extern "C" int laml_plan_measure(const laml_plan_input* in, laml_plan_sizes* sz)
         sz->n_in_items += (int64_t)(N - n) * NG;
         sz->n_out_items += (int64_t)(N - n) * NG;
         sz->n_root_items += NG;
-        nb += N;
     }
     sz->n_in_levels = hmax;
     sz->n_out_levels = dmax;
@@ -657,59 +697,84 @@ extern "C" int laml_plan_measure(const laml_plan_input* in, laml_plan_sizes* sz)
     return LAML_OK;
 }
 
+}  // namespace
+
+extern "C" int laml_plan_measure(const laml_plan_input* in, laml_plan_sizes* sz) {
+    PlanScratch S;
+    return plan_levels(in, S, sz);
+}
+
 extern "C" int laml_plan_fill(const laml_plan_input* in, laml_plan_output* o) {
     laml_plan_sizes sz;
-    int rc = laml_plan_measure(in, &sz);
+    PlanScratch S;
+    int rc = plan_levels(in, S, &sz);
     if (rc) return rc;
     const int T = in->n_trees;
     const int H = sz.n_in_levels, D = sz.n_out_levels;
-    std::vector<std::vector<int>> in_lv(H + 1), out_lv(D + 1);
-    int64_t nb = 0, pb = 0, sb = 0, tb = 0, cb = 0, qb = 0;
     int maxNG = 0;
-    for (int p = 0; p < T; ++p) {
-        int N = in->tree_nodes[p], n = in->tree_leaves[p], d = in->tree_dataset[p];
-        const int32_t* c0 = in->child0 + nb;
-        const int32_t* c1 = in->child1 + nb;
-        TreeLevels L;
-        int root;
-        tree_levels(N, n, c0, c1, L, &root);
-        int NG = in->ds_groups[d], Kp = in->ds_sites_pad[d];
-        int64_t R = in->ds_row_len[d];
-        maxNG = std::max(maxNG, NG);
-        o->tr_node_base[p] = (int32_t)nb;
-        o->tr_root[p] = (int32_t)(nb + root);
-        o->tr_quirk[p] = (int32_t)(nb + N - 1);   // parent_sibling[root] = (-1,-1) -> node N-1
-        o->tr_site_base[p] = tb;
-        o->tr_cnt_base[p] = cb;
-        o->tr_post_base[p] = qb;
-        for (int u = 0; u < N; ++u) {
-            int64_t g = nb + u;
-            o->nd_tree[g] = p;
-            o->nd_c0[g] = c0[u] >= 0 ? (int32_t)(nb + c0[u]) : -1;
-            o->nd_c1[g] = c1[u] >= 0 ? (int32_t)(nb + c1[u]) : -1;
-            int par = L.parent[u];
-            o->nd_parent[g] = par >= 0 ? (int32_t)(nb + par) : -1;
-            int sib = -1;
-            if (par >= 0) sib = (c0[par] == u) ? c1[par] : c0[par];
-            o->nd_sib[g] = sib >= 0 ? (int32_t)(nb + sib) : -1;
-            if (u < n) {
-                o->nd_leafrow[g] = u;
-                o->nd_prow[g] = -1;
-                o->nd_srow[g] = -1;
-            } else {
-                o->nd_leafrow[g] = -1;
-                o->nd_prow[g] = pb + (int64_t)(u - n) * R;
-                o->nd_srow[g] = sb + (int64_t)(u - n) * Kp;
-                in_lv[L.height[u]].push_back((int)g);
-            }
-            if (u >= n) out_lv[L.depth[u] + 1].push_back((int)g);   // outside by parent depth
+    std::vector<int64_t> pbase(T), sbase(T), tbase(T), cbase(T), qbase(T);
+    {
+        int64_t pb = 0, sb = 0, tb = 0, cb = 0, qb = 0;
+        for (int p = 0; p < T; ++p) {
+            const int N = in->tree_nodes[p], n = in->tree_leaves[p], d = in->tree_dataset[p];
+            const int NG = in->ds_groups[d], Kp = in->ds_sites_pad[d];
+            maxNG = std::max(maxNG, NG);
+            pbase[p] = pb; sbase[p] = sb; tbase[p] = tb; cbase[p] = cb; qbase[p] = qb;
+            pb += (int64_t)(N - n) * in->ds_row_len[d];
+            sb += (int64_t)(N - n) * Kp;
+            tb += Kp;
+            cb += (int64_t)N * NG * 8;
+            qb += (int64_t)N * Kp;
         }
-        pb += (int64_t)(N - n) * R;
-        sb += (int64_t)(N - n) * Kp;
-        tb += Kp;
-        cb += (int64_t)N * NG * 8;
-        qb += (int64_t)N * Kp;
-        nb += N;
+    }
+    // node and tree arrays (parallel over trees)
+    parallel_for(T, [&](int64_t a, int64_t e) {
+        for (int64_t p = a; p < e; ++p) {
+            const int N = in->tree_nodes[p], n = in->tree_leaves[p], d = in->tree_dataset[p];
+            const int64_t nb = S.node_base[p];
+            const int32_t* c0 = in->child0 + nb;
+            const int32_t* c1 = in->child1 + nb;
+            const TreeLevels& L = S.lv[p];
+            const int Kp = in->ds_sites_pad[d];
+            const int64_t R = in->ds_row_len[d];
+            o->tr_node_base[p] = (int32_t)nb;
+            o->tr_root[p] = (int32_t)(nb + S.root[p]);
+            o->tr_quirk[p] = (int32_t)(nb + N - 1);   // parent_sibling[root] = (-1,-1) -> node N-1
+            o->tr_site_base[p] = tbase[p];
+            o->tr_cnt_base[p] = cbase[p];
+            o->tr_post_base[p] = qbase[p];
+            for (int u = 0; u < N; ++u) {
+                const int64_t g = nb + u;
+                o->nd_tree[g] = (int32_t)p;
+                o->nd_c0[g] = c0[u] >= 0 ? (int32_t)(nb + c0[u]) : -1;
+                o->nd_c1[g] = c1[u] >= 0 ? (int32_t)(nb + c1[u]) : -1;
+                const int par = L.parent[u];
+                o->nd_parent[g] = par >= 0 ? (int32_t)(nb + par) : -1;
+                int sib = -1;
+                if (par >= 0) sib = (c0[par] == u) ? c1[par] : c0[par];
+                o->nd_sib[g] = sib >= 0 ? (int32_t)(nb + sib) : -1;
+                if (u < n) {
+                    o->nd_leafrow[g] = u;
+                    o->nd_prow[g] = -1;
+                    o->nd_srow[g] = -1;
+                } else {
+                    o->nd_leafrow[g] = -1;
+                    o->nd_prow[g] = pbase[p] + (int64_t)(u - n) * R;
+                    o->nd_srow[g] = sbase[p] + (int64_t)(u - n) * Kp;
+                }
+            }
+        }
+    });
+    // level buckets: inside by height, outside by the depth of the internal parent
+    std::vector<std::vector<int>> in_lv(H + 1), out_lv(D + 1);
+    for (int p = 0; p < T; ++p) {
+        const int N = in->tree_nodes[p], n = in->tree_leaves[p];
+        const int64_t nb = S.node_base[p];
+        const TreeLevels& L = S.lv[p];
+        for (int u = n; u < N; ++u) {
+            in_lv[L.height[u]].push_back((int)(nb + u));
+            out_lv[L.depth[u] + 1].push_back((int)(nb + u));
+        }
     }
     // items, group-major within a level (groups are sorted by state count)
     auto emit = [&](const std::vector<std::vector<int>>& lv, int first, int last, int32_t* off,
@@ -719,7 +784,7 @@ extern "C" int laml_plan_fill(const laml_plan_input* in, laml_plan_output* o) {
             off[l - first] = (int32_t)k;
             for (int g = 0; g < maxNG; ++g)
                 for (int node : lv[l]) {
-                    int d = in->tree_dataset[o->nd_tree[node]];
+                    const int d = in->tree_dataset[o->nd_tree[node]];
                     if (g < in->ds_groups[d]) {
                         items[2 * k] = node;
                         items[2 * k + 1] = g;
@@ -731,14 +796,20 @@ extern "C" int laml_plan_fill(const laml_plan_input* in, laml_plan_output* o) {
     };
     emit(in_lv, 1, H, o->in_level_off, o->in_items);
     emit(out_lv, 1, D, o->out_level_off, o->out_items);
-    // global group table and item descriptors
-    if (o->grp_desc || o->in_desc || o->out_desc) {
-        if (!in->ds_sites || !in->ds_leaves || !in->group_off) {
-            set_error("plan: descriptors need ds_sites, ds_leaves and group_off");
-            return LAML_ERR_ARG;
+    int64_t k = 0;
+    for (int g = 0; g < maxNG; ++g)
+        for (int p = 0; p < T; ++p) {
+            if (g < in->ds_groups[in->tree_dataset[p]]) {
+                o->root_items[2 * k] = o->tr_root[p];
+                o->root_items[2 * k + 1] = g;
+                ++k;
+            }
         }
-        std::vector<int64_t> site_base(in->n_datasets), q_base(in->n_datasets),
-            code_base(in->n_datasets);
+    // global group table and item descriptors (the 32-bit range check holds
+    // for descriptors built later on the device as well)
+    std::vector<int64_t> site_base(in->n_datasets), q_base(in->n_datasets),
+        code_base(in->n_datasets);
+    {
         int64_t sb = 0, qb2 = 0, cb2 = 0;
         for (int d = 0; d < in->n_datasets; ++d) {
             site_base[d] = sb;
@@ -746,11 +817,17 @@ extern "C" int laml_plan_fill(const laml_plan_input* in, laml_plan_output* o) {
             code_base[d] = cb2;
             sb += in->ds_sites_pad[d];
             qb2 += in->ds_row_len[d];
-            cb2 += (int64_t)in->ds_leaves[d] * in->ds_sites_pad[d];
+            if (in->ds_leaves) cb2 += (int64_t)in->ds_leaves[d] * in->ds_sites_pad[d];
         }
         if (qb2 >= INT32_MAX || cb2 >= INT32_MAX || sz.part_floats / 8 >= INT32_MAX ||
-            sz.scalar_len >= INT32_MAX) {
+            sz.scalar_len >= INT32_MAX || sz.n_nodes >= INT32_MAX) {
             set_error("plan: batch too large for 32-bit descriptors");
+            return LAML_ERR_ARG;
+        }
+    }
+    if (o->grp_desc || o->in_desc || o->out_desc) {
+        if (!in->ds_sites || !in->ds_leaves || !in->group_off) {
+            set_error("plan: descriptors need ds_sites, ds_leaves and group_off");
             return LAML_ERR_ARG;
         }
         if (o->grp_desc) {
@@ -773,7 +850,8 @@ extern "C" int laml_plan_fill(const laml_plan_input* in, laml_plan_output* o) {
             return o->nd_c0[x] < 0 ? o->nd_leafrow[x] : (int32_t)(o->nd_prow[x] / 8);
         };
         auto fill = [&](const int32_t* items, int64_t n_items, int32_t* desc) {
-            for (int64_t k = 0; k < n_items; ++k) {
+          parallel_for(n_items, [&](int64_t ka, int64_t ke) {
+            for (int64_t k = ka; k < ke; ++k) {
                 const int u = items[2 * k], g = items[2 * k + 1];
                 const int tree = o->nd_tree[u];
                 const int d = in->tree_dataset[tree];
@@ -787,18 +865,10 @@ extern "C" int laml_plan_fill(const laml_plan_input* in, laml_plan_output* o) {
                 e[8] = ref(v); e[9] = ref(w);
                 e[10] = (int32_t)o->nd_srow[v]; e[11] = (int32_t)o->nd_srow[w];
             }
+          });
         };
         if (o->in_desc) fill(o->in_items, sz.n_in_items, o->in_desc);
         if (o->out_desc) fill(o->out_items, sz.n_out_items, o->out_desc);
     }
-    int64_t k = 0;
-    for (int g = 0; g < maxNG; ++g)
-        for (int p = 0; p < T; ++p) {
-            if (g < in->ds_groups[in->tree_dataset[p]]) {
-                o->root_items[2 * k] = o->tr_root[p];
-                o->root_items[2 * k + 1] = g;
-                ++k;
-            }
-        }
     return LAML_OK;
 }

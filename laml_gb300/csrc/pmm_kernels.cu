@@ -882,6 +882,9 @@ __device__ __forceinline__ T branch_F(T a, T b, T c, T nu, T d, T* dFdu) {
 __device__ float solve_branch_f(float a, float bb, float c, float nu, float d0, float lo,
                                 float hi) {
     float t;
+    // a branch without expected counts has a flat objective: its gradient is
+    // zero and fast_em's L-BFGS leaves it where it is
+    if (a == 0.f && bb == 0.f && c == 0.f) return fminf(fmaxf(d0, lo), hi);
     if (branch_F<float>(a, bb, c, nu, lo, &t) <= 0.f) return lo;
     if (branch_F<float>(a, bb, c, nu, hi, &t) >= 0.f) return hi;
     float ulo = logf(lo), uhi = logf(hi);
@@ -904,6 +907,7 @@ __device__ float solve_branch_f(float a, float bb, float c, float nu, float d0, 
 __device__ double solve_branch(double a, double bb, double c, double nu, double d0, double lo,
                                double hi, bool polish) {
     float t;
+    if (a == 0.0 && bb == 0.0 && c == 0.0) return fmin(fmax(d0, lo), hi);   // flat objective
     const float af = (float)a, bf = (float)bb, cf = (float)c, nf = (float)nu;
     if (branch_F<float>(af, bf, cf, nf, (float)lo, &t) <= 0.f) return lo;
     if (branch_F<float>(af, bf, cf, nf, (float)hi, &t) >= 0.f) return hi;
@@ -1318,6 +1322,42 @@ __global__ void k_branch_terms(laml_batch b) {
     }
 }
 
+// Item descriptors from the node arrays already on the device: the same 12
+// int32 per item that laml_plan_fill writes on the host, three 16-byte stores.
+__global__ void k_item_desc(laml_batch b, const int32_t* __restrict__ items, int64_t n,
+                            int32_t* __restrict__ desc) {
+    for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n;
+         k += (int64_t)gridDim.x * blockDim.x) {
+        const int u = items[2 * k], g = items[2 * k + 1];
+        const int tree = b.nd_tree[u];
+        const int d = b.tr_ds[tree];
+        const int v = b.nd_c0[u], w = b.nd_c1[u];
+        const bool vl = b.nd_c0[v] < 0, wl = b.nd_c0[w] < 0;
+        const int flags = (vl ? 1 : 0) | (wl ? 2 : 0) | (b.tr_root[tree] == u ? 4 : 0);
+        const int32_t rv = vl ? b.nd_leafrow[v] : (int32_t)(b.nd_prow[v] / 8);
+        const int32_t rw = wl ? b.nd_leafrow[w] : (int32_t)(b.nd_prow[w] / 8);
+        int4* e = reinterpret_cast<int4*>(desc + 12 * k);
+        e[0] = make_int4(u, v, w, tree | (flags << 24));
+        e[1] = make_int4(g, b.ds_group_base[d] + g, (int32_t)b.nd_srow[u],
+                         (int32_t)(b.nd_prow[u] / 8));
+        e[2] = make_int4(rv, rw, (int32_t)b.nd_srow[v], (int32_t)b.nd_srow[w]);
+    }
+}
+
+// Group table: one block per dataset.
+__global__ void k_group_desc(laml_batch b, int32_t* __restrict__ grp) {
+    const int d = blockIdx.x;
+    const int NG = b.ds_groups[d];
+    for (int g = threadIdx.x; g < NG; g += blockDim.x) {
+        const int gi = b.ds_group_base[d] + g;
+        const int off = b.group_off[gi];
+        int4* e = reinterpret_cast<int4*>(grp + 8 * (int64_t)gi);
+        e[0] = make_int4(off, b.ds_site_base[d] + g * b.group_sites,
+                         (int32_t)(b.ds_q_base[d] + off), d);
+        e[1] = make_int4((int32_t)b.ds_code_base[d], b.ds_sites_pad[d], b.ds_sites[d], 0);
+    }
+}
+
 template <int G>
 __global__ void __launch_bounds__(kBlock, LAML_MINB) k_em_persistent(laml_batch b, int iters, int rounds,
                                                            double rel_tol, int max_iters, int flags) {
@@ -1540,6 +1580,28 @@ extern "C" int laml_branch_terms(const laml_batch* b, void* stream) {
     const int64_t blocks = (b->n_nodes + kBlock - 1) / kBlock;
     k_branch_terms<<<(unsigned)blocks, kBlock, 0, st>>>(*b);
     return check(cudaGetLastError(), "k_branch_terms");
+}
+
+extern "C" int laml_plan_descriptors(const laml_batch* b, int32_t* in_desc, int32_t* out_desc,
+                                     int32_t* grp_desc, void* stream) {
+    if (!b || b->n_trees <= 0 || b->n_nodes <= 0 || b->n_datasets <= 0) {
+        laml::set_error("laml_plan_descriptors: empty or null batch");
+        return LAML_ERR_ARG;
+    }
+    const uintptr_t mis = (uintptr_t)in_desc | (uintptr_t)out_desc | (uintptr_t)grp_desc;
+    if (!in_desc || !out_desc || !grp_desc || (mis & 15)) {
+        laml::set_error("laml_plan_descriptors: null or misaligned (16 B) output");
+        return LAML_ERR_ARG;
+    }
+    cudaStream_t st = (cudaStream_t)stream;
+    const int64_t cap = (int64_t)num_sms() * 8;
+    auto blocks = [&](int64_t n) { return (unsigned)std::max<int64_t>(1, std::min(cap, (n + kBlock - 1) / kBlock)); };
+    if (b->n_in_items > 0)
+        k_item_desc<<<blocks(b->n_in_items), kBlock, 0, st>>>(*b, b->in_items, b->n_in_items, in_desc);
+    if (b->n_out_items > 0)
+        k_item_desc<<<blocks(b->n_out_items), kBlock, 0, st>>>(*b, b->out_items, b->n_out_items, out_desc);
+    k_group_desc<<<b->n_datasets, 128, 0, st>>>(*b, grp_desc);
+    return check(cudaGetLastError(), "laml_plan_descriptors");
 }
 
 extern "C" int laml_inside(const laml_batch* b, int32_t update_em, void* stream) {

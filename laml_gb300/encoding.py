@@ -189,9 +189,11 @@ def encode_dataset(chars: np.ndarray, Q, compat: bool = True, group_sites: int =
 
 
 def plan_batch(trees: Sequence[EncodedTree], tree_ds: Sequence[int],
-               datasets: Sequence[EncodedDataset]):
+               datasets: Sequence[EncodedDataset], host_desc: bool = True):
     """Level schedule + buffer offsets of a batch (laml_plan_*).  Returns
-    (sizes: dict, arrays: dict of numpy arrays)."""
+    (sizes: dict, arrays: dict of numpy arrays).  With ``host_desc`` False
+    the item and group descriptors are left out (laml_plan_descriptors
+    builds them on the device)."""
     L = N.lib()
     T = len(trees)
     tn = np.asarray([t.num_nodes for t in trees], np.int32)
@@ -227,11 +229,12 @@ def plan_batch(trees: Sequence[EncodedTree], tree_ds: Sequence[int],
         "out_level_off": np.empty(sz.n_out_levels + 1, np.int32),
         "out_items": np.empty(2 * max(1, sz.n_out_items), np.int32),
         "root_items": np.empty(2 * max(1, sz.n_root_items), np.int32),
-        "in_desc": np.empty(12 * max(1, sz.n_in_items), np.int32),
-        "out_desc": np.empty(12 * max(1, sz.n_out_items), np.int32),
-        "grp_desc": np.empty(8 * max(1, sz.n_groups_total), np.int32),
     }
-    pout = N.PlanOutput(*[N.ptr(arr[k]) for k in N.PLAN_OUT_FIELDS])
+    if host_desc:
+        arr["in_desc"] = np.empty(12 * max(1, sz.n_in_items), np.int32)
+        arr["out_desc"] = np.empty(12 * max(1, sz.n_out_items), np.int32)
+        arr["grp_desc"] = np.empty(8 * max(1, sz.n_groups_total), np.int32)
+    pout = N.PlanOutput(*[N.ptr(arr[k]) if k in arr else None for k in N.PLAN_OUT_FIELDS])
     N.check(L.laml_plan_fill(C.byref(pin), C.byref(pout)))
     sizes = {k: getattr(sz, k) for k, _ in N.PlanSizes._fields_}
     arr["group_base"] = gbase

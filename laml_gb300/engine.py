@@ -88,7 +88,7 @@ class DeviceBatch:
         self.trees = list(trees)
         self.tree_ds = np.asarray(tree_ds, np.int32)
         self.datasets = list(datasets)
-        sizes, plan = plan_batch(trees, tree_ds, datasets)
+        sizes, plan = plan_batch(trees, tree_ds, datasets, host_desc=False)
         self.sizes = sizes
         self._node_base = plan["tr_node_base"].astype(np.int64)
         self.last_d2h_bytes = 0
@@ -140,8 +140,7 @@ class DeviceBatch:
         for k in ("tr_node_base", "tr_root", "tr_quirk", "tr_site_base", "tr_cnt_base",
                   "tr_post_base", "nd_tree", "nd_c0", "nd_c1", "nd_parent", "nd_sib",
                   "nd_leafrow", "nd_prow", "nd_srow", "in_level_off", "in_items",
-                  "out_level_off", "out_items", "root_items", "in_desc", "out_desc",
-                  "grp_desc"):
+                  "out_level_off", "out_items", "root_items"):
             pk.add(k, plan[k])
         self._h2d_bytes = pk.size
         ctx = torch.cuda.stream(stream) if stream is not None else _nullctx()
@@ -165,6 +164,10 @@ class DeviceBatch:
             "cnt_part": e(sizes["count_floats"], f32),
             "barrier": torch.zeros(2, dtype=i32, device=dev),
             "error": torch.zeros(1, dtype=i32, device=dev),
+            # item / group descriptors, built on the device below
+            "in_desc": e(12 * sizes["n_in_items"], i32),
+            "out_desc": e(12 * sizes["n_out_items"], i32),
+            "grp_desc": e(8 * sizes["n_groups_total"], i32),
         }
         if want_post:
             self.work["post0"] = e(sizes["post_len"], f32)
@@ -191,6 +194,8 @@ class DeviceBatch:
         b.h_out_level_off = self._h_out_off.ctypes.data
         self._stream_ptr = (stream.cuda_stream if stream is not None
                             else torch.cuda.current_stream(self.device).cuda_stream)
+        N.check(N.lib().laml_plan_descriptors(
+            C.byref(b), b.in_desc, b.out_desc, b.grp_desc, self._s()))
 
     # -- raw entry points -------------------------------------------------
     def _s(self):
@@ -305,22 +310,35 @@ class DeviceBatch:
         return out, lr
 
     def run_em(self, rounds=MSTEP_ROUNDS, rel_tol=None, max_iters=100000, chunk=4,
-               persistent=True, polish=None):
+               persistent=None, polish=None, path=None):
         """EM to convergence for every tree: inside at the start parameters,
-        then chunks of fused iterations until no tree is ACTIVE."""
+        then chunks of ``chunk`` fused iterations until no tree is ACTIVE.
+        ``path``: "graph" (a CUDA graph of the per-level launches, replayed
+        per chunk; the default), "levels" (the same launches issued directly)
+        or "persistent" (one cooperative kernel per chunk); ``persistent``
+        True / False is shorthand for "persistent" / "levels"."""
+        if path is None:
+            path = "graph" if persistent is None else ("persistent" if persistent else "levels")
+        if path not in ("graph", "levels", "persistent"):
+            raise ValueError(f"unknown EM path {path!r}")
         self.branch_terms()
         self.inside(update_em=True)
+        g = (self.em_graph(chunk, rounds=rounds, rel_tol=rel_tol, max_iters=max_iters,
+                           persistent=False, polish=polish) if path == "graph" else None)
         done = 0
         while True:
-            self.em_iterations(chunk, rounds=rounds, rel_tol=rel_tol, max_iters=max_iters,
-                               persistent=persistent, polish=polish)
+            if g is not None:
+                self.launch_graph(g)
+            else:
+                self.em_iterations(chunk, rounds=rounds, rel_tol=rel_tol, max_iters=max_iters,
+                                   persistent=path == "persistent", polish=polish)
             done += chunk
             st = self.work["tr_status"]
             if not bool((st == N.TREE_ACTIVE).any()):
                 break
             if done >= max_iters + chunk:
                 break
-        if persistent:
+        if path == "persistent":
             self.check_device_error()
         return self.results()
 

@@ -84,11 +84,11 @@ class _Cohort:
 
 def footprint_bytes(tree: EncodedTree, ds: EncodedDataset) -> int:
     """Device bytes a single-tree batch of this request holds."""
-    sizes, _ = plan_batch([tree], [0], [ds])
+    sizes, _ = plan_batch([tree], [0], [ds], host_desc=False)
     nn = sizes["n_nodes"]
     return int(8 * sizes["part_floats"] + 20 * sizes["scalar_len"] + 4 * sizes["count_floats"]
                + 200 * nn + ds.codes.nbytes + 4 * ds.row_len + 64 * ds.n_sites_pad
-               + 16 * sizes["n_in_items"] + 16 * sizes["n_out_items"])
+               + 56 * sizes["n_in_items"] + 56 * sizes["n_out_items"])
 
 
 class PMMServer:

@@ -221,7 +221,8 @@ static void mstep(ora_tree* T, const double* cnt, double lr, int rounds) {
             const double a = e[0] * (1 + nu) + (e[1] + e[3]) * nu, b = e[1], c = e[2] + e[4];
 #define FP(x) (-a + b * inv_em1(x) + c * nu * inv_em1(nu * (x)))
             double lo = CEPS, hi = 1.0 / CEPS, res;
-            if (FP(lo) <= 0) res = lo;
+            if (a == 0 && b == 0 && c == 0) res = T->d[v];   /* flat: a zero gradient keeps d */
+            else if (FP(lo) <= 0) res = lo;
             else if (FP(hi) >= 0) res = hi;
             else {
                 double ul = log(lo), uh = log(hi);

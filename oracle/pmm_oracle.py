@@ -596,7 +596,10 @@ def mstep_compat(counts, leaf_resp_total, R, M, d, nu, phi, branch_mask, fix_nu,
             lo = np.full(len(d), CALC_EPS)
             hi = np.full(len(d), 1.0 / CALC_EPS)
             dn = _bisect_decreasing(fp, lo, hi)
-            d = np.where(mask, dn, d)
+            # a branch without expected counts has a zero gradient: the
+            # L-BFGS of laml.py:94-119 leaves it unchanged
+            flat = (a == 0) & (b == 0) & (c == 0)
+            d = np.where(mask & ~flat, dn, d)
         if not fix_nu:
             A = float(np.sum((e[:, 0] + e[:, 1] + e[:, 3]) * d))
 

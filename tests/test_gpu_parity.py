@@ -134,14 +134,17 @@ def test_compat_em_test4():
 
 
 def test_persistent_equals_per_level_launches():
+    """The three EM drivers (graph replay, per-level launches, persistent
+    kernel) give bitwise the same trajectories."""
     w = _wl(seed=5, n=60, K=20, T=4)
     out = []
-    for persistent in (True, False):
+    for path in ("persistent", "levels", "graph"):
         b = PB.make_batch(w.newicks, w.rows, w.Q, w.leaf_order, compat=True)
-        out.append(b.run_em(persistent=persistent, max_iters=50))
-    for a, c in zip(*out):
-        assert a.llh == c.llh and a.iterations == c.iterations
+        out.append(b.run_em(path=path, max_iters=50))
+    for a, c, g in zip(*out):
+        assert a.llh == c.llh == g.llh and a.iterations == c.iterations == g.iterations
         np.testing.assert_array_equal(a.branch_lengths, c.branch_lengths)
+        np.testing.assert_array_equal(a.branch_lengths, g.branch_lengths)
 
 
 def test_batched_equals_alone():
@@ -189,3 +192,21 @@ def test_em_large_tree_uses_global_mstep_staging():
     ref = O.em_compat(prob, prob.tree.branch_lengths, 0.5, 0.5, max_iters=6)
     assert r.iterations == ref.iterations
     assert r.llh == pytest.approx(ref.llh, rel=1e-6)
+
+
+def test_device_descriptors_equal_host_plan():
+    """laml_plan_descriptors on the device writes laml_plan_fill's bytes."""
+    from laml_gb300.encoding import plan_batch
+    from laml_gb300.engine import DeviceBatch
+    wa = synth.pmm_workload(40, 13, 3, 12, 0.5, 0.1, 0.15, seed=21, n_trees=3)
+    wb = synth.pmm_workload(25, 29, 3, 12, 0.5, 0.1, 0.15, seed=22, n_trees=2)
+    dss = [PB.dataset_from_rows(w.rows, w.Q, w.leaf_order, True, 8) for w in (wa, wb)]
+    trees = PB.encode_trees(wa.newicks, wa.leaf_order) + PB.encode_trees(wb.newicks,
+                                                                          wb.leaf_order)
+    tds = [0, 0, 0, 1, 1]
+    b = DeviceBatch(dss, trees, tds, [t.branch_length for t in trees], 0.3, 0.2)
+    torch.cuda.synchronize()
+    sizes, plan = plan_batch(trees, tds, dss)
+    for k, n in (("in_desc", 12 * sizes["n_in_items"]), ("out_desc", 12 * sizes["n_out_items"]),
+                 ("grp_desc", 8 * sizes["n_groups_total"])):
+        np.testing.assert_array_equal(b.work[k][:n].cpu().numpy(), plan[k][:n], err_msg=k)
