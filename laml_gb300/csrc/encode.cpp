@@ -4,6 +4,8 @@
 #include "laml_gb300.h"
 
 #include <algorithm>
+#include <charconv>
+#include <cctype>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -25,6 +27,25 @@ extern "C" const char* laml_last_error(void) { return laml::g_last_error.c_str()
 namespace {
 
 using laml::set_error;
+
+// f(begin, end) over [0, n) split into one contiguous range per host thread
+template <class F>
+void parallel_for(int64_t n, F f, int64_t min_parallel = 4096) {
+    int nt = (int)std::min<unsigned>(std::max(1u, std::thread::hardware_concurrency()), 16u);
+    if (n < min_parallel || nt <= 1) {
+        f((int64_t)0, n);
+        return;
+    }
+    std::vector<std::thread> th;
+    const int64_t chunk = (n + nt - 1) / nt;
+    for (int t = 0; t < nt; ++t) {
+        const int64_t a = t * chunk, e = std::min(n, a + chunk);
+        if (a >= e) break;
+        th.emplace_back([&f, a, e]() { f(a, e); });
+    }
+    for (auto& x : th) x.join();
+}
+
 
 // ---------------------------------------------------------------------------
 // newick
@@ -249,7 +270,9 @@ extern "C" int laml_newick_encode(const char* newick, const char* const* leaf_or
 
 // ---------------------------------------------------------------------------
 // batch newick encoding: many trees over one leaf set, one parse each,
-// parallel over trees
+// parallel over trees.  The parser is the state machine of parse_newick over
+// flat arrays (labels are views into the newick string), so a tree costs no
+// per-node allocation.
 // ---------------------------------------------------------------------------
 namespace {
 
@@ -265,6 +288,125 @@ int64_t raw_node_count(const char* s) {
     return n;
 }
 
+void raw_counts(int32_t n_trees, const char* const* newicks, std::vector<int64_t>& raw) {
+    raw.assign((size_t)n_trees + 1, 0);
+    parallel_for(n_trees, [&](int64_t a, int64_t e) {
+        for (int64_t i = a; i < e; ++i) raw[i + 1] = raw_node_count(newicks[i]);
+    }, 8);
+    for (int i = 0; i < n_trees; ++i) raw[i + 1] += raw[i];
+}
+
+struct FNode {
+    int32_t nch, ch0, ch1;
+    uint32_t lab_off, lab_len;
+    double len;
+    uint8_t has_len;
+};
+
+struct SV {
+    const char* p;
+    size_t n;
+    bool operator==(const SV& o) const { return n == o.n && std::memcmp(p, o.p, n) == 0; }
+};
+struct SVHash {
+    size_t operator()(const SV& v) const {
+        uint64_t h = 1469598103934665603ull;   // FNV-1a
+        for (size_t i = 0; i < v.n; ++i) h = (h ^ (unsigned char)v.p[i]) * 1099511628211ull;
+        return (size_t)h;
+    }
+};
+
+// a branch length token: the decimal forms through from_chars, anything else
+// (a sign, hex, inf/nan) through strtod, as parse_newick does
+bool parse_length(const char* b, const char* e, double* out) {
+    bool plain = b < e;
+    for (const char* q = b; q < e && plain; ++q)
+        plain = (*q >= '0' && *q <= '9') || *q == '.' || *q == 'e' || *q == 'E' || *q == '-';
+    if (plain) {
+        auto r = std::from_chars(b, e, *out);
+        if (r.ec == std::errc() && r.ptr != b) return true;
+    }
+    std::string tok(b, e);
+    char* endp = nullptr;
+    *out = std::strtod(tok.c_str(), &endp);
+    return !tok.empty() && endp != tok.c_str();
+}
+
+bool parse_flat(const char* s, std::vector<FNode>& nodes, std::vector<int>& stack) {
+    nodes.clear();
+    stack.clear();
+    nodes.push_back(FNode{0, -1, -1, 0, 0, 0.0, 0});
+    int cur = 0;
+    const char* base = s;
+    const char* p = s;
+    auto is_delim = [](char c) {
+        return c == ',' || c == '(' || c == ')' || c == ':' || c == ';' || c == '[' || c == 0;
+    };
+    auto add_child = [&](int par) {
+        const int c = (int)nodes.size();
+        nodes.push_back(FNode{0, -1, -1, 0, 0, 0.0, 0});
+        FNode& P = nodes[par];
+        if (P.nch == 0) P.ch0 = c; else if (P.nch == 1) P.ch1 = c;
+        ++P.nch;
+        return c;
+    };
+    for (;;) {
+        const char ch = *p;
+        if (ch == 0 || ch == ';') break;
+        if (ch == '(') {
+            const int c = add_child(cur);
+            stack.push_back(cur);
+            cur = c;
+            ++p;
+        } else if (ch == ',') {
+            if (stack.empty()) { set_error("newick: ',' outside parentheses"); return false; }
+            cur = add_child(stack.back());
+            ++p;
+        } else if (ch == ')') {
+            if (stack.empty()) { set_error("newick: unbalanced ')'"); return false; }
+            cur = stack.back();
+            stack.pop_back();
+            ++p;
+        } else if (ch == ':') {
+            const char* b = p + 1;
+            const char* e = b;
+            while (!is_delim(*e)) ++e;
+            const char* tb = b;
+            const char* te = e;
+            while (tb < te && std::isspace((unsigned char)*tb)) ++tb;
+            while (te > tb && std::isspace((unsigned char)te[-1])) --te;
+            double v;
+            if (!parse_length(tb, te, &v)) {
+                set_error("newick: bad length '" + std::string(tb, te) + "'");
+                return false;
+            }
+            nodes[cur].len = v;
+            nodes[cur].has_len = 1;
+            p = e;
+        } else if (ch == '[') {
+            const char* e = std::strchr(p, ']');
+            if (!e) { set_error("newick: unterminated comment"); return false; }
+            p = e + 1;
+        } else if (std::isspace((unsigned char)ch)) {
+            ++p;
+        } else {
+            const char* e = p;
+            while (!is_delim(*e)) ++e;
+            const char* tb = p;
+            const char* te = e;
+            while (tb < te && std::isspace((unsigned char)*tb)) ++tb;
+            while (te > tb && std::isspace((unsigned char)te[-1])) --te;
+            if (te > tb) {
+                nodes[cur].lab_off = (uint32_t)(tb - base);
+                nodes[cur].lab_len = (uint32_t)(te - tb);
+            }
+            p = e;
+        }
+    }
+    if (!stack.empty()) { set_error("newick: unbalanced '('"); return false; }
+    return true;
+}
+
 }  // namespace
 
 extern "C" int laml_newick_batch_measure(int32_t n_trees, const char* const* newicks,
@@ -273,9 +415,9 @@ extern "C" int laml_newick_batch_measure(int32_t n_trees, const char* const* new
         set_error("laml_newick_batch_measure: bad argument");
         return LAML_ERR_ARG;
     }
-    int64_t t = 0;
-    for (int i = 0; i < n_trees; ++i) t += raw_node_count(newicks[i]);
-    *raw_nodes_total = t;
+    std::vector<int64_t> raw;
+    raw_counts(n_trees, newicks, raw);
+    *raw_nodes_total = raw[n_trees];
     return LAML_OK;
 }
 
@@ -290,41 +432,66 @@ extern "C" int laml_newick_encode_batch(int32_t n_trees, const char* const* newi
         return LAML_ERR_ARG;
     }
     // raw offsets (upper bounds); compacted offsets are written afterwards
-    std::vector<int64_t> raw(n_trees + 1, 0);
-    for (int i = 0; i < n_trees; ++i) raw[i + 1] = raw[i] + raw_node_count(newicks[i]);
-    std::unordered_map<std::string, int> order;
+    std::vector<int64_t> raw;
+    raw_counts(n_trees, newicks, raw);
+    std::unordered_map<SV, int, SVHash> order;
     order.reserve((size_t)n_leaf_order * 2);
-    for (int k = 0; k < n_leaf_order; ++k) order.emplace(leaf_order[k], k);
+    for (int k = 0; k < n_leaf_order; ++k)
+        order.emplace(SV{leaf_order[k], std::strlen(leaf_order[k])}, k);
     std::vector<int64_t> used(n_trees, 0);
     std::vector<int> rc(n_trees, LAML_OK);
     std::vector<std::string> msg(n_trees);
     std::atomic<int> next{0};
     auto work = [&]() {
-        std::vector<PNode> nodes;
+        std::vector<FNode> nodes;
+        std::vector<int> stack, pre, id;
+        std::vector<uint8_t> seen((size_t)n_leaf_order, 0);
         for (;;) {
             const int i = next.fetch_add(1);
             if (i >= n_trees) break;
-            if (!parse_newick(newicks[i], nodes)) { rc[i] = LAML_ERR_PARSE; msg[i] = laml::g_last_error; continue; }
-            std::vector<int> pre = ts_preorder(nodes, 0);
-            int root = pre[0];
+            const char* s = newicks[i];
+            if (!parse_flat(s, nodes, stack)) { rc[i] = LAML_ERR_PARSE; msg[i] = laml::g_last_error; continue; }
+            const int NN = (int)nodes.size();
+            // treeswift preorder: children pushed in newick order, popped last-first
+            pre.clear();
+            stack.clear();
+            stack.push_back(0);
+            bool binary = true;
+            while (!stack.empty()) {
+                const int v = stack.back();
+                stack.pop_back();
+                pre.push_back(v);
+                const FNode& F = nodes[v];
+                if (F.nch > 2 || (F.nch == 1 && v != 0)) binary = false;
+                if (F.nch >= 1) stack.push_back(F.ch0);
+                if (F.nch >= 2) stack.push_back(F.ch1);
+            }
+            int root = 0;
             size_t first = 0;
-            if (nodes[root].children.size() == 1) { first = 1; root = nodes[root].children[0]; }
+            if (nodes[0].nch == 1) { first = 1; root = nodes[0].ch0; }
+            if (!binary || nodes[root].nch == 1) {
+                rc[i] = LAML_ERR_NOT_BINARY;
+                msg[i] = "tree " + std::to_string(i) + ": a node that does not have two children";
+                continue;
+            }
             // leaves take their leaf-order position; internal nodes follow in preorder
-            std::vector<int> id(nodes.size(), -1);
-            int nl = 0, ni = 0;
+            id.assign(NN, -1);
+            std::fill(seen.begin(), seen.end(), 0);
+            int nl = 0;
             for (size_t k = first; k < pre.size(); ++k) {
-                const PNode& v = nodes[pre[k]];
-                if (v.children.empty()) {
-                    auto it = v.has_label ? order.find(v.label) : order.end();
-                    if (it == order.end()) {
+                const FNode& v = nodes[pre[k]];
+                if (v.nch == 0) {
+                    auto it = v.lab_len ? order.find(SV{s + v.lab_off, v.lab_len}) : order.end();
+                    if (it == order.end() || seen[it->second]) {
                         rc[i] = LAML_ERR_LEAF;
-                        msg[i] = "leaf '" + v.label + "' is not in the leaf order";
+                        msg[i] = "leaf '" + std::string(s + v.lab_off, v.lab_len) +
+                                 (it == order.end() ? "' is not in the leaf order"
+                                                    : "' appears twice");
                         break;
                     }
+                    seen[it->second] = 1;
                     id[pre[k]] = it->second;
                     ++nl;
-                } else {
-                    ++ni;
                 }
             }
             if (rc[i]) continue;
@@ -335,32 +502,28 @@ extern "C" int laml_newick_encode_batch(int32_t n_trees, const char* const* newi
             }
             int nxt = nl;
             for (size_t k = first; k < pre.size(); ++k)
-                if (!nodes[pre[k]].children.empty()) id[pre[k]] = nxt++;
+                if (nodes[pre[k]].nch) id[pre[k]] = nxt++;
             const int64_t o = raw[i];
             int32_t* P = parent + o; int32_t* A = child0 + o; int32_t* B = child1 + o;
             double* D = branch_length + o; uint8_t* H = has_length + o;
             for (size_t k = first; k < pre.size(); ++k) {
-                const PNode& v = nodes[pre[k]];
+                const FNode& v = nodes[pre[k]];
                 const int u = id[pre[k]];
-                D[u] = v.has_length ? v.length : 0.0;
-                H[u] = v.has_length ? 1 : 0;
+                D[u] = v.has_len ? v.len : 0.0;
+                H[u] = v.has_len;
                 if (pre[k] == root) P[u] = -1;
-                if (v.children.size() == 2) {
-                    A[u] = id[v.children[1]];
-                    B[u] = id[v.children[0]];
-                    P[id[v.children[0]]] = u;
-                    P[id[v.children[1]]] = u;
-                } else if (!v.children.empty()) {
-                    rc[i] = LAML_ERR_NOT_BINARY;
-                    msg[i] = "tree " + std::to_string(i) + ": a node with " +
-                             std::to_string(v.children.size()) + " children";
-                    break;
+                if (v.nch == 2) {
+                    // networkx successor order = preorder visit order = reversed newick order
+                    A[u] = id[v.ch1];
+                    B[u] = id[v.ch0];
+                    P[id[v.ch0]] = u;
+                    P[id[v.ch1]] = u;
                 } else {
                     A[u] = -1;
                     B[u] = -1;
                 }
             }
-            used[i] = nl + ni;
+            used[i] = nxt;
             num_leaves[i] = nl;
         }
     };
@@ -621,23 +784,6 @@ int tree_levels(int N, int n, const int32_t* c0, const int32_t* c1, TreeLevels& 
 
 namespace {
 
-template <class F>
-void parallel_for(int64_t n, F f) {
-    int nt = (int)std::min<unsigned>(std::max(1u, std::thread::hardware_concurrency()), 16u);
-    if (n < 4096 || nt <= 1) {
-        f((int64_t)0, n);
-        return;
-    }
-    std::vector<std::thread> th;
-    const int64_t chunk = (n + nt - 1) / nt;
-    for (int t = 0; t < nt; ++t) {
-        const int64_t a = t * chunk, e = std::min(n, a + chunk);
-        if (a >= e) break;
-        th.emplace_back([&f, a, e]() { f(a, e); });
-    }
-    for (auto& x : th) x.join();
-}
-
 struct PlanScratch {
     std::vector<TreeLevels> lv;
     std::vector<int> root;
@@ -668,7 +814,7 @@ int plan_levels(const laml_plan_input* in, PlanScratch& S, laml_plan_sizes* sz) 
                                  in->child1 + nb, S.lv[p], &S.root[p]);
             if (rcs[p]) msgs[p] = laml::g_last_error;
         }
-    });
+    }, 8);
     for (int p = 0; p < T; ++p)
         if (rcs[p]) { set_error(msgs[p]); return rcs[p]; }
     int hmax = 0, dmax = 0;
@@ -764,38 +910,90 @@ extern "C" int laml_plan_fill(const laml_plan_input* in, laml_plan_output* o) {
                 }
             }
         }
-    });
-    // level buckets: inside by height, outside by the depth of the internal parent
-    std::vector<std::vector<int>> in_lv(H + 1), out_lv(D + 1);
-    for (int p = 0; p < T; ++p) {
-        const int N = in->tree_nodes[p], n = in->tree_leaves[p];
-        const int64_t nb = S.node_base[p];
-        const TreeLevels& L = S.lv[p];
-        for (int u = n; u < N; ++u) {
-            in_lv[L.height[u]].push_back((int)(nb + u));
-            out_lv[L.depth[u] + 1].push_back((int)(nb + u));
+    }, 8);
+    // level buckets: inside by height, outside by the depth of the internal
+    // parent; within a level, trees in order and nodes ascending.  Per-tree
+    // level counts, a prefix over (level, tree), then a parallel scatter.
+    const int NL[2] = {H, D};
+    std::vector<int64_t> lcnt[2];
+    for (int s2 = 0; s2 < 2; ++s2) lcnt[s2].assign((size_t)T * (NL[s2] + 1), 0);
+    auto level_of = [&](const TreeLevels& L, int u, int side) {
+        return side == 0 ? L.height[u] : L.depth[u] + 1;
+    };
+    parallel_for(T, [&](int64_t a, int64_t e) {
+        for (int64_t p = a; p < e; ++p) {
+            const int N = in->tree_nodes[p], n = in->tree_leaves[p];
+            const TreeLevels& L = S.lv[p];
+            for (int side = 0; side < 2; ++side) {
+                int64_t* c = lcnt[side].data() + (size_t)p * (NL[side] + 1);
+                for (int u = n; u < N; ++u) ++c[level_of(L, u, side)];
+            }
         }
+    }, 8);
+    std::vector<int64_t> lstart[2];     // [level + 1]: first slot of the level
+    std::vector<int32_t> lnodes[2];
+    for (int side = 0; side < 2; ++side) {
+        const int nl = NL[side];
+        lstart[side].assign(nl + 2, 0);
+        int64_t acc = 0;
+        for (int l = 0; l <= nl; ++l) {
+            lstart[side][l] = acc;
+            for (int p = 0; p < T; ++p) {
+                int64_t& c = lcnt[side][(size_t)p * (nl + 1) + l];
+                const int64_t x = c;
+                c = acc;          // becomes the tree's first slot in the level
+                acc += x;
+            }
+        }
+        lstart[side][nl + 1] = acc;
+        lnodes[side].assign(acc, 0);
     }
+    parallel_for(T, [&](int64_t a, int64_t e) {
+        for (int64_t p = a; p < e; ++p) {
+            const int N = in->tree_nodes[p], n = in->tree_leaves[p];
+            const int64_t nb = S.node_base[p];
+            const TreeLevels& L = S.lv[p];
+            for (int side = 0; side < 2; ++side) {
+                int64_t* c = lcnt[side].data() + (size_t)p * (NL[side] + 1);
+                for (int u = n; u < N; ++u) lnodes[side][c[level_of(L, u, side)]++] = (int32_t)(nb + u);
+            }
+        }
+    }, 8);
     // items, group-major within a level (groups are sorted by state count)
-    auto emit = [&](const std::vector<std::vector<int>>& lv, int first, int last, int32_t* off,
-                    int32_t* items) {
+    bool uniform = true;
+    for (int p = 0; p < T; ++p) uniform = uniform && in->ds_groups[in->tree_dataset[p]] == maxNG;
+    auto emit = [&](int side, int first, int last, int32_t* off, int32_t* items) {
+        const int32_t* nodes = lnodes[side].data();
         int64_t k = 0;
         for (int l = first; l <= last; ++l) {
             off[l - first] = (int32_t)k;
-            for (int g = 0; g < maxNG; ++g)
-                for (int node : lv[l]) {
-                    const int d = in->tree_dataset[o->nd_tree[node]];
-                    if (g < in->ds_groups[d]) {
-                        items[2 * k] = node;
-                        items[2 * k + 1] = g;
-                        ++k;
+            const int64_t a = lstart[side][l], e = lstart[side][l + 1], cnt = e - a;
+            if (uniform) {
+                int32_t* it = items + 2 * k;
+                parallel_for(cnt, [&](int64_t x0, int64_t x1) {
+                    for (int g = 0; g < maxNG; ++g)
+                        for (int64_t x = x0; x < x1; ++x) {
+                            it[2 * (g * cnt + x)] = nodes[a + x];
+                            it[2 * (g * cnt + x) + 1] = g;
+                        }
+                }, 1 << 15);
+                k += cnt * maxNG;
+            } else {
+                for (int g = 0; g < maxNG; ++g)
+                    for (int64_t x = a; x < e; ++x) {
+                        const int node = nodes[x];
+                        if (g < in->ds_groups[in->tree_dataset[o->nd_tree[node]]]) {
+                            items[2 * k] = node;
+                            items[2 * k + 1] = g;
+                            ++k;
+                        }
                     }
-                }
+            }
         }
         off[last - first + 1] = (int32_t)k;
     };
-    emit(in_lv, 1, H, o->in_level_off, o->in_items);
-    emit(out_lv, 1, D, o->out_level_off, o->out_items);
+    emit(0, 1, H, o->in_level_off, o->in_items);
+    emit(1, 1, D, o->out_level_off, o->out_items);
     int64_t k = 0;
     for (int g = 0; g < maxNG; ++g)
         for (int p = 0; p < T; ++p) {

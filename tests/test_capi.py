@@ -181,3 +181,83 @@ def test_item_descriptors_match_plan():
             assert e[1] == sum(kp[:d]) + g * 8
             assert e[2] == sum(x.row_len for x in dss[:d]) + ds.group_off[g]
             assert e[4] == sum(x.codes.size for x in dss[:d]) and e[6] == ds.n_sites
+
+
+@pytest.mark.parametrize("nw", [
+    "((a:1,b:2):0.5,(c:+1e-3,d:0x1p-2):0.25);",
+    "(((a,b),c),d);",
+    "( a : 1.5 , [note] b:2 ) ;",
+    "((a:1,b:1)n1:1,(c:1e-7,d:1):1)root;",
+    "(((a:0.1,b:0.2):0.3,c:1):0.7);",
+])
+def test_batch_parser_equals_single_tree_parser(nw):
+    """laml_newick_encode_batch (flat parser) and laml_newick_encode agree
+    on signs, hex lengths, comments, whitespace, unifurcating roots."""
+    lo = sorted({ch for ch in "abcd" if ch in nw})
+    s = E.encode_newick(nw, lo)
+    b = E.encode_newick_batch([nw], lo)[0]
+    for f in ("parent", "child0", "child1", "branch_length", "has_length"):
+        np.testing.assert_array_equal(getattr(s, f), getattr(b, f), err_msg=f)
+
+
+def test_batch_parser_errors():
+    with pytest.raises(N.LamlError):
+        E.encode_newick_batch(["((a,b),(a,c));"], ["a", "b", "c"])     # duplicate leaf
+    with pytest.raises(N.LamlError):
+        E.encode_newick_batch(["((a,b,c),d);"], ["a", "b", "c", "d"])  # not binary
+    with pytest.raises(N.LamlError):
+        E.encode_newick_batch(["((a,b),c"], ["a", "b", "c"])           # unbalanced
+    with pytest.raises(N.LamlError):
+        E.encode_newick_batch(["((((a,b))),c);"], ["a", "b", "c"])     # inner unifurcation
+
+
+def _expected_items(trees, tree_ds, dss, side):
+    """The schedule spelled out: per level (inside: node height; outside:
+    depth of the internal parent + 1), groups outermost, then trees in order
+    and nodes ascending."""
+    levels = {}
+    base = 0
+    for p, t in enumerate(trees):
+        N, n = t.num_nodes, t.num_leaves
+        h = np.zeros(N, int)
+        dep = np.zeros(N, int)
+        par = t.parent
+        # depth by walking up; height by relaxation until nothing changes
+        for u in range(N):
+            x, k = u, 0
+            while par[x] >= 0:
+                x, k = par[x], k + 1
+            dep[u] = k
+        changed = True
+        while changed:
+            changed = False
+            for u in range(n, N):
+                hu = 1 + max(h[t.child0[u]], h[t.child1[u]])
+                if hu != h[u]:
+                    h[u], changed = hu, True
+        ng = dss[tree_ds[p]].n_groups
+        for u in range(n, N):
+            lv = h[u] if side == "in" else dep[u] + 1
+            levels.setdefault(lv, []).append((base + u, ng))
+        base += N
+    out = []
+    for lv in sorted(levels):
+        for g in range(max(d.n_groups for d in dss)):
+            out += [(node, g) for node, ng in levels[lv] if g < ng]
+    return np.asarray(out, np.int32)
+
+
+@pytest.mark.parametrize("site_counts", [(5, 5), (21, 5), (12, 40)])
+def test_item_order_is_the_documented_schedule(site_counts):
+    """Uniform group counts take the parallel scatter, mixed ones the general
+    loop; both give the documented order."""
+    rng = np.random.default_rng(17)
+    trees = [E.encode_newick(synth.yule_tree(n, rng).newick()) for n in (9, 31, 4, 17)]
+    mats = [np.zeros((31, k), np.int32) for k in site_counts]
+    dss = [E.encode_dataset(m, [{1: 1.0}] * m.shape[1], compat=True, group_sites=8)
+           for m in mats]
+    tree_ds = [0, 1, 0, 1]
+    sizes, a = E.plan_batch(trees, tree_ds, dss)
+    for side in ("in", "out"):
+        got = a[f"{side}_items"][:2 * sizes[f"n_{side}_items"]].reshape(-1, 2)
+        np.testing.assert_array_equal(got, _expected_items(trees, tree_ds, dss, side))
