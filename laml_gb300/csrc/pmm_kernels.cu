@@ -27,6 +27,7 @@
 // with P00 = e^{-d(1+nu)}, Pmut = (1-e^{-d}) e^{-nu d}, Pstay = e^{-nu d},
 // Psil = 1-e^{-nu d}.
 #include <cuda_runtime.h>
+#include <math_constants.h>
 #include <stdint.h>
 
 #include <algorithm>
@@ -173,176 +174,113 @@ __device__ __forceinline__ bool site_ctx(const laml_batch& b, int node, int g, i
 }
 
 // ---------------------------------------------------------------------------
-// inside: one internal node, one site
+// The root edge in log space.  fast_em's root E-step row reads node N-1
+// (parent_sibling[root] = (-1, -1)), so the counts that set the root's branch
+// length are not the root's own, and EM can drive that length far past where
+// e^{-d(1+nu)} has an FP32 (or FP64) value while the root itself stays in
+// state 0 at every site.  Everything that multiplies by a root-edge term is
+// therefore formed from the terms' logarithms in FP64: the site likelihood
+// (kept as an FP32 mantissa in [0.5, 1) and an int exponent), the root's
+// posteriors, its E-step row and the outside inputs of its two children.
 // ---------------------------------------------------------------------------
-template <int G>
-__device__ void inside_item(const laml_batch& b, int u, int g, int lane, bool respect_status) {
-    SiteCtx s;
-    if (!site_ctx<G>(b, u, g, lane, respect_status, s)) return;
-    const Leaf L = leaf_params(b, s.tree);
-    const int v = __ldg(b.nd_c0 + u), w = __ldg(b.nd_c1 + u);
-    const Child cv = load_child<G>(b, v, s.ds, s.site, s.goff, lane, s.qrow, s.sumq, L);
-    const Child cw = load_child<G>(b, w, s.ds, s.site, s.goff, lane, s.qrow, s.sumq, L);
-    const float4 bv = load_bt(b, v), bw = load_bt(b, w);   // P00, Pmut, Pstay, Psil
-    const float ev0 = bv.x * cv.s0 + bv.y * cv.D + bv.w * cv.ss;
-    const float ew0 = bw.x * cw.s0 + bw.y * cw.D + bw.w * cw.ss;
-    const float kv = bv.w * cv.ss, kw = bw.w * cw.ss;
-    float* row = b.in_part + __ldg(b.nd_prow + u) + s.goff + lane;
-    const float s0 = ev0 * ew0, ss = cv.ss * cw.ss;
-    __stcg(row, s0);
-    __stcg(row + G, ss);
-    float mx = fmaxf(s0, ss), dot = 0.f;
-    int j = 2;
-    // CH states per step: every load of a step is issued before its stores
-    for (; j + kChunk <= s.C; j += kChunk) {
-        float av[kChunk], aw[kChunk], qv[kChunk];
-#pragma unroll
-        for (int k = 0; k < kChunk; ++k) {
-            av[k] = child_val<G>(cv, j + k);
-            aw[k] = child_val<G>(cw, j + k);
-            qv[k] = __ldg(s.qrow + (j + k) * G);
-        }
-#pragma unroll
-        for (int k = 0; k < kChunk; ++k) {
-            const float x = fmaf(bv.z, av[k], kv) * fmaf(bw.z, aw[k], kw);
-            __stcg(row + (j + k) * G, x);
-            dot = fmaf(qv[k], x, dot);
-            mx = fmaxf(mx, x);
-        }
+struct RootEdge {
+    double l00, lm, lst, ls;   // log P00, log Pmut (without q), log Pstay, log Psil
+};
+
+__device__ __forceinline__ RootEdge root_edge_logs(const laml_batch& b, int tree) {
+    const int r = __ldg(b.tr_root + tree);
+    const double d = __ldcg(b.nd_d + r), nu = __ldcg(b.tr_nu + tree), nd = d * nu;
+    RootEdge e;
+    e.l00 = -d * (1.0 + nu);
+    e.lst = -nd;
+    e.lm = log((b.compat && d < kEPSd) ? kEPSd : -expm1(-d)) - nd;
+    e.ls = (b.compat && nd < kEPSd) ? log(kEPSd) : log(-expm1(-nd));
+    return e;
+}
+
+// log of a non-negative FP32 value (-inf at 0)
+__device__ __forceinline__ double logz(float x) {
+    return x > 0.f ? log((double)x) : -CUDART_INF;
+}
+
+__device__ __forceinline__ double lse3(double a, double b, double c) {
+    const double m = fmax(a, fmax(b, c));
+    if (m == -CUDART_INF) return m;
+    return m + log(exp(a - m) + exp(b - m) + exp(c - m));
+}
+
+// exp(l) as an FP32 value (0 below its range)
+__device__ __forceinline__ float expz(double l) { return (float)exp(l); }
+
+// Root edge from a progenitor in state 0 (calculations.py:270-276, 504): s0,
+// dt (= sum_a q_a in_a) and ss are the root's inside values at scale 2^X.
+__device__ __forceinline__ void root_site_llh(const laml_batch& b, int tree, int site,
+                                              const RootEdge& re, float s0, float dt, float ss,
+                                              int X) {
+    const double l = lse3(re.l00 + logz(s0), re.lm + logz(dt), re.ls + logz(ss));
+    const int64_t t = __ldg(b.tr_site_base + tree) + site;
+    int e = 0;
+    float m = 0.f;
+    if (l > -CUDART_INF) {
+        e = (int)floor(l / kLn2) + 1;
+        m = (float)exp(l - (double)e * kLn2);
     }
-    for (; j < s.C; ++j) {
-        const float av = child_val<G>(cv, j), aw = child_val<G>(cw, j);
-        const float x = fmaf(bv.z, av, kv) * fmaf(bw.z, aw, kw);
-        __stcg(row + j * G, x);
-        dot = fmaf(__ldg(s.qrow + j * G), x, dot);
-        mx = fmaxf(mx, x);
-    }
-    const int h = scale_exp(mx);
-    const float f = pow2i(-h);
-    const int X = cv.X + cw.X + h;
-    const int64_t sr = __ldg(b.nd_srow + u) + s.site;
-    __stcg(b.in_h + sr, h);
-    __stcg(b.in_x + sr, X);
-    __stcg(b.in_dot + sr, dot * f);
-    if (u == __ldg(b.tr_root + s.tree)) {
-        // the root edge from a progenitor in state 0 (calculations.py:270-276, 504)
-        const float4 br = load_bt(b, u);
-        const float lr = br.x * (s0 * f) + br.y * (dot * f) + br.w * (ss * f);
-        const int64_t t = __ldg(b.tr_site_base + s.tree) + s.site;
-        __stcg(b.root_lr + t, lr);
-        __stcg(b.root_x + t, X);
-        __stcg(b.llh_site + t, (double)logf(lr) + (double)X * kLn2);
-    }
+    __stcg(b.root_lr + t, m);
+    __stcg(b.root_x + t, X + e);
+    __stcg(b.llh_site + t, l + (double)X * kLn2);
+}
+
+// log of 1 / (site likelihood) at scale 2^X
+__device__ __forceinline__ double root_log_scale(const laml_batch& b, int tree, int site, int X) {
+    const int64_t t = __ldg(b.tr_site_base + tree) + site;
+    const float m = __ldcg(b.root_lr + t);
+    if (!(m > 0.f)) return -CUDART_INF;   // a zero likelihood: no responsibilities
+    return (double)(X - __ldcg(b.root_x + t)) * kLn2 - log((double)m);
 }
 
 // ---------------------------------------------------------------------------
-// outside + counts: one node v (leaf or internal, not the root), one site.
-// mode 0: x = out[parent] * E[sibling]; mode 1: the root with
-// parent = sibling = node N-1 (fast_em/laml.py:244-246 + calculations.py:418);
-// mode 2: the root below a progenitor in state 0 (EM_solver.py:282-286).
+// E-step row of a root (the root edge's expected counts), one site.
+// mode 1: fast_em's row with parent = sibling = node N-1 (fast_em/laml.py:
+// 244-246 + calculations.py:418); mode 2: below a progenitor in state 0
+// (EM_solver.py:282-286).
 // ---------------------------------------------------------------------------
 template <int G>
-__device__ void outside_item(const laml_batch& b, int v, int g, int lane, bool act, int mode,
-                             bool want_post) {
-    float c00 = 0.f, c0a = 0.f, c0s = 0.f, caa = 0.f, cas = 0.f, css = 0.f, lr = 0.f, lro = 0.f;
+__device__ void root_counts_item(const laml_batch& b, int v, int g, int lane, bool act,
+                                 int mode) {
+    float c00 = 0.f, c0a = 0.f, c0s = 0.f, caa = 0.f, cas = 0.f, css = 0.f;
     SiteCtx s;
-    bool live = act && site_ctx<G>(b, v, g, lane, true, s);
-    const bool leaf_v = act && __ldg(b.nd_c0 + v) < 0;
+    const bool live = act && site_ctx<G>(b, v, g, lane, true, s);
     if (live) {
         const Leaf L = leaf_params(b, s.tree);
         const Child cv = load_child<G>(b, v, s.ds, s.site, s.goff, lane, s.qrow, s.sumq, L);
-        const float4 bv = load_bt(b, v);
-        float x0, xs, sumx = 0.f, dotxv = 0.f, out0, outs;
-        int Xx;
-        float* orow = nullptr;
-        float mx = 0.f;
-        if (mode == 2) {
-            x0 = 1.f;
-            xs = 0.f;
-            Xx = 0;
-        } else {
-            const int u = mode == 0 ? __ldg(b.nd_parent + v) : __ldg(b.tr_quirk + s.tree);
-            const int w = mode == 0 ? __ldg(b.nd_sib + v) : u;
-            const Child cw = load_child<G>(b, w, s.ds, s.site, s.goff, lane, s.qrow, s.sumq, L);
-            const float4 bw = load_bt(b, w);
+        const RootEdge re = root_edge_logs(b, s.tree);
+        float x0 = 1.f, xs = 0.f, sumx = 0.f, dotxv = 0.f;
+        int Xx = 0;
+        if (mode == 1) {
+            const int u = __ldg(b.tr_quirk + s.tree);
+            const Child cw = load_child<G>(b, u, s.ds, s.site, s.goff, lane, s.qrow, s.sumq, L);
+            const float4 bw = load_bt(b, u);
             const int64_t su = __ldg(b.nd_srow + u) + s.site;
             const float fo = pow2i(-__ldcg(b.out_h + su));
-            const int Xo = __ldcg(b.out_x + su);
             const float* urow = b.out_part + __ldg(b.nd_prow + u) + s.goff + lane;
-            const float o0 = __ldcg(urow) * fo, os = __ldcg(urow + G) * fo;
-            x0 = o0 * (bw.x * cw.s0 + bw.y * cw.D + bw.w * cw.ss);
-            xs = os * cw.ss;
-            Xx = Xo + cw.X;
+            x0 = __ldcg(urow) * fo * (bw.x * cw.s0 + bw.y * cw.D + bw.w * cw.ss);
+            xs = __ldcg(urow + G) * fo * cw.ss;
+            Xx = __ldcg(b.out_x + su) + cw.X;
             const float kw = bw.w * cw.ss;
-            const bool write = (mode == 0) && cv.row != nullptr;
-            if (write) orow = b.out_part + __ldg(b.nd_prow + v) + s.goff + lane;
-            const float px = bv.y * x0;
-            int j = 2;
-            for (; j + kChunk <= s.C; j += kChunk) {
-                float ou[kChunk], aw[kChunk], av[kChunk], qv[kChunk];
-#pragma unroll
-                for (int k = 0; k < kChunk; ++k) {
-                    ou[k] = __ldcg(urow + (j + k) * G);
-                    aw[k] = child_val<G>(cw, j + k);
-                    av[k] = child_val<G>(cv, j + k);
-                    qv[k] = __ldg(s.qrow + (j + k) * G);
-                }
-#pragma unroll
-                for (int k = 0; k < kChunk; ++k) {
-                    const float xa = ou[k] * fo * fmaf(bw.z, aw[k], kw);
-                    sumx += xa;
-                    dotxv = fmaf(xa, av[k], dotxv);
-                    if (write) {
-                        const float o = fmaf(px, qv[k], bv.z * xa);
-                        __stcg(orow + (j + k) * G, o);
-                        mx = fmaxf(mx, o);
-                    }
-                }
-            }
-            for (; j < s.C; ++j) {
-                const float ou = __ldcg(urow + j * G) * fo;
-                const float xa = ou * fmaf(bw.z, child_val<G>(cw, j), kw);
+            for (int j = 2; j < s.C; ++j) {
+                const float xa = __ldcg(urow + j * G) * fo * fmaf(bw.z, child_val<G>(cw, j), kw);
                 sumx += xa;
                 dotxv = fmaf(xa, child_val<G>(cv, j), dotxv);
-                if (write) {
-                    const float o = fmaf(px, __ldg(s.qrow + j * G), bv.z * xa);
-                    __stcg(orow + j * G, o);
-                    mx = fmaxf(mx, o);
-                }
             }
         }
-        out0 = bv.x * x0;
-        outs = bv.w * (x0 + sumx) + xs;
-        if (orow) {
-            __stcg(orow, out0);
-            __stcg(orow + G, outs);
-            const int h = scale_exp(fmaxf(mx, fmaxf(out0, outs)));
-            const int64_t sv = __ldg(b.nd_srow + v) + s.site;
-            __stcg(b.out_h + sv, h);
-            __stcg(b.out_x + sv, Xx + h);
-        }
-        // responsibilities (calculations.py:418-451), divided by the site likelihood
-        const int64_t t = __ldg(b.tr_site_base + s.tree) + s.site;
-        const float lroot = __ldcg(b.root_lr + t);
-        const int e = Xx + cv.X - __ldcg(b.root_x + t);
-        const float sc = (lroot > 0.f) ? ldexpf(1.f / lroot, e) : 0.f;
-        c00 = x0 * cv.s0 * bv.x * sc;
-        c0a = x0 * bv.y * cv.D * sc;
-        c0s = x0 * cv.ss * bv.w * sc;
-        caa = bv.z * dotxv * sc;
-        cas = bv.w * cv.ss * sumx * sc;
-        css = xs * cv.ss * sc;
-        if (leaf_v) {   // P(leaf silenced | D): '?' entries and observed entries apart
-            const float pl = cv.ss * outs * sc;
-            if (cv.code == -1) lr = pl; else lro = pl;
-        }
-        if (want_post && b.post0 && mode == 0) {
-            const int64_t pb = __ldg(b.tr_post_base + s.tree) +
-                               (int64_t)(v - __ldg(b.tr_node_base + s.tree)) *
-                                   __ldg(b.ds_sites_pad + s.ds) + s.site;
-            __stcg(b.post0 + pb, cv.s0 * out0 * sc);
-            __stcg(b.post1 + pb, cv.ss * outs * sc);
-        }
+        // responsibilities (calculations.py:418-451) over the site likelihood
+        const double lsc = root_log_scale(b, s.tree, s.site, Xx + cv.X);
+        c00 = expz(logz(x0 * cv.s0) + re.l00 + lsc);
+        c0a = expz(logz(x0 * cv.D) + re.lm + lsc);
+        c0s = expz(logz(x0 * cv.ss) + re.ls + lsc);
+        caa = expz(logz(dotxv) + re.lst + lsc);
+        cas = expz(logz(cv.ss * sumx) + re.ls + lsc);
+        css = expz(logz(xs * cv.ss) + lsc);
     }
     // sum over the G sites of the group
 #pragma unroll
@@ -353,8 +291,6 @@ __device__ void outside_item(const laml_batch& b, int v, int g, int lane, bool a
         caa += __shfl_xor_sync(kFull, caa, off);
         cas += __shfl_xor_sync(kFull, cas, off);
         css += __shfl_xor_sync(kFull, css, off);
-        lr += __shfl_xor_sync(kFull, lr, off);
-        lro += __shfl_xor_sync(kFull, lro, off);
     }
     if (act && lane == 0) {
         const int tree = __ldg(b.nd_tree + v);
@@ -365,7 +301,7 @@ __device__ void outside_item(const laml_batch& b, int v, int g, int lane, bool a
                 b.cnt_part + __ldg(b.tr_cnt_base + tree) +
                 ((int64_t)(v - __ldg(b.tr_node_base + tree)) * NG + g) * 8);
             __stcg(dst, make_float4(c00, c0a, c0s, caa));
-            __stcg(dst + 1, make_float4(cas, css, lr, lro));
+            __stcg(dst + 1, make_float4(cas, css, 0.f, 0.f));
         }
     }
 }
@@ -429,109 +365,6 @@ __device__ __forceinline__ void write_counts(const laml_batch& b, int tree, int 
         ((int64_t)(v - __ldg(b.tr_node_base + tree)) * NG + g) * 8);
     __stcg(dst, make_float4(c[0], c[1], c[2], c[3]));
     __stcg(dst + 1, make_float4(c[4], c[5], c[6], c[7]));
-}
-
-template <int G>
-__device__ void outside_parent_item(const laml_batch& b, int u, int g, int lane, bool act,
-                                    bool want_post) {
-    float cv_[8] = {0, 0, 0, 0, 0, 0, 0, 0}, cw_[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-    SiteCtx s;
-    const bool live = act && site_ctx<G>(b, u, g, lane, true, s);
-    const int v = act ? __ldg(b.nd_c0 + u) : 0, w = act ? __ldg(b.nd_c1 + u) : 0;
-    if (live) {
-        const Leaf L = leaf_params(b, s.tree);
-        const Child cv = load_child<G>(b, v, s.ds, s.site, s.goff, lane, s.qrow, s.sumq, L);
-        const Child cw = load_child<G>(b, w, s.ds, s.site, s.goff, lane, s.qrow, s.sumq, L);
-        const float4 bv = load_bt(b, v), bw = load_bt(b, w);
-        const int64_t su = __ldg(b.nd_srow + u) + s.site;
-        const float fo = pow2i(-__ldcg(b.out_h + su));
-        const int Xo = __ldcg(b.out_x + su);
-        const float* urow = b.out_part + __ldg(b.nd_prow + u) + s.goff + lane;
-        const float o0 = __ldcg(urow) * fo, os = __ldcg(urow + G) * fo;
-        const float ev0 = bv.x * cv.s0 + bv.y * cv.D + bv.w * cv.ss;
-        const float ew0 = bw.x * cw.s0 + bw.y * cw.D + bw.w * cw.ss;
-        ChildOut A, B;   // A: child v (uses E[w]), B: child w (uses E[v])
-        A.x0 = o0 * ew0; A.xs = os * cw.ss; A.X = Xo + cw.X;
-        B.x0 = o0 * ev0; B.xs = os * cv.ss; B.X = Xo + cv.X;
-        A.sumx = A.dot = A.mx = 0.f;
-        B.sumx = B.dot = B.mx = 0.f;
-        A.orow = cv.row ? b.out_part + __ldg(b.nd_prow + v) + s.goff + lane : nullptr;
-        B.orow = cw.row ? b.out_part + __ldg(b.nd_prow + w) + s.goff + lane : nullptr;
-        const float kv = bv.w * cv.ss, kw = bw.w * cw.ss;
-        const float pxa = bv.y * A.x0, pxb = bw.y * B.x0;
-        int j = 2;
-        for (; j + kChunk <= s.C; j += kChunk) {
-            float ou[kChunk], av[kChunk], aw[kChunk], qv[kChunk];
-#pragma unroll
-            for (int k = 0; k < kChunk; ++k) {
-                ou[k] = __ldcg(urow + (j + k) * G);
-                av[k] = child_val<G>(cv, j + k);
-                aw[k] = child_val<G>(cw, j + k);
-                qv[k] = __ldg(s.qrow + (j + k) * G);
-            }
-#pragma unroll
-            for (int k = 0; k < kChunk; ++k) {
-                const float o = ou[k] * fo;
-                const float xa = o * fmaf(bw.z, aw[k], kw);   // into v
-                const float xb = o * fmaf(bv.z, av[k], kv);   // into w
-                A.sumx += xa;
-                A.dot = fmaf(xa, av[k], A.dot);
-                B.sumx += xb;
-                B.dot = fmaf(xb, aw[k], B.dot);
-                if (A.orow) {
-                    const float r = fmaf(pxa, qv[k], bv.z * xa);
-                    __stcg(A.orow + (j + k) * G, r);
-                    A.mx = fmaxf(A.mx, r);
-                }
-                if (B.orow) {
-                    const float r = fmaf(pxb, qv[k], bw.z * xb);
-                    __stcg(B.orow + (j + k) * G, r);
-                    B.mx = fmaxf(B.mx, r);
-                }
-            }
-        }
-        for (; j < s.C; ++j) {
-            const float o = __ldcg(urow + j * G) * fo;
-            const float av = child_val<G>(cv, j), aw = child_val<G>(cw, j);
-            const float qj = __ldg(s.qrow + j * G);
-            const float xa = o * fmaf(bw.z, aw, kw);
-            const float xb = o * fmaf(bv.z, av, kv);
-            A.sumx += xa;
-            A.dot = fmaf(xa, av, A.dot);
-            B.sumx += xb;
-            B.dot = fmaf(xb, aw, B.dot);
-            if (A.orow) {
-                const float r = fmaf(pxa, qj, bv.z * xa);
-                __stcg(A.orow + j * G, r);
-                A.mx = fmaxf(A.mx, r);
-            }
-            if (B.orow) {
-                const float r = fmaf(pxb, qj, bw.z * xb);
-                __stcg(B.orow + j * G, r);
-                B.mx = fmaxf(B.mx, r);
-            }
-        }
-        const int64_t t = __ldg(b.tr_site_base + s.tree) + s.site;
-        const float lroot = __ldcg(b.root_lr + t);
-        const int xroot = __ldcg(b.root_x + t);
-        child_finish<G>(b, s, v, cv, bv, A, want_post, lroot, xroot, cv_);
-        child_finish<G>(b, s, w, cw, bw, B, want_post, lroot, xroot, cw_);
-    }
-#pragma unroll
-    for (int off = G / 2; off > 0; off >>= 1) {
-#pragma unroll
-        for (int k = 0; k < 8; ++k) {
-            cv_[k] += __shfl_xor_sync(kFull, cv_[k], off);
-            cw_[k] += __shfl_xor_sync(kFull, cw_[k], off);
-        }
-    }
-    if (act && lane == 0) {
-        const int tree = __ldg(b.nd_tree + u);
-        if (__ldcg(b.tr_status + tree) == LAML_TREE_ACTIVE) {
-            write_counts<G>(b, tree, v, g, cv_);
-            write_counts<G>(b, tree, w, g, cw_);
-        }
-    }
 }
 
 // ---------------------------------------------------------------------------
@@ -659,15 +492,8 @@ __device__ void inside_item_d(const laml_batch& b, const ItemDesc& d, int lane,
     __stcg(b.in_h + sr, h);
     __stcg(b.in_x + sr, X);
     __stcg(b.in_dot + sr, dot * f);
-    if (d.flags & 4) {
-        // the root edge from a progenitor in state 0 (calculations.py:270-276, 504)
-        const float4 br = load_bt(b, d.u);
-        const float lr = br.x * (s0 * f) + br.y * (dot * f) + br.w * (ss * f);
-        const int64_t t = __ldg(b.tr_site_base + s.tree) + s.site;
-        __stcg(b.root_lr + t, lr);
-        __stcg(b.root_x + t, X);
-        __stcg(b.llh_site + t, (double)logf(lr) + (double)X * kLn2);
-    }
+    if (d.flags & 4)
+        root_site_llh(b, s.tree, s.site, root_edge_logs(b, s.tree), s0 * f, dot * f, ss * f, X);
 }
 
 template <int G>
@@ -771,6 +597,90 @@ __device__ void outside_item_d(const laml_batch& b, const ItemDesc& d, int lane,
     }
 }
 
+// Outside of the two children of a root (out level 1).  The root's outside
+// vector is the root edge itself, o = (P00, Pmut q_a, Psil), whose terms can
+// lie further apart than FP32 spans; each child's inputs x = o * E[sibling]
+// are formed from the terms' logs and scaled as one vector, so the class that
+// dominates x keeps full precision whatever the branch length.
+template <int G>
+__device__ void outside_root_item_d(const laml_batch& b, const ItemDesc& d, int lane, bool act,
+                                    bool want_post) {
+    float cv_[8] = {0, 0, 0, 0, 0, 0, 0, 0}, cw_[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    SiteCtx s;
+    GroupCtx gc;
+    const bool live = act && site_ctx_d<G>(b, d, lane, true, s, gc);
+    if (live) {
+        const Leaf L = leaf_params(b, s.tree);
+        const Child cv = load_child_d<G>(b, d.flags & 1, d.v_ref, d.v_srow, s, gc, lane, L);
+        const Child cw = load_child_d<G>(b, d.flags & 2, d.w_ref, d.w_srow, s, gc, lane, L);
+        const float4 bv = load_bt(b, d.v), bw = load_bt(b, d.w);
+        const RootEdge re = root_edge_logs(b, s.tree);
+        const float ev0 = bv.x * cv.s0 + bv.y * cv.D + bv.w * cv.ss;
+        const float ew0 = bw.x * cw.s0 + bw.y * cw.D + bw.w * cw.ss;
+        const float kv = bv.w * cv.ss, kw = bw.w * cw.ss;
+        // largest q_a E[.]_a of each child: the mutated class's share of x
+        float ma = 0.f, mb = 0.f;
+        for (int j = 2; j < s.C; ++j) {
+            const float qj = __ldg(s.qrow + j * G);
+            ma = fmaxf(ma, qj * fmaf(bw.z, child_val<G>(cw, j), kw));
+            mb = fmaxf(mb, qj * fmaf(bv.z, child_val<G>(cv, j), kv));
+        }
+        auto scale_of = [](double l) { return l > -CUDART_INF ? (int)floor(l / kLn2) + 1 : 0; };
+        const int Ea = scale_of(fmax(re.l00 + logz(ew0), fmax(re.ls + logz(cw.ss), re.lm + logz(ma))));
+        const int Eb = scale_of(fmax(re.l00 + logz(ev0), fmax(re.ls + logz(cv.ss), re.lm + logz(mb))));
+        ChildOut A, B;   // A: child v (uses E[w]), B: child w (uses E[v])
+        A.x0 = expz(re.l00 - Ea * kLn2 + logz(ew0));
+        A.xs = expz(re.ls - Ea * kLn2 + logz(cw.ss));
+        A.X = Ea + cw.X;
+        B.x0 = expz(re.l00 - Eb * kLn2 + logz(ev0));
+        B.xs = expz(re.ls - Eb * kLn2 + logz(cv.ss));
+        B.X = Eb + cv.X;
+        const double lma = re.lm - Ea * kLn2, lmb = re.lm - Eb * kLn2;
+        A.sumx = A.dot = A.mx = 0.f;
+        B.sumx = B.dot = B.mx = 0.f;
+        A.orow = cv.row ? b.out_part + (int64_t)d.v_ref * 8 + s.goff + lane : nullptr;
+        B.orow = cw.row ? b.out_part + (int64_t)d.w_ref * 8 + s.goff + lane : nullptr;
+        const float pxa = bv.y * A.x0, pxb = bw.y * B.x0;
+        for (int j = 2; j < s.C; ++j) {
+            const float av = child_val<G>(cv, j), aw = child_val<G>(cw, j);
+            const float qj = __ldg(s.qrow + j * G);
+            const float xa = expz(lma + logz(qj * fmaf(bw.z, aw, kw)));
+            const float xb = expz(lmb + logz(qj * fmaf(bv.z, av, kv)));
+            A.sumx += xa;
+            A.dot = fmaf(xa, av, A.dot);
+            B.sumx += xb;
+            B.dot = fmaf(xb, aw, B.dot);
+            if (A.orow) {
+                const float r = fmaf(pxa, qj, bv.z * xa);
+                __stcg(A.orow + j * G, r);
+                A.mx = fmaxf(A.mx, r);
+            }
+            if (B.orow) {
+                const float r = fmaf(pxb, qj, bw.z * xb);
+                __stcg(B.orow + j * G, r);
+                B.mx = fmaxf(B.mx, r);
+            }
+        }
+        const int64_t t = __ldg(b.tr_site_base + s.tree) + s.site;
+        const float lroot = __ldcg(b.root_lr + t);
+        const int xroot = __ldcg(b.root_x + t);
+        child_finish<G>(b, s, d.v, cv, bv, A, want_post, lroot, xroot, cv_);
+        child_finish<G>(b, s, d.w, cw, bw, B, want_post, lroot, xroot, cw_);
+    }
+#pragma unroll
+    for (int off = G / 2; off > 0; off >>= 1) {
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+            cv_[k] += __shfl_xor_sync(kFull, cv_[k], off);
+            cw_[k] += __shfl_xor_sync(kFull, cw_[k], off);
+        }
+    }
+    if (act && lane == 0 && __ldcg(b.tr_status + d.tree) == LAML_TREE_ACTIVE) {
+        write_counts<G>(b, d.tree, d.v, d.g, cv_);
+        write_counts<G>(b, d.tree, d.w, d.g, cw_);
+    }
+}
+
 // outside row of a root (calculations.py:172-175) + the root's posteriors
 template <int G>
 __device__ void root_init_item(const laml_batch& b, int r, int g, int lane, bool want_post) {
@@ -793,14 +703,13 @@ __device__ void root_init_item(const laml_batch& b, int r, int g, int lane, bool
     if (want_post && b.post0) {
         const Leaf L = leaf_params(b, s.tree);
         const Child cr = load_child<G>(b, r, s.ds, s.site, s.goff, lane, s.qrow, s.sumq, L);
-        const int64_t t = __ldg(b.tr_site_base + s.tree) + s.site;
-        const float lroot = __ldcg(b.root_lr + t);
-        const float sc = lroot > 0.f ? ldexpf(1.f / lroot, cr.X - __ldcg(b.root_x + t)) : 0.f;
+        const RootEdge re = root_edge_logs(b, s.tree);
+        const double lsc = root_log_scale(b, s.tree, s.site, cr.X);
         const int64_t pb = __ldg(b.tr_post_base + s.tree) +
                            (int64_t)(r - __ldg(b.tr_node_base + s.tree)) *
                                __ldg(b.ds_sites_pad + s.ds) + s.site;
-        __stcg(b.post0 + pb, cr.s0 * br.x * sc);
-        __stcg(b.post1 + pb, cr.ss * br.w * sc);
+        __stcg(b.post0 + pb, expz(logz(cr.s0) + re.l00 + lsc));
+        __stcg(b.post1 + pb, expz(logz(cr.ss) + re.ls + lsc));
     }
 }
 
@@ -1228,12 +1137,14 @@ __device__ __forceinline__ void for_items(const laml_batch& b, const int32_t* it
     for (int64_t wi = gwarp; wi < nw; wi += nwarps) {
         const int64_t it = wi * IPW + sub;
         const bool act = it < n;
-        if constexpr (KIND <= 1) {   // descriptor-driven inside / outside
+        if constexpr (KIND <= 1 || KIND == 5) {   // descriptor-driven inside / outside
             const ItemDesc d = load_desc(desc, act ? it : 0);
-            if (kind == 0) {
+            if constexpr (KIND == 0) {
                 if (act) inside_item_d<G>(b, d, lane, respect_status);
-            } else {
+            } else if constexpr (KIND == 1) {
                 outside_item_d<G>(b, d, lane, act, want_post);
+            } else {
+                outside_root_item_d<G>(b, d, lane, act, want_post);
             }
         } else {
             const int node = act ? __ldg(items + 2 * it) : 0;
@@ -1241,7 +1152,7 @@ __device__ __forceinline__ void for_items(const laml_batch& b, const int32_t* it
             if constexpr (KIND == 2) {
                 if (act) root_init_item<G>(b, node, g, lane, want_post);
             } else {
-                outside_item<G>(b, node, g, lane, act, (b.compat && kind == 3) ? 1 : 2, false);
+                root_counts_item<G>(b, node, g, lane, act, (b.compat && kind == 3) ? 1 : 2);
             }
         }
     }
@@ -1372,8 +1283,12 @@ __global__ void __launch_bounds__(kBlock, LAML_MINB) k_em_persistent(laml_batch 
         if (!grid_barrier(b, gen)) return;
         for (int l = 0; l < b.n_out_levels; ++l) {
             const int64_t o = b.out_level_off[l], e = b.out_level_off[l + 1];
-            for_items<G, 1>(b, b.out_items + 2 * o, e - o, gwarp, nwarps, false, true,
-                            b.out_desc + 12 * o);
+            if (l == 0)   // the roots
+                for_items<G, 5>(b, b.out_items + 2 * o, e - o, gwarp, nwarps, false, true,
+                                b.out_desc + 12 * o);
+            else
+                for_items<G, 1>(b, b.out_items + 2 * o, e - o, gwarp, nwarps, false, true,
+                                b.out_desc + 12 * o);
             if (!grid_barrier(b, gen)) return;
         }
         for_items<G, 3>(b, b.root_items, b.n_root_items, gwarp, nwarps, false, true);
@@ -1446,6 +1361,7 @@ int launch_items(const laml_batch& b, const int32_t* items, int64_t n, int kind,
         case 1: k_items<G, 1><<<(unsigned)blocks, kBlock, 0, st>>>(b, items, n, want_post, respect_status, desc); break;
         case 2: k_items<G, 2><<<(unsigned)blocks, kBlock, 0, st>>>(b, items, n, want_post, respect_status, desc); break;
         case 3: k_items<G, 3><<<(unsigned)blocks, kBlock, 0, st>>>(b, items, n, want_post, respect_status, desc); break;
+        case 5: k_items<G, 5><<<(unsigned)blocks, kBlock, 0, st>>>(b, items, n, want_post, respect_status, desc); break;
         default: k_items<G, 4><<<(unsigned)blocks, kBlock, 0, st>>>(b, items, n, want_post, respect_status, desc); break;
     }
     return check(cudaGetLastError(), "k_items launch");
@@ -1491,8 +1407,9 @@ int outside_t(const laml_batch& b, int flags, cudaStream_t st, const Levels& L) 
     int rc = launch_items<G>(b, b.root_items, b.n_root_items, 2, want_post, 1, st);
     if (rc) return rc;
     for (int l = 0; l < b.n_out_levels; ++l) {
-        rc = launch_items<G>(b, b.out_items + 2 * (int64_t)L.out[l], L.out[l + 1] - L.out[l], 1,
-                             want_post, 1, st,
+        // level 0 holds the roots (parents at depth 0)
+        rc = launch_items<G>(b, b.out_items + 2 * (int64_t)L.out[l], L.out[l + 1] - L.out[l],
+                             l == 0 ? 5 : 1, want_post, 1, st,
                              b.out_desc + 12 * (int64_t)L.out[l]);
         if (rc) return rc;
     }

@@ -102,19 +102,32 @@ def char_matrix(rows: Sequence[Sequence], exact: bool = False) -> np.ndarray:
     (fastEM replaces '?' by -1, fastEM_solver.py:29)."""
     n = len(rows)
     K = len(rows[0]) if n else 0
-    out = np.empty((n, K), np.int32)
-    for i, r in enumerate(rows):
-        for c, x in enumerate(r):
-            if isinstance(x, str):
-                try:
-                    v = int(x)
-                except ValueError:
-                    out[i, c] = MISSING
-                    continue
-            else:
+    if any(len(r) != K for r in rows):
+        raise ValueError("character matrix rows have different lengths")
+    memo = {}
+
+    def code(x):
+        if isinstance(x, str):
+            try:
                 v = int(x)
-            out[i, c] = v if v >= 0 else (SILENCED if (exact and v == -1) else MISSING)
-    return out
+            except ValueError:
+                return MISSING
+        else:
+            v = int(x)
+        return v if v >= 0 else (SILENCED if (exact and v == -1) else MISSING)
+
+    def lookup(x):
+        # rows repeat few distinct values: decode each once
+        try:
+            return memo[x]
+        except KeyError:
+            memo[x] = c = code(x)
+            return c
+        except TypeError:           # unhashable entry
+            return code(x)
+
+    flat = [lookup(x) for r in rows for x in r]
+    return np.asarray(flat, np.int32).reshape(n, K)
 
 
 def priors_csr(Q: Sequence[Dict], n_sites: int):

@@ -44,6 +44,25 @@ def pow2(e):
     return f32(2.0 ** e)
 
 
+def logz(x):
+    return math.log(float(x)) if x > 0 else -math.inf
+
+
+def expz(l):
+    return f32(math.exp(l)) if l > -745 else f32(0)
+
+
+def lse3(a, b, c):
+    m = max(a, b, c)
+    if m == -math.inf:
+        return m
+    return m + math.log(math.exp(a - m) + math.exp(b - m) + math.exp(c - m))
+
+
+def scale_of(l):
+    return int(math.floor(l / math.log(2))) + 1 if l > -math.inf else 0
+
+
 class Model:
     def __init__(self, datasets, trees, tree_ds, d, nu, phi, compat):
         self.G = G = datasets[0].group_sites
@@ -78,6 +97,20 @@ class Model:
         e1mnd = 1e-6 if (self.compat and nd < 1e-6) else -math.expm1(-nd)
         pst = math.exp(-nd)
         return (f32(math.exp(-d * (1 + nu))), f32(e1md * pst), f32(pst), f32(e1mnd))
+
+    def root_edge(self, t):
+        """log P00, log Pmut (without q), log Pstay, log Psil of tree t's root
+        edge, in float64 (the kernels form every root-edge product from these)."""
+        r = int(self.p["tr_root"][t])
+        d, nu = float(self.d[r]), self.nu[t]
+        nd = d * nu
+        lm = math.log(1e-6 if (self.compat and d < 1e-6) else -math.expm1(-d)) - nd
+        if self.compat and nd < 1e-6:
+            ls = math.log(1e-6)
+        else:
+            e = -math.expm1(-nd)
+            ls = math.log(e) if e > 0 else -math.inf
+        return -d * (1 + nu), lm, -nd, ls
 
     def leaf(self, t):
         phi = self.phi[t]
@@ -160,12 +193,13 @@ class Model:
         self.in_dot[sr] = dot * f
         t = c["t"]
         if u == p["tr_root"][t]:
-            br = self.bt[u]
-            lr = f32(br[0] * (s0 * f) + br[1] * (dot * f) + br[3] * (ss * f))
+            l00, lm, _, ls = self.root_edge(t)
+            lv = lse3(l00 + logz(s0 * f), lm + logz(dot * f), ls + logz(ss * f))
             k = int(p["tr_site_base"][t]) + c["site"]
-            self.root_lr[k] = lr
-            self.root_x[k] = X
-            self.llh_site[k] = math.log(lr) + X * math.log(2) if lr > 0 else -math.inf
+            e = scale_of(lv)
+            self.root_lr[k] = f32(math.exp(lv - e * math.log(2))) if lv > -math.inf else f32(0)
+            self.root_x[k] = X + e
+            self.llh_site[k] = lv + X * math.log(2)
 
     def run_inside(self):
         p, s, G = self.p, self.sizes, self.G
@@ -204,28 +238,50 @@ class Model:
         bv = self.bt[v]
         sumx, dotxv, mx = f32(0), f32(0), f32(0)
         orow = None
+        t = c["t"]
+        u = p["nd_parent"][v] if mode == 0 else p["tr_quirk"][t]
+        at_root = mode == 0 and u == p["tr_root"][t]
         if mode == 2:
             x0, xs, Xx = f32(1), f32(0), 0
         else:
-            t = c["t"]
-            u = p["nd_parent"][v] if mode == 0 else p["tr_quirk"][t]
             w = p["nd_sib"][v] if mode == 0 else u
             cw = self.child(w, c, lane)
             bw = self.bt[w]
-            su = int(p["nd_srow"][u]) + c["site"]
-            fo = pow2(-int(self.out_h[su]))
-            Xo = int(self.out_x[su])
-            urow = int(p["nd_prow"][u]) + c["goff"] + lane
-            o0, os_ = self.out_part[urow] * fo, self.out_part[urow + G] * fo
-            x0 = f32(o0 * (bw[0] * cw["s0"] + bw[1] * cw["D"] + bw[3] * cw["ss"]))
-            xs = f32(os_ * cw["ss"])
-            Xx = Xo + cw["X"]
             kw = bw[3] * cw["ss"]
+            ew0 = f32(bw[0] * cw["s0"] + bw[1] * cw["D"] + bw[3] * cw["ss"])
+            if at_root:
+                # the root's outside is its edge: x = o * E[w] from the logs
+                l00, lm, _, ls = self.root_edge(t)
+                ma = max([f32(self.q(c, j) * (bw[2] * self.val(cw, j) + kw))
+                          for j in range(2, c["C"])] + [f32(0)])
+                E = scale_of(max(l00 + logz(ew0), ls + logz(cw["ss"]), lm + logz(ma)))
+                x0 = expz(l00 - E * math.log(2) + logz(ew0))
+                xs = expz(ls - E * math.log(2) + logz(cw["ss"]))
+                Xx = E + cw["X"]
+                lmE = lm - E * math.log(2)
+            else:
+                su = int(p["nd_srow"][u]) + c["site"]
+                fo = pow2(-int(self.out_h[su]))
+                Xo = int(self.out_x[su])
+                urow = int(p["nd_prow"][u]) + c["goff"] + lane
+                o0, os_ = self.out_part[urow] * fo, self.out_part[urow + G] * fo
+                x0 = f32(o0 * ew0)
+                xs = f32(os_ * cw["ss"])
+                Xx = Xo + cw["X"]
             write = mode == 0 and not cv["leaf"]
             if write:
                 orow = int(p["nd_prow"][v]) + c["goff"] + lane
             px = bv[1] * x0
             for j in range(2, c["C"]):
+                if at_root:
+                    xa = expz(lmE + logz(f32(self.q(c, j) * (bw[2] * self.val(cw, j) + kw))))
+                    sumx = f32(sumx + xa)
+                    dotxv = f32(dotxv + xa * self.val(cv, j))
+                    if write:
+                        o = f32(px * self.q(c, j) + bv[2] * xa)
+                        self.out_part[orow + j * G] = o
+                        mx = max(mx, o)
+                    continue
                 ou = self.out_part[urow + j * G] * fo
                 xa = f32(ou * (bw[2] * self.val(cw, j) + kw))
                 sumx = f32(sumx + xa)
@@ -245,6 +301,17 @@ class Model:
             self.out_x[sv] = Xx + h
         k = int(p["tr_site_base"][c["t"]]) + c["site"]
         lroot = self.root_lr[k]
+        if mode != 0:
+            # the root's own row: every root-edge product from the logs
+            l00, lm, lst, ls = self.root_edge(t)
+            lsc = ((Xx + cv["X"] - int(self.root_x[k])) * math.log(2) - math.log(float(lroot))
+                   if lroot > 0 else -math.inf)
+            return [expz(logz(f32(x0 * cv["s0"])) + l00 + lsc),
+                    expz(logz(f32(x0 * cv["D"])) + lm + lsc),
+                    expz(logz(f32(x0 * cv["ss"])) + ls + lsc),
+                    expz(logz(dotxv) + lst + lsc),
+                    expz(logz(f32(cv["ss"] * sumx)) + ls + lsc),
+                    expz(logz(f32(xs * cv["ss"])) + lsc), f32(0)]
         e = Xx + cv["X"] - int(self.root_x[k])
         sc = f32(math.ldexp(1.0 / float(lroot), e)) if lroot > 0 else f32(0)
         res = [x0 * cv["s0"] * bv[0] * sc, x0 * bv[1] * cv["D"] * sc, x0 * cv["ss"] * bv[3] * sc,

@@ -31,3 +31,4 @@ def test_kernel_model_matches_oracle(compat, G):
                                    rtol=1e-4, atol=1e-5)
         np.testing.assert_allclose(lr[nb[t]:nb[t] + trees[t].num_leaves], es.leaf_resp,
                                    rtol=1e-4, atol=1e-5)
+
