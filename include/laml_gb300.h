@@ -196,6 +196,9 @@ typedef struct laml_batch {
     const uint8_t* tr_fix;         /* bit0: nu fixed, bit1: phi fixed */
     double *tr_llh, *tr_llh_prev;
     int32_t *tr_iter, *tr_status;  /* status: LAML_TREE_* */
+    int32_t* tr_mode;              /* arithmetic of the tree's partials, set by
+                                    * laml_branch_terms and the M-step:
+                                    * LAML_MODE_LINEAR or LAML_MODE_LOG */
     /* nodes [n_nodes] */
     const int32_t *nd_tree, *nd_c0, *nd_c1, *nd_parent, *nd_sib, *nd_leafrow;
     const int64_t *nd_prow, *nd_srow;
@@ -223,6 +226,14 @@ typedef struct laml_batch {
     uint32_t* barrier;             /* 2 words, zeroed by the library before each persistent launch */
     int32_t* error;                /* 1 word: 0 or a negative LAML_ERR_* set on the device */
 } laml_batch;
+
+/* A tree's partials are FP32 values with power-of-two exponents (linear)
+ * unless some branch has d (1 + nu) > LAML_LOG_MODE_RATE: then they are FP32
+ * natural logs (the reference's own representation), whose range covers the
+ * branch lengths fast_em's root row can produce. */
+#define LAML_MODE_LINEAR 0
+#define LAML_MODE_LOG 1
+#define LAML_LOG_MODE_RATE 30.0
 
 #define LAML_TREE_ACTIVE 0
 #define LAML_TREE_CONVERGED 1

@@ -18,6 +18,7 @@ LAML_OK = 0
 ERRORS = {-1: "LAML_ERR_ARG", -2: "LAML_ERR_CUDA", -3: "LAML_ERR_PARSE", -4: "LAML_ERR_PRIOR",
           -5: "LAML_ERR_TIMEOUT", -6: "LAML_ERR_NOT_BINARY", -7: "LAML_ERR_LEAF"}
 TREE_ACTIVE, TREE_CONVERGED, TREE_NAN, TREE_MAXITER = 0, 1, 2, 3
+MODE_LINEAR, MODE_LOG = 0, 1
 MSTEP_FP64_POLISH = 1
 OUT_POSTERIORS, OUT_TRUE_ROOT = 1, 2
 
@@ -72,6 +73,7 @@ BATCH_FIELDS = [
     ("tr_quirk", vp), ("tr_site_base", vp), ("tr_cnt_base", vp), ("tr_post_base", vp),
     ("tr_nu", vp), ("tr_phi", vp), ("tr_prev", vp), ("tr_fix", vp), ("tr_llh", vp),
     ("tr_llh_prev", vp), ("tr_iter", vp), ("tr_status", vp),
+    ("tr_mode", vp),
     ("nd_tree", vp), ("nd_c0", vp), ("nd_c1", vp), ("nd_parent", vp), ("nd_sib", vp),
     ("nd_leafrow", vp), ("nd_prow", vp), ("nd_srow", vp), ("nd_d", vp), ("nd_d_prev", vp),
     ("nd_mask", vp), ("nd_bt", vp), ("nd_cnt", vp), ("nd_stage", vp),

@@ -27,7 +27,6 @@
 // with P00 = e^{-d(1+nu)}, Pmut = (1-e^{-d}) e^{-nu d}, Pstay = e^{-nu d},
 // Psil = 1-e^{-nu d}.
 #include <cuda_runtime.h>
-#include <math_constants.h>
 #include <stdint.h>
 
 #include <algorithm>
@@ -200,12 +199,12 @@ __device__ __forceinline__ RootEdge root_edge_logs(const laml_batch& b, int tree
 
 // log of a non-negative FP32 value (-inf at 0)
 __device__ __forceinline__ double logz(float x) {
-    return x > 0.f ? log((double)x) : -CUDART_INF;
+    return x > 0.f ? log((double)x) : -(double)INFINITY;
 }
 
 __device__ __forceinline__ double lse3(double a, double b, double c) {
     const double m = fmax(a, fmax(b, c));
-    if (m == -CUDART_INF) return m;
+    if (m == -(double)INFINITY) return m;
     return m + log(exp(a - m) + exp(b - m) + exp(c - m));
 }
 
@@ -221,7 +220,7 @@ __device__ __forceinline__ void root_site_llh(const laml_batch& b, int tree, int
     const int64_t t = __ldg(b.tr_site_base + tree) + site;
     int e = 0;
     float m = 0.f;
-    if (l > -CUDART_INF) {
+    if (l > -(double)INFINITY) {
         e = (int)floor(l / kLn2) + 1;
         m = (float)exp(l - (double)e * kLn2);
     }
@@ -234,77 +233,10 @@ __device__ __forceinline__ void root_site_llh(const laml_batch& b, int tree, int
 __device__ __forceinline__ double root_log_scale(const laml_batch& b, int tree, int site, int X) {
     const int64_t t = __ldg(b.tr_site_base + tree) + site;
     const float m = __ldcg(b.root_lr + t);
-    if (!(m > 0.f)) return -CUDART_INF;   // a zero likelihood: no responsibilities
+    if (!(m > 0.f)) return -(double)INFINITY;   // a zero likelihood: no responsibilities
     return (double)(X - __ldcg(b.root_x + t)) * kLn2 - log((double)m);
 }
 
-// ---------------------------------------------------------------------------
-// E-step row of a root (the root edge's expected counts), one site.
-// mode 1: fast_em's row with parent = sibling = node N-1 (fast_em/laml.py:
-// 244-246 + calculations.py:418); mode 2: below a progenitor in state 0
-// (EM_solver.py:282-286).
-// ---------------------------------------------------------------------------
-template <int G>
-__device__ void root_counts_item(const laml_batch& b, int v, int g, int lane, bool act,
-                                 int mode) {
-    float c00 = 0.f, c0a = 0.f, c0s = 0.f, caa = 0.f, cas = 0.f, css = 0.f;
-    SiteCtx s;
-    const bool live = act && site_ctx<G>(b, v, g, lane, true, s);
-    if (live) {
-        const Leaf L = leaf_params(b, s.tree);
-        const Child cv = load_child<G>(b, v, s.ds, s.site, s.goff, lane, s.qrow, s.sumq, L);
-        const RootEdge re = root_edge_logs(b, s.tree);
-        float x0 = 1.f, xs = 0.f, sumx = 0.f, dotxv = 0.f;
-        int Xx = 0;
-        if (mode == 1) {
-            const int u = __ldg(b.tr_quirk + s.tree);
-            const Child cw = load_child<G>(b, u, s.ds, s.site, s.goff, lane, s.qrow, s.sumq, L);
-            const float4 bw = load_bt(b, u);
-            const int64_t su = __ldg(b.nd_srow + u) + s.site;
-            const float fo = pow2i(-__ldcg(b.out_h + su));
-            const float* urow = b.out_part + __ldg(b.nd_prow + u) + s.goff + lane;
-            x0 = __ldcg(urow) * fo * (bw.x * cw.s0 + bw.y * cw.D + bw.w * cw.ss);
-            xs = __ldcg(urow + G) * fo * cw.ss;
-            Xx = __ldcg(b.out_x + su) + cw.X;
-            const float kw = bw.w * cw.ss;
-            for (int j = 2; j < s.C; ++j) {
-                const float xa = __ldcg(urow + j * G) * fo * fmaf(bw.z, child_val<G>(cw, j), kw);
-                sumx += xa;
-                dotxv = fmaf(xa, child_val<G>(cv, j), dotxv);
-            }
-        }
-        // responsibilities (calculations.py:418-451) over the site likelihood
-        const double lsc = root_log_scale(b, s.tree, s.site, Xx + cv.X);
-        c00 = expz(logz(x0 * cv.s0) + re.l00 + lsc);
-        c0a = expz(logz(x0 * cv.D) + re.lm + lsc);
-        c0s = expz(logz(x0 * cv.ss) + re.ls + lsc);
-        caa = expz(logz(dotxv) + re.lst + lsc);
-        cas = expz(logz(cv.ss * sumx) + re.ls + lsc);
-        css = expz(logz(xs * cv.ss) + lsc);
-    }
-    // sum over the G sites of the group
-#pragma unroll
-    for (int off = G / 2; off > 0; off >>= 1) {
-        c00 += __shfl_xor_sync(kFull, c00, off);
-        c0a += __shfl_xor_sync(kFull, c0a, off);
-        c0s += __shfl_xor_sync(kFull, c0s, off);
-        caa += __shfl_xor_sync(kFull, caa, off);
-        cas += __shfl_xor_sync(kFull, cas, off);
-        css += __shfl_xor_sync(kFull, css, off);
-    }
-    if (act && lane == 0) {
-        const int tree = __ldg(b.nd_tree + v);
-        if (__ldcg(b.tr_status + tree) == LAML_TREE_ACTIVE) {
-            const int ds = __ldg(b.tr_ds + tree);
-            const int NG = __ldg(b.ds_groups + ds);
-            float4* dst = reinterpret_cast<float4*>(
-                b.cnt_part + __ldg(b.tr_cnt_base + tree) +
-                ((int64_t)(v - __ldg(b.tr_node_base + tree)) * NG + g) * 8);
-            __stcg(dst, make_float4(c00, c0a, c0s, caa));
-            __stcg(dst + 1, make_float4(cas, css, 0.f, 0.f));
-        }
-    }
-}
 
 // ---------------------------------------------------------------------------
 // outside by parent: one internal node u, one site -> the outside rows and
@@ -443,12 +375,366 @@ __device__ __forceinline__ Child load_child_d(const laml_batch& b, bool leaf, in
     return c;
 }
 
+// ---------------------------------------------------------------------------
+// Log mode: a tree with a branch whose d (1 + nu) exceeds LAML_LOG_MODE_RATE
+// keeps its partials as FP32 natural logs, the reference's representation
+// (fast_em/calculations.py:11-133, 373-454), because the state classes of
+// such a tree (unmutated, mutated, silenced) lie further apart than one
+// power-of-two exponent per (node, site) can hold.  These items are
+// __noinline__ so the linear items keep their registers; they do not
+// shuffle (the caller reduces the counts).
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ bool tree_log(const laml_batch& b, int tree) {
+    return __ldcg(b.tr_mode + tree) == LAML_MODE_LOG;
+}
+
+struct EdgeL {
+    float l00, lm, lst, ls;   // log P00, log Pmut (without q), log Pstay, log Psil
+};
+
+__device__ __forceinline__ EdgeL edge_logs(const laml_batch& b, int x, int tree) {
+    const double d = __ldcg(b.nd_d + x), nu = __ldcg(b.tr_nu + tree), nd = d * nu;
+    EdgeL e;
+    e.l00 = (float)(-d * (1.0 + nu));
+    e.lst = (float)(-nd);
+    e.lm = (float)(log((b.compat && d < kEPSd) ? kEPSd : -expm1(-d)) - nd);
+    e.ls = (float)((b.compat && nd < kEPSd) ? log(kEPSd) : log(-expm1(-nd)));
+    return e;
+}
+
+__device__ __forceinline__ float lgz(float x) { return x > 0.f ? logf(x) : -INFINITY; }
+
+__device__ __forceinline__ float laddexp(float a, float c) {
+    const float m = fmaxf(a, c);
+    if (m == -INFINITY) return m;
+    return m + log1pf(expf(-fabsf(a - c)));
+}
+
+__device__ __forceinline__ float lse3f(float a, float c, float e) {
+    const float m = fmaxf(a, fmaxf(c, e));
+    if (m == -INFINITY) return m;
+    return m + logf(expf(a - m) + expf(c - m) + expf(e - m));
+}
+
+// running log-sum-exp
+struct Lse {
+    float m = -INFINITY, s = 0.f;
+    __device__ __forceinline__ void add(float x) {
+        if (x == -INFINITY) return;
+        if (x > m) {
+            s = s * expf(m - x) + 1.f;
+            m = x;
+        } else {
+            s += expf(x - m);
+        }
+    }
+    __device__ __forceinline__ float value() const { return m == -INFINITY ? m : m + logf(s); }
+};
+
+// exp(x - lL) for an FP32 log x and an FP64 log-likelihood
+__device__ __forceinline__ float rel_exp(float x, double lL) {
+    return x == -INFINITY ? 0.f : (float)exp((double)x - lL);
+}
+
+struct ChildL {
+    const float* row;   // null for a leaf
+    float s0, ss, ld;   // log of state 0, silenced, sum_a q_a in_a
+    float le1, lephi;
+    int code;
+};
+
+template <int G>
+__device__ __forceinline__ float child_val_log(const ChildL& c, int j) {
+    if (c.row) return __ldcg(c.row + j * G);
+    return c.code == j ? c.le1 : (c.code == -1 ? c.lephi : -INFINITY);
+}
+
+template <int G>
+__device__ __forceinline__ ChildL load_child_log(const laml_batch& b, bool leaf, int ref, int srow,
+                                                 const SiteCtx& s, const GroupCtx& gc,
+                                                 const Leaf& L) {
+    ChildL c;
+    c.le1 = lgz(L.e1);
+    c.lephi = lgz(L.ephi);
+    if (leaf) {
+        const int code = __ldg(b.codes + gc.code_base + (int64_t)ref * gc.kpad + s.site);
+        c.row = nullptr;
+        c.code = code;
+        c.s0 = code == 0 ? c.le1 : (code == -1 ? c.lephi : -INFINITY);
+        c.ss = code < 0 ? 0.f : lgz(L.es);
+        c.ld = code >= 2 ? lgz(__ldg(s.qrow + code * G)) + c.le1
+                         : (code == -1 ? c.lephi + lgz(s.sumq) : -INFINITY);
+    } else {
+        c.row = b.in_part + (int64_t)ref * 8 + s.goff + (s.site % G);
+        c.code = 0;
+        c.s0 = __ldcg(c.row);
+        c.ss = __ldcg(c.row + G);
+        c.ld = __ldcg(b.in_dot + (int64_t)srow + s.site);
+    }
+    return c;
+}
+
+__device__ __forceinline__ void root_store_log(const laml_batch& b, int tree, int site, double l) {
+    const int64_t t = __ldg(b.tr_site_base + tree) + site;
+    int e = 0;
+    float m = 0.f;
+    if (l > -(double)INFINITY) {
+        e = (int)floor(l / kLn2) + 1;
+        m = (float)exp(l - (double)e * kLn2);
+    }
+    __stcg(b.root_lr + t, m);
+    __stcg(b.root_x + t, e);
+    __stcg(b.llh_site + t, l);
+}
+
+template <int G>
+__device__ __noinline__ void inside_log_item(const laml_batch& b, const ItemDesc& d,
+                                             const SiteCtx& s, const GroupCtx& gc) {
+    const Leaf L = leaf_params(b, s.tree);
+    const ChildL cv = load_child_log<G>(b, d.flags & 1, d.v_ref, d.v_srow, s, gc, L);
+    const ChildL cw = load_child_log<G>(b, d.flags & 2, d.w_ref, d.w_srow, s, gc, L);
+    const EdgeL ev = edge_logs(b, d.v, s.tree), ew = edge_logs(b, d.w, s.tree);
+    float* row = b.in_part + (int64_t)d.u_prow8 * 8 + s.goff + (s.site % G);
+    const float s0 = lse3f(ev.l00 + cv.s0, ev.lm + cv.ld, ev.ls + cv.ss) +
+                     lse3f(ew.l00 + cw.s0, ew.lm + cw.ld, ew.ls + cw.ss);
+    const float ss = cv.ss + cw.ss;
+    __stcg(row, s0);
+    __stcg(row + G, ss);
+    const float kv = ev.ls + cv.ss, kw = ew.ls + cw.ss;
+    Lse dot;
+    for (int j = 2; j < s.C; ++j) {
+        const float x = laddexp(ev.lst + child_val_log<G>(cv, j), kv) +
+                        laddexp(ew.lst + child_val_log<G>(cw, j), kw);
+        __stcg(row + j * G, x);
+        dot.add(lgz(__ldg(s.qrow + j * G)) + x);
+    }
+    const int64_t sr = (int64_t)d.u_srow + s.site;
+    const float ld = dot.value();
+    __stcg(b.in_h + sr, 0);
+    __stcg(b.in_x + sr, 0);
+    __stcg(b.in_dot + sr, ld);
+    if (d.flags & 4) {
+        const RootEdge re = root_edge_logs(b, s.tree);
+        root_store_log(b, s.tree, s.site,
+                       lse3(re.l00 + (double)s0, re.lm + (double)ld, re.ls + (double)ss));
+    }
+}
+
+// the six responsibilities of a child (and its leaf / posterior terms) from
+// x = out[parent] + E[sibling] in logs
+template <int G>
+__device__ __forceinline__ void child_counts_log(const laml_batch& b, const SiteCtx& s, int v,
+                                                 const ChildL& cv, const EdgeL& ev, float x0,
+                                                 float xs, float lsx, float ldx, float out0,
+                                                 float outs, double lL, bool want_post,
+                                                 float* cnt) {
+    cnt[0] = rel_exp(x0 + cv.s0 + ev.l00, lL);
+    cnt[1] = rel_exp(x0 + ev.lm + cv.ld, lL);
+    cnt[2] = rel_exp(x0 + cv.ss + ev.ls, lL);
+    cnt[3] = rel_exp(ev.lst + ldx, lL);
+    cnt[4] = rel_exp(ev.ls + cv.ss + lsx, lL);
+    cnt[5] = rel_exp(xs + cv.ss, lL);
+    cnt[6] = 0.f;
+    cnt[7] = 0.f;
+    if (cv.row == nullptr) {
+        const float pl = rel_exp(cv.ss + outs, lL);
+        if (cv.code == -1) cnt[6] = pl; else cnt[7] = pl;
+    }
+    if (want_post && b.post0) {
+        const int64_t pb = __ldg(b.tr_post_base + s.tree) +
+                           (int64_t)(v - __ldg(b.tr_node_base + s.tree)) *
+                               __ldg(b.ds_sites_pad + s.ds) + s.site;
+        __stcg(b.post0 + pb, rel_exp(cv.s0 + out0, lL));
+        __stcg(b.post1 + pb, rel_exp(cv.ss + outs, lL));
+    }
+}
+
+// outside of both children of internal node u (compute_Q_v_product,
+// calculations.py:11-45, with x = out[u] + edge-inside of the sibling); for a
+// root, out[u] is its edge from a progenitor in state 0 (calculations.py:
+// 172-175)
+template <int G>
+__device__ __noinline__ void outside_log_lane(const laml_batch& b, const ItemDesc& d,
+                                              const SiteCtx& s, const GroupCtx& gc,
+                                              bool want_post, float* cv_, float* cw_) {
+    const int lane = s.site % G;
+    const Leaf L = leaf_params(b, s.tree);
+    const ChildL cv = load_child_log<G>(b, d.flags & 1, d.v_ref, d.v_srow, s, gc, L);
+    const ChildL cw = load_child_log<G>(b, d.flags & 2, d.w_ref, d.w_srow, s, gc, L);
+    const EdgeL ev = edge_logs(b, d.v, s.tree), ew = edge_logs(b, d.w, s.tree);
+    const bool at_root = d.flags & 4;
+    const float* urow = b.out_part + (int64_t)d.u_prow8 * 8 + s.goff + lane;
+    float o0, os, olm = 0.f;
+    if (at_root) {
+        const RootEdge re = root_edge_logs(b, s.tree);
+        o0 = (float)re.l00;
+        os = (float)re.ls;
+        olm = (float)re.lm;
+    } else {
+        o0 = __ldcg(urow);
+        os = __ldcg(urow + G);
+    }
+    const float E0v = lse3f(ev.l00 + cv.s0, ev.lm + cv.ld, ev.ls + cv.ss);
+    const float E0w = lse3f(ew.l00 + cw.s0, ew.lm + cw.ld, ew.ls + cw.ss);
+    const float xa0 = o0 + E0w, xas = os + cw.ss;   // child v: x = out[u] + E[w]
+    const float xb0 = o0 + E0v, xbs = os + cv.ss;   // child w: x = out[u] + E[v]
+    const float kv = ev.ls + cv.ss, kw = ew.ls + cw.ss;
+    float* arow = cv.row ? b.out_part + (int64_t)d.v_ref * 8 + s.goff + lane : nullptr;
+    float* brow = cw.row ? b.out_part + (int64_t)d.w_ref * 8 + s.goff + lane : nullptr;
+    Lse sa, sb, da, db;
+    for (int j = 2; j < s.C; ++j) {
+        const float lq = lgz(__ldg(s.qrow + j * G));
+        const float oj = at_root ? olm + lq : __ldcg(urow + j * G);
+        const float av = child_val_log<G>(cv, j), aw = child_val_log<G>(cw, j);
+        const float xa = oj + laddexp(ew.lst + aw, kw);
+        const float xb = oj + laddexp(ev.lst + av, kv);
+        sa.add(xa);
+        da.add(xa + av);
+        sb.add(xb);
+        db.add(xb + aw);
+        if (arow) __stcg(arow + j * G, laddexp(lq + ev.lm + xa0, ev.lst + xa));
+        if (brow) __stcg(brow + j * G, laddexp(lq + ew.lm + xb0, ew.lst + xb));
+    }
+    const float lsa = sa.value(), lsb = sb.value();
+    const float outa0 = ev.l00 + xa0, outas = laddexp(ev.ls + laddexp(xa0, lsa), xas);
+    const float outb0 = ew.l00 + xb0, outbs = laddexp(ew.ls + laddexp(xb0, lsb), xbs);
+    if (arow) {
+        __stcg(arow, outa0);
+        __stcg(arow + G, outas);
+        __stcg(b.out_h + (int64_t)d.v_srow + s.site, 0);
+        __stcg(b.out_x + (int64_t)d.v_srow + s.site, 0);
+    }
+    if (brow) {
+        __stcg(brow, outb0);
+        __stcg(brow + G, outbs);
+        __stcg(b.out_h + (int64_t)d.w_srow + s.site, 0);
+        __stcg(b.out_x + (int64_t)d.w_srow + s.site, 0);
+    }
+    const double lL = __ldcg(b.llh_site + __ldg(b.tr_site_base + s.tree) + s.site);
+    child_counts_log<G>(b, s, d.v, cv, ev, xa0, xas, lsa, da.value(), outa0, outas, lL,
+                        want_post, cv_);
+    child_counts_log<G>(b, s, d.w, cw, ew, xb0, xbs, lsb, db.value(), outb0, outbs, lL,
+                        want_post, cw_);
+}
+
+// the root's E-step row in logs (see root_counts_item for the modes)
+template <int G>
+__device__ __noinline__ void root_counts_log(const laml_batch& b, int v, const SiteCtx& s,
+                                             int mode, float* c) {
+    const int lane = s.site % G;
+    const Leaf L = leaf_params(b, s.tree);
+    const GroupCtx gc{0, 0};
+    const ChildL cv = load_child_log<G>(b, false, (int)(__ldg(b.nd_prow + v) / 8),
+                                        (int)__ldg(b.nd_srow + v), s, gc, L);
+    const RootEdge re = root_edge_logs(b, s.tree);
+    float x0 = 0.f, xs = -INFINITY;
+    Lse sx, dx;
+    if (mode == 1) {
+        const int u = __ldg(b.tr_quirk + s.tree);
+        const ChildL cu = load_child_log<G>(b, false, (int)(__ldg(b.nd_prow + u) / 8),
+                                            (int)__ldg(b.nd_srow + u), s, gc, L);
+        const EdgeL eu = edge_logs(b, u, s.tree);
+        const float* urow = b.out_part + __ldg(b.nd_prow + u) + s.goff + lane;
+        x0 = __ldcg(urow) + lse3f(eu.l00 + cu.s0, eu.lm + cu.ld, eu.ls + cu.ss);
+        xs = __ldcg(urow + G) + cu.ss;
+        const float ku = eu.ls + cu.ss;
+        for (int j = 2; j < s.C; ++j) {
+            const float xj = __ldcg(urow + j * G) + laddexp(eu.lst + child_val_log<G>(cu, j), ku);
+            sx.add(xj);
+            dx.add(xj + child_val_log<G>(cv, j));
+        }
+    }
+    const double lL = __ldcg(b.llh_site + __ldg(b.tr_site_base + s.tree) + s.site);
+    c[0] = rel_exp(x0 + cv.s0 + (float)re.l00, lL);
+    c[1] = rel_exp(x0 + (float)re.lm + cv.ld, lL);
+    c[2] = rel_exp(x0 + cv.ss + (float)re.ls, lL);
+    c[3] = rel_exp((float)re.lst + dx.value(), lL);
+    c[4] = rel_exp((float)re.ls + cv.ss + sx.value(), lL);
+    c[5] = rel_exp(xs + cv.ss, lL);
+}
+
+// ---------------------------------------------------------------------------
+// E-step row of a root (the root edge's expected counts), one site.
+// mode 1: fast_em's row with parent = sibling = node N-1 (fast_em/laml.py:
+// 244-246 + calculations.py:418); mode 2: below a progenitor in state 0
+// (EM_solver.py:282-286).
+// ---------------------------------------------------------------------------
+template <int G>
+__device__ void root_counts_item(const laml_batch& b, int v, int g, int lane, bool act,
+                                 int mode) {
+    float c00 = 0.f, c0a = 0.f, c0s = 0.f, caa = 0.f, cas = 0.f, css = 0.f;
+    SiteCtx s;
+    const bool live = act && site_ctx<G>(b, v, g, lane, true, s);
+    if (live && tree_log(b, s.tree)) {
+        float c[6];
+        root_counts_log<G>(b, v, s, mode, c);
+        c00 = c[0]; c0a = c[1]; c0s = c[2]; caa = c[3]; cas = c[4]; css = c[5];
+    } else if (live) {
+        const Leaf L = leaf_params(b, s.tree);
+        const Child cv = load_child<G>(b, v, s.ds, s.site, s.goff, lane, s.qrow, s.sumq, L);
+        const RootEdge re = root_edge_logs(b, s.tree);
+        float x0 = 1.f, xs = 0.f, sumx = 0.f, dotxv = 0.f;
+        int Xx = 0;
+        if (mode == 1) {
+            const int u = __ldg(b.tr_quirk + s.tree);
+            const Child cw = load_child<G>(b, u, s.ds, s.site, s.goff, lane, s.qrow, s.sumq, L);
+            const float4 bw = load_bt(b, u);
+            const int64_t su = __ldg(b.nd_srow + u) + s.site;
+            const float fo = pow2i(-__ldcg(b.out_h + su));
+            const float* urow = b.out_part + __ldg(b.nd_prow + u) + s.goff + lane;
+            x0 = __ldcg(urow) * fo * (bw.x * cw.s0 + bw.y * cw.D + bw.w * cw.ss);
+            xs = __ldcg(urow + G) * fo * cw.ss;
+            Xx = __ldcg(b.out_x + su) + cw.X;
+            const float kw = bw.w * cw.ss;
+            for (int j = 2; j < s.C; ++j) {
+                const float xa = __ldcg(urow + j * G) * fo * fmaf(bw.z, child_val<G>(cw, j), kw);
+                sumx += xa;
+                dotxv = fmaf(xa, child_val<G>(cv, j), dotxv);
+            }
+        }
+        // responsibilities (calculations.py:418-451) over the site likelihood
+        const double lsc = root_log_scale(b, s.tree, s.site, Xx + cv.X);
+        c00 = expz(logz(x0 * cv.s0) + re.l00 + lsc);
+        c0a = expz(logz(x0 * cv.D) + re.lm + lsc);
+        c0s = expz(logz(x0 * cv.ss) + re.ls + lsc);
+        caa = expz(logz(dotxv) + re.lst + lsc);
+        cas = expz(logz(cv.ss * sumx) + re.ls + lsc);
+        css = expz(logz(xs * cv.ss) + lsc);
+    }
+    // sum over the G sites of the group
+#pragma unroll
+    for (int off = G / 2; off > 0; off >>= 1) {
+        c00 += __shfl_xor_sync(kFull, c00, off);
+        c0a += __shfl_xor_sync(kFull, c0a, off);
+        c0s += __shfl_xor_sync(kFull, c0s, off);
+        caa += __shfl_xor_sync(kFull, caa, off);
+        cas += __shfl_xor_sync(kFull, cas, off);
+        css += __shfl_xor_sync(kFull, css, off);
+    }
+    if (act && lane == 0) {
+        const int tree = __ldg(b.nd_tree + v);
+        if (__ldcg(b.tr_status + tree) == LAML_TREE_ACTIVE) {
+            const int ds = __ldg(b.tr_ds + tree);
+            const int NG = __ldg(b.ds_groups + ds);
+            float4* dst = reinterpret_cast<float4*>(
+                b.cnt_part + __ldg(b.tr_cnt_base + tree) +
+                ((int64_t)(v - __ldg(b.tr_node_base + tree)) * NG + g) * 8);
+            __stcg(dst, make_float4(c00, c0a, c0s, caa));
+            __stcg(dst + 1, make_float4(cas, css, 0.f, 0.f));
+        }
+    }
+}
+
 template <int G>
 __device__ void inside_item_d(const laml_batch& b, const ItemDesc& d, int lane,
                               bool respect_status) {
     SiteCtx s;
     GroupCtx gc;
     if (!site_ctx_d<G>(b, d, lane, respect_status, s, gc)) return;
+    if (tree_log(b, s.tree)) {
+        inside_log_item<G>(b, d, s, gc);
+        return;
+    }
     const Leaf L = leaf_params(b, s.tree);
     const Child cv = load_child_d<G>(b, d.flags & 1, d.v_ref, d.v_srow, s, gc, lane, L);
     const Child cw = load_child_d<G>(b, d.flags & 2, d.w_ref, d.w_srow, s, gc, lane, L);
@@ -503,7 +789,15 @@ __device__ void outside_item_d(const laml_batch& b, const ItemDesc& d, int lane,
     SiteCtx s;
     GroupCtx gc;
     const bool live = act && site_ctx_d<G>(b, d, lane, true, s, gc);
-    if (live) {
+    if (live && tree_log(b, s.tree)) {
+        float tv[8], tw[8];
+        outside_log_lane<G>(b, d, s, gc, want_post, tv, tw);
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+            cv_[k] = tv[k];
+            cw_[k] = tw[k];
+        }
+    } else if (live) {
         const Leaf L = leaf_params(b, s.tree);
         const Child cv = load_child_d<G>(b, d.flags & 1, d.v_ref, d.v_srow, s, gc, lane, L);
         const Child cw = load_child_d<G>(b, d.flags & 2, d.w_ref, d.w_srow, s, gc, lane, L);
@@ -609,7 +903,15 @@ __device__ void outside_root_item_d(const laml_batch& b, const ItemDesc& d, int 
     SiteCtx s;
     GroupCtx gc;
     const bool live = act && site_ctx_d<G>(b, d, lane, true, s, gc);
-    if (live) {
+    if (live && tree_log(b, s.tree)) {
+        float tv[8], tw[8];
+        outside_log_lane<G>(b, d, s, gc, want_post, tv, tw);
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+            cv_[k] = tv[k];
+            cw_[k] = tw[k];
+        }
+    } else if (live) {
         const Leaf L = leaf_params(b, s.tree);
         const Child cv = load_child_d<G>(b, d.flags & 1, d.v_ref, d.v_srow, s, gc, lane, L);
         const Child cw = load_child_d<G>(b, d.flags & 2, d.w_ref, d.w_srow, s, gc, lane, L);
@@ -625,7 +927,7 @@ __device__ void outside_root_item_d(const laml_batch& b, const ItemDesc& d, int 
             ma = fmaxf(ma, qj * fmaf(bw.z, child_val<G>(cw, j), kw));
             mb = fmaxf(mb, qj * fmaf(bv.z, child_val<G>(cv, j), kv));
         }
-        auto scale_of = [](double l) { return l > -CUDART_INF ? (int)floor(l / kLn2) + 1 : 0; };
+        auto scale_of = [](double l) { return l > -(double)INFINITY ? (int)floor(l / kLn2) + 1 : 0; };
         const int Ea = scale_of(fmax(re.l00 + logz(ew0), fmax(re.ls + logz(cw.ss), re.lm + logz(ma))));
         const int Eb = scale_of(fmax(re.l00 + logz(ev0), fmax(re.ls + logz(cv.ss), re.lm + logz(mb))));
         ChildOut A, B;   // A: child v (uses E[w]), B: child w (uses E[v])
@@ -681,13 +983,43 @@ __device__ void outside_root_item_d(const laml_batch& b, const ItemDesc& d, int 
     }
 }
 
+// the root's outside row in logs: its edge from a progenitor in state 0
+template <int G>
+__device__ __noinline__ void root_init_log(const laml_batch& b, int r, const SiteCtx& s,
+                                           float* row, bool want_post) {
+    const RootEdge re = root_edge_logs(b, s.tree);
+    __stcg(row, (float)re.l00);
+    __stcg(row + G, (float)re.ls);
+    for (int j = 2; j < s.C; ++j)
+        __stcg(row + j * G, (float)re.lm + lgz(__ldg(s.qrow + j * G)));
+    const int64_t sr = __ldg(b.nd_srow + r) + s.site;
+    __stcg(b.out_h + sr, 0);
+    __stcg(b.out_x + sr, 0);
+    if (want_post && b.post0) {
+        const Leaf L = leaf_params(b, s.tree);
+        const GroupCtx gc{0, 0};
+        const ChildL cr = load_child_log<G>(b, false, (int)(__ldg(b.nd_prow + r) / 8),
+                                            (int)__ldg(b.nd_srow + r), s, gc, L);
+        const double lL = __ldcg(b.llh_site + __ldg(b.tr_site_base + s.tree) + s.site);
+        const int64_t pb = __ldg(b.tr_post_base + s.tree) +
+                           (int64_t)(r - __ldg(b.tr_node_base + s.tree)) *
+                               __ldg(b.ds_sites_pad + s.ds) + s.site;
+        __stcg(b.post0 + pb, rel_exp(cr.s0 + (float)re.l00, lL));
+        __stcg(b.post1 + pb, rel_exp(cr.ss + (float)re.ls, lL));
+    }
+}
+
 // outside row of a root (calculations.py:172-175) + the root's posteriors
 template <int G>
 __device__ void root_init_item(const laml_batch& b, int r, int g, int lane, bool want_post) {
     SiteCtx s;
     if (!site_ctx<G>(b, r, g, lane, true, s)) return;
-    const float4 br = load_bt(b, r);
     float* row = b.out_part + __ldg(b.nd_prow + r) + s.goff + lane;
+    if (tree_log(b, s.tree)) {
+        root_init_log<G>(b, r, s, row, want_post);
+        return;
+    }
+    const float4 br = load_bt(b, r);
     float mx = fmaxf(br.x, br.w);
     __stcg(row, br.x);
     __stcg(row + G, br.w);
@@ -1041,8 +1373,22 @@ __device__ void mstep_tree(const laml_batch& b, int p, int rounds, double2* sh, 
         b.tr_nu[p] = nu;
         b.tr_phi[p] = phi;
     }
-    for (int v = threadIdx.x; v < N; v += blockDim.x)
+    // the arithmetic of the next passes: log mode once a branch's
+    // d (1 + nu) leaves the range of the linear partials
+    __shared__ int s_rate;
+    if (threadIdx.x == 0) s_rate = 0;
+    __syncthreads();
+    int rate = 0;
+    for (int v = threadIdx.x; v < N; v += blockDim.x) {
         reinterpret_cast<float4*>(b.nd_bt)[base + v] = branch_terms_of((double)Dd[v], nu, b.compat);
+        rate = max(rate, __float_as_int(fmaxf(Dd[v] * (1.f + (float)nu), 0.f)));
+    }
+    atomicMax(&s_rate, rate);
+    __syncthreads();
+    if (threadIdx.x == 0)
+        b.tr_mode[p] = __int_as_float(s_rate) > (float)LAML_LOG_MODE_RATE ? LAML_MODE_LOG
+                                                                           : LAML_MODE_LINEAR;
+    __syncthreads();
 }
 
 // per-tree log-likelihood (FP64 sum over sites) and the EM stopping rule
@@ -1225,6 +1571,26 @@ __global__ void k_tree_llh(laml_batch b, int mode, double rel_tol, int max_iters
     if (p < b.n_trees) tree_llh_item(b, p, mode, rel_tol, max_iters);
 }
 
+// per tree: log mode if some branch has d (1 + nu) > LAML_LOG_MODE_RATE
+__global__ void k_tree_mode(laml_batch b) {
+    __shared__ int s_rate;
+    for (int p = blockIdx.x; p < b.n_trees; p += gridDim.x) {
+        if (threadIdx.x == 0) s_rate = 0;
+        __syncthreads();
+        const int N = b.tr_nodes[p], base = b.tr_node_base[p];
+        const double nu = b.tr_nu[p];
+        int rate = 0;
+        for (int v = threadIdx.x; v < N; v += blockDim.x)
+            rate = max(rate, __float_as_int(fmaxf((float)(b.nd_d[base + v] * (1.0 + nu)), 0.f)));
+        atomicMax(&s_rate, rate);
+        __syncthreads();
+        if (threadIdx.x == 0)
+            b.tr_mode[p] = __int_as_float(s_rate) > (float)LAML_LOG_MODE_RATE ? LAML_MODE_LOG
+                                                                               : LAML_MODE_LINEAR;
+        __syncthreads();
+    }
+}
+
 __global__ void k_branch_terms(laml_batch b) {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i < b.n_nodes) {
@@ -1339,6 +1705,10 @@ int validate(const laml_batch* b) {
     }
     if (b->group_sites != 8 && b->group_sites != 16 && b->group_sites != 32) {
         laml::set_error("laml_batch: group_sites must be 8, 16 or 32");
+        return LAML_ERR_ARG;
+    }
+    if (!b->tr_mode) {
+        laml::set_error("laml_batch: tr_mode (one int32 per tree) is required");
         return LAML_ERR_ARG;
     }
     if (!b->in_desc || !b->out_desc || !b->grp_desc) {
@@ -1496,7 +1866,10 @@ extern "C" int laml_branch_terms(const laml_batch* b, void* stream) {
     cudaStream_t st = (cudaStream_t)stream;
     const int64_t blocks = (b->n_nodes + kBlock - 1) / kBlock;
     k_branch_terms<<<(unsigned)blocks, kBlock, 0, st>>>(*b);
-    return check(cudaGetLastError(), "k_branch_terms");
+    if ((rc = check(cudaGetLastError(), "k_branch_terms"))) return rc;
+    const int tb = std::min(b->n_trees, num_sms() * 8);
+    k_tree_mode<<<tb, 128, 0, st>>>(*b);
+    return check(cudaGetLastError(), "k_tree_mode");
 }
 
 extern "C" int laml_plan_descriptors(const laml_batch* b, int32_t* in_desc, int32_t* out_desc,

@@ -723,9 +723,11 @@ def exact_leaf_stats(prob: Problem, es: EStep):
 
 
 def em_exact(prob: Problem, d, nu, phi, branch_mask=None, fix_nu=False, fix_phi=False,
-             max_iters=1000) -> EMResult:
+             max_iters=1000, stop=None) -> EMResult:
     """EM_solver.EM_optimization (EM_solver.py:461-512): E-step, M-step,
-    logL; stop when |(cur-pre)/pre| < conv_eps = 1e-8 or after 1000 iterations."""
+    logL; stop when |(cur-pre)/pre| < conv_eps = 1e-8 (``stop``; negative:
+    never) or after 1000 iterations."""
+    stop = CONV_EPS_EXACT if stop is None else stop
     N = len(prob.tree.parent)
     d = np.asarray(d, dtype=np.float64).copy()
     mask = np.ones(N, dtype=bool) if branch_mask is None else np.asarray(branch_mask, bool)
@@ -742,7 +744,7 @@ def em_exact(prob: Problem, d, nu, phi, branch_mask=None, fix_nu=False, fix_phi=
                                  opt_phi=not fix_phi, opt_nu=not fix_nu)
         cur, _ = log_likelihood(prob, d, nu, phi)
         trace.append(cur)
-        if abs((cur - pre) / pre) < CONV_EPS_EXACT:
+        if abs((cur - pre) / pre) < stop:
             break
         pre = cur
         it += 1
