@@ -7,13 +7,18 @@ under PMM (nu = 0.1, phi = 0.15, M_k ~ U{5..50}, q ~ Dirichlet(0.5)); fastEM
 (compat) semantics.
 
 A step is one EM iteration over the whole batch (outside + expected counts ->
-M-step -> inside + log-likelihood), one persistent cooperative launch.
-``value`` is tree-EM-iterations per second with the batch resident in HBM
-(convergence disabled so every step does the full work; the partial buffers,
-~3.7 GB, are far larger than L2, so no flush is needed).  ``e2e`` scores the
-same 512 candidates through the public API from host newick strings and the
-host character matrix to converged results back on the host, timed by wall
-clock with the copies inside.
+M-step -> inside + log-likelihood): one replay of a CUDA graph of the
+per-level launches (``--path``).  ``value`` is tree-EM-iterations per second
+with the batch resident in HBM (convergence disabled so every step does the
+full work; the partial buffers, ~2.6 GB, are far larger than L2, so no flush
+is needed).  ``roofline`` is the outside pass (the dominant kernel), timed
+alone on the same stream; ``roofline_inside`` and ``roofline_em_iteration``
+give the inside pass and the whole iteration.  ``e2e`` scores the same 512
+candidates through the public API (api.score_candidates) from host newick
+strings and the host character matrix to converged results back on the host,
+timed by wall clock with the copies inside; ``plain_gpu_dropin`` scores a
+sample of candidates one at a time through the drop-in solver, the way the
+reference's topology search calls it.
 
 --impl reference times the CPU restatement of the reference's fastEM path
 (the oracle port) on the host cores, on a bounded sample of the same
@@ -100,20 +105,51 @@ class Clocks:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def algorithmic_bytes(b):
-    """Bytes one fused EM iteration must move (the layout's own words):
-    inside reads each internal child row and writes each internal row (2A);
-    outside reads the parent's outside row, the sibling's and the node's own
-    inside rows and writes the node's outside row (4A); per internal
-    (node, site) scalars: 24 B inside + 40 B outside; leaf codes 2 B per leaf
-    site read three times; count partials 32 B per (node, group) written and
-    read back by the M-step; 8 B per node of branch lengths in the M-step."""
+def pass_bytes(b):
+    """Algorithmic bytes of one inside pass, one outside pass and one M-step
+    in this layout (A = 4 B x part_floats, one FP32 partial array over the
+    internal nodes):
+
+    * inside: every internal row written once and read once by its parent
+      (2A); per internal (node, site) 12 B of scalars (exponent, cumulative
+      exponent, q-dot) written and read (24 B); leaf codes 2 B per leaf site;
+      16 B of branch terms per node.
+    * outside, one item per internal parent for both children: the parent's
+      outside row, the children's inside rows and the children's outside rows
+      once each (3A); scalars 8 B read + 12 B read + 8 B written per internal
+      (node, site); leaf codes; branch terms; count partials written (32 B
+      per (node, group)).
+    * M-step: count partials read, branch lengths read and written, branch
+      terms written (16 + 16 B per node)."""
     s = b.sizes
     A = 4 * s["part_floats"]
     leaf_sites = sum(t.num_leaves * b.datasets[b.tree_ds[p]].n_sites_pad
                      for p, t in enumerate(b.trees))
-    return (6 * A + 64 * s["scalar_len"] + 6 * leaf_sites + 2 * 4 * s["count_floats"]
-            + 8 * 4 * s["n_nodes"])
+    nn = s["n_nodes"]
+    inside = 2 * A + 24 * s["scalar_len"] + 2 * leaf_sites + 16 * nn
+    outside = 3 * A + 28 * s["scalar_len"] + 2 * leaf_sites + 16 * nn + 4 * s["count_floats"]
+    mstep = 4 * s["count_floats"] + 32 * nn
+    return {"inside": inside, "outside": outside, "mstep": mstep,
+            "em_iteration": inside + outside + mstep}
+
+
+def plain_dropin(w, n, device):
+    """The plain drop-in: candidates one at a time through the fastEM_solver
+    mirror (one solver object, one EM to convergence per candidate), as the
+    reference's topology search calls its solver."""
+    import torch
+
+    from laml_gb300.fastEM_solver import fastEM_solver
+    data = {"charMtrx": w.rows, "ordered_leaf_labels": [w.leaf_order]}
+    prior = {"Q": w.Q}
+    fastEM_solver([w.newicks[0]], data, prior, device=device).score_tree()   # warm
+    torch.cuda.synchronize(device)
+    iters, t0 = 0, time.perf_counter()
+    for nw in w.newicks[:n]:
+        s = fastEM_solver([nw], data, prior, device=device)
+        s.score_tree()
+        iters += s.last_em_iterations
+    return iters / (time.perf_counter() - t0)
 
 
 def peaks():
@@ -240,6 +276,8 @@ def main():
     ap.add_argument("--ref-trees", type=int, default=16)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--plain-trees", type=int, default=8,
+                    help="candidates timed one at a time through the drop-in solver")
     ap.add_argument("--path", default="graph", choices=["graph", "persistent", "levels"],
                     help="graph: a CUDA graph of the per-level launches of one EM iteration "
                          "(one graph launch per step); persistent: one cooperative launch "
@@ -312,6 +350,22 @@ def main():
         stream.synchronize()
         t1 = time.perf_counter()
     b.check_device_error()
+
+    # device time of the inside and the outside pass alone (their level
+    # kernels), for the per-kernel roofline
+    def pass_ms(fn, reps=5):
+        fn()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(reps):
+            fn()
+        e1.record(stream)
+        stream.synchronize()
+        return e0.elapsed_time(e1) / reps
+
+    with torch.cuda.stream(stream):
+        ms_out = pass_ms(lambda: b.outside())
+        ms_in = pass_ms(lambda: b.inside(update_em=True))
     launch_ms = [ev[i].elapsed_time(ev[i + 1]) for i in range(args.steps)]
     total_ms = ev[0].elapsed_time(ev[-1])
     if world > 1:
@@ -321,10 +375,25 @@ def main():
     ms = total_ms / args.steps
     value = T * world * args.steps / (total_ms / 1e3)
     nsu = 2.0 * nodes * K * world * args.steps / (total_ms / 1e3)
-    bytes_it = algorithmic_bytes(b)
+    pb = pass_bytes(b)
     avg_launch_s = statistics.mean(launch_ms) / 1e3
     peak, peak_kind = peaks()
-    achieved = bytes_it / avg_launch_s / 1e9
+
+    def roof(nbytes, seconds, kernel, launches):
+        a = nbytes / seconds / 1e9
+        return {"bound": "hbm", "achieved": a, "peak": peak, "unit": "GB/s", "frac": a / peak,
+                "traffic": None, "kernel": kernel, "bytes_per_launch": nbytes / launches,
+                "launches": launches, "seconds": seconds, "peak_kind": peak_kind}
+
+    n_out, n_in = b.sizes["n_out_levels"], b.sizes["n_in_levels"]
+    roof_out = roof(pb["outside"], ms_out / 1e3, "k_items outside levels (one launch per level "
+                    "of internal parents, both children per item)", n_out + 2)
+    roof_in = roof(pb["inside"], ms_in / 1e3, "k_items inside levels (one launch per height)",
+                   n_in + 1)
+    roof_it = roof(pb["em_iteration"], avg_launch_s,
+                   {"graph": "EM-iteration graph (k_items per level, k_mstep)",
+                    "persistent": "k_em_persistent",
+                    "levels": "k_items per level, k_mstep"}[args.path], 1)
     llh_now = b.work["tr_llh"].cpu().numpy()
 
     # e2e: public API from host strings / matrix to host results
@@ -343,6 +412,13 @@ def main():
         e2e = {"value": tot_iters * world / t_e2e, "unit": UNIT, "h2d_bytes_per_step": h2d,
                "d2h_bytes_per_step": d2h, "seconds_per_step": t_e2e / args.e2e_steps,
                "em_iterations_per_step": tot_iters / args.e2e_steps}
+
+    plain = None
+    if not args.no_e2e and args.plain_trees > 0:
+        pv = plain_dropin(w, args.plain_trees, dev)
+        plain = {"value": pv, "unit": UNIT,
+                 "sample": f"{args.plain_trees} candidates one at a time through the "
+                           "fastEM_solver mirror (EM to convergence each)"}
 
     cpu = None
     if rank == 0 and not args.no_cpu:
@@ -368,14 +444,12 @@ def main():
                        f"{2 * 4 * b.sizes['part_floats'] / 1e9:.2f} GB)",
                        "parallelism": f"replicas{world}" if world > 1 else "single"},
             "node_site_updates_per_s": nsu,
-            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                         "frac": achieved / peak, "traffic": None,
-                         "kernel": {"graph": "EM-iteration graph (k_items per level, k_mstep)",
-                                    "persistent": "k_em_persistent",
-                                    "levels": "k_items per level, k_mstep"}[args.path],
-                         "bytes_per_launch": bytes_it,
-                         "peak_kind": peak_kind},
+            "roofline": roof_out,
+            "roofline_inside": roof_in,
+            "roofline_em_iteration": roof_it,
             "e2e": e2e,
+            "plain_gpu_dropin": plain,
+            "batched_over_plain": (e2e["value"] / plain["value"]) if (e2e and plain) else None,
             "cpu_baseline": cpu,
             "clocks": clk.summary(),
             "gpu_launches": args.steps * (1 if args.path == "persistent" else

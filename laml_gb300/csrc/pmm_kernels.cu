@@ -30,6 +30,7 @@
 #include <stdint.h>
 
 #include <algorithm>
+#include <cfloat>
 #include <cmath>
 #include <cstdio>
 #include <string>
@@ -95,6 +96,16 @@ __device__ __forceinline__ Leaf leaf_params(const laml_batch& b, int tree) {
         L.es = 0.f;
     }
     return L;
+}
+
+// fast_em exponentiates its log-responsibilities in float32 with denormals
+// flushed (calculations.py:576-577): in the compat model a per-site count
+// term below the smallest normal float is zero
+__device__ __forceinline__ void flush_counts(const laml_batch& b, float* c, int n) {
+    if (!b.compat) return;
+#pragma unroll
+    for (int k = 0; k < 8; ++k)
+        if (k < n && c[k] < FLT_MIN) c[k] = 0.f;
 }
 
 // One child's inside vector at one site, normalised.
@@ -278,6 +289,7 @@ __device__ __forceinline__ void child_finish(const laml_batch& b, const SiteCtx&
         const float pl = cv.ss * outs * sc;
         if (cv.code == -1) cnt[6] = pl; else cnt[7] = pl;
     }
+    flush_counts(b, cnt, 8);
     if (want_post && b.post0) {
         const int64_t pb = __ldg(b.tr_post_base + s.tree) +
                            (int64_t)(v - __ldg(b.tr_node_base + s.tree)) *
@@ -540,6 +552,7 @@ __device__ __forceinline__ void child_counts_log(const laml_batch& b, const Site
         const float pl = rel_exp(cv.ss + outs, lL);
         if (cv.code == -1) cnt[6] = pl; else cnt[7] = pl;
     }
+    flush_counts(b, cnt, 8);
     if (want_post && b.post0) {
         const int64_t pb = __ldg(b.tr_post_base + s.tree) +
                            (int64_t)(v - __ldg(b.tr_node_base + s.tree)) *
@@ -651,6 +664,7 @@ __device__ __noinline__ void root_counts_log(const laml_batch& b, int v, const S
     c[3] = rel_exp((float)re.lst + dx.value(), lL);
     c[4] = rel_exp((float)re.ls + cv.ss + sx.value(), lL);
     c[5] = rel_exp(xs + cv.ss, lL);
+    flush_counts(b, c, 6);
 }
 
 // ---------------------------------------------------------------------------
@@ -700,6 +714,9 @@ __device__ void root_counts_item(const laml_batch& b, int v, int g, int lane, bo
         caa = expz(logz(dotxv) + re.lst + lsc);
         cas = expz(logz(cv.ss * sumx) + re.ls + lsc);
         css = expz(logz(xs * cv.ss) + lsc);
+        float c[6] = {c00, c0a, c0s, caa, cas, css};
+        flush_counts(b, c, 6);
+        c00 = c[0]; c0a = c[1]; c0s = c[2]; caa = c[3]; cas = c[4]; css = c[5];
     }
     // sum over the G sites of the group
 #pragma unroll

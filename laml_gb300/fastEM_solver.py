@@ -207,6 +207,7 @@ class fastEM_solver:
             r = b.run_em(rounds=MSTEP_ROUNDS)[0]
             self.params.nu, self.params.phi = r.nu, r.phi
             self._d[i] = r.branch_lengths
+            self.last_em_iterations = r.iterations
             score = r.llh
         return score, "optimal"
 
@@ -287,4 +288,71 @@ def _ts_postorder(t: EncodedTree):
         if t.child0[u] >= 0:
             st.append((int(t.child0[u]), False))
             st.append((int(t.child1[u]), False))
+    return out
+
+
+class CandidateScore:
+    """One candidate of score_candidate_batch: its fastEM score (the last
+    tree's log-likelihood, as score_tree returns), parameters and -- built
+    on first use -- its newick strings with the optimised branch lengths."""
+
+    def __init__(self, score, params, topos, lengths, leaf_order):
+        self.score = score
+        self.params = params
+        self._topos, self._lengths, self._leaf_order = topos, lengths, leaf_order
+        self._newicks = None
+
+    @property
+    def newicks(self):
+        if self._newicks is None:
+            self._newicks = [write_newick(encode_newick(nw, self._leaf_order), d)
+                             for nw, d in zip(self._topos, self._lengths)]
+        return self._newicks
+
+
+def score_candidate_batch(candidates, strategies, data, prior, params, group_sites=8,
+                          device="cuda"):
+    """fastEM_solver(treeList, data, prior, params).score_tree(strategy) for
+    many candidates at once (each a treeList over the same leaves), as one
+    batched EM on the device.  Per tree: missing lengths drawn U(0.01, 0.5) in
+    node order (fastEM_solver.py:95-126, candidates in order), nu, phi start
+    at the strategy's fixed values or 0.5 (320-321) and are optimised
+    (323-324), every branch fixed when ``fixed_brlen`` is given (310-316)."""
+    from .encoding import encode_newick_batch
+    lo = data.get("ordered_leaf_labels")
+    leaf_order = list(lo[0]) if lo else None
+    flat, owner = [], []
+    for ci, topos in enumerate(candidates):
+        for nw in topos:
+            flat.append(nw)
+            owner.append(ci)
+    if leaf_order is None:
+        first = encode_newick(flat[0])
+        leaf_order = first.labels[:first.num_leaves]
+    trees = encode_newick_batch(flat, leaf_order)
+    mat = char_matrix([data["charMtrx"][c] for c in leaf_order])
+    ds = encode_dataset(mat, prior["Q"], compat=True, group_sites=group_sites)
+    d, masks, nus, phis = [], [], [], []
+    for t, ci in zip(trees, owner):
+        st = strategies[ci]
+        x = t.branch_length.copy()
+        for i in np.flatnonzero(~t.has_length):
+            x[i] = _random.uniform(0.01, 0.5)
+        d.append(np.maximum(x, 1e-6))
+        fixed = st.get('fixed_brlen') is not None
+        masks.append(np.zeros(t.num_nodes, bool) if fixed else np.ones(t.num_nodes, bool))
+        nu = st.get('fixed_nu') or 0.5
+        phi = st.get('fixed_phi') or 0.5
+        nus.append(min(max(nu, 1e-6), 1 - 1e-6))
+        phis.append(min(max(phi, 1e-6), 1 - 1e-6))
+    b = DeviceBatch([ds], trees, [0] * len(trees), d, nus, phis, compat=True, mask=masks,
+                    device=device)
+    res = b.run_em(rounds=MSTEP_ROUNDS)
+    out = []
+    k = 0
+    for ci, topos in enumerate(candidates):
+        rs = res[k:k + len(topos)]
+        k += len(topos)
+        out.append(CandidateScore(rs[-1].llh, {'phi': rs[-1].phi, 'nu': rs[-1].nu}, topos,
+                                  [r.branch_lengths for r in rs], leaf_order))
     return out

@@ -45,6 +45,11 @@ static double lse2(double a, double b) {
     return m + log1p(exp(-fabs(a - b)));
 }
 
+/* fast_em exponentiates its log-responsibilities in float32 with denormals
+ * flushed (calculations.py:576-577): a per-site term below the smallest
+ * normal float is zero */
+static double ftz(double x) { return x < 1.1754943508222875e-38 ? 0.0 : x; }
+
 typedef struct {
     int R;          /* doubles per node row: sum_c (k_c + 2) */
     int* off;       /* [K] */
@@ -184,19 +189,19 @@ static double outside_counts(const ora_tree* T, work* W, double* cnt) {
         for (int c = 0; c < T->K; ++c) {
             const int k = T->kc[c], of = W->off[c], s = of + k + 1;
             const double L = W->L[c];
-            acc[0] += exp(x[of] + iv[of] + W->a0[v] - L);
+            acc[0] += ftz(exp(x[of] + iv[of] + W->a0[v] - L));
             double s1 = 0, s3 = 0, s4 = 0;
             for (int a = 1; a <= k; ++a) {
                 s1 += exp(x[of] + iv[of + a] + W->t1[v] + W->logq[of + a] + W->t3[v] - L);
                 s3 += exp(x[of + a] + iv[of + a] + W->t1[v] - L);
                 s4 += exp(x[of + a] + iv[s] + W->t2[v] - L);
             }
-            acc[1] += s1;
-            acc[2] += exp(x[of] + iv[s] + W->t2[v] - L);
-            acc[3] += s3;
-            acc[4] += s4;
-            acc[5] += exp(x[s] + iv[s] - L);
-            if (v < T->n) lr += exp(iv[s] + W->out[(size_t)v * R + s] - L);
+            acc[1] += ftz(s1);
+            acc[2] += ftz(exp(x[of] + iv[s] + W->t2[v] - L));
+            acc[3] += ftz(s3);
+            acc[4] += ftz(s4);
+            acc[5] += ftz(exp(x[s] + iv[s] - L));
+            if (v < T->n) lr += ftz(exp(iv[s] + W->out[(size_t)v * R + s] - L));
         }
         for (int i = 0; i < 6; ++i) cnt[(size_t)v * 6 + i] = acc[i];
     }

@@ -469,6 +469,17 @@ class EStep:
     post1: np.ndarray         # (N, K) log P(v = silenced | D)
 
 
+FLT_MIN = 1.1754943508222875e-38
+
+
+def _ftz(x, compat):
+    """fast_em exponentiates its log-responsibilities in float32 with
+    denormals flushed (calculations.py:576-577): in the compat model a
+    per-site term below the smallest normal float is zero.  The exact model
+    (EM_solver, float64) keeps them."""
+    return np.where(x < FLT_MIN, 0.0, x) if compat else x
+
+
 def e_step(prob: Problem, d, nu, phi) -> EStep:
     """compute_E_step (calculations.py:506-577) plus the posteriors of
     EM_solver.Estep_posterior (EM_solver.py:247-300)."""
@@ -510,9 +521,11 @@ def e_step(prob: Problem, d, nu, phi) -> EStep:
         cas = lse(x[:, 1:-1] + iv[:, -1:] + t2 - lr, axis=1)
         css = x[:, -1] + iv[:, -1] - L
         with np.errstate(over="ignore"):
-            counts[v] = np.exp(np.stack([c00, c0a, c0s, caa, cas, css])).sum(axis=1)
+            counts[v] = _ftz(np.exp(np.stack([c00, c0a, c0s, caa, cas, css])),
+                             prob.compat).sum(axis=1)
     with np.errstate(over="ignore"):
-        leaf_resp = np.exp(ins[:n, :, -1] + out[:n, :, -1] - L[None, :]).sum(axis=1)
+        leaf_resp = _ftz(np.exp(ins[:n, :, -1] + out[:n, :, -1] - L[None, :]),
+                         prob.compat).sum(axis=1)
     post0 = ins[:, :, 0] + out[:, :, 0] - L[None, :]
     post1 = ins[:, :, -1] + out[:, :, -1] - L[None, :]
     return EStep(float(np.sum(L)), L, counts, leaf_resp, ins, out, ein, post0, post1)

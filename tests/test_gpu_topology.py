@@ -1,0 +1,69 @@
+"""NNI topology search on the GPU solver: the 4-leaf brute-force checks of
+laml_unit_tests/unit_tests_TopoSearch_wfastEMSolver.py (test_1: a resolved
+start; test_3: a star start whose polytomy is resolved first), one candidate
+at a time and in device batches."""
+import random
+
+import pytest
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+from laml_gb300 import topology_search as TS  # noqa: E402
+from laml_gb300.fastEM_solver import fastEM_solver  # noqa: E402
+from laml_gb300.tree import Node, read_tree_newick  # noqa: E402
+
+Q = [{0: 0, 1: 1.0}] * 5
+MSA = {'a': [1, 1, 0, 0, 0], 'b': [1, 1, 1, 0, 0], 'c': [0, 0, 0, 1, 0], 'd': [0, 0, 0, 1, 0]}
+
+
+def _rooted_topologies(leaves):
+    """Every rooted binary topology of the leaves: stepwise addition of each
+    leaf above every node of the three starting triplets, under a
+    unifurcating root so the new leaf can also join above the old root."""
+    a, b, c = leaves[-3:]
+    topos = [f"((({x},{y}),{z}));" for x, y, z in ((a, b, c), (a, c, b), (b, c, a))]
+    for new in reversed(leaves[:-3]):
+        nxt = []
+        for T in topos:
+            n_nodes = sum(1 for _ in read_tree_newick(T).traverse_preorder())
+            for k in range(1, n_nodes):
+                t = read_tree_newick(T)
+                node = list(t.traverse_preorder())[k]
+                p = node.parent
+                p.remove_child(node)
+                m = Node()
+                p.add_child(m)
+                m.add_child(node)
+                m.add_child(Node(label=new))
+                nxt.append(t.newick())
+        topos = nxt
+    out = []
+    for T in topos:
+        t = read_tree_newick(T)
+        t.suppress_unifurcations()
+        out.append(t.newick())
+    return out
+
+
+def _brute_force():
+    best = float("inf")
+    for T in _rooted_topologies(list("abcd")):
+        nllh, _ = fastEM_solver([T], {'charMtrx': MSA}, {'Q': Q}).optimize(initials=1,
+                                                                            verbose=-1)
+        best = min(best, nllh)
+    return best
+
+
+@pytest.mark.parametrize("start", ["((a,c),(b,d));", "(a,b,c,d);"])
+@pytest.mark.parametrize("batched", [False, True])
+def test_nni_search_reaches_brute_force_optimum(start, batched):
+    random.seed(11)
+    nllh_bf = _brute_force()
+    data = {'charMtrx': MSA}
+    prior = {'Q': Q}
+    params = {'phi': 0, 'nu': 0}
+    cls = TS.Topology_search_batched if batched else TS.Topology_search
+    s = cls([start], fastEM_solver, data=data, prior=prior, params=params)
+    trees, score, best_params = s.search(maxiter=200, nreps=10, verbose=False)
+    assert -score == pytest.approx(nllh_bf, abs=5e-5)
