@@ -222,6 +222,16 @@ __device__ __forceinline__ double lse3(double a, double b, double c) {
 // exp(l) as an FP32 value (0 below its range)
 __device__ __forceinline__ float expz(double l) { return (float)exp(l); }
 
+// exp(l) = m * 2^e with m in [0.5, 1) (m = 0, e = 0 for l = -inf)
+__device__ __forceinline__ float split_exp(double l, int& e) {
+    if (!(l > -(double)INFINITY)) {
+        e = 0;
+        return 0.f;
+    }
+    e = (int)floor(l / kLn2) + 1;
+    return (float)exp(l - (double)e * kLn2);
+}
+
 // Root edge from a progenitor in state 0 (calculations.py:270-276, 504): s0,
 // dt (= sum_a q_a in_a) and ss are the root's inside values at scale 2^X.
 __device__ __forceinline__ void root_site_llh(const laml_batch& b, int tree, int site,
@@ -954,7 +964,11 @@ __device__ void outside_root_item_d(const laml_batch& b, const ItemDesc& d, int 
         B.x0 = expz(re.l00 - Eb * kLn2 + logz(ev0));
         B.xs = expz(re.ls - Eb * kLn2 + logz(cv.ss));
         B.X = Eb + cv.X;
-        const double lma = re.lm - Ea * kLn2, lmb = re.lm - Eb * kLn2;
+        // exp(re.lm - E ln 2) as an FP32 mantissa times 2^e: the per-state
+        // terms q_a E_a exp(re.lm - E ln 2) then need no FP64 (one exact
+        // power-of-two scaling each)
+        int ea, eb;
+        const float fa = split_exp(re.lm - Ea * kLn2, ea), fb = split_exp(re.lm - Eb * kLn2, eb);
         A.sumx = A.dot = A.mx = 0.f;
         B.sumx = B.dot = B.mx = 0.f;
         A.orow = cv.row ? b.out_part + (int64_t)d.v_ref * 8 + s.goff + lane : nullptr;
@@ -963,8 +977,8 @@ __device__ void outside_root_item_d(const laml_batch& b, const ItemDesc& d, int 
         for (int j = 2; j < s.C; ++j) {
             const float av = child_val<G>(cv, j), aw = child_val<G>(cw, j);
             const float qj = __ldg(s.qrow + j * G);
-            const float xa = expz(lma + logz(qj * fmaf(bw.z, aw, kw)));
-            const float xb = expz(lmb + logz(qj * fmaf(bv.z, av, kv)));
+            const float xa = ldexpf(fa * (qj * fmaf(bw.z, aw, kw)), ea);
+            const float xb = ldexpf(fb * (qj * fmaf(bv.z, av, kv)), eb);
             A.sumx += xa;
             A.dot = fmaf(xa, av, A.dot);
             B.sumx += xb;
@@ -1136,6 +1150,26 @@ __device__ __forceinline__ T branch_F(T a, T b, T c, T nu, T d, T* dFdu) {
     return -a + s / d;
 }
 
+// One step of a safeguarded Newton iteration for the root of a decreasing
+// function (value f, Newton step `step`) in the bracket [lo, hi]; true when
+// converged.  A step below `tol` (relative to u) ends the iteration at
+// u + step without touching the bracket: such a step can be smaller than the
+// FP32 spacing of u, so u + step would round back to u, fail the bracket test
+// and send the iterate to the middle of a bracket that may still span the
+// whole starting interval.
+__device__ __forceinline__ bool newton_step(float f, float step, float tol, float& u, float& lo,
+                                            float& hi) {
+    if (fabsf(step) <= tol * fmaxf(1.f, fabsf(u))) {
+        u += step;
+        return true;
+    }
+    if (f > 0.f) lo = u; else hi = u;
+    float un = u + step;
+    if (!(un > lo && un < hi)) un = 0.5f * (lo + hi);
+    u = un;
+    return hi - lo < 1e-6f;
+}
+
 // FP32 safeguarded Newton in log d on [lo, hi] from the previous value.
 __device__ float solve_branch_f(float a, float bb, float c, float nu, float d0, float lo,
                                 float hi) {
@@ -1150,12 +1184,7 @@ __device__ float solve_branch_f(float a, float bb, float c, float nu, float d0, 
     for (int it = 0; it < 24; ++it) {
         float dF;
         const float f = branch_F<float>(a, bb, c, nu, expf(u), &dF);
-        if (f > 0.f) ulo = u; else uhi = u;
-        float un = u - f / dF;
-        if (!(un > ulo && un < uhi)) un = 0.5f * (ulo + uhi);
-        const bool done = fabsf(un - u) <= 2e-6f * fmaxf(1.f, fabsf(u)) || uhi - ulo < 1e-6f;
-        u = un;
-        if (done) break;
+        if (newton_step(f, -f / dF, 2e-6f, u, ulo, uhi)) break;
     }
     return fminf(fmaxf(expf(u), lo), hi);
 }
@@ -1176,12 +1205,7 @@ __device__ double solve_branch(double a, double bb, double c, double nu, double 
     for (int it = 0; it < 24; ++it) {
         float dF;
         const float f = branch_F<float>(af, bf, cf, nf, expf(u), &dF);
-        if (f > 0.f) ulo = u; else uhi = u;
-        float un = u - f / dF;
-        if (!(un > ulo && un < uhi)) un = 0.5f * (ulo + uhi);
-        const bool done = fabsf(un - u) <= 2e-6f * fmaxf(1.f, fabsf(u)) || uhi - ulo < 1e-6f;
-        u = un;
-        if (done) break;
+        if (newton_step(f, -f / dF, 2e-6f, u, ulo, uhi)) break;
     }
     if (!polish) return fmin(fmax((double)expf(u), lo), hi);
     double ud = (double)u;
@@ -1357,12 +1381,7 @@ __device__ void mstep_tree(const laml_batch& b, int p, int rounds, double2* sh, 
                     const float x = expf(w);
                     const double2 S = sums(x, false);
                     const float H = (float)(-A * x + S.x);   // same sign as G
-                    if (H > 0.f) wlo = w; else whi = w;
-                    float wn = w + H / (float)S.y;
-                    if (!(wn > wlo && wn < whi)) wn = 0.5f * (wlo + whi);
-                    const bool done = fabsf(wn - w) <= 1e-6f * fmaxf(1.f, fabsf(w)) || whi - wlo < 1e-6f;
-                    w = wn;
-                    if (done) break;
+                    if (newton_step(H, H / (float)S.y, 1e-6f, w, wlo, whi)) break;
                 }
                 double wd = (double)w;
                 if (last && polish) {   // FP64 Newton polish
