@@ -225,6 +225,12 @@ typedef struct laml_batch {
     /* control */
     uint32_t* barrier;             /* 2 words, zeroed by the library before each persistent launch */
     int32_t* error;                /* 1 word: 0 or a negative LAML_ERR_* set on the device */
+    /* the largest group_C of the batch's datasets (states incl. unmutated and
+     * silenced).  > 0 selects the staged per-level kernels, which copy each
+     * item's partial rows into shared memory with the bulk-copy engine
+     * (cp.async.bulk) one item ahead of the computation; 0 keeps the direct
+     * kernels.  A group above it sets LAML_ERR_ARG in the error word. */
+    int32_t max_states;
 } laml_batch;
 
 /* A tree's partials are FP32 values with power-of-two exponents (linear)

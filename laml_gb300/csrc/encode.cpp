@@ -959,6 +959,22 @@ extern "C" int laml_plan_fill(const laml_plan_input* in, laml_plan_output* o) {
             }
         }
     }, 8);
+    // within a level, nodes grouped (stably) by which of their children are
+    // leaves: consecutive items -- the items of one warp -- then take the same
+    // specialised state loop
+    auto leaf_key = [&](int32_t g) {
+        return (o->nd_c0[o->nd_c0[g]] < 0 ? 1 : 0) | (o->nd_c0[o->nd_c1[g]] < 0 ? 2 : 0);
+    };
+    for (int side = 0; side < 2; ++side) {
+        parallel_for(NL[side] + 1, [&](int64_t a, int64_t e) {
+            for (int64_t l = a; l < e; ++l) {
+                int32_t* first = lnodes[side].data() + lstart[side][l];
+                int32_t* last = lnodes[side].data() + lstart[side][l + 1];
+                std::stable_sort(first, last,
+                                 [&](int32_t x, int32_t y) { return leaf_key(x) < leaf_key(y); });
+            }
+        }, 2);
+    }
     // items, group-major within a level (groups are sorted by state count)
     bool uniform = true;
     for (int p = 0; p < T; ++p) uniform = uniform && in->ds_groups[in->tree_dataset[p]] == maxNG;

@@ -50,6 +50,7 @@ constexpr double kCalcEps = 1e-10;     // fast_em/laml.py:47
 constexpr double kDmin = 0.005, kDmax = 10.0;   // core_constants.py:7-8
 constexpr double kEpsS = 1e-6, kEpsNu = 1e-5;   // EM_solver.Mstep defaults (EM_solver.py:307)
 constexpr double kLn2 = 0.69314718055994530942;
+constexpr double kLogEps = -13.815510557964274;   // log(1e-6)
 constexpr int kBlock = 256;
 constexpr unsigned kFull = 0xffffffffu;
 #ifndef LAML_CHUNK
@@ -60,7 +61,7 @@ constexpr int kChunk = LAML_CHUNK;   // states loaded ahead per step of a state 
 #define LAML_MINB 4
 #endif
 #ifndef LAML_MINB_OUT
-#define LAML_MINB_OUT LAML_MINB   // resident blocks per SM asked of the outside kernel
+#define LAML_MINB_OUT 3   // resident blocks per SM asked of the outside kernel (85 registers)
 #endif
 constexpr int kMstepStage = 2048;    // branches of a tree staged in shared memory by the M-step
 
@@ -69,6 +70,12 @@ constexpr int kMstepStage = 2048;    // branches of a tree staged in shared memo
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ float pow2i(int e) {   // 2^e for e in [-126, 127]
     return __int_as_float((127 + e) << 23);
+}
+
+// bulk prefetch of [p, p + bytes) into L2 (16-byte aligned, a multiple of
+// 16 bytes); a hint with no completion to wait for
+__device__ __forceinline__ void prefetch_l2(const void* p, uint32_t bytes) {
+    asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(p), "r"(bytes) : "memory");
 }
 
 __device__ __forceinline__ int scale_exp(float m) {
@@ -192,6 +199,10 @@ __device__ __forceinline__ bool site_ctx(const laml_batch& b, int node, int g, i
 // therefore formed from the terms' logarithms in FP64: the site likelihood
 // (kept as an FP32 mantissa in [0.5, 1) and an int exponent), the root's
 // posteriors, its E-step row and the outside inputs of its two children.
+// FP64 carries the large parts (exponents, d (1 + nu), nu d) and the sums;
+// the transcendental parts, whose arguments lie in a small range after that
+// split, run in FP32 (GB300's FP64 pipe is narrow): each result is rounded
+// to FP32 anyway.
 // ---------------------------------------------------------------------------
 struct RootEdge {
     double l00, lm, lst, ls;   // log P00, log Pmut (without q), log Pstay, log Psil
@@ -203,24 +214,36 @@ __device__ __forceinline__ RootEdge root_edge_logs(const laml_batch& b, int tree
     RootEdge e;
     e.l00 = -d * (1.0 + nu);
     e.lst = -nd;
-    e.lm = log((b.compat && d < kEPSd) ? kEPSd : -expm1(-d)) - nd;
-    e.ls = (b.compat && nd < kEPSd) ? log(kEPSd) : log(-expm1(-nd));
+    e.lm = (double)logf((b.compat && d < kEPSd) ? kEPS : -expm1f(-(float)d)) - nd;
+    e.ls = (b.compat && nd < kEPSd) ? kLogEps : (double)logf(-expm1f(-(float)nd));
     return e;
 }
 
-// log of a non-negative FP32 value (-inf at 0)
+// log of a non-negative FP32 value (-inf at 0): the binary exponent exactly,
+// the mantissa in [0.5, 1) through logf
 __device__ __forceinline__ double logz(float x) {
-    return x > 0.f ? log((double)x) : -(double)INFINITY;
+    if (!(x > 0.f)) return -(double)INFINITY;
+    int e;
+    const float m = frexpf(x, &e);
+    return (double)e * kLn2 + (double)logf(m);
+}
+
+// exp(l) rounded to FP32 (0 below its range): 2^k exactly times expf of the
+// remainder in [0, ln 2)
+__device__ __forceinline__ float expz(double l) {
+    if (isnan(l)) return NAN;
+    if (!(l > -110.0)) return 0.f;
+    if (l > 89.0) return INFINITY;
+    const double k = floor(l / kLn2);
+    return ldexpf(expf((float)(l - k * kLn2)), (int)k);
 }
 
 __device__ __forceinline__ double lse3(double a, double b, double c) {
     const double m = fmax(a, fmax(b, c));
     if (m == -(double)INFINITY) return m;
-    return m + log(exp(a - m) + exp(b - m) + exp(c - m));
+    const float s = expf((float)(a - m)) + expf((float)(b - m)) + expf((float)(c - m));
+    return m + (double)logf(s);
 }
-
-// exp(l) as an FP32 value (0 below its range)
-__device__ __forceinline__ float expz(double l) { return (float)exp(l); }
 
 // exp(l) = m * 2^e with m in [0.5, 1) (m = 0, e = 0 for l = -inf)
 __device__ __forceinline__ float split_exp(double l, int& e) {
@@ -229,7 +252,7 @@ __device__ __forceinline__ float split_exp(double l, int& e) {
         return 0.f;
     }
     e = (int)floor(l / kLn2) + 1;
-    return (float)exp(l - (double)e * kLn2);
+    return expf((float)(l - (double)e * kLn2));
 }
 
 // Root edge from a progenitor in state 0 (calculations.py:270-276, 504): s0,
@@ -241,10 +264,7 @@ __device__ __forceinline__ void root_site_llh(const laml_batch& b, int tree, int
     const int64_t t = __ldg(b.tr_site_base + tree) + site;
     int e = 0;
     float m = 0.f;
-    if (l > -(double)INFINITY) {
-        e = (int)floor(l / kLn2) + 1;
-        m = (float)exp(l - (double)e * kLn2);
-    }
+    if (l > -(double)INFINITY) m = split_exp(l, e);
     __stcg(b.root_lr + t, m);
     __stcg(b.root_x + t, X + e);
     __stcg(b.llh_site + t, l + (double)X * kLn2);
@@ -255,7 +275,7 @@ __device__ __forceinline__ double root_log_scale(const laml_batch& b, int tree, 
     const int64_t t = __ldg(b.tr_site_base + tree) + site;
     const float m = __ldcg(b.root_lr + t);
     if (!(m > 0.f)) return -(double)INFINITY;   // a zero likelihood: no responsibilities
-    return (double)(X - __ldcg(b.root_x + t)) * kLn2 - log((double)m);
+    return (double)(X - __ldcg(b.root_x + t)) * kLn2 - logz(m);
 }
 
 
@@ -419,8 +439,8 @@ __device__ __forceinline__ EdgeL edge_logs(const laml_batch& b, int x, int tree)
     EdgeL e;
     e.l00 = (float)(-d * (1.0 + nu));
     e.lst = (float)(-nd);
-    e.lm = (float)(log((b.compat && d < kEPSd) ? kEPSd : -expm1(-d)) - nd);
-    e.ls = (float)((b.compat && nd < kEPSd) ? log(kEPSd) : log(-expm1(-nd)));
+    e.lm = logf((b.compat && d < kEPSd) ? kEPS : -expm1f(-(float)d)) - (float)nd;
+    e.ls = (b.compat && nd < kEPSd) ? (float)kLogEps : logf(-expm1f(-(float)nd));
     return e;
 }
 
@@ -455,7 +475,14 @@ struct Lse {
 
 // exp(x - lL) for an FP32 log x and an FP64 log-likelihood
 __device__ __forceinline__ float rel_exp(float x, double lL) {
-    return x == -INFINITY ? 0.f : (float)exp((double)x - lL);
+    return x == -INFINITY ? 0.f : expz((double)x - lL);
+}
+
+// exp(x + y - lL) with an FP32 log x and FP64 logs y, lL: a root-edge term y
+// can be thousands in magnitude, far beyond the FP32 spacing it would get
+// folded into x
+__device__ __forceinline__ float rel_exp2(float x, double y, double lL) {
+    return (x == -INFINITY || y == -(double)INFINITY) ? 0.f : expz((double)x + y - lL);
 }
 
 struct ChildL {
@@ -500,10 +527,7 @@ __device__ __forceinline__ void root_store_log(const laml_batch& b, int tree, in
     const int64_t t = __ldg(b.tr_site_base + tree) + site;
     int e = 0;
     float m = 0.f;
-    if (l > -(double)INFINITY) {
-        e = (int)floor(l / kLn2) + 1;
-        m = (float)exp(l - (double)e * kLn2);
-    }
+    if (l > -(double)INFINITY) m = split_exp(l, e);
     __stcg(b.root_lr + t, m);
     __stcg(b.root_x + t, e);
     __stcg(b.llh_site + t, l);
@@ -587,30 +611,59 @@ __device__ __noinline__ void outside_log_lane(const laml_batch& b, const ItemDes
     const EdgeL ev = edge_logs(b, d.v, s.tree), ew = edge_logs(b, d.w, s.tree);
     const bool at_root = d.flags & 4;
     const float* urow = b.out_part + (int64_t)d.u_prow8 * 8 + s.goff + lane;
-    float o0, os, olm = 0.f;
-    if (at_root) {
-        const RootEdge re = root_edge_logs(b, s.tree);
-        o0 = (float)re.l00;
-        os = (float)re.ls;
-        olm = (float)re.lm;
-    } else {
-        o0 = __ldcg(urow);
-        os = __ldcg(urow + G);
-    }
     const float E0v = lse3f(ev.l00 + cv.s0, ev.lm + cv.ld, ev.ls + cv.ss);
     const float E0w = lse3f(ew.l00 + cw.s0, ew.lm + cw.ld, ew.ls + cw.ss);
-    const float xa0 = o0 + E0w, xas = os + cw.ss;   // child v: x = out[u] + E[w]
-    const float xb0 = o0 + E0v, xbs = os + cv.ss;   // child w: x = out[u] + E[v]
     const float kv = ev.ls + cv.ss, kw = ew.ls + cw.ss;
+    // Outside rows in log mode are stored relative to XoA / XoB * ln 2 (the
+    // children's out_x).  Below a root the offset is the parent's; at a root
+    // the outside vector is the root edge (FP64 logs, thousands in magnitude
+    // after a blow-up), so each child's inputs x = out[root] + E[sibling] are
+    // formed in FP64 and offset by their own maximum: the class that carries
+    // the likelihood keeps full FP32 precision.
+    float xa0, xas, xb0, xbs;      // child v: x = out[u] + E[w]; child w: x = out[u] + E[v]
+    double lmA = 0.0, lmB = 0.0;   // at a root: log Pmut - offset, per child
+    int XoA, XoB;
+    if (at_root) {
+        const RootEdge re = root_edge_logs(b, s.tree);
+        float ta = -INFINITY, tb = -INFINITY;   // max_j log q_j + E[.]_j
+        for (int j = 2; j < s.C; ++j) {
+            const float lq = lgz(__ldg(s.qrow + j * G));
+            ta = fmaxf(ta, lq + laddexp(ew.lst + child_val_log<G>(cw, j), kw));
+            tb = fmaxf(tb, lq + laddexp(ev.lst + child_val_log<G>(cv, j), kv));
+        }
+        auto offset = [](double a, double c, double e) {
+            const double m = fmax(a, fmax(c, e));
+            return m > -(double)INFINITY ? (int)floor(m / kLn2) + 1 : 0;
+        };
+        XoA = offset(re.l00 + (double)E0w, re.ls + (double)cw.ss, re.lm + (double)ta);
+        XoB = offset(re.l00 + (double)E0v, re.ls + (double)cv.ss, re.lm + (double)tb);
+        // x is summed in FP64: a root-edge term and its offset can each be
+        // thousands while their sum is what carries the likelihood
+        const double offA = XoA * kLn2, offB = XoB * kLn2;
+        xa0 = (float)(re.l00 + (double)E0w - offA);
+        xas = (float)(re.ls + (double)cw.ss - offA);
+        xb0 = (float)(re.l00 + (double)E0v - offB);
+        xbs = (float)(re.ls + (double)cv.ss - offB);
+        lmA = re.lm - offA;
+        lmB = re.lm - offB;
+    } else {
+        XoA = XoB = __ldcg(b.out_x + (int64_t)d.u_srow + s.site);
+        const float o0 = __ldcg(urow), os = __ldcg(urow + G);
+        xa0 = o0 + E0w;
+        xas = os + cw.ss;
+        xb0 = o0 + E0v;
+        xbs = os + cv.ss;
+    }
     float* arow = cv.row ? b.out_part + (int64_t)d.v_ref * 8 + s.goff + lane : nullptr;
     float* brow = cw.row ? b.out_part + (int64_t)d.w_ref * 8 + s.goff + lane : nullptr;
     Lse sa, sb, da, db;
     for (int j = 2; j < s.C; ++j) {
         const float lq = lgz(__ldg(s.qrow + j * G));
-        const float oj = at_root ? olm + lq : __ldcg(urow + j * G);
+        const float oj = at_root ? 0.f : __ldcg(urow + j * G);
         const float av = child_val_log<G>(cv, j), aw = child_val_log<G>(cw, j);
-        const float xa = oj + laddexp(ew.lst + aw, kw);
-        const float xb = oj + laddexp(ev.lst + av, kv);
+        const float ea = laddexp(ew.lst + aw, kw), eb = laddexp(ev.lst + av, kv);
+        const float xa = at_root ? (float)(lmA + (double)(lq + ea)) : oj + ea;
+        const float xb = at_root ? (float)(lmB + (double)(lq + eb)) : oj + eb;
         sa.add(xa);
         da.add(xa + av);
         sb.add(xb);
@@ -625,19 +678,19 @@ __device__ __noinline__ void outside_log_lane(const laml_batch& b, const ItemDes
         __stcg(arow, outa0);
         __stcg(arow + G, outas);
         __stcg(b.out_h + (int64_t)d.v_srow + s.site, 0);
-        __stcg(b.out_x + (int64_t)d.v_srow + s.site, 0);
+        __stcg(b.out_x + (int64_t)d.v_srow + s.site, XoA);
     }
     if (brow) {
         __stcg(brow, outb0);
         __stcg(brow + G, outbs);
         __stcg(b.out_h + (int64_t)d.w_srow + s.site, 0);
-        __stcg(b.out_x + (int64_t)d.w_srow + s.site, 0);
+        __stcg(b.out_x + (int64_t)d.w_srow + s.site, XoB);
     }
     const double lL = __ldcg(b.llh_site + __ldg(b.tr_site_base + s.tree) + s.site);
-    child_counts_log<G>(b, s, d.v, cv, ev, xa0, xas, lsa, da.value(), outa0, outas, lL,
-                        want_post, cv_);
-    child_counts_log<G>(b, s, d.w, cw, ew, xb0, xbs, lsb, db.value(), outb0, outbs, lL,
-                        want_post, cw_);
+    child_counts_log<G>(b, s, d.v, cv, ev, xa0, xas, lsa, da.value(), outa0, outas,
+                        lL - XoA * kLn2, want_post, cv_);
+    child_counts_log<G>(b, s, d.w, cw, ew, xb0, xbs, lsb, db.value(), outb0, outbs,
+                        lL - XoB * kLn2, want_post, cw_);
 }
 
 // the root's E-step row in logs (see root_counts_item for the modes)
@@ -651,6 +704,7 @@ __device__ __noinline__ void root_counts_log(const laml_batch& b, int v, const S
                                         (int)__ldg(b.nd_srow + v), s, gc, L);
     const RootEdge re = root_edge_logs(b, s.tree);
     float x0 = 0.f, xs = -INFINITY;
+    int Xo = 0;   // offset of node u's outside row (log mode: out_x in ln 2 units)
     Lse sx, dx;
     if (mode == 1) {
         const int u = __ldg(b.tr_quirk + s.tree);
@@ -658,6 +712,7 @@ __device__ __noinline__ void root_counts_log(const laml_batch& b, int v, const S
                                             (int)__ldg(b.nd_srow + u), s, gc, L);
         const EdgeL eu = edge_logs(b, u, s.tree);
         const float* urow = b.out_part + __ldg(b.nd_prow + u) + s.goff + lane;
+        Xo = __ldcg(b.out_x + __ldg(b.nd_srow + u) + s.site);
         x0 = __ldcg(urow) + lse3f(eu.l00 + cu.s0, eu.lm + cu.ld, eu.ls + cu.ss);
         xs = __ldcg(urow + G) + cu.ss;
         const float ku = eu.ls + cu.ss;
@@ -667,12 +722,12 @@ __device__ __noinline__ void root_counts_log(const laml_batch& b, int v, const S
             dx.add(xj + child_val_log<G>(cv, j));
         }
     }
-    const double lL = __ldcg(b.llh_site + __ldg(b.tr_site_base + s.tree) + s.site);
-    c[0] = rel_exp(x0 + cv.s0 + (float)re.l00, lL);
-    c[1] = rel_exp(x0 + (float)re.lm + cv.ld, lL);
-    c[2] = rel_exp(x0 + cv.ss + (float)re.ls, lL);
-    c[3] = rel_exp((float)re.lst + dx.value(), lL);
-    c[4] = rel_exp((float)re.ls + cv.ss + sx.value(), lL);
+    const double lL = __ldcg(b.llh_site + __ldg(b.tr_site_base + s.tree) + s.site) - Xo * kLn2;
+    c[0] = rel_exp2(x0 + cv.s0, re.l00, lL);
+    c[1] = rel_exp2(x0 + cv.ld, re.lm, lL);
+    c[2] = rel_exp2(x0 + cv.ss, re.ls, lL);
+    c[3] = rel_exp2(dx.value(), re.lst, lL);
+    c[4] = rel_exp2(cv.ss + sx.value(), re.ls, lL);
     c[5] = rel_exp(xs + cv.ss, lL);
     flush_counts(b, c, 6);
 }
@@ -752,12 +807,116 @@ __device__ void root_counts_item(const laml_batch& b, int v, int g, int lane, bo
     }
 }
 
+// State loops of the per-thread items, specialised on which children are
+// leaves (a leaf's slots come from its code, an internal child's from its
+// row).  Every pointer is __restrict__: the rows read (children's inside rows,
+// the parent's outside row, priors) and the rows written are distinct, so the
+// loads of later slots need not wait for the stores of earlier ones.
+template <int G, bool LEAF>
+__device__ __forceinline__ float slot_val(const float* __restrict__ row, float f, int code,
+                                          float e1, float cst, int j) {
+    if (LEAF) return code == j ? e1 : cst;
+    return __ldcg(row + j * G) * f;
+}
+
+template <int G, bool VL, bool WL>
+__device__ __forceinline__ void inside_states(const Child& cv, const Child& cw, const float4& bv,
+                                              const float4& bw, const float* __restrict__ qrow,
+                                              float* __restrict__ row, int C, float& dot,
+                                              float& mx) {
+    const float* __restrict__ rv = cv.row;
+    const float* __restrict__ rw = cw.row;
+    const float cstv = cv.code == -1 ? cv.ephi : 0.f, cstw = cw.code == -1 ? cw.ephi : 0.f;
+    const float kv = bv.w * cv.ss, kw = bw.w * cw.ss;
+    int j = 2;
+    for (; j + kChunk <= C; j += kChunk) {
+        float av[kChunk], aw[kChunk], qv[kChunk];
+#pragma unroll
+        for (int k = 0; k < kChunk; ++k) {
+            av[k] = slot_val<G, VL>(rv, cv.f, cv.code, cv.e1, cstv, j + k);
+            aw[k] = slot_val<G, WL>(rw, cw.f, cw.code, cw.e1, cstw, j + k);
+            qv[k] = __ldg(qrow + (j + k) * G);
+        }
+#pragma unroll
+        for (int k = 0; k < kChunk; ++k) {
+            const float x = fmaf(bv.z, av[k], kv) * fmaf(bw.z, aw[k], kw);
+            __stcg(row + (j + k) * G, x);
+            dot = fmaf(qv[k], x, dot);
+            mx = fmaxf(mx, x);
+        }
+    }
+    for (; j < C; ++j) {
+        const float av = slot_val<G, VL>(rv, cv.f, cv.code, cv.e1, cstv, j);
+        const float aw = slot_val<G, WL>(rw, cw.f, cw.code, cw.e1, cstw, j);
+        const float x = fmaf(bv.z, av, kv) * fmaf(bw.z, aw, kw);
+        __stcg(row + j * G, x);
+        dot = fmaf(__ldg(qrow + j * G), x, dot);
+        mx = fmaxf(mx, x);
+    }
+}
+
+template <int G, bool VL, bool WL>
+__device__ __forceinline__ void outside_states(const float* __restrict__ urow, float fo,
+                                               const Child& cv, const Child& cw, const float4& bv,
+                                               const float4& bw, const float* __restrict__ qrow,
+                                               int C, ChildOut& A, ChildOut& B) {
+    const float* __restrict__ rv = cv.row;
+    const float* __restrict__ rw = cw.row;
+    float* __restrict__ ra = A.orow;
+    float* __restrict__ rb = B.orow;
+    const float cstv = cv.code == -1 ? cv.ephi : 0.f, cstw = cw.code == -1 ? cw.ephi : 0.f;
+    const float kv = bv.w * cv.ss, kw = bw.w * cw.ss;
+    const float pxa = bv.y * A.x0, pxb = bw.y * B.x0;
+    float sa = 0.f, da = 0.f, ma = 0.f, sb = 0.f, db = 0.f, mb = 0.f;
+    auto step = [&](float o, float av, float aw, float qj, int j) {
+        const float xa = o * fmaf(bw.z, aw, kw);
+        const float xb = o * fmaf(bv.z, av, kv);
+        sa += xa;
+        da = fmaf(xa, av, da);
+        sb += xb;
+        db = fmaf(xb, aw, db);
+        if (!VL) {
+            const float r = fmaf(pxa, qj, bv.z * xa);
+            __stcg(ra + j * G, r);
+            ma = fmaxf(ma, r);
+        }
+        if (!WL) {
+            const float r = fmaf(pxb, qj, bw.z * xb);
+            __stcg(rb + j * G, r);
+            mb = fmaxf(mb, r);
+        }
+    };
+    int j = 2;
+    for (; j + kChunk <= C; j += kChunk) {
+        float ou[kChunk], av[kChunk], aw[kChunk], qv[kChunk];
+#pragma unroll
+        for (int k = 0; k < kChunk; ++k) {
+            ou[k] = __ldcg(urow + (j + k) * G) * fo;
+            av[k] = slot_val<G, VL>(rv, cv.f, cv.code, cv.e1, cstv, j + k);
+            aw[k] = slot_val<G, WL>(rw, cw.f, cw.code, cw.e1, cstw, j + k);
+            qv[k] = __ldg(qrow + (j + k) * G);
+        }
+#pragma unroll
+        for (int k = 0; k < kChunk; ++k) step(ou[k], av[k], aw[k], qv[k], j + k);
+    }
+    for (; j < C; ++j)
+        step(__ldcg(urow + j * G) * fo, slot_val<G, VL>(rv, cv.f, cv.code, cv.e1, cstv, j),
+             slot_val<G, WL>(rw, cw.f, cw.code, cw.e1, cstw, j), __ldg(qrow + j * G), j);
+    A.sumx = sa; A.dot = da; A.mx = ma;
+    B.sumx = sb; B.dot = db; B.mx = mb;
+}
+
 template <int G>
 __device__ void inside_item_d(const laml_batch& b, const ItemDesc& d, int lane,
                               bool respect_status) {
     SiteCtx s;
     GroupCtx gc;
     if (!site_ctx_d<G>(b, d, lane, respect_status, s, gc)) return;
+    if (lane == 0) {   // the children's rows into L2 while the first slots load
+        const uint32_t bytes = (uint32_t)s.C * G * sizeof(float);
+        if (!(d.flags & 1)) prefetch_l2(b.in_part + (int64_t)d.v_ref * 8 + s.goff, bytes);
+        if (!(d.flags & 2)) prefetch_l2(b.in_part + (int64_t)d.w_ref * 8 + s.goff, bytes);
+    }
     if (tree_log(b, s.tree)) {
         inside_log_item<G>(b, d, s, gc);
         return;
@@ -774,29 +933,11 @@ __device__ void inside_item_d(const laml_batch& b, const ItemDesc& d, int lane,
     __stcg(row, s0);
     __stcg(row + G, ss);
     float mx = fmaxf(s0, ss), dot = 0.f;
-    int j = 2;
-    for (; j + kChunk <= s.C; j += kChunk) {
-        float av[kChunk], aw[kChunk], qv[kChunk];
-#pragma unroll
-        for (int k = 0; k < kChunk; ++k) {
-            av[k] = child_val<G>(cv, j + k);
-            aw[k] = child_val<G>(cw, j + k);
-            qv[k] = __ldg(s.qrow + (j + k) * G);
-        }
-#pragma unroll
-        for (int k = 0; k < kChunk; ++k) {
-            const float x = fmaf(bv.z, av[k], kv) * fmaf(bw.z, aw[k], kw);
-            __stcg(row + (j + k) * G, x);
-            dot = fmaf(qv[k], x, dot);
-            mx = fmaxf(mx, x);
-        }
-    }
-    for (; j < s.C; ++j) {
-        const float av = child_val<G>(cv, j), aw = child_val<G>(cw, j);
-        const float x = fmaf(bv.z, av, kv) * fmaf(bw.z, aw, kw);
-        __stcg(row + j * G, x);
-        dot = fmaf(__ldg(s.qrow + j * G), x, dot);
-        mx = fmaxf(mx, x);
+    switch ((cv.row ? 0 : 1) | (cw.row ? 0 : 2)) {   // warp-uniform: items are sorted by it
+        case 0: inside_states<G, false, false>(cv, cw, bv, bw, s.qrow, row, s.C, dot, mx); break;
+        case 1: inside_states<G, true, false>(cv, cw, bv, bw, s.qrow, row, s.C, dot, mx); break;
+        case 2: inside_states<G, false, true>(cv, cw, bv, bw, s.qrow, row, s.C, dot, mx); break;
+        default: inside_states<G, true, true>(cv, cw, bv, bw, s.qrow, row, s.C, dot, mx); break;
     }
     const int h = scale_exp(mx);
     const float f = pow2i(-h);
@@ -816,6 +957,12 @@ __device__ void outside_item_d(const laml_batch& b, const ItemDesc& d, int lane,
     SiteCtx s;
     GroupCtx gc;
     const bool live = act && site_ctx_d<G>(b, d, lane, true, s, gc);
+    if (live && lane == 0) {   // the parent's outside row and the children's rows into L2
+        const uint32_t bytes = (uint32_t)s.C * G * sizeof(float);
+        prefetch_l2(b.out_part + (int64_t)d.u_prow8 * 8 + s.goff, bytes);
+        if (!(d.flags & 1)) prefetch_l2(b.in_part + (int64_t)d.v_ref * 8 + s.goff, bytes);
+        if (!(d.flags & 2)) prefetch_l2(b.in_part + (int64_t)d.w_ref * 8 + s.goff, bytes);
+    }
     if (live && tree_log(b, s.tree)) {
         float tv[8], tw[8];
         outside_log_lane<G>(b, d, s, gc, want_post, tv, tw);
@@ -844,59 +991,11 @@ __device__ void outside_item_d(const laml_batch& b, const ItemDesc& d, int lane,
         B.sumx = B.dot = B.mx = 0.f;
         A.orow = cv.row ? b.out_part + (int64_t)d.v_ref * 8 + s.goff + lane : nullptr;
         B.orow = cw.row ? b.out_part + (int64_t)d.w_ref * 8 + s.goff + lane : nullptr;
-        const float kv = bv.w * cv.ss, kw = bw.w * cw.ss;
-        const float pxa = bv.y * A.x0, pxb = bw.y * B.x0;
-        int j = 2;
-        for (; j + kChunk <= s.C; j += kChunk) {
-            float ou[kChunk], av[kChunk], aw[kChunk], qv[kChunk];
-#pragma unroll
-            for (int k = 0; k < kChunk; ++k) {
-                ou[k] = __ldcg(urow + (j + k) * G);
-                av[k] = child_val<G>(cv, j + k);
-                aw[k] = child_val<G>(cw, j + k);
-                qv[k] = __ldg(s.qrow + (j + k) * G);
-            }
-#pragma unroll
-            for (int k = 0; k < kChunk; ++k) {
-                const float o = ou[k] * fo;
-                const float xa = o * fmaf(bw.z, aw[k], kw);
-                const float xb = o * fmaf(bv.z, av[k], kv);
-                A.sumx += xa;
-                A.dot = fmaf(xa, av[k], A.dot);
-                B.sumx += xb;
-                B.dot = fmaf(xb, aw[k], B.dot);
-                if (A.orow) {
-                    const float r = fmaf(pxa, qv[k], bv.z * xa);
-                    __stcg(A.orow + (j + k) * G, r);
-                    A.mx = fmaxf(A.mx, r);
-                }
-                if (B.orow) {
-                    const float r = fmaf(pxb, qv[k], bw.z * xb);
-                    __stcg(B.orow + (j + k) * G, r);
-                    B.mx = fmaxf(B.mx, r);
-                }
-            }
-        }
-        for (; j < s.C; ++j) {
-            const float o = __ldcg(urow + j * G) * fo;
-            const float av = child_val<G>(cv, j), aw = child_val<G>(cw, j);
-            const float qj = __ldg(s.qrow + j * G);
-            const float xa = o * fmaf(bw.z, aw, kw);
-            const float xb = o * fmaf(bv.z, av, kv);
-            A.sumx += xa;
-            A.dot = fmaf(xa, av, A.dot);
-            B.sumx += xb;
-            B.dot = fmaf(xb, aw, B.dot);
-            if (A.orow) {
-                const float r = fmaf(pxa, qj, bv.z * xa);
-                __stcg(A.orow + j * G, r);
-                A.mx = fmaxf(A.mx, r);
-            }
-            if (B.orow) {
-                const float r = fmaf(pxb, qj, bw.z * xb);
-                __stcg(B.orow + j * G, r);
-                B.mx = fmaxf(B.mx, r);
-            }
+        switch ((cv.row ? 0 : 1) | (cw.row ? 0 : 2)) {   // warp-uniform: items are sorted by it
+            case 0: outside_states<G, false, false>(urow, fo, cv, cw, bv, bw, s.qrow, s.C, A, B); break;
+            case 1: outside_states<G, true, false>(urow, fo, cv, cw, bv, bw, s.qrow, s.C, A, B); break;
+            case 2: outside_states<G, false, true>(urow, fo, cv, cw, bv, bw, s.qrow, s.C, A, B); break;
+            default: outside_states<G, true, true>(urow, fo, cv, cw, bv, bw, s.qrow, s.C, A, B); break;
         }
         const int64_t t = __ldg(b.tr_site_base + s.tree) + s.site;
         const float lroot = __ldcg(b.root_lr + t);
@@ -1035,8 +1134,8 @@ __device__ __noinline__ void root_init_log(const laml_batch& b, int r, const Sit
         const int64_t pb = __ldg(b.tr_post_base + s.tree) +
                            (int64_t)(r - __ldg(b.tr_node_base + s.tree)) *
                                __ldg(b.ds_sites_pad + s.ds) + s.site;
-        __stcg(b.post0 + pb, rel_exp(cr.s0 + (float)re.l00, lL));
-        __stcg(b.post1 + pb, rel_exp(cr.ss + (float)re.ls, lL));
+        __stcg(b.post0 + pb, rel_exp2(cr.s0, re.l00, lL));
+        __stcg(b.post1 + pb, rel_exp2(cr.ss, re.ls, lL));
     }
 }
 
@@ -1289,8 +1388,12 @@ __device__ void mstep_tree(const laml_batch& b, int p, int rounds, double2* sh, 
     if (!(fix & 2)) {
         const double M = __ldg(b.ds_missing + ds), total = (double)n * K;
         if (compat) {
+            // stationary point of R log(1 - phi) + B log(phi); with B <= 0
+            // (leaf silencing explains every '?') the objective decreases in
+            // phi and the bound is the maximum -- also when B < -R, where the
+            // closed form's denominator changes sign
             const double Bm = M - LR, R = total - M;
-            phi = (R + Bm) > 0.0 ? Bm / (R + Bm) : phi;
+            phi = Bm <= 0.0 ? kCalcEps : ((R + Bm) > 0.0 ? Bm / (R + Bm) : phi);
             phi = fmin(fmax(phi, kCalcEps), 1.0 - kCalcEps);
         } else {
             const double Rt = M - LRs.x, R = total - M;   // '?' entries only
@@ -1305,9 +1408,10 @@ __device__ void mstep_tree(const laml_batch& b, int p, int rounds, double2* sh, 
         const bool last = r == R - 1;
         const bool use_s = compat || nu > kEpsNu;
         const float nuf = (float)nu;
-        for (int v = threadIdx.x; v < N; v += blockDim.x) {
-            if (!__ldg(b.nd_mask + base + v)) continue;
-            if (last && polish) {   // the FP64 counts for the polished solve
+        if (last && polish) {
+            for (int v = threadIdx.x; v < N; v += blockDim.x) {
+                if (!__ldg(b.nd_mask + base + v)) continue;
+                // the FP64 counts for the polished solve
                 const double* c = b.nd_cnt + (int64_t)(base + v) * 6;
                 const double c0 = __ldcg(c), c1 = __ldcg(c + 1), c2 = __ldcg(c + 2),
                              c3 = __ldcg(c + 3), c4 = __ldcg(c + 4);
@@ -1316,7 +1420,10 @@ __device__ void mstep_tree(const laml_batch& b, int p, int rounds, double2* sh, 
                                                dhi, true);
                 Dd[v] = (float)dn;
                 __stcg(b.nd_d + base + v, dn);
-            } else {
+            }
+        } else {
+            for (int v = threadIdx.x; v < N; v += blockDim.x) {
+                if (!__ldg(b.nd_mask + base + v)) continue;
                 const float4 q = C4[v];
                 const float dn = solve_branch_f(q.x + nuf * q.y, q.z, use_s ? q.w : 0.f, nuf,
                                                 Dd[v], (float)dlo, (float)dhi);
@@ -1506,6 +1613,495 @@ __device__ bool grid_barrier(const laml_batch& b, unsigned& gen) {
 }
 
 // ---------------------------------------------------------------------------
+// Staged warp-per-item levels (linear partials, inside and non-root outside).
+//
+// A warp owns one (node, group) item at a time.  Lane = p * G + l works on
+// site l of the group and on the state slots j = 2 + p, 2 + p + P, ...
+// (P = 32 / G lanes per site), so a warp load or store of a slot range covers
+// P consecutive slots of all G sites: 32 consecutive floats.  The item's
+// partial rows (C * G floats each, contiguous in HBM) are copied into shared
+// memory by the bulk-copy engine (cp.async.bulk, completion counted on an
+// mbarrier) while the warp computes the previous item; descriptors are read
+// two items ahead.  A descriptor lives spread over the warp: lanes 0..11 hold
+// the item's 12 words, lanes 12..19 its group's 8 words, lane 20 the group's
+// state count, lanes 21, 22 its tree's status and mode; fields are read with a
+// shuffle.
+// Trees in log mode take the per-lane path (global loads) on the first G
+// lanes.  Every wait is bounded: on timeout the warp records
+// LAML_ERR_TIMEOUT, waits (bounded) for its own copies and returns.
+// ---------------------------------------------------------------------------
+constexpr int kWWarps = 4;   // warps per block of the staged kernels
+
+// A level is narrow when it has fewer items than a few per SM: its time is
+// the latency of one item, which the one-warp-per-item kernels minimise; the
+// wide levels are throughput-bound and run G sites x (32 / G) items per warp.
+// The rule depends on the item count only, so every path (staged, direct,
+// persistent) makes the same choice and computes the same values.
+constexpr int64_t kNarrowItems = 8192;
+__host__ __device__ __forceinline__ bool narrow_level(int64_t n) { return n <= kNarrowItems; }
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+    return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count)
+                 : "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive_tx(uint64_t* bar, uint32_t bytes) {
+    asm volatile("{\n\t.reg .b64 st;\n\tmbarrier.arrive.expect_tx.shared::cta.b64 st, [%0], %1;\n\t}"
+                 ::"r"(smem_u32(bar)), "r"(bytes)
+                 : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile("{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+                 "selp.u32 %0, 1, 0, p;\n\t}"
+                 : "=r"(ok)
+                 : "r"(smem_u32(bar)), "r"(parity)
+                 : "memory");
+    return ok != 0;
+}
+
+// global -> shared bulk copy (16-byte aligned addresses, size a multiple of 16)
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes,
+                                         uint64_t* bar) {
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+        ::"r"(smem_u32(dst)), "l"(src), "r"(bytes), "r"(smem_u32(bar))
+        : "memory");
+}
+
+// order this thread's earlier generic-proxy accesses of shared memory before
+// later async-proxy (bulk copy) writes
+__device__ __forceinline__ void fence_proxy_async_smem() {
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+__device__ __forceinline__ void fence_mbar_init() {
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+// bounded wait for a phase of an mbarrier (2 s, then LAML_ERR_TIMEOUT)
+__device__ __forceinline__ bool mbar_wait(const laml_batch& b, uint64_t* bar, uint32_t parity) {
+    if (mbar_try_wait(bar, parity)) return true;
+    const unsigned long long t0 = gtimer();
+    for (uint32_t it = 0; it < (1u << 26); ++it) {
+        if (mbar_try_wait(bar, parity)) return true;
+        if ((it & 63) == 0 && gtimer() - t0 > 2000000000ull) break;
+    }
+    atomicCAS(b.error, 0, LAML_ERR_TIMEOUT);
+    return false;
+}
+
+struct WItem {
+    int u, v, w, tree, flags, g, gd, u_srow, u_prow8, v_ref, w_ref, v_srow, w_srow;
+    int goff, site0, qoff, ds, code_base, kpad, nsites, C, status, mode;
+};
+
+__device__ __forceinline__ int wf(int r, int k) { return __shfl_sync(kFull, r, k); }
+
+__device__ __forceinline__ WItem witem(int r) {
+    WItem t;
+    t.u = wf(r, 0); t.v = wf(r, 1); t.w = wf(r, 2);
+    const int a3 = wf(r, 3);
+    t.tree = a3 & 0xffffff;
+    t.flags = (int)((unsigned)a3 >> 24);
+    t.g = wf(r, 4); t.gd = wf(r, 5); t.u_srow = wf(r, 6); t.u_prow8 = wf(r, 7);
+    t.v_ref = wf(r, 8); t.w_ref = wf(r, 9); t.v_srow = wf(r, 10); t.w_srow = wf(r, 11);
+    t.goff = wf(r, 12); t.site0 = wf(r, 13); t.qoff = wf(r, 14); t.ds = wf(r, 15);
+    t.code_base = wf(r, 16); t.kpad = wf(r, 17); t.nsites = wf(r, 18);
+    t.C = wf(r, 20); t.status = wf(r, 21); t.mode = wf(r, 22);
+    return t;
+}
+
+__device__ __forceinline__ int wload_desc(const int32_t* desc, int64_t it, int lane) {
+    return lane < 12 ? __ldg(desc + 12 * it + lane) : 0;
+}
+
+// group words, state count, tree status and tree mode of the item whose
+// descriptor words r holds
+__device__ __forceinline__ int wload_grp(const laml_batch& b, int r, int lane) {
+    const int gd = __shfl_sync(kFull, r, 5);
+    const int tree = __shfl_sync(kFull, r, 3) & 0xffffff;
+    if (lane >= 12 && lane < 20) return __ldg(b.grp_desc + 8 * (int64_t)gd + (lane - 12));
+    if (lane == 20) return __ldg(b.group_C + gd);
+    if (lane == 21) return __ldcg(b.tr_status + tree);
+    if (lane == 22) return __ldcg(b.tr_mode + tree);
+    return r;
+}
+
+// start the bulk copies of an item's rows: KIND 1 (outside) the parent's
+// outside row, then the children's inside rows (internal children only);
+// KIND 0 (inside) the children's inside rows.  All lanes call (shuffles).
+template <int KIND, int G>
+__device__ __forceinline__ void wissue(const laml_batch& b, int r, float* buf, int cmax,
+                                       uint64_t* bar, int lane, bool respect_status) {
+    const int flags = (int)((unsigned)wf(r, 3) >> 24);
+    const int u_prow8 = wf(r, 7), v_ref = wf(r, 8), w_ref = wf(r, 9);
+    const int goff = wf(r, 12), C = wf(r, 20), status = wf(r, 21), mode = wf(r, 22);
+    if (lane != 0) return;
+    const bool skip = C > cmax || (respect_status && status != LAML_TREE_ACTIVE) ||
+                      mode == LAML_MODE_LOG;
+    if (C > cmax) atomicCAS(b.error, 0, LAML_ERR_ARG);
+    const uint32_t rb = (uint32_t)C * G * 4;
+    const bool uin = KIND == 1, vin = !(flags & 1), win = !(flags & 2);
+    const uint32_t tx = skip ? 0u : (uin ? rb : 0u) + (vin ? rb : 0u) + (win ? rb : 0u);
+    fence_proxy_async_smem();
+    mbar_arrive_tx(bar, tx);
+    if (skip) return;
+    const int cmaxG = cmax * G;
+    if (uin) bulk_g2s(buf, b.out_part + (int64_t)u_prow8 * 8 + goff, rb, bar);
+    float* dv = buf + (uin ? cmaxG : 0);
+    if (vin) bulk_g2s(dv, b.in_part + (int64_t)v_ref * 8 + goff, rb, bar);
+    if (win) bulk_g2s(dv + cmaxG, b.in_part + (int64_t)w_ref * 8 + goff, rb, bar);
+}
+
+__device__ __forceinline__ ItemDesc witem_desc(const WItem& t) {
+    ItemDesc d;
+    d.u = t.u; d.v = t.v; d.w = t.w; d.tree = t.tree; d.flags = t.flags; d.g = t.g; d.gd = t.gd;
+    d.u_srow = t.u_srow; d.u_prow8 = t.u_prow8; d.v_ref = t.v_ref; d.w_ref = t.w_ref;
+    d.v_srow = t.v_srow; d.w_srow = t.w_srow;
+    return d;
+}
+
+template <int G>
+__device__ __forceinline__ void witem_ctx(const laml_batch& b, const WItem& t, int l, SiteCtx& s,
+                                          GroupCtx& gc) {
+    s.tree = t.tree;
+    s.ds = t.ds;
+    s.site = t.g * G + l;
+    s.goff = t.goff;
+    s.C = __ldg(b.site_C + t.site0 + l);
+    s.sumq = __ldg(b.site_sumq + t.site0 + l);
+    s.qrow = b.q + t.qoff + l;
+    gc.code_base = t.code_base;
+    gc.kpad = t.kpad;
+}
+
+// one child of a staged item at site l: inside values from shared memory
+// (internal) or from the leaf's character code
+template <int G, bool LEAF>
+__device__ __forceinline__ Child wchild(const laml_batch& b, const WItem& t, int ref, int srow,
+                                        const float* srow_smem, const SiteCtx& s, const Leaf& L,
+                                        bool act) {
+    Child c;
+    c.e1 = L.e1;
+    c.ephi = L.ephi;
+    if (LEAF) {
+        const int code = act ? __ldg(b.codes + t.code_base + (int64_t)ref * t.kpad + s.site) : 0;
+        c.row = nullptr;
+        c.f = 1.f;
+        c.X = 0;
+        c.code = code;
+        c.s0 = code == 0 ? L.e1 : (code == -1 ? L.ephi : 0.f);
+        c.ss = code < 0 ? 1.f : L.es;
+        c.D = code >= 2 ? __ldg(s.qrow + code * G) * L.e1 : (code == -1 ? L.ephi * s.sumq : 0.f);
+    } else {
+        const int64_t si = (int64_t)srow + s.site;
+        const int h = act ? __ldcg(b.in_h + si) : 0;
+        c.f = pow2i(-h);
+        c.X = act ? __ldcg(b.in_x + si) : 0;
+        c.D = act ? __ldcg(b.in_dot + si) : 0.f;
+        c.row = srow_smem;   // marks an internal child; values come from shared memory
+        c.code = 0;
+    }
+    return c;
+}
+
+// slot j of a child of a staged item (leaf: from its code)
+template <int G, bool LEAF, bool STAGED>
+__device__ __forceinline__ float wval(const Child& c, const float* r, int j, float cst) {
+    if (LEAF) return c.code == j ? c.e1 : cst;
+    return (STAGED ? r[j * G] : __ldcg(r + j * G)) * c.f;
+}
+
+template <bool STAGED>
+__device__ __forceinline__ float wrow(const float* r, int k) {
+    return STAGED ? r[k] : __ldcg(r + k);
+}
+
+// STAGED: the children's rows are in shared memory (buf, after waiting on
+// bar); otherwise they are read from HBM (persistent kernel)
+template <int G, bool VL, bool WL, bool STAGED>
+__device__ void inside_w(const laml_batch& b, const WItem& t, const float* buf, int cmax, int lane,
+                         bool& waited, uint64_t* bar, uint32_t parity) {
+    constexpr int P = 32 / G;
+    const int l = lane % G, p = lane / G;
+    SiteCtx s;
+    GroupCtx gc;
+    witem_ctx<G>(b, t, l, s, gc);
+    const bool act = s.site < t.nsites;
+    if (!act) s.C = 0;
+    const Leaf L = leaf_params(b, t.tree);
+    const int cmaxG = cmax * G;
+    const float* rv = STAGED ? buf + l : b.in_part + (int64_t)t.v_ref * 8 + t.goff + l;
+    const float* rw = STAGED ? buf + cmaxG + l : b.in_part + (int64_t)t.w_ref * 8 + t.goff + l;
+    Child cv = wchild<G, VL>(b, t, t.v_ref, t.v_srow, rv, s, L, act);
+    Child cw = wchild<G, WL>(b, t, t.w_ref, t.w_srow, rw, s, L, act);
+    const float4 bv = load_bt(b, t.v), bw = load_bt(b, t.w);
+    if (STAGED) {
+        waited = mbar_wait(b, bar, parity);
+        if (!waited) return;
+    }
+    if (!VL) { cv.s0 = wrow<STAGED>(rv, 0) * cv.f; cv.ss = wrow<STAGED>(rv, G) * cv.f; }
+    if (!WL) { cw.s0 = wrow<STAGED>(rw, 0) * cw.f; cw.ss = wrow<STAGED>(rw, G) * cw.f; }
+    const float ev0 = bv.x * cv.s0 + bv.y * cv.D + bv.w * cv.ss;
+    const float ew0 = bw.x * cw.s0 + bw.y * cw.D + bw.w * cw.ss;
+    const float kv = bv.w * cv.ss, kw = bw.w * cw.ss;
+    const float cstv = cv.code == -1 ? L.ephi : 0.f, cstw = cw.code == -1 ? L.ephi : 0.f;
+    float* row = b.in_part + (int64_t)t.u_prow8 * 8 + t.goff + l;
+    const float s0 = ev0 * ew0, ss = cv.ss * cw.ss;
+    float mx = 0.f, dot = 0.f;
+    if (act && p == 0) {
+        __stcg(row, s0);
+        __stcg(row + G, ss);
+        mx = fmaxf(s0, ss);
+    }
+#pragma unroll 4
+    for (int j = 2 + p; j < s.C; j += P) {
+        const float av = wval<G, VL, STAGED>(cv, rv, j, cstv);
+        const float aw = wval<G, WL, STAGED>(cw, rw, j, cstw);
+        const float x = fmaf(bv.z, av, kv) * fmaf(bw.z, aw, kw);
+        __stcg(row + j * G, x);
+        dot = fmaf(__ldg(s.qrow + j * G), x, dot);
+        mx = fmaxf(mx, x);
+    }
+#pragma unroll
+    for (int off = G; off < 32; off <<= 1) {
+        dot += __shfl_xor_sync(kFull, dot, off);
+        mx = fmaxf(mx, __shfl_xor_sync(kFull, mx, off));
+    }
+    if (act && p == 0) {
+        const int h = scale_exp(mx);
+        const float f = pow2i(-h);
+        const int X = cv.X + cw.X + h;
+        const int64_t sr = (int64_t)t.u_srow + s.site;
+        __stcg(b.in_h + sr, h);
+        __stcg(b.in_x + sr, X);
+        __stcg(b.in_dot + sr, dot * f);
+        if (t.flags & 4)
+            root_site_llh(b, t.tree, s.site, root_edge_logs(b, t.tree), s0 * f, dot * f, ss * f,
+                          X);
+    }
+}
+
+template <int G, bool VL, bool WL, bool STAGED>
+__device__ void outside_w(const laml_batch& b, const WItem& t, const float* buf, int cmax,
+                          int lane, bool want_post, bool& waited, uint64_t* bar,
+                          uint32_t parity) {
+    constexpr int P = 32 / G;
+    const int l = lane % G, p = lane / G;
+    SiteCtx s;
+    GroupCtx gc;
+    witem_ctx<G>(b, t, l, s, gc);
+    const bool act = s.site < t.nsites;
+    if (!act) s.C = 0;
+    const Leaf L = leaf_params(b, t.tree);
+    const int cmaxG = cmax * G;
+    const float* ru = STAGED ? buf + l : b.out_part + (int64_t)t.u_prow8 * 8 + t.goff + l;
+    const float* rv = STAGED ? buf + cmaxG + l : b.in_part + (int64_t)t.v_ref * 8 + t.goff + l;
+    const float* rw = STAGED ? buf + 2 * cmaxG + l : b.in_part + (int64_t)t.w_ref * 8 + t.goff + l;
+    Child cv = wchild<G, VL>(b, t, t.v_ref, t.v_srow, rv, s, L, act);
+    Child cw = wchild<G, WL>(b, t, t.w_ref, t.w_srow, rw, s, L, act);
+    const float4 bv = load_bt(b, t.v), bw = load_bt(b, t.w);
+    const int64_t su = (int64_t)t.u_srow + s.site;
+    const float fo = pow2i(act ? -__ldcg(b.out_h + su) : 0);
+    const int Xo = act ? __ldcg(b.out_x + su) : 0;
+    const int64_t ts = __ldg(b.tr_site_base + t.tree) + s.site;
+    const float lroot = act ? __ldcg(b.root_lr + ts) : 0.f;
+    const int xroot = act ? __ldcg(b.root_x + ts) : 0;
+    if (STAGED) {
+        waited = mbar_wait(b, bar, parity);
+        if (!waited) return;
+    }
+    if (!VL) { cv.s0 = wrow<STAGED>(rv, 0) * cv.f; cv.ss = wrow<STAGED>(rv, G) * cv.f; }
+    if (!WL) { cw.s0 = wrow<STAGED>(rw, 0) * cw.f; cw.ss = wrow<STAGED>(rw, G) * cw.f; }
+    const float o0 = wrow<STAGED>(ru, 0) * fo, os = wrow<STAGED>(ru, G) * fo;
+    const float ev0 = bv.x * cv.s0 + bv.y * cv.D + bv.w * cv.ss;
+    const float ew0 = bw.x * cw.s0 + bw.y * cw.D + bw.w * cw.ss;
+    ChildOut A, B;   // A: child v (uses E[w]), B: child w (uses E[v])
+    A.x0 = o0 * ew0; A.xs = os * cw.ss; A.X = Xo + cw.X;
+    B.x0 = o0 * ev0; B.xs = os * cv.ss; B.X = Xo + cv.X;
+    A.sumx = A.dot = A.mx = 0.f;
+    B.sumx = B.dot = B.mx = 0.f;
+    A.orow = VL ? nullptr : b.out_part + (int64_t)t.v_ref * 8 + t.goff + l;
+    B.orow = WL ? nullptr : b.out_part + (int64_t)t.w_ref * 8 + t.goff + l;
+    const float kv = bv.w * cv.ss, kw = bw.w * cw.ss;
+    const float pxa = bv.y * A.x0, pxb = bw.y * B.x0;
+    const float cstv = cv.code == -1 ? L.ephi : 0.f, cstw = cw.code == -1 ? L.ephi : 0.f;
+#pragma unroll 4
+    for (int j = 2 + p; j < s.C; j += P) {
+        const float o = wrow<STAGED>(ru, j * G) * fo;
+        const float av = wval<G, VL, STAGED>(cv, rv, j, cstv);
+        const float aw = wval<G, WL, STAGED>(cw, rw, j, cstw);
+        const float qj = __ldg(s.qrow + j * G);
+        const float xa = o * fmaf(bw.z, aw, kw);
+        const float xb = o * fmaf(bv.z, av, kv);
+        A.sumx += xa;
+        A.dot = fmaf(xa, av, A.dot);
+        B.sumx += xb;
+        B.dot = fmaf(xb, aw, B.dot);
+        if (!VL) {
+            const float r = fmaf(pxa, qj, bv.z * xa);
+            __stcg(A.orow + j * G, r);
+            A.mx = fmaxf(A.mx, r);
+        }
+        if (!WL) {
+            const float r = fmaf(pxb, qj, bw.z * xb);
+            __stcg(B.orow + j * G, r);
+            B.mx = fmaxf(B.mx, r);
+        }
+    }
+#pragma unroll
+    for (int off = G; off < 32; off <<= 1) {
+        A.sumx += __shfl_xor_sync(kFull, A.sumx, off);
+        A.dot += __shfl_xor_sync(kFull, A.dot, off);
+        A.mx = fmaxf(A.mx, __shfl_xor_sync(kFull, A.mx, off));
+        B.sumx += __shfl_xor_sync(kFull, B.sumx, off);
+        B.dot += __shfl_xor_sync(kFull, B.dot, off);
+        B.mx = fmaxf(B.mx, __shfl_xor_sync(kFull, B.mx, off));
+    }
+    // child v's finish on phase 0, child w's on phase 1 (both on phase 0 when
+    // a site has one lane)
+    constexpr int PW = P > 1 ? 1 : 0;
+    float cv_[8] = {0, 0, 0, 0, 0, 0, 0, 0}, cw_[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    if (act && p == 0) child_finish<G>(b, s, t.v, cv, bv, A, want_post, lroot, xroot, cv_);
+    if (act && p == PW) child_finish<G>(b, s, t.w, cw, bw, B, want_post, lroot, xroot, cw_);
+    if (P > 1) {
+        float c[8];   // phase 0 lanes carry child v's counts, phase 1 lanes child w's
+#pragma unroll
+        for (int k = 0; k < 8; ++k) c[k] = p == 0 ? cv_[k] : cw_[k];
+#pragma unroll
+        for (int off = G / 2; off > 0; off >>= 1)
+#pragma unroll
+            for (int k = 0; k < 8; ++k) c[k] += __shfl_xor_sync(kFull, c[k], off);
+        if (l == 0 && p < 2) write_counts<G>(b, t.tree, p == 0 ? t.v : t.w, t.g, c);
+    } else {
+#pragma unroll
+        for (int off = G / 2; off > 0; off >>= 1)
+#pragma unroll
+            for (int k = 0; k < 8; ++k) {
+                cv_[k] += __shfl_xor_sync(kFull, cv_[k], off);
+                cw_[k] += __shfl_xor_sync(kFull, cw_[k], off);
+            }
+        if (l == 0) {
+            write_counts<G>(b, t.tree, t.v, t.g, cv_);
+            write_counts<G>(b, t.tree, t.w, t.g, cw_);
+        }
+    }
+}
+
+// one staged or direct item of kind 0 (inside) / 1 (outside below the roots),
+// dispatched on which children are leaves; log-mode trees take the per-lane
+// path on lanes 0..G-1
+template <int G, int KIND, bool STAGED>
+__device__ __forceinline__ bool witem_run(const laml_batch& b, const WItem& t, const float* buf,
+                                          int cmax, int lane, bool want_post, bool respect_status,
+                                          uint64_t* bar, uint32_t parity) {
+    const bool skip = (STAGED && t.C > cmax) ||
+                      ((KIND == 1 || respect_status) && t.status != LAML_TREE_ACTIVE);
+    bool waited = true;
+    if (skip || t.mode == LAML_MODE_LOG) {
+        if (STAGED) waited = mbar_wait(b, bar, parity);
+        if (!waited || skip) return waited;
+        const int l = lane % G, p = lane / G;
+        SiteCtx s;
+        GroupCtx gc;
+        witem_ctx<G>(b, t, l, s, gc);
+        const bool act = p == 0 && s.site < t.nsites;
+        const ItemDesc d = witem_desc(t);
+        if (KIND == 0) {
+            if (act) inside_log_item<G>(b, d, s, gc);
+        } else {
+            float cv_[8] = {0, 0, 0, 0, 0, 0, 0, 0}, cw_[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+            if (act) outside_log_lane<G>(b, d, s, gc, want_post, cv_, cw_);
+#pragma unroll
+            for (int off = G / 2; off > 0; off >>= 1)
+#pragma unroll
+                for (int k = 0; k < 8; ++k) {
+                    cv_[k] += __shfl_xor_sync(kFull, cv_[k], off);
+                    cw_[k] += __shfl_xor_sync(kFull, cw_[k], off);
+                }
+            if (lane == 0) {
+                write_counts<G>(b, t.tree, t.v, t.g, cv_);
+                write_counts<G>(b, t.tree, t.w, t.g, cw_);
+            }
+        }
+        return true;
+    }
+    const int leaves = t.flags & 3;
+#define LAML_W_CALL(VL, WL)                                                                  \
+    if (KIND == 0)                                                                           \
+        inside_w<G, VL, WL, STAGED>(b, t, buf, cmax, lane, waited, bar, parity);             \
+    else                                                                                     \
+        outside_w<G, VL, WL, STAGED>(b, t, buf, cmax, lane, want_post, waited, bar, parity);
+    switch (leaves) {
+        case 0: LAML_W_CALL(false, false) break;
+        case 1: LAML_W_CALL(true, false) break;
+        case 2: LAML_W_CALL(false, true) break;
+        default: LAML_W_CALL(true, true) break;
+    }
+#undef LAML_W_CALL
+    return waited;
+}
+
+// Staged level kernel: dynamic shared memory holds, per warp, two buffers of
+// NR rows of cmax * G floats (NR = 3 outside, 2 inside) and two mbarriers.
+template <int G, int KIND>
+__global__ void __launch_bounds__(kWWarps * 32) k_items_w(laml_batch b, const int32_t* desc,
+                                                          int64_t n, int cmax, int want_post,
+                                                          int respect_status) {
+    extern __shared__ __align__(128) unsigned char wsm[];
+    constexpr int NR = KIND == 1 ? 3 : 2;
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    const int64_t per = (int64_t)NR * cmax * G;   // floats of one buffer
+    float* bufs = reinterpret_cast<float*>(wsm) + (int64_t)wib * 2 * per;
+    uint64_t* bars = reinterpret_cast<uint64_t*>(reinterpret_cast<float*>(wsm) +
+                                                 (int64_t)kWWarps * 2 * per) + 2 * wib;
+    const int64_t gw = (int64_t)blockIdx.x * kWWarps + wib;
+    const int64_t nw = (int64_t)gridDim.x * kWWarps;
+    if (gw >= n) return;
+    if (lane == 0) {
+        mbar_init(bars, 1);
+        mbar_init(bars + 1, 1);
+        fence_mbar_init();
+    }
+    __syncwarp();
+    int r0 = wload_grp(b, wload_desc(desc, gw, lane), lane);
+    int r1 = gw + nw < n ? wload_grp(b, wload_desc(desc, gw + nw, lane), lane) : 0;
+    int r2 = gw + 2 * nw < n ? wload_desc(desc, gw + 2 * nw, lane) : 0;
+    wissue<KIND, G>(b, r0, bufs, cmax, bars, lane, KIND == 1 || respect_status);
+    uint32_t ph = 0;   // bit k: phase parity of buffer k
+    int cur = 0;
+    for (int64_t it = gw; it < n; it += nw) {
+        const bool has1 = it + nw < n, has2 = it + 2 * nw < n, has3 = it + 3 * nw < n;
+        if (has2) r2 = wload_grp(b, r2, lane);
+        if (has1)
+            wissue<KIND, G>(b, r1, bufs + (cur ^ 1) * per, cmax, bars + (cur ^ 1), lane,
+                            KIND == 1 || respect_status);
+        const int r3 = has3 ? wload_desc(desc, it + 3 * nw, lane) : 0;
+        const WItem t = witem(r0);
+        const uint32_t par = (ph >> cur) & 1u;
+        ph ^= 1u << cur;
+        if (!witem_run<G, KIND, true>(b, t, bufs + cur * per, cmax, lane, want_post != 0,
+                                      respect_status != 0, bars + cur, par)) {
+            // timed out: wait (bounded) for this warp's copies still in flight
+            mbar_wait(b, bars + cur, par);
+            if (has1) mbar_wait(b, bars + (cur ^ 1), (ph >> (cur ^ 1)) & 1u);
+            return;
+        }
+        __syncwarp();
+        r0 = r1;
+        r1 = r2;
+        r2 = r3;
+        cur ^= 1;
+    }
+}
+
+// ---------------------------------------------------------------------------
 // kernels
 // ---------------------------------------------------------------------------
 template <int G, int KIND>
@@ -1513,6 +2109,17 @@ __device__ __forceinline__ void for_items(const laml_batch& b, const int32_t* it
                                           int gwarp, int nwarps, bool want_post,
                                           bool respect_status, const int32_t* desc = nullptr) {
     constexpr int kind = KIND;
+    if constexpr (KIND <= 1) {
+        if (narrow_level(n)) {   // one item per warp: the shortest latency per item
+            const int lane = threadIdx.x & 31;
+            for (int64_t it = gwarp; it < n; it += nwarps) {
+                const WItem t = witem(wload_grp(b, wload_desc(desc, it, lane), lane));
+                witem_run<G, KIND, false>(b, t, nullptr, 0, lane, want_post, respect_status,
+                                          nullptr, 0);
+            }
+            return;
+        }
+    }
     constexpr int IPW = 32 / G;
     const int lane32 = threadIdx.x & 31, lane = lane32 % G, sub = lane32 / G;
     const int64_t nw = (n + IPW - 1) / IPW;
@@ -1754,11 +2361,55 @@ int validate(const laml_batch* b) {
     return LAML_OK;
 }
 
+// shared memory of a staged level kernel: per warp two buffers of NR rows of
+// max_states * G floats, then two 8-byte mbarriers per warp
+size_t staged_smem(const laml_batch& b, int kind) {
+    const size_t NR = kind == 1 ? 3 : 2;
+    return (size_t)kWWarps * (2 * NR * (size_t)b.max_states * b.group_sites * sizeof(float) + 16);
+}
+
+constexpr size_t kStagedSmemMax = 200 * 1024;
+
+template <int G, int KIND>
+int launch_staged(const laml_batch& b, const int32_t* desc, int64_t n, int want_post,
+                  int respect_status, cudaStream_t st) {
+    static bool attr_set = false;   // per process: the opt-in limit is a function attribute
+    if (!attr_set) {
+        int rc = check(cudaFuncSetAttribute(k_items_w<G, KIND>,
+                                            cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                            (int)kStagedSmemMax),
+                       "staged kernel shared memory limit");
+        if (rc) return rc;
+        attr_set = true;
+    }
+    const size_t smem = staged_smem(b, KIND);
+    int per_sm = 0;
+    int rc = check(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_items_w<G, KIND>,
+                                                                 kWWarps * 32, smem),
+                   "staged kernel occupancy");
+    if (rc) return rc;
+    if (per_sm < 1) per_sm = 1;
+    int64_t blocks = (n + kWWarps - 1) / kWWarps;
+    const int64_t cap = (int64_t)per_sm * num_sms();
+    if (blocks > cap) blocks = cap;
+    k_items_w<G, KIND><<<(unsigned)blocks, kWWarps * 32, smem, st>>>(b, desc, n, b.max_states,
+                                                                     want_post, respect_status);
+    return check(cudaGetLastError(), "k_items_w launch");
+}
+
 template <int G>
 int launch_items(const laml_batch& b, const int32_t* items, int64_t n, int kind, int want_post,
                  int respect_status, cudaStream_t st, const int32_t* desc = nullptr) {
     if (n <= 0) return LAML_OK;
-    const int ipb = (kBlock / 32) * (32 / G);
+    // inside / outside below the roots: the staged kernels when the batch
+    // states its largest group and the buffers fit in shared memory
+    if ((kind == 0 || kind == 1) && narrow_level(n) && b.max_states > 0 &&
+        staged_smem(b, kind) <= kStagedSmemMax) {
+        return kind == 0 ? launch_staged<G, 0>(b, desc, n, want_post, respect_status, st)
+                         : launch_staged<G, 1>(b, desc, n, want_post, respect_status, st);
+    }
+    const int ipb = ((kind == 0 || kind == 1) && narrow_level(n)) ? kBlock / 32
+                                                                   : (kBlock / 32) * (32 / G);
     int64_t blocks = (n + ipb - 1) / ipb;
     const int64_t cap = (int64_t)num_sms() * 16;
     if (blocks > cap) blocks = cap;

@@ -180,6 +180,8 @@ class DeviceBatch:
         b.n_in_levels, b.n_out_levels = sizes["n_in_levels"], sizes["n_out_levels"]
         b.n_in_items, b.n_out_items = sizes["n_in_items"], sizes["n_out_items"]
         b.n_root_items = sizes["n_root_items"]
+        # the largest group: sizes the staged kernels' shared-memory row buffers
+        b.max_states = int(max(int(np.max(x.group_C)) for x in datasets))
         for name, _ in N.BATCH_FIELDS:
             if name in v:
                 setattr(b, name, v[name].data_ptr())

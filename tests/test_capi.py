@@ -213,8 +213,9 @@ def test_batch_parser_errors():
 
 def _expected_items(trees, tree_ds, dss, side):
     """The schedule spelled out: per level (inside: node height; outside:
-    depth of the internal parent + 1), groups outermost, then trees in order
-    and nodes ascending."""
+    depth of the internal parent + 1), groups outermost, then the nodes
+    grouped by which children are leaves (bit 0: first child, bit 1: second),
+    and within that trees in order and nodes ascending."""
     levels = {}
     base = 0
     for p, t in enumerate(trees):
@@ -238,12 +239,14 @@ def _expected_items(trees, tree_ds, dss, side):
         ng = dss[tree_ds[p]].n_groups
         for u in range(n, N):
             lv = h[u] if side == "in" else dep[u] + 1
-            levels.setdefault(lv, []).append((base + u, ng))
+            key = (1 if t.child0[u] < n else 0) | (2 if t.child1[u] < n else 0)
+            levels.setdefault(lv, []).append((key, base + u, ng))
         base += N
     out = []
     for lv in sorted(levels):
+        nodes = sorted(levels[lv], key=lambda x: x[0])   # stable: trees, nodes ascending
         for g in range(max(d.n_groups for d in dss)):
-            out += [(node, g) for node, ng in levels[lv] if g < ng]
+            out += [(node, g) for _, node, ng in nodes if g < ng]
     return np.asarray(out, np.int32)
 
 
