@@ -206,6 +206,8 @@ def run_serving(args):
     import numpy as np
     import torch
 
+    import concurrent.futures as cf
+
     from laml_gb300 import serving as S
     from laml_gb300 import synth
 
@@ -225,10 +227,14 @@ def run_serving(args):
             break
         arrivals.append((t, int(rng.integers(len(pool))), "llh" if rng.random() < 0.5 else "em"))
     srv = S.PMMServer(hbm_budget=args.serve_budget << 30)
+    # each client's matrix is encoded once (as a search client scoring many
+    # trees against it would), outside the timed replay
+    dsets = [srv.encode_dataset(w.rows, w.Q, w.leaf_order) for w in pool]
     # warm the kernels and the allocator with one small request of each kind
     for kind in ("llh", "em"):
         w = pool[0]
-        srv.submit(S.Request(w.newicks[0], w.rows, w.Q, w.leaf_order, kind=kind)).result()
+        srv.submit(S.Request(w.newicks[0], w.rows, w.Q, w.leaf_order, kind=kind,
+                             dataset=dsets[0])).result()
     futs = []
     t0 = time.perf_counter()
     with Clocks(0) as clk:
@@ -238,18 +244,29 @@ def run_serving(args):
                 time.sleep(ta - now)
             w = pool[k]
             futs.append((kind, srv.submit(S.Request(w.newicks[0], w.rows, w.Q, w.leaf_order,
-                                                    kind=kind))))
-        replies = [(kind, f.result()) for kind, f in futs]
+                                                    kind=kind, dataset=dsets[k]))))
+        # wait for the replies up to a drain deadline after the last arrival;
+        # the offered EM load can exceed what one GPU completes (each EM
+        # request is tens of iterations over up to 10,000 leaves x 300
+        # sites), so requests still running then are reported, not awaited
+        deadline = time.perf_counter() + args.serve_drain
+        replies, unfinished = [], {"llh": 0, "em": 0}
+        for kind, f in futs:
+            try:
+                replies.append((kind, f.result(timeout=max(0.0, deadline - time.perf_counter()))))
+            except cf.TimeoutError:
+                unfinished[kind] += 1
         t_end = time.perf_counter()
-    srv.close()
+    srv.close(wait=not any(unfinished.values()))
     lat = np.array([r.latency for _, r in replies])
     lat_em = np.array([r.latency for k, r in replies if k == "em"])
     lat_llh = np.array([r.latency for k, r in replies if k == "llh"])
     iters = sum(r.result.iterations for _, r in replies)
     span = t_end - t0
     line = {"metric": METRIC, "mode": "serving", "value": iters / span, "unit": UNIT,
-            "n_gpus": 1, "requests": len(replies), "offered_rate_per_s": rate,
-            "completed_per_s": len(replies) / span,
+            "n_gpus": 1, "requests": len(futs), "completed": len(replies),
+            "unfinished_at_deadline": unfinished, "drain_deadline_s": args.serve_drain,
+            "offered_rate_per_s": rate, "completed_per_s": len(replies) / span,
             "p50_latency_s": float(np.percentile(lat, 50)),
             "p99_latency_s": float(np.percentile(lat, 99)),
             "p50_latency_em_s": float(np.percentile(lat_em, 50)) if len(lat_em) else None,
@@ -261,6 +278,124 @@ def run_serving(args):
                                    "M_k U{5..100}, nu U(0,0.2), phi U(0,0.3); half llh, half EM",
                        "pool": len(pool), "seconds": dur, "hbm_budget_gb": args.serve_budget},
             "clocks": clk.summary()}
+    print(json.dumps(line), flush=True)
+
+
+def _timed(fn, stream, reps):
+    import torch
+    fn()
+    stream.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(reps):
+        fn()
+    e1.record(stream)
+    stream.synchronize()
+    return e0.elapsed_time(e1) / reps
+
+
+def run_workload(args):
+    """The other configurations, one JSON line each (rank 0, one GPU):
+
+    * fixed250: one 250-leaf Yule tree, 30 sites, M_k ~ U{5..30}: negative_llh
+      (one inside pass) and 50 EM iterations; the C restatement timed beside.
+    * grad4096: one 4096-leaf tree, 100 sites, M_k ~ U{10..100}, q ~ Dir(0.3),
+      nu = 0.05, phi = 0.1: forward log-likelihood plus the adjoint gradient
+      in d (8,190 branches), nu, phi through torch.autograd.
+    * large50k: one 50,000-leaf tree, 300 sites, M_k ~ U{20..100},
+      q ~ Dir(0.2), nu = 0.1, phi = 0.2: EM until the relative log-likelihood
+      change is below 1e-8, with the inside and outside passes timed alone
+      for their HBM rooflines."""
+    import numpy as np
+    import torch
+
+    from laml_gb300 import autograd as AG
+    from laml_gb300 import problem as PB
+    from laml_gb300 import synth
+
+    name = args.workload
+    w = synth.workload_config(name, seed=args.seed)
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    stream = torch.cuda.Stream(dev)
+    peak, peak_kind = peaks()
+    nu0, phi0 = {"fixed250": (0.1, 0.15), "grad4096": (0.05, 0.1), "large50k": (0.1, 0.2)}[name]
+    with torch.cuda.stream(stream):
+        b = PB.make_batch(w.newicks, w.rows, w.Q, w.leaf_order, compat=True, group_sites=8,
+                          nu=nu0, phi=phi0, device=dev, stream=stream)
+    ds = b.datasets[0]
+    cfg = {"workload": name, "leaves": b.trees[0].num_leaves, "sites": ds.n_sites,
+           "nodes": b.sizes["n_nodes"], "group_sites": 8,
+           "partial_buffer_gb": 4 * b.sizes["part_floats"] / 1e9}
+    line = {"metric": METRIC, "mode": name, "n_gpus": 1, "dtype": "f32", "data": "synthetic",
+            "config": cfg}
+    pb = pass_bytes(b)
+    with torch.cuda.stream(stream):
+        b.branch_terms()
+        ms_in = _timed(lambda: b.inside(update_em=True), stream, max(3, args.steps))
+        ms_out = _timed(lambda: b.outside(), stream, max(3, args.steps))
+    line["inside_ms"], line["outside_ms"] = ms_in, ms_out
+    line["roofline_inside"] = {"bound": "hbm", "achieved": pb["inside"] / ms_in / 1e6,
+                               "peak": peak, "unit": "GB/s",
+                               "frac": pb["inside"] / ms_in / 1e6 / peak, "peak_kind": peak_kind}
+    line["roofline"] = {"bound": "hbm", "achieved": pb["outside"] / ms_out / 1e6, "peak": peak,
+                        "unit": "GB/s", "frac": pb["outside"] / ms_out / 1e6 / peak,
+                        "peak_kind": peak_kind, "kernel": "outside pass (all levels)"}
+    if name == "fixed250":
+        with torch.cuda.stream(stream):
+            ms_llh = _timed(lambda: b.inside(update_em=False), stream, 20)
+            iters = 50
+
+            def em50():
+                b.set_params(d=np.maximum(b.trees[0].branch_length, 1e-6), nu=[nu0], phi=[phi0])
+                b.branch_terms()
+                b.inside(update_em=True)
+                b.em_iterations(iters, rel_tol=-1.0, max_iters=1 << 30, persistent=False)
+            ms_em = _timed(em50, stream, max(3, args.steps))
+        line.update({"value": iters / (ms_em / 1e3), "unit": "EM iters/s",
+                     "negative_llh_ms": ms_llh, "em50_ms": ms_em,
+                     "negative_llh": -float(b.work["tr_llh"][0].item())})
+        if not args.no_cpu:
+            from oracle import cpu_port
+            t0 = time.perf_counter()
+            cpu_port.em(w.newicks, w.rows, w.Q, w.leaf_order, nu0, phi0, iters=iters)
+            dt = time.perf_counter() - t0
+            line["cpu_baseline"] = {"value": iters / dt, "unit": "EM iters/s", "cores": 1,
+                                    "kind": "port", "sample": "the same tree, 50 EM "
+                                    "iterations, FP64 C restatement, one core"}
+    elif name == "grad4096":
+        d = b.v["nd_d"].clone().requires_grad_(True)
+        nu = b.v["tr_nu"].clone().requires_grad_(True)
+        phi = b.v["tr_phi"].clone().requires_grad_(True)
+
+        def fb():
+            for t in (d, nu, phi):
+                t.grad = None
+            AG.log_likelihood(d, nu, phi, b).sum().backward()
+        with torch.cuda.stream(stream):
+            ms_fb = _timed(fb, stream, max(3, args.steps))
+            ms_f = _timed(lambda: AG.log_likelihood(d, nu, phi, b), stream, max(3, args.steps))
+        line.update({"value": 1e3 / ms_fb, "unit": "forward+adjoint evaluations/s",
+                     "forward_ms": ms_f, "forward_backward_ms": ms_fb,
+                     "grad_norm_d": float(d.grad.norm().item()),
+                     "grad_nu": float(nu.grad[0].item()), "grad_phi": float(phi.grad[0].item())})
+    else:   # large50k: EM to convergence
+        with torch.cuda.stream(stream):
+            t0 = time.perf_counter()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            res = b.run_em(rel_tol=1e-8, max_iters=2000, chunk=8)
+            e1.record(stream)
+            stream.synchronize()
+            wall = time.perf_counter() - t0
+        r = res[0]
+        ms = e0.elapsed_time(e1)
+        line.update({"value": r.iterations / (ms / 1e3), "unit": "EM iters/s",
+                     "em_iterations": r.iterations, "em_seconds": ms / 1e3,
+                     "wall_seconds": wall, "llh": r.llh, "status": r.status,
+                     "node_site_updates_per_s": 2.0 * b.sizes["n_nodes"] * ds.n_sites *
+                     r.iterations / (ms / 1e3)})
+    b.check_device_error()
     print(json.dumps(line), flush=True)
 
 
@@ -284,17 +419,24 @@ def main():
                          "per step; levels: the per-level launches issued directly")
     ap.add_argument("--trees", type=int, default=512,
                     help="use the first N candidates (smaller cases for profiling)")
+    ap.add_argument("--workload", default="nni512",
+                    choices=["nni512", "fixed250", "grad4096", "large50k"],
+                    help="nni512 (the default bench line) or one of the other configurations")
     ap.add_argument("--serving", action="store_true",
                     help="Poisson request stream through the continuous-batching server")
     ap.add_argument("--serve-rate", type=float, default=200.0)
     ap.add_argument("--serve-seconds", type=float, default=5.0)
     ap.add_argument("--serve-pool", type=int, default=16)
     ap.add_argument("--serve-budget", type=int, default=64, help="HBM budget in GiB")
+    ap.add_argument("--serve-drain", type=float, default=60.0,
+                    help="seconds to wait for replies after the last arrival")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
     if args.serving:
         return run_serving(args)
+    if args.workload != "nni512":
+        return run_workload(args)
 
     import numpy as np
     import torch

@@ -231,6 +231,11 @@ typedef struct laml_batch {
      * (cp.async.bulk) one item ahead of the computation; 0 keeps the direct
      * kernels.  A group above it sets LAML_ERR_ARG in the error word. */
     int32_t max_states;
+    /* the largest tree's node count.  The M-step runs trees above 16384 nodes
+     * on a cluster of 8 blocks each (reductions through distributed shared
+     * memory); 0 = unknown, in which case that kernel is launched every
+     * M-step and skips the smaller trees. */
+    int32_t max_tree_nodes;
 } laml_batch;
 
 /* A tree's partials are FP32 values with power-of-two exponents (linear)

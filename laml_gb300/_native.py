@@ -83,7 +83,7 @@ BATCH_FIELDS = [
     ("in_level_off", vp), ("in_items", vp), ("out_level_off", vp), ("out_items", vp),
     ("root_items", vp), ("in_desc", vp), ("out_desc", vp), ("grp_desc", vp),
     ("h_in_level_off", vp), ("h_out_level_off", vp),
-    ("barrier", vp), ("error", vp), ("max_states", i32),
+    ("barrier", vp), ("error", vp), ("max_states", i32), ("max_tree_nodes", i32),
 ]
 
 

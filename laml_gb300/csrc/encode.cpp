@@ -967,11 +967,16 @@ extern "C" int laml_plan_fill(const laml_plan_input* in, laml_plan_output* o) {
     };
     for (int side = 0; side < 2; ++side) {
         parallel_for(NL[side] + 1, [&](int64_t a, int64_t e) {
-            for (int64_t l = a; l < e; ++l) {
+            std::vector<int32_t> tmp;
+            for (int64_t l = a; l < e; ++l) {   // a counting sort on the 4 keys
                 int32_t* first = lnodes[side].data() + lstart[side][l];
-                int32_t* last = lnodes[side].data() + lstart[side][l + 1];
-                std::stable_sort(first, last,
-                                 [&](int32_t x, int32_t y) { return leaf_key(x) < leaf_key(y); });
+                const int64_t cnt = lstart[side][l + 1] - lstart[side][l];
+                int64_t at[5] = {0, 0, 0, 0, 0};
+                for (int64_t x = 0; x < cnt; ++x) ++at[leaf_key(first[x]) + 1];
+                for (int k = 1; k < 5; ++k) at[k] += at[k - 1];
+                tmp.resize((size_t)cnt);
+                for (int64_t x = 0; x < cnt; ++x) tmp[at[leaf_key(first[x])]++] = first[x];
+                std::copy(tmp.begin(), tmp.end(), first);
             }
         }, 2);
     }

@@ -26,6 +26,7 @@
 //   out_v[s] = Psil (x0 + sum_a x_a) + x_s,  x = out_parent * E_sibling
 // with P00 = e^{-d(1+nu)}, Pmut = (1-e^{-d}) e^{-nu d}, Pstay = e^{-nu d},
 // Psil = 1-e^{-nu d}.
+#include <cooperative_groups.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -1215,6 +1216,20 @@ __device__ __forceinline__ float2 block_sum2f(float a, float c, double2* shd) {
     return r;
 }
 
+// block-wide max of an int
+__device__ __forceinline__ int block_maxi(int x, double2* shd) {
+    int* sh = reinterpret_cast<int*>(shd);
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) x = max(x, __shfl_xor_sync(kFull, x, off));
+    const int wid = threadIdx.x >> 5, ln = threadIdx.x & 31;
+    __syncthreads();
+    if (ln == 0) sh[wid] = x;
+    __syncthreads();
+    int r = sh[0];
+    for (int k = 1; k < (int)(blockDim.x >> 5); ++k) r = max(r, sh[k]);
+    return r;
+}
+
 __device__ float4 branch_terms_of(double d, double nu, int compat) {
     // FP32 is the storage precision of the terms: compute them in FP32
     const float df = (float)d, nf = (float)nu, nd = df * nf;
@@ -1327,7 +1342,70 @@ __device__ double solve_branch(double a, double bb, double c, double nu, double 
 // memory (global scratch for trees above kMstepStage nodes); the final round
 // polishes d and nu with FP64 Newton steps on the FP64 counts.
 // ---------------------------------------------------------------------------
-__device__ void mstep_tree(const laml_batch& b, int p, int rounds, double2* sh, float4* s_cnt,
+// The thread teams an M-step runs on: one block (trees up to kClusterNodes
+// nodes), or a cluster of kMstepCluster blocks of 1024 threads whose
+// reductions go through distributed shared memory (larger trees).  Either
+// way every thread owns the branches v = tid, tid + size, ... in every phase,
+// so the only data threads exchange are the reductions, which are summed in
+// a fixed order (warp, then block, then cluster rank).
+struct BlockTeam {
+    double2* sh;
+    __device__ int tid() const { return threadIdx.x; }
+    __device__ int size() const { return blockDim.x; }
+    __device__ bool leader() const { return threadIdx.x == 0; }
+    __device__ void sync() const { __syncthreads(); }
+    __device__ float2 sum2f(float a, float c) const { return block_sum2f(a, c, sh); }
+    __device__ double2 sum2(double a, double c) const { return block_sum2(a, c, sh); }
+    __device__ int maxi(int x) const { return block_maxi(x, sh); }
+};
+
+constexpr int kMstepCluster = 8;        // blocks per cluster (the portable size)
+constexpr int kMstepClusterThreads = 1024;
+constexpr int kClusterNodes = 16384;    // trees above this many nodes take a cluster
+
+struct ClusterTeam {
+    double2* sh;      // this block's warp partials
+    double2* part;    // [kMstepCluster] block partials, read from the rank-0 block
+    __device__ int rank() const { return (int)cooperative_groups::this_cluster().block_rank(); }
+    __device__ int tid() const { return rank() * (int)blockDim.x + (int)threadIdx.x; }
+    __device__ int size() const { return kMstepCluster * (int)blockDim.x; }
+    __device__ bool leader() const { return threadIdx.x == 0 && rank() == 0; }
+    __device__ void sync() const { cooperative_groups::this_cluster().sync(); }
+    __device__ double2 gather(double2 mine) const {
+        auto cl = cooperative_groups::this_cluster();
+        double2* p0 = cl.map_shared_rank(part, 0);
+        if (threadIdx.x == 0) p0[cl.block_rank()] = mine;
+        cl.sync();
+        double2 r = make_double2(0.0, 0.0);
+        for (int k = 0; k < kMstepCluster; ++k) {
+            const double2 x = p0[k];
+            r.x += x.x;
+            r.y += x.y;
+        }
+        cl.sync();   // every rank has read before the slots are written again
+        return r;
+    }
+    __device__ float2 sum2f(float a, float c) const {
+        const float2 m = block_sum2f(a, c, sh);
+        const double2 r = gather(make_double2((double)m.x, (double)m.y));
+        return make_float2((float)r.x, (float)r.y);
+    }
+    __device__ double2 sum2(double a, double c) const { return gather(block_sum2(a, c, sh)); }
+    __device__ int maxi(int x) const {
+        auto cl = cooperative_groups::this_cluster();
+        const int m = block_maxi(x, sh);
+        double2* p0 = cl.map_shared_rank(part, 0);
+        if (threadIdx.x == 0) p0[cl.block_rank()] = make_double2((double)m, 0.0);
+        cl.sync();
+        int r = 0;
+        for (int k = 0; k < kMstepCluster; ++k) r = max(r, (int)p0[k].x);
+        cl.sync();
+        return r;
+    }
+};
+
+template <class Team>
+__device__ void mstep_tree(const laml_batch& b, int p, int rounds, Team& T, float4* s_cnt,
                            float* s_d, bool polish) {
     if (__ldcg(b.tr_status + p) != LAML_TREE_ACTIVE) return;
     const int N = __ldg(b.tr_nodes + p), n = __ldg(b.tr_leaves + p), base = __ldg(b.tr_node_base + p);
@@ -1346,7 +1424,7 @@ __device__ void mstep_tree(const laml_batch& b, int p, int rounds, double2* sh, 
     //    the exact model), d saved
     // (FP32 accumulation: the FP64 pipe of this part is narrow)
     float lr = 0.f, lro = 0.f;
-    for (int v = threadIdx.x; v < N; v += blockDim.x) {
+    for (int v = T.tid(); v < N; v += T.size()) {
         float c[8] = {0, 0, 0, 0, 0, 0, 0, 0};
         const float4* src = reinterpret_cast<const float4*>(b.cnt_part + cb + (int64_t)v * NG * 8);
         for (int g = 0; g < NG; ++g) {
@@ -1377,10 +1455,10 @@ __device__ void mstep_tree(const laml_batch& b, int p, int rounds, double2* sh, 
         lr += c[6];
         lro += c[7];
     }
-    const float2 LRf = block_sum2f(lr, lro, sh);   // also orders the staging writes
+    const float2 LRf = T.sum2f(lr, lro);   // also orders the staging writes
     const double2 LRs = make_double2((double)LRf.x, (double)LRf.y);
     const double LR = LRs.x + LRs.y;
-    if (threadIdx.x == 0) {
+    if (T.leader()) {
         b.tr_prev[2 * p] = nu;
         b.tr_prev[2 * p + 1] = phi;
     }
@@ -1409,7 +1487,7 @@ __device__ void mstep_tree(const laml_batch& b, int p, int rounds, double2* sh, 
         const bool use_s = compat || nu > kEpsNu;
         const float nuf = (float)nu;
         if (last && polish) {
-            for (int v = threadIdx.x; v < N; v += blockDim.x) {
+            for (int v = T.tid(); v < N; v += T.size()) {
                 if (!__ldg(b.nd_mask + base + v)) continue;
                 // the FP64 counts for the polished solve
                 const double* c = b.nd_cnt + (int64_t)(base + v) * 6;
@@ -1422,7 +1500,7 @@ __device__ void mstep_tree(const laml_batch& b, int p, int rounds, double2* sh, 
                 __stcg(b.nd_d + base + v, dn);
             }
         } else {
-            for (int v = threadIdx.x; v < N; v += blockDim.x) {
+            for (int v = T.tid(); v < N; v += T.size()) {
                 if (!__ldg(b.nd_mask + base + v)) continue;
                 const float4 q = C4[v];
                 const float dn = solve_branch_f(q.x + nuf * q.y, q.z, use_s ? q.w : 0.f, nuf,
@@ -1431,18 +1509,18 @@ __device__ void mstep_tree(const laml_batch& b, int p, int rounds, double2* sh, 
                 if (last) __stcg(b.nd_d + base + v, (double)dn);
             }
         }
-        __syncthreads();
+        T.sync();
         if (!(fix & 1)) {
             // -A nu + sum_v c_v log(1 - e^{-nu d_v}); compat: every branch,
             // exact: the optimised branches (EM_solver.py:392-407)
             float Af = 0.f, Csf = 0.f;
-            for (int v = threadIdx.x; v < N; v += blockDim.x) {
+            for (int v = T.tid(); v < N; v += T.size()) {
                 if (!compat && !__ldg(b.nd_mask + base + v)) continue;
                 const float4 q = C4[v];
                 Af += q.y * Dd[v];
                 Csf += q.w;
             }
-            const float2 acf = block_sum2f(Af, Csf, sh);
+            const float2 acf = T.sum2f(Af, Csf);
             const double2 ac = make_double2((double)acf.x, (double)acf.y);
             double A = ac.x;
             const double nlo = compat ? kCalcEps : 1e-30, nhi = compat ? 1.0 - kCalcEps : 1.0;
@@ -1451,7 +1529,7 @@ __device__ void mstep_tree(const laml_batch& b, int p, int rounds, double2* sh, 
             auto sums = [&](double x, bool fp64) {
                 if (fp64) {
                     double s1 = 0.0, s2 = 0.0;
-                    for (int v = threadIdx.x; v < N; v += blockDim.x) {
+                    for (int v = T.tid(); v < N; v += T.size()) {
                         if (!compat && !__ldg(b.nd_mask + base + v)) continue;
                         const double* c = b.nd_cnt + (int64_t)(base + v) * 6;
                         const double cc = __ldcg(c + 2) + __ldcg(c + 4);
@@ -1460,11 +1538,11 @@ __device__ void mstep_tree(const laml_batch& b, int p, int rounds, double2* sh, 
                         s1 += cc * h;
                         s2 += cc * h * (h + y);
                     }
-                    return block_sum2(s1, s2, sh);
+                    return T.sum2(s1, s2);
                 }
                 float s1 = 0.f, s2 = 0.f;
                 const float xf = (float)x;
-                for (int v = threadIdx.x; v < N; v += blockDim.x) {
+                for (int v = T.tid(); v < N; v += T.size()) {
                     if (!compat && !__ldg(b.nd_mask + base + v)) continue;
                     const float cc = C4[v].w;
                     if (cc <= 0.f) continue;
@@ -1472,7 +1550,7 @@ __device__ void mstep_tree(const laml_batch& b, int p, int rounds, double2* sh, 
                     s1 += cc * h;
                     s2 += cc * h * (h + y);
                 }
-                const float2 r = block_sum2f(s1, s2, sh);
+                const float2 r = T.sum2f(s1, s2);
                 return make_double2((double)r.x, (double)r.y);
             };
             if (ac.y <= 0.0) {
@@ -1493,12 +1571,12 @@ __device__ void mstep_tree(const laml_batch& b, int p, int rounds, double2* sh, 
                 double wd = (double)w;
                 if (last && polish) {   // FP64 Newton polish
                     double A64 = 0.0;
-                    for (int v = threadIdx.x; v < N; v += blockDim.x) {
+                    for (int v = T.tid(); v < N; v += T.size()) {
                         if (!compat && !__ldg(b.nd_mask + base + v)) continue;
                         const double* c = b.nd_cnt + (int64_t)(base + v) * 6;
                         A64 += (__ldcg(c) + __ldcg(c + 1) + __ldcg(c + 3)) * __ldcg(b.nd_d + base + v);
                     }
-                    A64 = block_sum2(A64, 0.0, sh).x;
+                    A64 = T.sum2(A64, 0.0).x;
                     for (int it = 0; it < 2; ++it) {
                         const double x = exp(wd);
                         const double2 S = sums(x, true);
@@ -1510,28 +1588,24 @@ __device__ void mstep_tree(const laml_batch& b, int p, int rounds, double2* sh, 
                 nu = fmin(fmax(polish ? exp(wd) : (double)expf(w), nlo), nhi);
             }
         }
-        __syncthreads();
+        T.sync();
     }
-    if (threadIdx.x == 0) {
+    if (T.leader()) {
         b.tr_nu[p] = nu;
         b.tr_phi[p] = phi;
     }
     // the arithmetic of the next passes: log mode once a branch's
     // d (1 + nu) leaves the range of the linear partials
-    __shared__ int s_rate;
-    if (threadIdx.x == 0) s_rate = 0;
-    __syncthreads();
     int rate = 0;
-    for (int v = threadIdx.x; v < N; v += blockDim.x) {
+    for (int v = T.tid(); v < N; v += T.size()) {
         reinterpret_cast<float4*>(b.nd_bt)[base + v] = branch_terms_of((double)Dd[v], nu, b.compat);
         rate = max(rate, __float_as_int(fmaxf(Dd[v] * (1.f + (float)nu), 0.f)));
     }
-    atomicMax(&s_rate, rate);
-    __syncthreads();
-    if (threadIdx.x == 0)
-        b.tr_mode[p] = __int_as_float(s_rate) > (float)LAML_LOG_MODE_RATE ? LAML_MODE_LOG
-                                                                           : LAML_MODE_LINEAR;
-    __syncthreads();
+    rate = T.maxi(rate);
+    if (T.leader())
+        b.tr_mode[p] = __int_as_float(rate) > (float)LAML_LOG_MODE_RATE ? LAML_MODE_LOG
+                                                                        : LAML_MODE_LINEAR;
+    T.sync();
 }
 
 // per-tree log-likelihood (FP64 sum over sites) and the EM stopping rule
@@ -2156,12 +2230,32 @@ __global__ void __launch_bounds__(kBlock, KIND == 1 ? LAML_MINB_OUT : LAML_MINB)
     for_items<G, KIND>(b, items, n, gwarp, nwarps, want_post != 0, respect_status != 0, desc);
 }
 
-__global__ void __launch_bounds__(kBlock, 4) k_mstep(laml_batch b, int rounds, int flags) {
+// M-step, one block per tree; with skip_big the trees above kClusterNodes
+// nodes are left to k_mstep_cluster
+__global__ void __launch_bounds__(kBlock, 4) k_mstep(laml_batch b, int rounds, int flags,
+                                                    int skip_big) {
     __shared__ double2 sh[kBlock / 32];
     __shared__ float4 s_cnt[kMstepStage];
     __shared__ float s_d[kMstepStage];
-    for (int p = blockIdx.x; p < b.n_trees; p += gridDim.x)
-        mstep_tree(b, p, rounds, sh, s_cnt, s_d, (flags & LAML_MSTEP_FP64_POLISH) != 0);
+    BlockTeam T{sh};
+    for (int p = blockIdx.x; p < b.n_trees; p += gridDim.x) {
+        if (skip_big && __ldg(b.tr_nodes + p) > kClusterNodes) continue;
+        mstep_tree(b, p, rounds, T, s_cnt, s_d, (flags & LAML_MSTEP_FP64_POLISH) != 0);
+    }
+}
+
+// M-step of the trees above kClusterNodes nodes, one cluster of
+// kMstepCluster blocks per tree
+__global__ void __cluster_dims__(kMstepCluster, 1, 1) __launch_bounds__(kMstepClusterThreads, 1)
+    k_mstep_cluster(laml_batch b, int rounds, int flags) {
+    __shared__ double2 sh[kMstepClusterThreads / 32];
+    __shared__ double2 part[kMstepCluster];
+    ClusterTeam T{sh, part};
+    const int ncl = gridDim.x / kMstepCluster;
+    for (int p = blockIdx.x / kMstepCluster; p < b.n_trees; p += ncl) {
+        if (__ldg(b.tr_nodes + p) <= kClusterNodes) continue;   // uniform over the cluster
+        mstep_tree(b, p, rounds, T, nullptr, nullptr, (flags & LAML_MSTEP_FP64_POLISH) != 0);
+    }
 }
 
 // d logL / d(d_v, nu, phi) from the expected counts (Fisher's identity: the
@@ -2284,6 +2378,7 @@ __global__ void __launch_bounds__(kBlock, LAML_MINB) k_em_persistent(laml_batch 
     __shared__ double2 sh[kBlock / 32];
     __shared__ float4 s_cnt[kMstepStage];
     __shared__ float s_d[kMstepStage];
+    BlockTeam T{sh};   // one block per tree here, whatever its size
     const int gwarp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int nwarps = (gridDim.x * blockDim.x) >> 5;
     unsigned gen = 0;
@@ -2303,7 +2398,7 @@ __global__ void __launch_bounds__(kBlock, LAML_MINB) k_em_persistent(laml_batch 
         for_items<G, 3>(b, b.root_items, b.n_root_items, gwarp, nwarps, false, true);
         if (!grid_barrier(b, gen)) return;
         for (int p = blockIdx.x; p < b.n_trees; p += gridDim.x)
-            mstep_tree(b, p, rounds, sh, s_cnt, s_d, (flags & LAML_MSTEP_FP64_POLISH) != 0);
+            mstep_tree(b, p, rounds, T, s_cnt, s_d, (flags & LAML_MSTEP_FP64_POLISH) != 0);
         if (!grid_barrier(b, gen)) return;
         for (int l = 0; l < b.n_in_levels; ++l) {
             const int64_t o = b.in_level_off[l], e = b.in_level_off[l + 1];
@@ -2476,6 +2571,18 @@ int outside_t(const laml_batch& b, int flags, cudaStream_t st, const Levels& L) 
                            (flags & LAML_OUT_TRUE_ROOT) ? 4 : 3, 0, 1, st);
 }
 
+// the M-step launches: every tree up to kClusterNodes nodes in k_mstep, the
+// larger ones (when the batch may hold any) in k_mstep_cluster
+int launch_mstep(const laml_batch& b, int rounds, int flags, cudaStream_t st) {
+    const bool big = b.max_tree_nodes <= 0 || b.max_tree_nodes > kClusterNodes;
+    k_mstep<<<b.n_trees, kBlock, 0, st>>>(b, rounds, flags, big ? 1 : 0);
+    int rc = check(cudaGetLastError(), "k_mstep");
+    if (rc || !big) return rc;
+    const int clusters = std::max(1, std::min(b.n_trees, num_sms() / kMstepCluster));
+    k_mstep_cluster<<<clusters * kMstepCluster, kMstepClusterThreads, 0, st>>>(b, rounds, flags);
+    return check(cudaGetLastError(), "k_mstep_cluster");
+}
+
 template <int G>
 int em_levels_t(const laml_batch& b, int iters, int rounds, double tol, int max_iters,
                 int flags, cudaStream_t st) {
@@ -2485,8 +2592,7 @@ int em_levels_t(const laml_batch& b, int iters, int rounds, double tol, int max_
     const int tb = (b.n_trees + 127) / 128;
     for (int it = 0; it < iters; ++it) {
         if ((rc = outside_t<G>(b, 0, st, L))) return rc;
-        k_mstep<<<b.n_trees, kBlock, 0, st>>>(b, rounds, flags);
-        if ((rc = check(cudaGetLastError(), "k_mstep"))) return rc;
+        if ((rc = launch_mstep(b, rounds, flags, st))) return rc;
         if ((rc = inside_t<G>(b, 0, st, L, 1))) return rc;
         k_tree_llh<<<tb, 128, 0, st>>>(b, 2, tol, max_iters);
         if ((rc = check(cudaGetLastError(), "k_tree_llh"))) return rc;
@@ -2610,8 +2716,7 @@ extern "C" int laml_outside(const laml_batch* b, int32_t flags, void* stream) {
 extern "C" int laml_mstep(const laml_batch* b, int32_t rounds, int32_t flags, void* stream) {
     int rc = validate(b);
     if (rc) return rc;
-    k_mstep<<<b->n_trees, kBlock, 0, (cudaStream_t)stream>>>(*b, rounds, flags);
-    return check(cudaGetLastError(), "k_mstep");
+    return launch_mstep(*b, rounds, flags, (cudaStream_t)stream);
 }
 
 extern "C" int laml_em_run(const laml_batch* b, int32_t iters, int32_t rounds, double rel_tol,

@@ -182,6 +182,8 @@ class DeviceBatch:
         b.n_root_items = sizes["n_root_items"]
         # the largest group: sizes the staged kernels' shared-memory row buffers
         b.max_states = int(max(int(np.max(x.group_C)) for x in datasets))
+        # the largest tree: whether the M-step needs its cluster kernel
+        b.max_tree_nodes = int(max(t.num_nodes for t in trees))
         for name, _ in N.BATCH_FIELDS:
             if name in v:
                 setattr(b, name, v[name].data_ptr())

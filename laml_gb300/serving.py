@@ -45,6 +45,10 @@ class Request:
     kind: str = "em"              # "llh" or "em"
     nu: float = 0.5
     phi: float = 0.5
+    # the matrix already encoded (PMMServer.encode_dataset): a client that
+    # scores many trees against one matrix -- topology-search candidates --
+    # encodes it once instead of with every request
+    dataset: Optional[EncodedDataset] = None
 
 
 @dataclass
@@ -109,6 +113,7 @@ class PMMServer:
         self._active: List[_Cohort] = []
         self._used = 0
         self._closing = False
+        self._abort = False
         self._streams = [torch.cuda.Stream(self.device) for _ in range(max_cohorts)]
         self._free_streams = list(self._streams)
         self.error: Optional[BaseException] = None
@@ -116,13 +121,24 @@ class PMMServer:
         self._thread.start()
 
     # -- client side ------------------------------------------------------
+    def encode_dataset(self, rows: Dict[str, list], Q: List[dict],
+                       leaf_order: List[str]) -> EncodedDataset:
+        """The site layout of a matrix, for Request.dataset."""
+        return encode_dataset(char_matrix([rows[c] for c in leaf_order]), Q, compat=True,
+                              group_sites=self.G)
+
     def submit(self, req: Request) -> Future:
         t0 = time.perf_counter()
         lo = req.leaf_order
         tree = encode_newick(req.newick, lo)
-        order = lo if lo is not None else tree.labels[:tree.num_leaves]
-        ds = encode_dataset(char_matrix([req.rows[c] for c in order]), req.Q, compat=True,
-                            group_sites=self.G)
+        if req.dataset is not None:
+            if req.dataset.group_sites != self.G or req.dataset.n_leaves != tree.num_leaves:
+                raise ValueError("Request.dataset does not match the server or the tree")
+            ds = req.dataset
+        else:
+            order = lo if lo is not None else tree.labels[:tree.num_leaves]
+            ds = encode_dataset(char_matrix([req.rows[c] for c in order]), req.Q, compat=True,
+                                group_sites=self.G)
         fp = footprint_bytes(tree, ds)
         if fp > self.budget:
             raise ValueError(f"request needs {fp} bytes of HBM, the budget is {self.budget}")
@@ -133,10 +149,14 @@ class PMMServer:
         return fut
 
     def close(self, wait: bool = True):
+        """Stop the server.  wait=True: finish every submitted request first;
+        wait=False: launch no further work and fail the requests not yet
+        answered (work already queued on the GPU finishes on its own)."""
         self._closing = True
+        if not wait:
+            self._abort = True
         self._wake.set()
-        if wait:
-            self._thread.join()
+        self._thread.join()
         if self.error is not None:
             raise self.error
 
@@ -153,7 +173,16 @@ class PMMServer:
             with self._lock:
                 if not self._pending:
                     return
-                kind = self._pending[0].req.kind
+                # log-likelihood requests (one inside pass) go first; EM
+                # cohorts -- dozens of iterations each -- leave one stream
+                # free for them, so a burst of EM work cannot starve them
+                kinds = {j.req.kind for j in self._pending}
+                if "llh" in kinds:
+                    kind = "llh"
+                elif len(self._free_streams) > 1 or self.max_cohorts == 1:
+                    kind = "em"
+                else:
+                    return
                 jobs, used = [], 0
                 rest = collections.deque()
                 while self._pending and len(jobs) < self.max_cohort:
@@ -181,8 +210,13 @@ class PMMServer:
             nu = np.clip([j.req.nu for j in jobs], EPS, 1 - EPS)
             phi = np.clip([j.req.phi for j in jobs], EPS, 1 - EPS)
             d = [np.maximum(j.tree.branch_length, EPS) for j in jobs]
-            b = DeviceBatch([j.ds for j in jobs], [j.tree for j in jobs], list(range(len(jobs))),
-                            d, nu, phi, compat=True, device=self.device, stream=stream)
+            # one copy of each distinct encoded matrix in the cohort
+            uniq, tree_ds = {}, []
+            for j in jobs:
+                tree_ds.append(uniq.setdefault(id(j.ds), (len(uniq), j.ds))[0])
+            dsets = [x for _, x in sorted(uniq.values(), key=lambda t: t[0])]
+            b = DeviceBatch(dsets, [j.tree for j in jobs], tree_ds, d, nu, phi, compat=True,
+                            device=self.device, stream=stream)
             b.branch_terms()
             b.inside(update_em=True)
             if kind == "em":
@@ -230,6 +264,17 @@ class PMMServer:
     def _run(self):
         try:
             while True:
+                if self._abort:
+                    gone = RuntimeError("server closed before the request finished")
+                    with self._lock:
+                        for j in self._pending:
+                            j.future.set_exception(gone)
+                        self._pending.clear()
+                    for c in self._active:
+                        for j in c.jobs:
+                            if not j.future.done():
+                                j.future.set_exception(gone)
+                    return
                 self._admit()
                 finished = [c for c in self._active if self._progress(c)]
                 for c in finished:

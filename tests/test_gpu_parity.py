@@ -212,6 +212,25 @@ def test_em_large_tree_uses_global_mstep_staging():
     assert r.llh == pytest.approx(ref.llh, rel=1e-6)
 
 
+def test_em_tree_above_cluster_threshold():
+    """A tree above 16384 nodes: its M-step runs on a cluster of 8 blocks with
+    the reductions through distributed shared memory; EM against the C
+    restatement, and two copies of the tree in one batch."""
+    from oracle import cpu_port
+    w = synth.pmm_workload(8400, 6, 3, 8, 0.5, 0.1, 0.15, seed=32)
+    b = PB.make_batch(w.newicks, w.rows, w.Q, w.leaf_order, compat=True)
+    assert b.trees[0].num_nodes > 16384
+    r = b.run_em(max_iters=3, rel_tol=-1.0, chunk=1)[0]
+    llh, nu, phi, ds, _ = cpu_port.em(w.newicks, w.rows, w.Q, w.leaf_order, 0.5, 0.5, iters=3)
+    assert r.llh == pytest.approx(llh[0], rel=1e-6)
+    assert r.nu == pytest.approx(nu[0], rel=1e-3)
+    assert r.phi == pytest.approx(phi[0], rel=1e-3)
+    # two copies in one batch (two clusters at once): each result is the tree's own
+    b2 = PB.make_batch(w.newicks + w.newicks, w.rows, w.Q, w.leaf_order, compat=True)
+    r2 = b2.run_em(max_iters=3, rel_tol=-1.0, chunk=1)
+    assert r2[0].llh == r.llh and r2[1].llh == r.llh
+
+
 def test_device_descriptors_equal_host_plan():
     """laml_plan_descriptors on the device writes laml_plan_fill's bytes."""
     from laml_gb300.encoding import plan_batch
