@@ -38,6 +38,11 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "EM iters/s & node-site updates/s, batched+served vs plain GPU; p50/p99 latency"
+# DRAM bytes per launch of the outside and inside passes of the 512-candidate
+# batch (G = 8): ncu dram__bytes_read.sum + dram__bytes_write.sum summed over
+# one pass of the first 128 candidates (`--passes-only --trees 128`), times 4
+# -- the full batch holds 4x the same-shaped rows -- over the pass's launches
+TRAFFIC_PER_LAUNCH = {"outside": 185.1e6, "inside": 134.6e6}
 UNIT = "tree-EM-iters/s"
 WORKLOAD = "nni512"
 
@@ -257,13 +262,17 @@ def run_serving(args):
             except cf.TimeoutError:
                 unfinished[kind] += 1
         t_end = time.perf_counter()
+        launched = srv.em_tree_iterations
     srv.close(wait=not any(unfinished.values()))
-    lat = np.array([r.latency for _, r in replies])
+    lat = np.array([r.latency for _, r in replies]) if replies else np.zeros(1)
     lat_em = np.array([r.latency for k, r in replies if k == "em"])
     lat_llh = np.array([r.latency for k, r in replies if k == "llh"])
     iters = sum(r.result.iterations for _, r in replies)
     span = t_end - t0
-    line = {"metric": METRIC, "mode": "serving", "value": iters / span, "unit": UNIT,
+    # value: tree-EM-iterations the server queued by the end of the window
+    # (finished requests and those still iterating)
+    line = {"metric": METRIC, "mode": "serving", "value": launched / span, "unit": UNIT,
+            "em_iterations_of_completed_requests": iters,
             "n_gpus": 1, "requests": len(futs), "completed": len(replies),
             "unfinished_at_deadline": unfinished, "drain_deadline_s": args.serve_drain,
             "offered_rate_per_s": rate, "completed_per_s": len(replies) / span,
@@ -279,6 +288,26 @@ def run_serving(args):
                        "pool": len(pool), "seconds": dur, "hbm_budget_gb": args.serve_budget},
             "clocks": clk.summary()}
     print(json.dumps(line), flush=True)
+
+
+def run_passes_only(args):
+    """One inside and one outside pass of the first --trees candidates, no
+    timing: the command the kernel profiles are captured on."""
+    import torch
+
+    from laml_gb300 import problem as PB
+    from laml_gb300 import synth
+    w = synth.workload_config(WORKLOAD, seed=args.seed)
+    w.newicks = w.newicks[:args.trees]
+    b = PB.make_batch(w.newicks, w.rows, w.Q, w.leaf_order, compat=True,
+                      group_sites=args.group_sites or 8, nu=0.5, phi=0.5)
+    b.branch_terms()
+    b.inside(update_em=True)
+    b.outside()
+    torch.cuda.synchronize()
+    b.check_device_error()
+    print(json.dumps({"passes_only": True, "trees": b.T, "n_in_levels": b.sizes["n_in_levels"],
+                      "n_out_levels": b.sizes["n_out_levels"]}), flush=True)
 
 
 def _timed(fn, stream, reps):
@@ -422,6 +451,8 @@ def main():
     ap.add_argument("--workload", default="nni512",
                     choices=["nni512", "fixed250", "grad4096", "large50k"],
                     help="nni512 (the default bench line) or one of the other configurations")
+    ap.add_argument("--passes-only", action="store_true",
+                    help="one inside and one outside pass of --trees candidates (profiling)")
     ap.add_argument("--serving", action="store_true",
                     help="Poisson request stream through the continuous-batching server")
     ap.add_argument("--serve-rate", type=float, default=200.0)
@@ -437,6 +468,8 @@ def main():
         return run_serving(args)
     if args.workload != "nni512":
         return run_workload(args)
+    if args.passes_only:
+        return run_passes_only(args)
 
     import numpy as np
     import torch
@@ -532,6 +565,9 @@ def main():
                     "of internal parents, both children per item)", n_out + 2)
     roof_in = roof(pb["inside"], ms_in / 1e3, "k_items inside levels (one launch per height)",
                    n_in + 1)
+    if T == 512 and G == 8:
+        roof_out["traffic"] = TRAFFIC_PER_LAUNCH["outside"]
+        roof_in["traffic"] = TRAFFIC_PER_LAUNCH["inside"]
     roof_it = roof(pb["em_iteration"], avg_launch_s,
                    {"graph": "EM-iteration graph (k_items per level, k_mstep)",
                     "persistent": "k_em_persistent",

@@ -236,6 +236,11 @@ typedef struct laml_batch {
      * memory); 0 = unknown, in which case that kernel is launched every
      * M-step and skips the smaller trees. */
     int32_t max_tree_nodes;
+    /* [2T] FP32 leaf emission terms of each tree's phi (max(1-phi, eps),
+     * max(phi, eps) in compat; 1-phi, phi in exact), kept by
+     * laml_branch_terms and the M-step; NULL = derived from tr_phi wherever
+     * needed */
+    float* tr_leaf;
 } laml_batch;
 
 /* A tree's partials are FP32 values with power-of-two exponents (linear)

@@ -84,6 +84,7 @@ BATCH_FIELDS = [
     ("root_items", vp), ("in_desc", vp), ("out_desc", vp), ("grp_desc", vp),
     ("h_in_level_off", vp), ("h_out_level_off", vp),
     ("barrier", vp), ("error", vp), ("max_states", i32), ("max_tree_nodes", i32),
+    ("tr_leaf", vp),
 ]
 
 

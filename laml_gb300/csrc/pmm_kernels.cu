@@ -91,9 +91,23 @@ struct Leaf {
     float e1, ephi, es;   // max(1-phi, eps), max(phi, eps), eps
 };
 
+// the leaf emission terms of a tree's phi (FP32 pair in tr_leaf when the
+// batch keeps one: GB300's FP64 pipe is narrow, and every item reads them)
+__device__ __forceinline__ float2 leaf_pair(double phi, int compat) {
+    return compat ? make_float2(fmaxf((float)(1.0 - phi), kEPS), fmaxf((float)phi, kEPS))
+                  : make_float2((float)(1.0 - phi), (float)phi);
+}
+
 __device__ __forceinline__ Leaf leaf_params(const laml_batch& b, int tree) {
-    double phi = __ldcg(b.tr_phi + tree);
     Leaf L;
+    if (b.tr_leaf) {
+        const float2 e = __ldcg(reinterpret_cast<const float2*>(b.tr_leaf) + tree);
+        L.e1 = e.x;
+        L.ephi = e.y;
+        L.es = b.compat ? kEPS : 0.f;
+        return L;
+    }
+    double phi = __ldcg(b.tr_phi + tree);
     if (b.compat) {
         L.e1 = fmaxf((float)(1.0 - phi), kEPS);
         L.ephi = fmaxf((float)phi, kEPS);
@@ -1593,6 +1607,7 @@ __device__ void mstep_tree(const laml_batch& b, int p, int rounds, Team& T, floa
     if (T.leader()) {
         b.tr_nu[p] = nu;
         b.tr_phi[p] = phi;
+        if (b.tr_leaf) reinterpret_cast<float2*>(b.tr_leaf)[p] = leaf_pair(phi, b.compat);
     }
     // the arithmetic of the next passes: log mode once a branch's
     // d (1 + nu) leaves the range of the linear partials
@@ -2334,6 +2349,8 @@ __global__ void k_branch_terms(laml_batch b) {
         const int p = b.nd_tree[i];
         reinterpret_cast<float4*>(b.nd_bt)[i] = branch_terms_of(b.nd_d[i], b.tr_nu[p], b.compat);
     }
+    if (b.tr_leaf && i < b.n_trees)
+        reinterpret_cast<float2*>(b.tr_leaf)[i] = leaf_pair(b.tr_phi[i], b.compat);
 }
 
 // Item descriptors from the node arrays already on the device: the same 12

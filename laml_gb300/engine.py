@@ -155,6 +155,7 @@ class DeviceBatch:
             "tr_iter": torch.zeros(T, dtype=i32, device=dev),
             "tr_status": torch.zeros(T, dtype=i32, device=dev),
             "tr_mode": torch.zeros(T, dtype=i32, device=dev),
+            "tr_leaf": e(2 * T, f32),
             "nd_d_prev": e(nn, f64), "nd_bt": e(4 * nn, f32), "nd_cnt": e(6 * nn, f64),
             "nd_stage": e(5 * nn, f32),
             "in_part": e(sizes["part_floats"], f32), "out_part": e(sizes["part_floats"], f32),

@@ -97,12 +97,15 @@ def footprint_bytes(tree: EncodedTree, ds: EncodedDataset) -> int:
 
 class PMMServer:
     def __init__(self, device="cuda", hbm_budget: int = 64 << 30, max_cohort: int = 256,
-                 max_cohorts: int = 4, group_sites: int = 8, rounds: int = MSTEP_ROUNDS,
-                 chunk: int = 2, max_iters: int = 100000):
+                 max_cohorts: int = 6, group_sites: int = 8, rounds: int = MSTEP_ROUNDS,
+                 chunk: int = 2, max_iters: int = 100000, max_em_cohort: int = 64):
         self.device = torch.device(device)
         self.budget = hbm_budget
         self.max_cohort = max_cohort
+        self.max_em_cohort = max_em_cohort   # EM cohorts smaller: a slow tree holds its cohort
         self.max_cohorts = max_cohorts
+        # tree-EM-iterations launched (counted when each chunk is queued)
+        self.em_tree_iterations = 0
         self.G = group_sites
         self.rounds = rounds
         self.chunk = chunk
@@ -185,7 +188,8 @@ class PMMServer:
                     return
                 jobs, used = [], 0
                 rest = collections.deque()
-                while self._pending and len(jobs) < self.max_cohort:
+                cap = self.max_cohort if kind == "llh" else self.max_em_cohort
+                while self._pending and len(jobs) < cap:
                     j = self._pending.popleft()
                     if j.req.kind == kind and self._used + used + j.footprint <= self.budget:
                         jobs.append(j)
@@ -222,6 +226,7 @@ class PMMServer:
             if kind == "em":
                 b.em_iterations(self.chunk, rounds=self.rounds, max_iters=self.max_iters,
                                 persistent=False)
+                self.em_tree_iterations += self.chunk * len(jobs)
             host = torch.empty(len(jobs), dtype=torch.int32, pin_memory=True)
             host.copy_(b.work["tr_status"], non_blocking=True)
             ev = torch.cuda.Event()
@@ -257,6 +262,7 @@ class PMMServer:
         with torch.cuda.stream(c.stream):
             b.em_iterations(self.chunk, rounds=self.rounds, max_iters=self.max_iters,
                             persistent=False)
+            self.em_tree_iterations += self.chunk * int((~c.done).sum())
             c.host_status.copy_(b.work["tr_status"], non_blocking=True)
             c.event.record(c.stream)
         return False
