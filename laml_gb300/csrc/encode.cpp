@@ -985,21 +985,37 @@ extern "C" int laml_plan_fill(const laml_plan_input* in, laml_plan_output* o) {
     for (int p = 0; p < T; ++p) uniform = uniform && in->ds_groups[in->tree_dataset[p]] == maxNG;
     auto emit = [&](int side, int first, int last, int32_t* off, int32_t* items) {
         const int32_t* nodes = lnodes[side].data();
+        if (uniform) {
+            // every tree has maxNG groups: item k of level l is node
+            // a_l + (k - off_l) % cnt_l of group (k - off_l) / cnt_l; one
+            // parallel pass over all items of all levels
+            const int nl = last - first + 1;
+            std::vector<int64_t> o64((size_t)nl + 1, 0);
+            for (int l = first; l <= last; ++l) {
+                const int64_t cnt = lstart[side][l + 1] - lstart[side][l];
+                o64[l - first + 1] = o64[l - first] + cnt * maxNG;
+                off[l - first] = (int32_t)o64[l - first];
+            }
+            off[nl] = (int32_t)o64[nl];
+            parallel_for(o64[nl], [&](int64_t k0, int64_t k1) {
+                int li = (int)(std::upper_bound(o64.begin(), o64.end(), k0) - o64.begin()) - 1;
+                for (int64_t k = k0; k < k1; ++k) {
+                    while (k >= o64[li + 1]) ++li;
+                    const int l = li + first;
+                    const int64_t a = lstart[side][l], cnt = lstart[side][l + 1] - a;
+                    const int64_t r = k - o64[li];
+                    const int64_t g = r / cnt;
+                    items[2 * k] = nodes[a + (r - g * cnt)];
+                    items[2 * k + 1] = (int32_t)g;
+                }
+            }, 1 << 15);
+            return;
+        }
         int64_t k = 0;
         for (int l = first; l <= last; ++l) {
             off[l - first] = (int32_t)k;
-            const int64_t a = lstart[side][l], e = lstart[side][l + 1], cnt = e - a;
-            if (uniform) {
-                int32_t* it = items + 2 * k;
-                parallel_for(cnt, [&](int64_t x0, int64_t x1) {
-                    for (int g = 0; g < maxNG; ++g)
-                        for (int64_t x = x0; x < x1; ++x) {
-                            it[2 * (g * cnt + x)] = nodes[a + x];
-                            it[2 * (g * cnt + x) + 1] = g;
-                        }
-                }, 1 << 15);
-                k += cnt * maxNG;
-            } else {
+            const int64_t a = lstart[side][l], e = lstart[side][l + 1];
+            {
                 for (int g = 0; g < maxNG; ++g)
                     for (int64_t x = a; x < e; ++x) {
                         const int node = nodes[x];

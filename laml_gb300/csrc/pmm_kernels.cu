@@ -53,6 +53,10 @@ constexpr double kEpsS = 1e-6, kEpsNu = 1e-5;   // EM_solver.Mstep defaults (EM_
 constexpr double kLn2 = 0.69314718055994530942;
 constexpr double kLogEps = -13.815510557964274;   // log(1e-6)
 constexpr int kBlock = 256;
+#ifndef LAML_ITEMS_BLOCK
+#define LAML_ITEMS_BLOCK 128   // threads per block of the per-level item kernels
+#endif
+constexpr int kItemsBlock = LAML_ITEMS_BLOCK;
 constexpr unsigned kFull = 0xffffffffu;
 #ifndef LAML_CHUNK
 #define LAML_CHUNK 4
@@ -61,8 +65,11 @@ constexpr int kChunk = LAML_CHUNK;   // states loaded ahead per step of a state 
 #ifndef LAML_MINB
 #define LAML_MINB 4
 #endif
+#ifndef LAML_MINB_IN
+#define LAML_MINB_IN 8   // resident blocks per SM asked of the other item kernels (64 registers)
+#endif
 #ifndef LAML_MINB_OUT
-#define LAML_MINB_OUT 3   // resident blocks per SM asked of the outside kernel (85 registers)
+#define LAML_MINB_OUT 6   // resident blocks per SM asked of the outside kernel (85 registers)
 #endif
 constexpr int kMstepStage = 2048;    // branches of a tree staged in shared memory by the M-step
 
@@ -2237,7 +2244,7 @@ __device__ __forceinline__ void for_items(const laml_batch& b, const int32_t* it
 }
 
 template <int G, int KIND>
-__global__ void __launch_bounds__(kBlock, KIND == 1 ? LAML_MINB_OUT : LAML_MINB) k_items(laml_batch b, const int32_t* items, int64_t n,
+__global__ void __launch_bounds__(kItemsBlock, KIND == 1 ? LAML_MINB_OUT : LAML_MINB_IN) k_items(laml_batch b, const int32_t* items, int64_t n,
                                                    int want_post, int respect_status,
                                                    const int32_t* desc) {
     const int gwarp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -2520,18 +2527,18 @@ int launch_items(const laml_batch& b, const int32_t* items, int64_t n, int kind,
         return kind == 0 ? launch_staged<G, 0>(b, desc, n, want_post, respect_status, st)
                          : launch_staged<G, 1>(b, desc, n, want_post, respect_status, st);
     }
-    const int ipb = ((kind == 0 || kind == 1) && narrow_level(n)) ? kBlock / 32
-                                                                   : (kBlock / 32) * (32 / G);
+    const int ipb = ((kind == 0 || kind == 1) && narrow_level(n)) ? kItemsBlock / 32
+                                                                   : (kItemsBlock / 32) * (32 / G);
     int64_t blocks = (n + ipb - 1) / ipb;
     const int64_t cap = (int64_t)num_sms() * 16;
     if (blocks > cap) blocks = cap;
     switch (kind) {
-        case 0: k_items<G, 0><<<(unsigned)blocks, kBlock, 0, st>>>(b, items, n, want_post, respect_status, desc); break;
-        case 1: k_items<G, 1><<<(unsigned)blocks, kBlock, 0, st>>>(b, items, n, want_post, respect_status, desc); break;
-        case 2: k_items<G, 2><<<(unsigned)blocks, kBlock, 0, st>>>(b, items, n, want_post, respect_status, desc); break;
-        case 3: k_items<G, 3><<<(unsigned)blocks, kBlock, 0, st>>>(b, items, n, want_post, respect_status, desc); break;
-        case 5: k_items<G, 5><<<(unsigned)blocks, kBlock, 0, st>>>(b, items, n, want_post, respect_status, desc); break;
-        default: k_items<G, 4><<<(unsigned)blocks, kBlock, 0, st>>>(b, items, n, want_post, respect_status, desc); break;
+        case 0: k_items<G, 0><<<(unsigned)blocks, kItemsBlock, 0, st>>>(b, items, n, want_post, respect_status, desc); break;
+        case 1: k_items<G, 1><<<(unsigned)blocks, kItemsBlock, 0, st>>>(b, items, n, want_post, respect_status, desc); break;
+        case 2: k_items<G, 2><<<(unsigned)blocks, kItemsBlock, 0, st>>>(b, items, n, want_post, respect_status, desc); break;
+        case 3: k_items<G, 3><<<(unsigned)blocks, kItemsBlock, 0, st>>>(b, items, n, want_post, respect_status, desc); break;
+        case 5: k_items<G, 5><<<(unsigned)blocks, kItemsBlock, 0, st>>>(b, items, n, want_post, respect_status, desc); break;
+        default: k_items<G, 4><<<(unsigned)blocks, kItemsBlock, 0, st>>>(b, items, n, want_post, respect_status, desc); break;
     }
     return check(cudaGetLastError(), "k_items launch");
 }
