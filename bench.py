@@ -375,11 +375,13 @@ def run_workload(args):
             ms_llh = _timed(lambda: b.inside(update_em=False), stream, 20)
             iters = 50
 
-            def em50():
+            graph = b.em_graph(iters, rel_tol=-1.0, max_iters=1 << 30, persistent=False)
+
+            def em50():   # the solver's path: one CUDA-graph replay of 50 iterations
                 b.set_params(d=np.maximum(b.trees[0].branch_length, 1e-6), nu=[nu0], phi=[phi0])
                 b.branch_terms()
                 b.inside(update_em=True)
-                b.em_iterations(iters, rel_tol=-1.0, max_iters=1 << 30, persistent=False)
+                b.launch_graph(graph)
             ms_em = _timed(em50, stream, max(3, args.steps))
         line.update({"value": iters / (ms_em / 1e3), "unit": "EM iters/s",
                      "negative_llh_ms": ms_llh, "em50_ms": ms_em,
