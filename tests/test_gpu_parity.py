@@ -231,6 +231,56 @@ def test_em_tree_above_cluster_threshold():
     assert r2[0].llh == r.llh and r2[1].llh == r.llh
 
 
+def test_wide_levels_match_narrow_levels_and_oracle():
+    """48 NNI candidates of a 1000-leaf tree: the batch's wide levels run the
+    per-thread item kernels, a tree alone runs every level on the
+    warp-per-item kernels.  The two sum a node's states in different orders
+    (one thread's running sum against a warp's lane sums), so they agree to
+    FP32 rounding of the partial rows: the log-likelihood to 1e-9 relative,
+    the expected counts to 1e-5 and a 3-iteration EM to 1e-7 (log-likelihood)
+    and 1e-4 (branch lengths).  The batch matches the FP64 oracle and the C
+    restatement."""
+    from oracle import cpu_port
+    w = synth.pmm_workload(1000, 40, 5, 50, 0.5, 0.1, 0.15, 3, n_trees=48, nni=True)
+    for G in (8, 16):
+        big = PB.make_batch(w.newicks, w.rows, w.Q, w.leaf_order, compat=True, group_sites=G,
+                            nu=0.1, phi=0.15)
+        assert max(np.diff(big._h_in_off)) > 8192   # the batch has wide levels
+        big.e_step()
+        torch.cuda.synchronize()
+        llh_big = big.work["tr_llh"].cpu().numpy().copy()
+        cnt_big, _ = big.counts_from_partials()
+        for t in (0, 17):
+            one = PB.make_batch([w.newicks[t]], w.rows, w.Q, w.leaf_order, compat=True,
+                                group_sites=G, nu=0.1, phi=0.15)
+            assert max(np.diff(one._h_in_off)) <= 8192   # alone: every level narrow
+            one.e_step()
+            torch.cuda.synchronize()
+            assert float(one.work["tr_llh"][0]) == pytest.approx(float(llh_big[t]), rel=1e-9)
+            cnt_one, _ = one.counts_from_partials()
+            nb = int(big._node_base[t])
+            a = cnt_big[nb:nb + one.trees[0].num_nodes]
+            np.testing.assert_allclose(cnt_one[:one.trees[0].num_nodes], a, rtol=1e-5,
+                                       atol=1e-6 * float(np.abs(a).max()))
+        tr = O.parse_tree(w.newicks[0], w.leaf_order)
+        enc = O.recode([w.rows[c] for c in w.leaf_order], w.Q, compat=True)
+        ref = O.log_likelihood(O.Problem(tr, enc, True), np.maximum(tr.branch_lengths, 1e-6),
+                               0.1, 0.15)[0]
+        assert llh_big[0] == pytest.approx(ref, rel=1e-6)
+    # EM through the wide levels against the C restatement, and alone
+    big = PB.make_batch(w.newicks, w.rows, w.Q, w.leaf_order, compat=True)
+    res = big.run_em(max_iters=3, rel_tol=-1.0, chunk=1)
+    llh, nu, phi, ds, _ = cpu_port.em(w.newicks[:2], w.rows, w.Q, w.leaf_order, 0.5, 0.5,
+                                      iters=3)
+    for t in range(2):
+        assert res[t].llh == pytest.approx(llh[t], rel=1e-6)
+        alone = PB.make_batch([w.newicks[t]], w.rows, w.Q, w.leaf_order,
+                              compat=True).run_em(max_iters=3, rel_tol=-1.0, chunk=1)[0]
+        assert alone.llh == pytest.approx(res[t].llh, rel=1e-7)
+        np.testing.assert_allclose(alone.branch_lengths, res[t].branch_lengths, rtol=1e-4,
+                                   atol=1e-7)
+
+
 def test_device_descriptors_equal_host_plan():
     """laml_plan_descriptors on the device writes laml_plan_fill's bytes."""
     from laml_gb300.encoding import plan_batch
