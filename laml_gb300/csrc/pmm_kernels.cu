@@ -939,8 +939,11 @@ __device__ void inside_item_d(const laml_batch& b, const ItemDesc& d, int lane,
         if (!(d.flags & 1)) prefetch_l2(b.in_part + (int64_t)d.v_ref * 8 + s.goff, bytes);
         if (!(d.flags & 2)) prefetch_l2(b.in_part + (int64_t)d.w_ref * 8 + s.goff, bytes);
     }
-    if (tree_log(b, s.tree)) {
-        inside_log_item<G>(b, d, s, gc);
+    if (tree_log(b, s.tree)) {   // copies: the linear path's structs stay in registers
+        const ItemDesc dl = d;
+        const SiteCtx sl = s;
+        const GroupCtx gl = gc;
+        inside_log_item<G>(b, dl, sl, gl);
         return;
     }
     const Leaf L = leaf_params(b, s.tree);
@@ -985,9 +988,12 @@ __device__ void outside_item_d(const laml_batch& b, const ItemDesc& d, int lane,
         if (!(d.flags & 1)) prefetch_l2(b.in_part + (int64_t)d.v_ref * 8 + s.goff, bytes);
         if (!(d.flags & 2)) prefetch_l2(b.in_part + (int64_t)d.w_ref * 8 + s.goff, bytes);
     }
-    if (live && tree_log(b, s.tree)) {
+    if (live && tree_log(b, s.tree)) {   // copies: the linear path's structs stay in registers
         float tv[8], tw[8];
-        outside_log_lane<G>(b, d, s, gc, want_post, tv, tw);
+        const ItemDesc dl = d;
+        const SiteCtx sl = s;
+        const GroupCtx gl = gc;
+        outside_log_lane<G>(b, dl, sl, gl, want_post, tv, tw);
 #pragma unroll
         for (int k = 0; k < 8; ++k) {
             cv_[k] = tv[k];
@@ -1051,9 +1057,12 @@ __device__ void outside_root_item_d(const laml_batch& b, const ItemDesc& d, int 
     SiteCtx s;
     GroupCtx gc;
     const bool live = act && site_ctx_d<G>(b, d, lane, true, s, gc);
-    if (live && tree_log(b, s.tree)) {
+    if (live && tree_log(b, s.tree)) {   // copies: the linear path's structs stay in registers
         float tv[8], tw[8];
-        outside_log_lane<G>(b, d, s, gc, want_post, tv, tw);
+        const ItemDesc dl = d;
+        const SiteCtx sl = s;
+        const GroupCtx gl = gc;
+        outside_log_lane<G>(b, dl, sl, gl, want_post, tv, tw);
 #pragma unroll
         for (int k = 0; k < 8; ++k) {
             cv_[k] = tv[k];
