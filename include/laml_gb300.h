@@ -171,6 +171,20 @@ typedef struct laml_plan_output {
 int laml_plan_measure(const laml_plan_input* in, laml_plan_sizes* sizes);
 int laml_plan_fill(const laml_plan_input* in, laml_plan_output* out);
 
+/* Depth schedule of one binary tree for the ultrametric M-step
+ * (LAML_MSTEP_ULTRAMETRIC): parent[N] holds tree-local parent ids (-1 at the
+ * root).  Writes out[0] = L (levels: depths 0..L-1), out[1..L+1] = level
+ * offsets, then the N node ids grouped by depth from the root down (level l
+ * is out[L + 2 + out[1 + l] .. L + 2 + out[2 + l])).  `out_len` must be at
+ * least 2 * N + 2; *written receives N + L + 2.  The schedule stands in for
+ * the treeswift postorder walk of EM_solver.ultrametric_constr
+ * (EM_solver.py:53-89): the equalities it builds at every internal node are
+ * met by construction when the solve works on node heights, and the
+ * elimination of the heights' Newton systems runs one depth level at a
+ * time. */
+int laml_ultra_order(const int32_t* parent, int32_t n_nodes, int32_t* out, int64_t out_len,
+                     int64_t* written);
+
 /* ------------------------------------------------------------------------
  * Device batch: every pointer is a device address
  * --------------------------------------------------------------------- */
@@ -241,6 +255,12 @@ typedef struct laml_batch {
      * laml_branch_terms and the M-step; NULL = derived from tr_phi wherever
      * needed */
     float* tr_leaf;
+    /* Ultrametric M-step (LAML_MSTEP_ULTRAMETRIC) only, else NULL:
+     * nd_uorder [2 * n_nodes + 2 * n_trees] -- tree p's depth schedule from
+     * laml_ultra_order at offset 2 * tr_node_base[p] + 2 * p;
+     * nd_uwork [LAML_UWORK_SLOTS * n_nodes] -- FP64 scratch of the solve. */
+    const int32_t* nd_uorder;
+    double* nd_uwork;
 } laml_batch;
 
 /* A tree's partials are FP32 values with power-of-two exponents (linear)
@@ -255,6 +275,11 @@ typedef struct laml_batch {
 #define LAML_TREE_CONVERGED 1
 #define LAML_TREE_NAN 2
 #define LAML_TREE_MAXITER 3
+/* the ultrametric M-step's constraints admit no branch lengths in
+ * [dmin, dmax] (EM_solver.Mstep's "d_infeasible", EM_solver.py:419-420,
+ * 491-495): the tree keeps the parameters and log-likelihood it had before
+ * that M-step */
+#define LAML_TREE_INFEASIBLE 4
 
 /* Number of sites per group the kernels were built for (bit mask of 8|16|32). */
 int laml_supported_group_sites(void);
@@ -306,6 +331,18 @@ int laml_gradient(const laml_batch* b, double* grad_d, double* grad_nu_phi, void
 /* M-step flags: FP64 Newton polish of the final branch-length and nu solves
  * (the solves otherwise run FP32 Newton iterations with FP64 accumulation). */
 #define LAML_MSTEP_FP64_POLISH 1
+/* Exact model only: branch lengths maximise the M-step objective jointly
+ * under EM_solver's ultrametric equalities (every root-to-leaf path of a
+ * tree has the same length; EM_solver.ultrametric_constr, EM_solver.py:53-89,
+ * used at 358-361) and the bounds [dmin, dmax]; the root's own branch is in
+ * no equality and is solved alone.  Needs nd_uorder and nd_uwork.  Fixed
+ * branches (nd_mask = 0) enter the equalities with their lengths, as the
+ * reference's node.constant does; a tree whose constraints admit no solution
+ * gets LAML_TREE_INFEASIBLE.  Ignored in compat mode (the fastEM path has no
+ * such constraint). */
+#define LAML_MSTEP_ULTRAMETRIC 2
+/* doubles per node of laml_batch.nd_uwork */
+#define LAML_UWORK_SLOTS 16
 
 /* M-step of every active tree: compat maximises the fastEM objective
  * (fast_em/laml.py:62-78) by `rounds` coordinate-ascent rounds; exact follows

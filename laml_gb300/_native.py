@@ -17,9 +17,10 @@ vp = C.c_void_p
 LAML_OK = 0
 ERRORS = {-1: "LAML_ERR_ARG", -2: "LAML_ERR_CUDA", -3: "LAML_ERR_PARSE", -4: "LAML_ERR_PRIOR",
           -5: "LAML_ERR_TIMEOUT", -6: "LAML_ERR_NOT_BINARY", -7: "LAML_ERR_LEAF"}
-TREE_ACTIVE, TREE_CONVERGED, TREE_NAN, TREE_MAXITER = 0, 1, 2, 3
+TREE_ACTIVE, TREE_CONVERGED, TREE_NAN, TREE_MAXITER, TREE_INFEASIBLE = 0, 1, 2, 3, 4
 MODE_LINEAR, MODE_LOG = 0, 1
-MSTEP_FP64_POLISH = 1
+MSTEP_FP64_POLISH, MSTEP_ULTRAMETRIC = 1, 2
+UWORK_SLOTS = 16   # LAML_UWORK_SLOTS: doubles per node of nd_uwork
 OUT_POSTERIORS, OUT_TRUE_ROOT = 1, 2
 
 
@@ -84,7 +85,7 @@ BATCH_FIELDS = [
     ("root_items", vp), ("in_desc", vp), ("out_desc", vp), ("grp_desc", vp),
     ("h_in_level_off", vp), ("h_out_level_off", vp),
     ("barrier", vp), ("error", vp), ("max_states", i32), ("max_tree_nodes", i32),
-    ("tr_leaf", vp),
+    ("tr_leaf", vp), ("nd_uorder", vp), ("nd_uwork", vp),
 ]
 
 
@@ -103,6 +104,7 @@ EXPORTS = {
                                   vp, vp]),
     "laml_plan_measure": (i32, [P(PlanInput), P(PlanSizes)]),
     "laml_plan_fill": (i32, [P(PlanInput), P(PlanOutput)]),
+    "laml_ultra_order": (i32, [vp, i32, vp, i64, P(i64)]),
     "laml_supported_group_sites": (i32, []),
     "laml_plan_descriptors": (i32, [P(Batch), vp, vp, vp, vp]),
     "laml_branch_terms": (i32, [P(Batch), vp]),

@@ -1107,3 +1107,75 @@ extern "C" int laml_plan_fill(const laml_plan_input* in, laml_plan_output* o) {
     }
     return LAML_OK;
 }
+
+// Depth schedule of one binary tree for the ultrametric M-step: node ids
+// grouped by depth from the root (a breadth-first walk, so each level lists
+// its nodes in the order their parents were reached).
+extern "C" int laml_ultra_order(const int32_t* parent, int32_t n_nodes, int32_t* out,
+                                int64_t out_len, int64_t* written) {
+    if (!parent || !out || n_nodes <= 0) {
+        set_error("laml_ultra_order: null argument or empty tree");
+        return LAML_ERR_ARG;
+    }
+    if (out_len < 2 * (int64_t)n_nodes + 2) {
+        set_error("laml_ultra_order: out_len below 2 * n_nodes + 2");
+        return LAML_ERR_ARG;
+    }
+    const int N = n_nodes;
+    std::vector<int32_t> c0(N, -1), c1(N, -1);
+    int root = -1;
+    for (int v = 0; v < N; ++v) {
+        const int p = parent[v];
+        if (p < 0) {
+            if (root >= 0) {
+                set_error("laml_ultra_order: more than one root");
+                return LAML_ERR_ARG;
+            }
+            root = v;
+        } else if (p >= N) {
+            set_error("laml_ultra_order: parent id out of range");
+            return LAML_ERR_ARG;
+        } else if (c0[p] < 0) {
+            c0[p] = v;
+        } else if (c1[p] < 0) {
+            c1[p] = v;
+        } else {
+            set_error("laml_ultra_order: a node with more than two children");
+            return LAML_ERR_NOT_BINARY;
+        }
+    }
+    if (root < 0) {
+        set_error("laml_ultra_order: no root");
+        return LAML_ERR_ARG;
+    }
+    std::vector<int32_t> ids;
+    std::vector<int32_t> off{0};
+    ids.reserve(N);
+    ids.push_back(root);
+    for (size_t a = 0; a < ids.size();) {   // one level per pass
+        const size_t e = ids.size();
+        off.push_back((int32_t)e);
+        for (size_t k = a; k < e; ++k) {
+            const int u = ids[k];
+            if (c0[u] >= 0) {
+                if (c1[u] < 0) {
+                    set_error("laml_ultra_order: a node with one child");
+                    return LAML_ERR_NOT_BINARY;
+                }
+                ids.push_back(c0[u]);
+                ids.push_back(c1[u]);
+            }
+        }
+        a = e;
+    }
+    if ((int)ids.size() != N) {
+        set_error("laml_ultra_order: the parent array is not one tree");
+        return LAML_ERR_ARG;
+    }
+    const int L = (int)off.size() - 1;
+    out[0] = L;
+    std::copy(off.begin(), off.end(), out + 1);
+    std::copy(ids.begin(), ids.end(), out + L + 2);
+    if (written) *written = (int64_t)N + L + 2;
+    return LAML_OK;
+}

@@ -72,6 +72,8 @@ constexpr int kChunk = LAML_CHUNK;   // states loaded ahead per step of a state 
 #define LAML_MINB_OUT 6   // resident blocks per SM asked of the outside kernel (85 registers)
 #endif
 constexpr int kMstepStage = 2048;    // branches of a tree staged in shared memory by the M-step
+constexpr int kOStash = 24;          // words per thread the outside item parks in shared memory
+static_assert(kItemsBlock <= kBlock, "the outside item's shared-memory stash has kBlock columns");
 
 // ---------------------------------------------------------------------------
 // small helpers
@@ -952,7 +954,6 @@ __device__ void inside_item_d(const laml_batch& b, const ItemDesc& d, int lane,
     const float4 bv = load_bt(b, d.v), bw = load_bt(b, d.w);
     const float ev0 = bv.x * cv.s0 + bv.y * cv.D + bv.w * cv.ss;
     const float ew0 = bw.x * cw.s0 + bw.y * cw.D + bw.w * cw.ss;
-    const float kv = bv.w * cv.ss, kw = bw.w * cw.ss;
     float* row = b.in_part + (int64_t)d.u_prow8 * 8 + s.goff + lane;
     const float s0 = ev0 * ew0, ss = cv.ss * cw.ss;
     __stcg(row, s0);
@@ -1019,17 +1020,50 @@ __device__ void outside_item_d(const laml_batch& b, const ItemDesc& d, int lane,
         B.sumx = B.dot = B.mx = 0.f;
         A.orow = cv.row ? b.out_part + (int64_t)d.v_ref * 8 + s.goff + lane : nullptr;
         B.orow = cw.row ? b.out_part + (int64_t)d.w_ref * 8 + s.goff + lane : nullptr;
+        // what child_finish needs after the state loop waits in shared memory
+        // (one column per thread; read back through volatile loads, so the
+        // values do not stay live in registers across the loop, which
+        // otherwise spills at this kernel's 80-register budget)
+        __shared__ float ostash[kOStash * kBlock];
+        {
+            float* sp = ostash + threadIdx.x;
+            sp[0 * kBlock] = cv.s0; sp[1 * kBlock] = cv.ss; sp[2 * kBlock] = cv.D;
+            sp[3 * kBlock] = __int_as_float(cv.X); sp[4 * kBlock] = __int_as_float(cv.code);
+            sp[5 * kBlock] = cw.s0; sp[6 * kBlock] = cw.ss; sp[7 * kBlock] = cw.D;
+            sp[8 * kBlock] = __int_as_float(cw.X); sp[9 * kBlock] = __int_as_float(cw.code);
+            sp[10 * kBlock] = bv.x; sp[11 * kBlock] = bv.y; sp[12 * kBlock] = bv.w;
+            sp[13 * kBlock] = bw.x; sp[14 * kBlock] = bw.y; sp[15 * kBlock] = bw.w;
+            sp[16 * kBlock] = A.x0; sp[17 * kBlock] = A.xs; sp[18 * kBlock] = __int_as_float(A.X);
+            sp[19 * kBlock] = B.x0; sp[20 * kBlock] = B.xs; sp[21 * kBlock] = __int_as_float(B.X);
+            sp[22 * kBlock] = bv.z; sp[23 * kBlock] = bw.z;
+        }
         switch ((cv.row ? 0 : 1) | (cw.row ? 0 : 2)) {   // warp-uniform: items are sorted by it
             case 0: outside_states<G, false, false>(urow, fo, cv, cw, bv, bw, s.qrow, s.C, A, B); break;
             case 1: outside_states<G, true, false>(urow, fo, cv, cw, bv, bw, s.qrow, s.C, A, B); break;
             case 2: outside_states<G, false, true>(urow, fo, cv, cw, bv, bw, s.qrow, s.C, A, B); break;
             default: outside_states<G, true, true>(urow, fo, cv, cw, bv, bw, s.qrow, s.C, A, B); break;
         }
+        const volatile float* vp = ostash + threadIdx.x;
+        Child cv2, cw2;   // child_finish reads row only as "leaf or not"
+        cv2.s0 = vp[0 * kBlock]; cv2.ss = vp[1 * kBlock]; cv2.D = vp[2 * kBlock];
+        cv2.X = __float_as_int(vp[3 * kBlock]); cv2.code = __float_as_int(vp[4 * kBlock]);
+        cv2.row = (d.flags & 1) ? nullptr : b.in_part;
+        cw2.s0 = vp[5 * kBlock]; cw2.ss = vp[6 * kBlock]; cw2.D = vp[7 * kBlock];
+        cw2.X = __float_as_int(vp[8 * kBlock]); cw2.code = __float_as_int(vp[9 * kBlock]);
+        cw2.row = (d.flags & 2) ? nullptr : b.in_part;
+        const float4 bv2 = make_float4(vp[10 * kBlock], vp[11 * kBlock], vp[22 * kBlock],
+                                       vp[12 * kBlock]);
+        const float4 bw2 = make_float4(vp[13 * kBlock], vp[14 * kBlock], vp[23 * kBlock],
+                                       vp[15 * kBlock]);
+        A.x0 = vp[16 * kBlock]; A.xs = vp[17 * kBlock]; A.X = __float_as_int(vp[18 * kBlock]);
+        B.x0 = vp[19 * kBlock]; B.xs = vp[20 * kBlock]; B.X = __float_as_int(vp[21 * kBlock]);
+        A.orow = (d.flags & 1) ? nullptr : b.out_part + (int64_t)d.v_ref * 8 + s.goff + lane;
+        B.orow = (d.flags & 2) ? nullptr : b.out_part + (int64_t)d.w_ref * 8 + s.goff + lane;
         const int64_t t = __ldg(b.tr_site_base + s.tree) + s.site;
         const float lroot = __ldcg(b.root_lr + t);
         const int xroot = __ldcg(b.root_x + t);
-        child_finish<G>(b, s, d.v, cv, bv, A, want_post, lroot, xroot, cv_);
-        child_finish<G>(b, s, d.w, cw, bw, B, want_post, lroot, xroot, cw_);
+        child_finish<G>(b, s, d.v, cv2, bv2, A, want_post, lroot, xroot, cv_);
+        child_finish<G>(b, s, d.w, cw2, bw2, B, want_post, lroot, xroot, cw_);
     }
 #pragma unroll
     for (int off = G / 2; off > 0; off >>= 1) {
@@ -1260,6 +1294,19 @@ __device__ __forceinline__ int block_maxi(int x, double2* shd) {
     return r;
 }
 
+// block-wide min of a double
+__device__ __forceinline__ double block_mind(double x, double2* sh) {
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) x = fmin(x, __shfl_xor_sync(kFull, x, off));
+    const int wid = threadIdx.x >> 5, ln = threadIdx.x & 31;
+    __syncthreads();
+    if (ln == 0) sh[wid].x = x;
+    __syncthreads();
+    double r = sh[0].x;
+    for (int k = 1; k < (int)(blockDim.x >> 5); ++k) r = fmin(r, sh[k].x);
+    return r;
+}
+
 __device__ float4 branch_terms_of(double d, double nu, int compat) {
     // FP32 is the storage precision of the terms: compute them in FP32
     const float df = (float)d, nf = (float)nu, nd = df * nf;
@@ -1387,6 +1434,7 @@ struct BlockTeam {
     __device__ float2 sum2f(float a, float c) const { return block_sum2f(a, c, sh); }
     __device__ double2 sum2(double a, double c) const { return block_sum2(a, c, sh); }
     __device__ int maxi(int x) const { return block_maxi(x, sh); }
+    __device__ double mind(double x) const { return block_mind(x, sh); }
 };
 
 constexpr int kMstepCluster = 8;        // blocks per cluster (the portable size)
@@ -1432,11 +1480,374 @@ struct ClusterTeam {
         cl.sync();
         return r;
     }
+    __device__ double mind(double x) const {
+        auto cl = cooperative_groups::this_cluster();
+        const double m = block_mind(x, sh);
+        double2* p0 = cl.map_shared_rank(part, 0);
+        if (threadIdx.x == 0) p0[cl.block_rank()] = make_double2(m, 0.0);
+        cl.sync();
+        double r = p0[0].x;
+        for (int k = 1; k < kMstepCluster; ++k) r = fmin(r, p0[k].x);
+        cl.sync();
+        return r;
+    }
 };
+
+// ---------------------------------------------------------------------------
+// Ultrametric branch lengths (EM_solver.Mstep with ultra_constr_cache,
+// EM_solver.py:349-366, under the equalities of ultrametric_constr, 53-89).
+// Given nu, maximise over the optimised branches
+//   sum_v f_v(d_v),  f_v(d) = -a_v d + b_v log(1 - e^{-d}) + c_v log(1 - e^{-nu d})
+// with d in [dmin, dmax] and every root-to-leaf path of the tree equally
+// long.  The solve works on node heights P (the path length from a node down
+// to its leaves, 0 at a leaf): d_x = P_parent(x) - P_x for every non-root x,
+// so the equalities hold by construction; a fixed branch (mask 0) ties
+// P_x = P_parent - d_x, as the reference's node.constant does, and a node
+// tied to a leaf through fixed branches is pinned (its height is a
+// constant).  The root's own branch is in no equality of a single tree and
+// is solved alone.
+//
+// Method: log-barrier interior point on the bounds.  The Newton system of
+// the heights is a weighted tree Laplacian (edge weight W_x = -phi''_x),
+// solved exactly by eliminating nodes from the deepest level up and
+// substituting back down, one depth level (nd_uorder) per team sync; a
+// node's reduced diagonal is kept as the sum of positive terms
+// W_c E_c / (W_c + E_c), which loses nothing to cancellation however large
+// the weights grow.  A backtracking line search tests the barrier
+// objective's change summed branch by branch from log1p/expm1 differences,
+// so no difference of large totals is taken.  Heights, branch lengths, the
+// elimination and every sum are FP64; the transcendental and reciprocal
+// cores (expm1, log1p, 1/x of values formed in FP64) run in FP32, since
+// GB300's FP64 pipe is narrow and each enters only a gradient, a weight or a
+// line-search term at FP32 relative precision (the solution moves by ~1e-7
+// relative).  Centring ends when lambda^2 / 2 < 1e-6 or, in the quadratic
+// phase, when lambda^2 stops falling (the rounding floor of large t).
+// Returns false when the constraints admit no branch lengths (an empty
+// height interval at some node).
+// ---------------------------------------------------------------------------
+namespace ultra {
+// per-node FP64 slots of nd_uwork (LAML_UWORK_SLOTS per node)
+constexpr int kP = 0;     // height (the warm start during the interval pass)
+constexpr int kW = 1;     // weight of the node's own branch (lo during the interval pass)
+constexpr int kG = 2;     // barrier-objective slope of that branch (hi during the interval pass)
+constexpr int kE = 3;     // reduced diagonal excess of the node's subtree
+constexpr int kR = 4;     // reduced right-hand side
+constexpr int kDel = 5;   // Newton step of the height
+constexpr int kPin = 6;   // 1: height fixed (leaves, nodes tied to a leaf by fixed branches)
+constexpr int kRaw = 7;   // gradient of the barrier objective in the height (during the
+                          // interval pass: 1 when the path down child1 is all fixed)
+constexpr int kA = 8, kB = 9, kC = 10;   // objective coefficients of the node's branch
+constexpr int kIE = 11, kIEN = 12;       // 1 / expm1(d), 1 / expm1(nu d) at the current d
+constexpr int kRL = 13, kRH = 14;        // 1 / (d - dmin), 1 / (dmax - d)
+constexpr int kSlots = LAML_UWORK_SLOTS;
+static_assert(kSlots >= 15, "nd_uwork slots");
+constexpr double kTheta = 0.1;        // pull of the start point toward its interval's middle
+constexpr double kMu = 20.0;          // barrier weight growth per centring
+constexpr double kGapRel = 1e-10;     // objective suboptimality m / t, relative
+constexpr double kNewtonTol = 1e-6;   // centred when lambda^2 / 2 is below this
+constexpr int kOuterMax = 30, kNewtonMax = 60, kLineMax = 60;
+
+__device__ __forceinline__ double rcp32(double x) { return (double)(1.f / (float)x); }
+__device__ __forceinline__ double log1p32(double x) { return (double)log1pf((float)x); }
+__device__ __forceinline__ double expm132(double x) { return (double)expm1f((float)x); }
+__device__ __forceinline__ double log1mexp32(double x) {   // log(1 - e^{-x}), x > 0
+    return (double)logf(-expm1f(-(float)x));
+}
+}  // namespace ultra
+
+template <class Team>
+__device__ __noinline__ bool ultra_dstep(const laml_batch& b, int p, Team& T, double nu,
+                                         bool use_s, float* Dd) {
+    using namespace ultra;
+    const int N = __ldg(b.tr_nodes + p), base = __ldg(b.tr_node_base + p);
+    const int root = __ldg(b.tr_root + p) - base;
+    const int32_t* ord = b.nd_uorder + 2 * (int64_t)base + 2 * (int64_t)p;
+    const int L = __ldg(ord);
+    const int32_t* off = ord + 1;
+    const int32_t* ids = ord + L + 2;
+    double* U = b.nd_uwork + (int64_t)kSlots * base;
+    const double dlo = kDmin, dhi = kDmax;
+    auto at = [&](int v, int k) -> double& { return U[(int64_t)kSlots * v + k]; };
+    auto leaf = [&](int v) { return __ldg(b.nd_c0 + base + v) < 0; };
+    auto c0_ = [&](int v) { return __ldg(b.nd_c0 + base + v) - base; };
+    auto c1_ = [&](int v) { return __ldg(b.nd_c1 + base + v) - base; };
+    auto par = [&](int v) { return __ldg(b.nd_parent + base + v) - base; };
+    auto freeb = [&](int v) { return __ldg(b.nd_mask + base + v) != 0; };
+    auto dold = [&](int v) { return __ldcg(b.nd_d + base + v); };
+    // a free branch between two pinned heights is as good as fixed
+    auto active = [&](int x) {
+        return x != root && freeb(x) && !(at(x, kPin) != 0.0 && at(par(x), kPin) != 0.0);
+    };
+
+    // 1. leaves, the branches' coefficients; then height intervals [lo, hi]
+    //    bottom-up, with the warm start (the mean over the children used of
+    //    d_c + P_c at the current d)
+    for (int v = T.tid(); v < N; v += T.size()) {
+        const double* q = b.nd_cnt + (int64_t)(base + v) * 6;
+        const double q0 = __ldcg(q), q1 = __ldcg(q + 1), q3 = __ldcg(q + 3);
+        at(v, kA) = q0 + nu * (q0 + q1 + q3);
+        at(v, kB) = q1;
+        at(v, kC) = use_s ? __ldcg(q + 2) + __ldcg(q + 4) : 0.0;
+        if (!leaf(v)) continue;
+        at(v, kP) = 0.0; at(v, kW) = 0.0; at(v, kG) = 0.0; at(v, kE) = 0.0;
+        at(v, kR) = 0.0; at(v, kDel) = 0.0; at(v, kPin) = 1.0; at(v, kRaw) = 1.0;
+    }
+    T.sync();
+    int bad = 0;
+    for (int l = L - 1; l >= 0; --l) {
+        for (int k = __ldg(off + l) + T.tid(); k < __ldg(off + l + 1); k += T.size()) {
+            const int u = __ldg(ids + k);
+            if (leaf(u)) continue;
+            double lo = -INFINITY, hi = INFINITY, pinv = NAN, warm = 0.0;
+            const int cs[2] = {c0_(u), c1_(u)};
+            // a child's path (its branch, then first children down to a leaf;
+            // treeswift's first child is child1 here) that holds no free
+            // branch is a constant; ultrametric_constr keeps no row between
+            // two constants (EM_solver.py:70-72), and the node's own path
+            // continues down child1 (EM_solver.py:73)
+            const bool cp0 = !freeb(cs[0]) && at(cs[0], kRaw) != 0.0;
+            const bool cp1 = !freeb(cs[1]) && at(cs[1], kRaw) != 0.0;
+            const int first = (cp0 && cp1) ? 1 : 0;
+            for (int i = first; i < 2; ++i) {
+                const int c = cs[i];
+                const double lc = at(c, kW), hc = at(c, kG);
+                if (freeb(c)) {
+                    lo = fmax(lo, lc + dlo);
+                    hi = fmin(hi, hc + dhi);
+                } else {
+                    const double df = dold(c);
+                    lo = fmax(lo, lc + df);
+                    hi = fmin(hi, hc + df);
+                    if (at(c, kPin) != 0.0) pinv = lc + df;
+                }
+                warm += (dold(c) + at(c, kP)) / (double)(2 - first);
+            }
+            const double tol = 1e-9 * fmax(1.0, fabs(hi));
+            bool pin = !isnan(pinv);
+            if (pin) {   // every other constraint must admit the pinned height
+                if (pinv < lo - tol || pinv > hi + tol) bad = 1;
+                lo = hi = pinv;
+            } else if (lo > hi + tol) {
+                bad = 1;
+            } else if (!(hi - lo > 1e-12 * fmax(1.0, fabs(hi)))) {
+                pin = true;   // a single admissible height
+                lo = hi = 0.5 * (lo + hi);
+            }
+            at(u, kW) = lo;
+            at(u, kG) = hi;
+            at(u, kPin) = pin ? 1.0 : 0.0;
+            at(u, kP) = warm;
+            at(u, kDel) = 0.0;
+            at(u, kRaw) = cp1 ? 1.0 : 0.0;
+        }
+        T.sync();
+    }
+    if (T.maxi(bad)) return false;
+
+    // 2. strictly feasible start, top-down: each height the warm start
+    //    clamped to what its parent's height leaves, pulled kTheta toward the
+    //    middle of that range
+    for (int l = 0; l < L; ++l) {
+        for (int k = __ldg(off + l) + T.tid(); k < __ldg(off + l + 1); k += T.size()) {
+            const int x = __ldg(ids + k);
+            if (leaf(x)) continue;
+            double lo = at(x, kW), hi = at(x, kG), P;
+            if (at(x, kPin) != 0.0) {
+                P = lo;
+            } else if (x != root && !freeb(x)) {
+                P = at(par(x), kP) - dold(x);
+            } else {
+                if (x != root) {
+                    const double Pu = at(par(x), kP);
+                    lo = fmax(lo, Pu - dhi);
+                    hi = fmin(hi, Pu - dlo);
+                }
+                const double w = fmin(fmax(at(x, kP), lo), hi);
+                P = (1.0 - kTheta) * w + kTheta * 0.5 * (lo + hi);
+            }
+            at(x, kP) = P;
+        }
+        T.sync();
+    }
+
+    // 3. barrier objective scale: m (bound constraints) and |F| at the start
+    double m_loc = 0.0, F_loc = 0.0;
+    for (int x = T.tid(); x < N; x += T.size()) {
+        if (!active(x)) continue;
+        const double a = at(x, kA), bb = at(x, kB), c = at(x, kC);
+        const double d = at(par(x), kP) - at(x, kP);
+        F_loc += -a * d + (bb > 0.0 ? bb * log1mexp32(d) : 0.0) +
+                 (c > 0.0 ? c * log1mexp32(nu * d) : 0.0);
+        m_loc += 2.0;
+    }
+    const double2 mF = T.sum2(m_loc, F_loc);
+    const double m = mF.x;
+    const double gap_tol = kGapRel * (fabs(mF.y) + 1.0);
+    double t = 1.0;
+
+    for (int outer = 0; outer < kOuterMax && m > 0.0; ++outer) {
+        double lam_prev = INFINITY;
+        for (int it = 0; it < kNewtonMax; ++it) {
+            // (a) slope and weight of every branch in the barrier objective
+            //     t f(d) + log(d - dmin) + log(dmax - d); the terms the line
+            //     search reuses are kept
+            for (int x = T.tid(); x < N; x += T.size()) {
+                if (x == root) continue;
+                if (!active(x)) {
+                    at(x, kW) = 0.0;
+                    at(x, kG) = 0.0;
+                    continue;
+                }
+                const double a = at(x, kA), bb = at(x, kB), c = at(x, kC);
+                const double d = at(par(x), kP) - at(x, kP);
+                double g = -a, h = 0.0, ie = 0.0, ien = 0.0;
+                if (bb > 0.0) {
+                    const double e = expm132(d);
+                    ie = rcp32(e);
+                    g += bb * ie;
+                    h -= bb * (e + 1.0) * ie * ie;
+                }
+                if (c > 0.0) {
+                    const double e = expm132(nu * d);
+                    ien = rcp32(e);
+                    g += c * nu * ien;
+                    h -= c * nu * nu * (e + 1.0) * ien * ien;
+                }
+                const double rl = rcp32(d - dlo), rh = rcp32(dhi - d);
+                at(x, kG) = t * g + rl - rh;
+                at(x, kW) = -(t * h) + rl * rl + rh * rh;
+                at(x, kIE) = ie;
+                at(x, kIEN) = ien;
+                at(x, kRL) = rl;
+                at(x, kRH) = rh;
+            }
+            T.sync();
+            // (b) elimination, deepest level first
+            for (int l = L - 1; l >= 0; --l) {
+                for (int k = __ldg(off + l) + T.tid(); k < __ldg(off + l + 1); k += T.size()) {
+                    const int u = __ldg(ids + k);
+                    if (leaf(u)) continue;
+                    const int cs[2] = {c0_(u), c1_(u)};
+                    double raw = at(cs[0], kG) + at(cs[1], kG) - (u == root ? 0.0 : at(u, kG));
+                    at(u, kRaw) = raw;
+                    if (at(u, kPin) != 0.0) {
+                        at(u, kE) = 0.0;
+                        at(u, kR) = 0.0;
+                        continue;
+                    }
+                    double E = 0.0, R = raw;
+                    for (int i = 0; i < 2; ++i) {
+                        const int c = cs[i];
+                        const double Wc = at(c, kW);
+                        if (at(c, kPin) != 0.0) {
+                            E += Wc;
+                        } else if (freeb(c)) {
+                            const double Ec = at(c, kE), D = Wc + Ec;
+                            E += Wc * (Ec / D);
+                            R += Wc * (at(c, kR) / D);
+                        } else {   // fixed branch: the child's height moves with this one
+                            E += at(c, kE);
+                            R += at(c, kR);
+                        }
+                    }
+                    at(u, kE) = E;
+                    at(u, kR) = R;
+                }
+                T.sync();
+            }
+            // (c) substitution, root first; lambda^2 = gradient . step
+            double lam = 0.0;
+            for (int l = 0; l < L; ++l) {
+                for (int k = __ldg(off + l) + T.tid(); k < __ldg(off + l + 1); k += T.size()) {
+                    const int x = __ldg(ids + k);
+                    if (leaf(x)) continue;
+                    double del;
+                    if (at(x, kPin) != 0.0) {
+                        del = 0.0;
+                    } else if (x == root) {
+                        const double E = at(x, kE);
+                        del = E > 0.0 ? at(x, kR) / E : 0.0;
+                    } else if (!freeb(x)) {
+                        del = at(par(x), kDel);
+                    } else {
+                        const double W = at(x, kW);
+                        del = (at(x, kR) + W * at(par(x), kDel)) / (W + at(x, kE));
+                    }
+                    at(x, kDel) = del;
+                    lam += at(x, kRaw) * del;
+                }
+                T.sync();
+            }
+            const double lam2 = T.sum2(lam, 0.0).x;
+            if (!(lam2 * 0.5 > kNewtonTol)) break;
+            // quadratic phase without progress: the rounding floor of this t
+            if (lam2 * 0.5 < 1e-2 && lam2 > 0.25 * lam_prev) break;
+            lam_prev = lam2;
+            // (d) the longest step that keeps every branch inside its bounds
+            double amax = INFINITY;
+            for (int x = T.tid(); x < N; x += T.size()) {
+                if (!active(x)) continue;
+                const int u = par(x);
+                const double d = at(u, kP) - at(x, kP);
+                const double s = at(u, kDel) - at(x, kDel);
+                if (s > 0.0) amax = fmin(amax, (dhi - d) / s);
+                else if (s < 0.0) amax = fmin(amax, (d - dlo) / -s);
+            }
+            amax = T.mind(amax);
+            double alpha = fmin(1.0, 0.99 * amax);
+            // (e) backtracking (Armijo) on the change of the barrier objective
+            bool ok = false;
+            for (int ls = 0; ls < kLineMax; ++ls) {
+                double dphi = 0.0;
+                for (int x = T.tid(); x < N; x += T.size()) {
+                    if (!active(x)) continue;
+                    const int u = par(x);
+                    const double s = alpha * (at(u, kDel) - at(x, kDel));
+                    const double bb = at(x, kB), c = at(x, kC);
+                    double df = -at(x, kA) * s;
+                    if (bb > 0.0) df += bb * log1p32(-expm132(-s) * at(x, kIE));
+                    if (c > 0.0) df += c * log1p32(-expm132(-nu * s) * at(x, kIEN));
+                    dphi += t * df + log1p32(s * at(x, kRL)) + log1p32(-s * at(x, kRH));
+                }
+                dphi = T.sum2(dphi, 0.0).x;
+                if (dphi >= 0.25 * alpha * lam2) {
+                    ok = true;
+                    break;
+                }
+                alpha *= 0.5;
+            }
+            if (!ok) break;   // no measurable ascent left at this t
+            for (int x = T.tid(); x < N; x += T.size())
+                if (!leaf(x) && at(x, kPin) == 0.0) at(x, kP) += alpha * at(x, kDel);
+            T.sync();
+        }
+        if (m / t <= gap_tol) break;
+        t *= kMu;
+    }
+
+    // 4. branch lengths from the heights; the root's branch alone
+    for (int x = T.tid(); x < N; x += T.size()) {
+        if (x == root) {
+            if (!freeb(x)) continue;
+            const double dn = solve_branch(at(x, kA), at(x, kB), at(x, kC), nu, (double)Dd[x],
+                                           dlo, dhi, true);
+            Dd[x] = (float)dn;
+            __stcg(b.nd_d + base + x, dn);
+        } else if (freeb(x)) {
+            const double dn = fmin(fmax(at(par(x), kP) - at(x, kP), dlo), dhi);
+            Dd[x] = (float)dn;
+            __stcg(b.nd_d + base + x, dn);
+        }
+    }
+    T.sync();
+    return true;
+}
 
 template <class Team>
 __device__ void mstep_tree(const laml_batch& b, int p, int rounds, Team& T, float4* s_cnt,
-                           float* s_d, bool polish) {
+                           float* s_d, int flags) {
+    const bool polish = (flags & LAML_MSTEP_FP64_POLISH) != 0;
+    const bool ultra = (flags & LAML_MSTEP_ULTRAMETRIC) != 0 && !b.compat;
     if (__ldcg(b.tr_status + p) != LAML_TREE_ACTIVE) return;
     const int N = __ldg(b.tr_nodes + p), n = __ldg(b.tr_leaves + p), base = __ldg(b.tr_node_base + p);
     const int ds = __ldg(b.tr_ds + p), NG = __ldg(b.ds_groups + ds), K = __ldg(b.ds_sites + ds);
@@ -1516,7 +1927,15 @@ __device__ void mstep_tree(const laml_batch& b, int p, int rounds, Team& T, floa
         const bool last = r == R - 1;
         const bool use_s = compat || nu > kEpsNu;
         const float nuf = (float)nu;
-        if (last && polish) {
+        if (ultra) {
+            // EM_solver.Mstep returns "d_infeasible" before it places any
+            // parameter (EM_solver.py:419-420): the tree keeps d, nu and phi
+            if (!ultra_dstep(b, p, T, nu, use_s, Dd)) {
+                if (T.leader()) b.tr_status[p] = LAML_TREE_INFEASIBLE;
+                T.sync();
+                return;
+            }
+        } else if (last && polish) {
             for (int v = T.tid(); v < N; v += T.size()) {
                 if (!__ldg(b.nd_mask + base + v)) continue;
                 // the FP64 counts for the polished solve
@@ -2271,7 +2690,7 @@ __global__ void __launch_bounds__(kBlock, 4) k_mstep(laml_batch b, int rounds, i
     BlockTeam T{sh};
     for (int p = blockIdx.x; p < b.n_trees; p += gridDim.x) {
         if (skip_big && __ldg(b.tr_nodes + p) > kClusterNodes) continue;
-        mstep_tree(b, p, rounds, T, s_cnt, s_d, (flags & LAML_MSTEP_FP64_POLISH) != 0);
+        mstep_tree(b, p, rounds, T, s_cnt, s_d, flags);
     }
 }
 
@@ -2285,7 +2704,7 @@ __global__ void __cluster_dims__(kMstepCluster, 1, 1) __launch_bounds__(kMstepCl
     const int ncl = gridDim.x / kMstepCluster;
     for (int p = blockIdx.x / kMstepCluster; p < b.n_trees; p += ncl) {
         if (__ldg(b.tr_nodes + p) <= kClusterNodes) continue;   // uniform over the cluster
-        mstep_tree(b, p, rounds, T, nullptr, nullptr, (flags & LAML_MSTEP_FP64_POLISH) != 0);
+        mstep_tree(b, p, rounds, T, nullptr, nullptr, flags);
     }
 }
 
@@ -2431,7 +2850,7 @@ __global__ void __launch_bounds__(kBlock, LAML_MINB) k_em_persistent(laml_batch 
         for_items<G, 3>(b, b.root_items, b.n_root_items, gwarp, nwarps, false, true);
         if (!grid_barrier(b, gen)) return;
         for (int p = blockIdx.x; p < b.n_trees; p += gridDim.x)
-            mstep_tree(b, p, rounds, T, s_cnt, s_d, (flags & LAML_MSTEP_FP64_POLISH) != 0);
+            mstep_tree(b, p, rounds, T, s_cnt, s_d, flags);
         if (!grid_barrier(b, gen)) return;
         for (int l = 0; l < b.n_in_levels; ++l) {
             const int64_t o = b.in_level_off[l], e = b.in_level_off[l + 1];
@@ -2484,6 +2903,15 @@ int validate(const laml_batch* b) {
     }
     if (!b->in_desc || !b->out_desc || !b->grp_desc) {
         laml::set_error("laml_batch: in_desc, out_desc and grp_desc (laml_plan_fill) are required");
+        return LAML_ERR_ARG;
+    }
+    return LAML_OK;
+}
+
+// an M-step flag set the batch cannot serve
+int validate_mstep_flags(const laml_batch* b, int32_t flags, const char* who) {
+    if ((flags & LAML_MSTEP_ULTRAMETRIC) && !b->compat && (!b->nd_uorder || !b->nd_uwork)) {
+        laml::set_error(std::string(who) + ": LAML_MSTEP_ULTRAMETRIC needs nd_uorder and nd_uwork");
         return LAML_ERR_ARG;
     }
     return LAML_OK;
@@ -2748,6 +3176,7 @@ extern "C" int laml_outside(const laml_batch* b, int32_t flags, void* stream) {
 
 extern "C" int laml_mstep(const laml_batch* b, int32_t rounds, int32_t flags, void* stream) {
     int rc = validate(b);
+    if (!rc) rc = validate_mstep_flags(b, flags, "laml_mstep");
     if (rc) return rc;
     return launch_mstep(*b, rounds, flags, (cudaStream_t)stream);
 }
@@ -2755,6 +3184,7 @@ extern "C" int laml_mstep(const laml_batch* b, int32_t rounds, int32_t flags, vo
 extern "C" int laml_em_run(const laml_batch* b, int32_t iters, int32_t rounds, double rel_tol,
                            int32_t max_iters, int32_t flags, void* stream) {
     int rc = validate(b);
+    if (!rc) rc = validate_mstep_flags(b, flags, "laml_em_run");
     if (rc) return rc;
     if (iters <= 0) return LAML_OK;
     DISPATCH_G(*b, (em_persistent_t<GG>(*b, iters, rounds, rel_tol, max_iters, flags,
@@ -2765,6 +3195,7 @@ extern "C" int laml_em_graph_create(const laml_batch* b, int32_t iters, int32_t 
                                     double rel_tol, int32_t max_iters, int32_t flags,
                                     int32_t persistent, void** graph) {
     int rc = validate(b);
+    if (!rc) rc = validate_mstep_flags(b, flags, "laml_em_graph_create");
     if (rc) return rc;
     if (!graph || iters <= 0) {
         laml::set_error("laml_em_graph_create: bad argument");
@@ -2823,6 +3254,7 @@ extern "C" void laml_graph_destroy(void* graph) {
 extern "C" int laml_em_run_levels(const laml_batch* b, int32_t iters, int32_t rounds,
                                   double rel_tol, int32_t max_iters, int32_t flags, void* stream) {
     int rc = validate(b);
+    if (!rc) rc = validate_mstep_flags(b, flags, "laml_em_run_levels");
     if (rc) return rc;
     if (iters <= 0) return LAML_OK;
     DISPATCH_G(*b, (em_levels_t<GG>(*b, iters, rounds, rel_tol, max_iters, flags,

@@ -65,24 +65,44 @@ class TreeResult:
     branch_lengths: np.ndarray
 
 
+def ultra_schedule(trees: Sequence[EncodedTree], node_base: np.ndarray) -> np.ndarray:
+    """nd_uorder of a batch: each tree's laml_ultra_order depth schedule at
+    offset 2 * node_base[p] + 2 * p."""
+    nn = int(sum(t.num_nodes for t in trees))
+    out = np.zeros(2 * nn + 2 * len(trees), np.int32)
+    w = N.i64()
+    for p, t in enumerate(trees):
+        o = 2 * int(node_base[p]) + 2 * p
+        par = np.ascontiguousarray(t.parent, np.int32)
+        N.check(N.lib().laml_ultra_order(par.ctypes.data, t.num_nodes,
+                                         out[o:].ctypes.data, 2 * t.num_nodes + 2, C.byref(w)))
+    return out
+
+
 class DeviceBatch:
     """Trees (EncodedTree) over datasets (EncodedDataset) resident on one GPU.
 
     ``d``: per-tree float64 branch lengths (node order of the tree);
     ``nu``, ``phi``: per-tree starting values; ``mask``: per-tree bool arrays
-    (True = branch length optimised); ``fix_nu`` / ``fix_phi``: per-tree flags.
+    (True = branch length optimised); ``fix_nu`` / ``fix_phi``: per-tree flags;
+    ``ultrametric``: exact model only -- every M-step solves the branch
+    lengths under EM_solver's ultrametric equalities (EM_solver.py:53-89).
     """
 
     def __init__(self, datasets: Sequence[EncodedDataset], trees: Sequence[EncodedTree],
                  tree_ds: Sequence[int], d: Sequence[np.ndarray], nu, phi, compat: bool = True,
                  mask: Optional[Sequence[np.ndarray]] = None, fix_nu=None, fix_phi=None,
-                 want_post: bool = False, device="cuda", stream: Optional[torch.cuda.Stream] = None):
+                 want_post: bool = False, device="cuda", stream: Optional[torch.cuda.Stream] = None,
+                 ultrametric: bool = False):
         G = datasets[0].group_sites
         for ds in datasets:
             if ds.group_sites != G or ds.compat != compat:
                 raise ValueError("every dataset of a batch needs the same group size and mode")
         T = len(trees)
+        if ultrametric and compat:
+            raise ValueError("the ultrametric M-step belongs to the exact model (compat=False)")
         self.T, self.compat, self.G = T, compat, G
+        self.ultrametric = bool(ultrametric)
         self.device = torch.device(device)
         self.stream = stream
         self.trees = list(trees)
@@ -137,6 +157,8 @@ class DeviceBatch:
                      ("tr_nu", nu), ("tr_phi", phi), ("tr_fix", fix),
                      ("nd_d", dcat), ("nd_mask", mcat)]:
             pk.add(k, a)
+        if ultrametric:
+            pk.add("nd_uorder", ultra_schedule(trees, self._node_base))
         for k in ("tr_node_base", "tr_root", "tr_quirk", "tr_site_base", "tr_cnt_base",
                   "tr_post_base", "nd_tree", "nd_c0", "nd_c1", "nd_parent", "nd_sib",
                   "nd_leafrow", "nd_prow", "nd_srow", "in_level_off", "in_items",
@@ -171,6 +193,8 @@ class DeviceBatch:
             "out_desc": e(12 * sizes["n_out_items"], i32),
             "grp_desc": e(8 * sizes["n_groups_total"], i32),
         }
+        if ultrametric:
+            self.work["nd_uwork"] = e(N.UWORK_SLOTS * nn, f64)
         if want_post:
             self.work["post0"] = e(sizes["post_len"], f32)
             self.work["post1"] = e(sizes["post_len"], f32)
@@ -239,31 +263,33 @@ class DeviceBatch:
         # the exact (EM_solver) model polishes its solves in FP64 by default
         return (not self.compat) if polish is None else bool(polish)
 
+    def _mflags(self, polish):
+        return ((N.MSTEP_FP64_POLISH if self._polish(polish) else 0) |
+                (N.MSTEP_ULTRAMETRIC if self.ultrametric else 0))
+
     def mstep(self, rounds=MSTEP_ROUNDS, polish=None):
-        N.check(N.lib().laml_mstep(C.byref(self.b), rounds,
-                                   N.MSTEP_FP64_POLISH if self._polish(polish) else 0,
-                                   self._s()))
+        N.check(N.lib().laml_mstep(C.byref(self.b), rounds, self._mflags(polish), self._s()))
 
     def em_iterations(self, iters, rounds=MSTEP_ROUNDS, rel_tol=None, max_iters=100000,
                       persistent=True, polish=None):
         tol = rel_tol if rel_tol is not None else (EM_STOP_COMPAT if self.compat else EM_STOP_EXACT)
         f = N.lib().laml_em_run if persistent else N.lib().laml_em_run_levels
-        N.check(f(C.byref(self.b), iters, rounds, tol, max_iters,
-                  N.MSTEP_FP64_POLISH if self._polish(polish) else 0, self._s()))
+        N.check(f(C.byref(self.b), iters, rounds, tol, max_iters, self._mflags(polish),
+                  self._s()))
 
     def em_graph(self, iters=1, rounds=MSTEP_ROUNDS, rel_tol=None, max_iters=100000,
                  persistent=False, polish=None):
         """A CUDA graph of ``iters`` EM iterations on this batch (replay with
         ``launch_graph``); cached per argument set."""
         tol = rel_tol if rel_tol is not None else (EM_STOP_COMPAT if self.compat else EM_STOP_EXACT)
-        key = (iters, rounds, tol, max_iters, bool(persistent), self._polish(polish))
+        key = (iters, rounds, tol, max_iters, bool(persistent), self._mflags(polish))
         if not hasattr(self, "_graphs"):
             self._graphs = {}
         if key not in self._graphs:
             h = C.c_void_p()
             N.check(N.lib().laml_em_graph_create(
-                C.byref(self.b), iters, rounds, tol, max_iters,
-                N.MSTEP_FP64_POLISH if key[5] else 0, int(persistent), C.byref(h)))
+                C.byref(self.b), iters, rounds, tol, max_iters, key[5], int(persistent),
+                C.byref(h)))
             self._graphs[key] = h
         return self._graphs[key]
 

@@ -19,10 +19,13 @@ ML_solver / EM_solver / fastEM_solver, laml_libs/*.py):
 * ``get_params()``, ``get_tree_newick()``, ``params.nu`` / ``params.phi``.
 
 Every likelihood, E-step and M-step runs on the GPU; there is no CPU path.
-Only binary trees are supported (a polytomy raises ValueError) and the
-ultrametric equality constraints of EM_solver.Mstep (EM_solver.py:53-89,
-358-361) are not implemented (``ultra_constr=True`` raises
-NotImplementedError).
+Only binary trees are supported (a polytomy raises ValueError).  With
+``ultra_constr=True`` every M-step solves the branch lengths under
+EM_solver's ultrametric equalities (EM_solver.py:53-89, 358-361) on the
+device; the equalities that tie the roots of several trees together are not
+implemented (``ultra_constr=True`` with more than one tree raises
+NotImplementedError).  Constraints without a solution end the EM with status
+"d_infeasible", as EM_solver.EM_optimization does (EM_solver.py:491-495).
 """
 from __future__ import annotations
 
@@ -32,6 +35,7 @@ from typing import List, Optional
 import numpy as np
 
 from .encoding import EncodedTree, char_matrix, encode_dataset, encode_newick
+from ._native import TREE_INFEASIBLE
 from .engine import MSTEP_ROUNDS, DeviceBatch
 from .fast_em.phylogeny import Phylogeny, build_phylogeny, tree_to_networkx
 
@@ -223,9 +227,9 @@ class fastEM_solver:
                  max_trials=100, random_seeds=None, ultra_constr=False):
         """EM_solver.optimize_one from ``initials`` starting points (the best
         nllh wins), seeds as ML_solver.optimize (ML_solver.py:263-282)."""
-        if ultra_constr:
-            raise NotImplementedError("ultrametric-constrained M-step is not implemented; "
-                                      "call with ultra_constr=False")
+        if ultra_constr and len(self.trees) > 1:
+            raise NotImplementedError("ultra_constr=True ties the roots of several trees "
+                                      "together (EM_solver.py:81-84); not implemented")
         if random_seeds is None:
             rseeds = [int(_random.random() * 10000) for _ in range(initials)]
         elif isinstance(random_seeds, int):
@@ -235,15 +239,16 @@ class fastEM_solver:
             rseeds = list(random_seeds)[:initials]
         best = None
         for rep in range(initials):
-            res = self._optimize_one(rseeds[rep], fixed_phi, fixed_nu, fixed_brlen)
+            res = self._optimize_one(rseeds[rep], fixed_phi, fixed_nu, fixed_brlen,
+                                     ultra_constr)
             if best is None or res[0] < best[0]:
                 best = res
-        nllh, nu, phi, ds = best
+        nllh, nu, phi, ds, status = best
         self.params = Params(nu, phi)
         self._d = ds
-        return nllh, "optimal"
+        return nllh, status
 
-    def _optimize_one(self, randseed, fixed_phi, fixed_nu, fixed_brlen):
+    def _optimize_one(self, randseed, fixed_phi, fixed_nu, fixed_brlen, ultra_constr=False):
         rs = _random.Random(randseed)
         ds, masks = [], []
         for i, t in enumerate(self.trees):
@@ -264,16 +269,19 @@ class fastEM_solver:
                 d[u] = max(2 * DMIN, self._d[i][u]) if has else x[k]
                 k += 1
             ds.append(d)
-        total, out_d = 0.0, []
+        total, out_d, status = 0.0, [], "optimal"
         for i, t in enumerate(self.trees):
             b = DeviceBatch([self._dataset(i, False)], [t], [0], [ds[i]], [nu], [phi],
                             compat=False, mask=[masks[i]], fix_nu=fixed_nu is not None,
-                            fix_phi=fixed_phi is not None, device=self.device)
+                            fix_phi=fixed_phi is not None, device=self.device,
+                            ultrametric=ultra_constr)
             r = b.run_em(max_iters=1000)[0]
+            if r.status == TREE_INFEASIBLE:
+                status = "d_infeasible"
             total += r.llh
             out_d.append(r.branch_lengths)
             nu, phi = r.nu, r.phi
-        return -total, nu, phi, out_d
+        return -total, nu, phi, out_d, status
 
 
 def _ts_postorder(t: EncodedTree):
@@ -289,6 +297,25 @@ def _ts_postorder(t: EncodedTree):
             st.append((int(t.child0[u]), False))
             st.append((int(t.child1[u]), False))
     return out
+
+
+class EM_solver(fastEM_solver):
+    """Drop-in for laml_libs/EM_solver.py's solver class (``--solver EM``):
+    ``score_tree(strategy)`` is ML_solver.score_tree (ML_solver.py:114-123),
+    one exact EM from one initial point with the strategy's
+    ``ultra_constr``, ``fixed_phi``, ``fixed_nu`` and ``fixed_brlen``; the
+    rest of the interface is fastEM_solver's.  Binary trees only: the
+    reference resolves polytomies into eps-length fixed branches
+    (EM_solver.py:26-43); here a polytomy raises ValueError."""
+
+    def __init__(self, treeList, data, prior, params={'nu': 0, 'phi': 0, 'sigma': 0},
+                 group_sites: int = 8, device="cuda"):
+        super().__init__(treeList, data, prior, params, group_sites=group_sites, device=device)
+        self.solver_name = "EM_solver"
+
+    def score_tree(self, strategy={'ultra_constr': False, 'fixed_phi': None, 'fixed_nu': None,
+                                   'fixed_brlen': None}):
+        return self.score_tree_oldEM(strategy)
 
 
 class CandidateScore:

@@ -32,7 +32,8 @@ def make_batch(newicks: Sequence[str], rows: dict, Q, leaf_order: Sequence[str],
                compat: bool = True, group_sites: int = 8, nu=0.5, phi=0.5,
                d: Optional[Sequence[np.ndarray]] = None, mask=None, fix_nu=None, fix_phi=None,
                want_post: bool = False, clamp: bool = True, device="cuda", stream=None,
-               trees: Optional[Sequence[EncodedTree]] = None, dataset=None) -> DeviceBatch:
+               trees: Optional[Sequence[EncodedTree]] = None, dataset=None,
+               ultrametric: bool = False) -> DeviceBatch:
     """One dataset shared by every tree.  With ``clamp`` (compat) the starting
     point is prepared as fast_em/laml.py:128-132 does: nu, phi clipped to
     [EPS, 1-EPS] and d floored at EPS."""
@@ -50,4 +51,4 @@ def make_batch(newicks: Sequence[str], rows: dict, Q, leaf_order: Sequence[str],
         d = [np.maximum(x, EPS) for x in d]
     return DeviceBatch([ds], trees, [0] * len(trees), d, nu, phi, compat=compat, mask=mask,
                        fix_nu=fix_nu, fix_phi=fix_phi, want_post=want_post, device=device,
-                       stream=stream)
+                       stream=stream, ultrametric=ultrametric)

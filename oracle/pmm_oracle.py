@@ -626,13 +626,16 @@ def mstep_compat(counts, leaf_resp_total, R, M, d, nu, phi, branch_mask, fix_nu,
 
 
 def mstep_exact(counts, post1_leaf_missing_sum, R, d, nu, phi, branch_mask, K, ncells,
-                opt_phi=True, opt_nu=True):
+                opt_phi=True, opt_nu=True, ultra_tree: Optional[ParsedTree] = None):
     """EM_solver.Mstep (EM_solver.py:307-459) without MOSEK: closed-form phi
     (318-326), per-branch S normalisation (339-348), d in [dmin, dmax] given
     the old nu (349-366) and nu in [0, 1] given the new d (392-407), each a
     1-D concave problem solved by bisection.  ``counts`` are the full-state
     C00..Cas = S0..S4.  ``post1_leaf_missing_sum`` is sum over '?' leaf
-    entries of P(leaf silenced | D)."""
+    entries of P(leaf silenced | D).  With ``ultra_tree`` the branch lengths
+    are solved jointly under that tree's ultrametric equalities
+    (ultrametric_d) and a fourth item reports whether that solve succeeded
+    (False: EM_solver's "d_infeasible")."""
     d = np.asarray(d, dtype=np.float64).copy()
     nmiss = post1_leaf_missing_sum[1]
     if opt_phi:
@@ -655,8 +658,13 @@ def mstep_exact(counts, post1_leaf_missing_sum, R, d, nu, phi, branch_mask, K, n
     def fp(x):
         return -a + S1 * _inv_expm1(x) + c * nu * _inv_expm1(nu * x)
 
-    dn = _bisect_decreasing(fp, np.full(len(d), DMIN), np.full(len(d), DMAX))
-    d = np.where(mask, dn, d)
+    if ultra_tree is not None:
+        d, ok = ultrametric_d(S, nu, d, mask, ultra_tree)
+        if not ok:
+            return d, nu, phi, False
+    else:
+        dn = _bisect_decreasing(fp, np.full(len(d), DMIN), np.full(len(d), DMAX))
+        d = np.where(mask, dn, d)
     if opt_nu:
         dm = d[mask]
         A = float(np.sum((Sm[:, 0] + Sm[:, 1] + Sm[:, 3]) * dm))
@@ -673,7 +681,140 @@ def mstep_exact(counts, post1_leaf_missing_sum, R, d, nu, phi, branch_mask, K, n
         else:
             nu = float(_bisect_decreasing(np.vectorize(gp), np.array(1e-300), np.array(1.0),
                                           iters=300))
+    if ultra_tree is not None:
+        return d, nu, phi_star, True
     return d, nu, phi_star
+
+
+def ultrametric_constraints(tree: ParsedTree, mask, d):
+    """EM_solver.ultrametric_constr (EM_solver.py:53-89) for one tree: rows M
+    and right-hand sides b of ``M @ d[free] = b``, columns the optimised
+    branches (``mask``) in treeswift postorder.  A node's path vector is its
+    own branch plus its first child's (treeswift's first child: the last
+    networkx successor); each internal node equates its two children's
+    paths, fixed branches entering as constants, and a row whose vector is
+    zero or repeats an earlier row (or its negation) is dropped, as there."""
+    post = treeswift_postorder_ids(tree)
+    mask = np.asarray(mask, bool)
+    free = [x for x in post if mask[x]]
+    col = {x: i for i, x in enumerate(free)}
+    n = len(free)
+    vec, const, rows = {}, {}, {}
+    for x in post:
+        ch = tree.children[x]
+        if not ch:
+            v = np.zeros(n)
+            c = 0.0 if mask[x] else float(d[x])
+        else:
+            c1, c2 = ch[-1], ch[0]
+            m = vec[c1] - vec[c2]
+            if np.any(m != 0):
+                key, neg = tuple(m), tuple(-m)
+                if key not in rows and neg not in rows:
+                    rows[key] = const[c2] - const[c1]
+            v = vec[c1].copy()
+            c = const[c1] + (0.0 if mask[x] else float(d[x]))
+        if mask[x]:
+            v[col[x]] = 1.0
+        vec[x], const[x] = v, c
+    M = np.array([list(k) for k in rows], dtype=np.float64).reshape(len(rows), n)
+    b = np.array(list(rows.values()), dtype=np.float64)
+    return M, b, np.array(free, dtype=np.int64)
+
+
+def ultrametric_d(S, nu, d, mask, tree: ParsedTree):
+    """The branch-length part of EM_solver.Mstep with ultra_constr_cache
+    (EM_solver.py:349-366): maximise over the optimised branches
+    sum -a d + S1 log(1-e^{-d}) + c log(1-e^{-nu d}) with d in [dmin, dmax]
+    and ``M d = b`` (ultrametric_constraints).  The reference hands this to
+    MOSEK (absent here).  This restatement: a strictly feasible start from a
+    linear program (maximise the smallest slack to the bounds on the affine
+    set), then a dense log-barrier Newton method in the null space of M
+    (FP64, duality gap below 1e-11 relative).  Returns (d, ok); ok is False
+    when the constraints leave no interior point (EM_solver's
+    "d_infeasible")."""
+    from scipy import linalg, optimize
+
+    S0, S1, S2, S3, S4 = (S[:, i] for i in range(5))
+    use_s = nu > EPS_NU
+    M, rhs, free = ultrametric_constraints(tree, mask, d)
+    n = len(free)
+    out = np.asarray(d, np.float64).copy()
+    if n == 0:
+        return out, True
+    a = ((nu + 1) * S0 + nu * S1 + nu * S3)[free]
+    b = S1[free]
+    c = (S2 + S4)[free] if use_s else np.zeros(n)
+    # strictly feasible start: max s s.t. M x = rhs, DMIN + s <= x <= DMAX - s
+    cost = np.zeros(n + 1)
+    cost[-1] = -1.0
+    A_ub = np.zeros((2 * n, n + 1))
+    A_ub[:n, :n] = -np.eye(n)
+    A_ub[:n, -1] = 1.0
+    A_ub[n:, :n] = np.eye(n)
+    A_ub[n:, -1] = 1.0
+    b_ub = np.concatenate([np.full(n, -DMIN), np.full(n, DMAX)])
+    A_eq = np.hstack([M, np.zeros((len(rhs), 1))]) if len(rhs) else None
+    lp = optimize.linprog(cost, A_ub=A_ub, b_ub=b_ub, A_eq=A_eq,
+                          b_eq=rhs if len(rhs) else None,
+                          bounds=[(None, None)] * n + [(None, (DMAX - DMIN) / 2)],
+                          method="highs")
+    if lp.status != 0 or lp.x[-1] <= 1e-12:
+        return out, False
+    x = lp.x[:n].copy()
+    Z = linalg.null_space(M) if len(rhs) else np.eye(n)
+    if Z.shape[1] == 0:
+        out[free] = x
+        return out, True
+
+    def fval(x):
+        v = -a * x + b * _log1mexp(x)
+        if use_s:
+            v = v + c * _log1mexp(nu * x)
+        return float(np.sum(v))
+
+    def derivs(x):
+        e = np.expm1(x)
+        g = -a + b / e
+        h = -b * (e + 1) / (e * e)
+        if use_s:
+            en = np.expm1(nu * x)
+            g = g + c * nu / en
+            h = h - c * nu * nu * (en + 1) / (en * en)
+        return g, h
+
+    def barrier(x, t):
+        return t * fval(x) + float(np.sum(np.log(x - DMIN) + np.log(DMAX - x)))
+
+    m = 2.0 * n
+    tol = 1e-11 * (abs(fval(x)) + 1.0)
+    t = 1.0
+    for _ in range(60):
+        for _ in range(100):
+            g, h = derivs(x)
+            gb = t * g + 1.0 / (x - DMIN) - 1.0 / (DMAX - x)
+            hb = t * h - 1.0 / (x - DMIN) ** 2 - 1.0 / (DMAX - x) ** 2
+            gy = Z.T @ gb
+            Hy = (Z.T * -hb) @ Z
+            dy = np.linalg.solve(Hy, gy)
+            lam2 = float(gy @ dy)
+            if lam2 / 2 <= 1e-12:
+                break
+            dx = Z @ dy
+            with np.errstate(divide="ignore"):
+                lim = np.where(dx > 0, (DMAX - x) / dx, np.where(dx < 0, (x - DMIN) / -dx, np.inf))
+            alpha = min(1.0, 0.99 * float(np.min(lim)))
+            f0 = barrier(x, t)
+            while alpha > 1e-20 and barrier(x + alpha * dx, t) < f0 + 0.25 * alpha * lam2:
+                alpha *= 0.5
+            if alpha <= 1e-20:
+                break
+            x = x + alpha * dx
+        if m / t <= tol:
+            break
+        t *= 10.0
+    out[free] = np.clip(x, DMIN, DMAX)
+    return out, True
 
 
 # ----------------------------------------------------------------------------
@@ -687,6 +828,7 @@ class EMResult:
     phi: float
     iterations: int
     trace: List[float] = field(default_factory=list)
+    status: str = "optimal"
 
 
 def em_compat(prob: Problem, d, nu, phi, branch_mask=None, fix_nu=False, fix_phi=False,
@@ -736,10 +878,12 @@ def exact_leaf_stats(prob: Problem, es: EStep):
 
 
 def em_exact(prob: Problem, d, nu, phi, branch_mask=None, fix_nu=False, fix_phi=False,
-             max_iters=1000, stop=None) -> EMResult:
+             max_iters=1000, stop=None, ultra=False) -> EMResult:
     """EM_solver.EM_optimization (EM_solver.py:461-512): E-step, M-step,
     logL; stop when |(cur-pre)/pre| < conv_eps = 1e-8 (``stop``; negative:
-    never) or after 1000 iterations."""
+    never) or after 1000 iterations.  ``ultra``: M-steps under the
+    ultrametric equalities; a failed solve ends the EM with the
+    log-likelihood before it and status "d_infeasible" (EM_solver.py:491-495)."""
     stop = CONV_EPS_EXACT if stop is None else stop
     N = len(prob.tree.parent)
     d = np.asarray(d, dtype=np.float64).copy()
@@ -753,8 +897,12 @@ def em_exact(prob: Problem, d, nu, phi, branch_mask=None, fix_nu=False, fix_phi=
     while it <= max_iters:
         es = e_step(prob, d, nu, phi)
         lstat, R = exact_leaf_stats(prob, es)
-        d, nu, phi = mstep_exact(es.counts, lstat, R, d, nu, phi, mask, K, ncells,
-                                 opt_phi=not fix_phi, opt_nu=not fix_nu)
+        out = mstep_exact(es.counts, lstat, R, d, nu, phi, mask, K, ncells,
+                          opt_phi=not fix_phi, opt_nu=not fix_nu,
+                          ultra_tree=prob.tree if ultra else None)
+        if ultra and not out[3]:
+            return EMResult(pre, d, nu, phi, it, trace, "d_infeasible")
+        d, nu, phi = out[:3]
         cur, _ = log_likelihood(prob, d, nu, phi)
         trace.append(cur)
         if abs((cur - pre) / pre) < stop:

@@ -8,7 +8,9 @@ It reads the reference's unit-test *sources as text* (``ast`` on
 laml_unit_tests/unit_tests_EMSolver.py and unit_tests_MLSolver.py) and pulls
 out every known-answer case: the literal ``Q``, ``T``, ``msa``, ``phi``,
 ``nu`` and ``true_nllh`` of the likelihood tests, and the arguments of each
-``__test_outllh__`` call (the reduced-tree outside identity tests).  It also
+``__test_outllh__`` call (the reduced-tree outside identity tests); from
+unit_tests_TopoSearch.py the ultrametric brute-force case with its
+pre-computed optimum.  It also
 copies the small data fixtures those tests load (test_EM/test1 and test4).
 Nothing here imports or runs reference code.
 """
@@ -89,6 +91,44 @@ def extract(path, source_name):
     return llh, outside
 
 
+def extract_ultrametric(path, source_name):
+    """The ultrametric brute-force cases of unit_tests_TopoSearch.py: tests
+    whose brute-force search runs with ultra_constr=True and whose source
+    keeps the pre-computed optimum in a ``nllh_bf = <value>`` comment
+    (test_10: 7.0063474330891236, the best ultrametric nllh over every
+    rooted topology of the four leaves)."""
+    import re
+    text = open(path).read()
+    lines = text.splitlines()
+    tree = ast.parse(text)
+    out = []
+    for cls in tree.body:
+        if not isinstance(cls, ast.ClassDef):
+            continue
+        for fn in cls.body:
+            if not isinstance(fn, ast.FunctionDef) or not fn.name.startswith("test_"):
+                continue
+            src = "\n".join(lines[fn.lineno - 1:fn.end_lineno])
+            m = re.search(r"nllh_bf\s*=\s*([0-9.eE+-]+)\s*#", src)
+            vals = _literal_assigns(fn)
+            leaves = None
+            ultra = False
+            for node in ast.walk(fn):
+                if isinstance(node, ast.Call) and isinstance(node.func, ast.Attribute) and \
+                        node.func.attr == "__brute_force_search__" and len(node.args) >= 3:
+                    try:
+                        leaves = ast.literal_eval(node.args[2])
+                    except Exception:
+                        leaves = None
+                    ultra = any(k.arg == "ultra_constr" and getattr(k.value, "value", None) is True
+                                for k in node.keywords)
+            if m and ultra and leaves and "Q" in vals and "msa" in vals:
+                out.append({"name": f"{source_name}:{fn.name}:{fn.lineno}",
+                            "Q": _jsonable(vals["Q"]), "msa": _jsonable(vals["msa"]),
+                            "leaves": leaves, "nllh_bf": float(m.group(1))})
+    return out
+
+
 def main(ref):
     ut = os.path.join(ref, "laml_unit_tests")
     llh, outside = [], []
@@ -96,13 +136,16 @@ def main(ref):
         a, b = extract(os.path.join(ut, f), "laml_unit_tests/" + f)
         llh += a
         outside += b
+    ultra = extract_ultrametric(os.path.join(ut, "unit_tests_TopoSearch.py"),
+                                "laml_unit_tests/unit_tests_TopoSearch.py")
     with open(os.path.join(HERE, "known_answers.json"), "w") as fo:
-        json.dump({"llh": llh, "outside": outside}, fo, indent=1)
+        json.dump({"llh": llh, "outside": outside, "ultrametric": ultra}, fo, indent=1)
     td = os.path.join(ut, "test_data", "test_EM")
     for f in ("test1.tre", "test1_charMtrx.txt", "test4.tre", "test4_charMtrx.txt",
               "test4_prior.csv"):
         shutil.copyfile(os.path.join(td, f), os.path.join(HERE, f))
-    print(f"{len(llh)} likelihood cases, {len(outside)} outside cases")
+    print(f"{len(llh)} likelihood cases, {len(outside)} outside cases, "
+          f"{len(ultra)} ultrametric brute-force cases")
 
 
 if __name__ == "__main__":

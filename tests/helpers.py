@@ -20,6 +20,31 @@ def known_answers():
         [{**c, "Q": _undict(c["Q"]), "msa": _undict(c["msa"])} for c in d["outside"]]
 
 
+def ultrametric_cases():
+    """The ultrametric brute-force known answers (unit_tests_TopoSearch.py)."""
+    with open(os.path.join(GOLDEN, "known_answers.json")) as f:
+        d = json.load(f)
+    return [{**c, "Q": _undict(c["Q"]), "msa": _undict(c["msa"])} for c in d["ultrametric"]]
+
+
+def rooted_topologies(leaves):
+    """Every rooted binary topology on ``leaves`` as a newick string (15 for
+    four leaves), children sorted so each topology appears once."""
+    import itertools
+    if len(leaves) == 1:
+        return [leaves[0]]
+    out = set()
+    first, rest = leaves[0], list(leaves[1:])
+    for k in range(len(rest)):
+        for comb in itertools.combinations(rest, k):
+            left = [first, *comb]
+            right = [x for x in rest if x not in comb]
+            for a in rooted_topologies(left):
+                for b in rooted_topologies(right):
+                    out.add("(" + ",".join(sorted([a, b])) + ")")
+    return sorted(out)
+
+
 def read_char_matrix(path, masked_symbol="?"):
     """sequence_lib.read_charMtrx (sequence_lib.py:139-175): first row holds
     site names; '?', the masked symbol, letters and negative integers become
