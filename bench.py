@@ -430,6 +430,75 @@ def run_workload(args):
     print(json.dumps(line), flush=True)
 
 
+def run_ultra(args):
+    """ultra250: EM_solver's default final optimisation (runner.py:287 calls
+    optimize with ultra_constr=True) on the 250-leaf, 30-site configuration:
+    the exact EM from a random start (ML_solver.ini_all's ranges) with every
+    M-step solved under the ultrametric equalities, to the 1e-8 stopping
+    rule.  One JSON line: EM iterations/s over the whole run, the time of
+    one ultrametric M-step alone, and the oracle's ultrametric EM (NumPy E-step,
+    LP start + dense barrier M-step) timed on the same tree for 3 iterations."""
+    import numpy as np
+    import torch
+
+    from laml_gb300 import problem as PB
+    from laml_gb300 import synth
+
+    w = synth.workload_config("fixed250", seed=args.seed)
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    stream = torch.cuda.Stream(dev)
+    rng = np.random.default_rng(args.seed + 7)
+    trees = PB.encode_trees(w.newicks, w.leaf_order)
+    N_ = trees[0].num_nodes
+    d0 = rng.uniform(2 * 0.005, 10.0 / 2, N_)        # ML_solver.ini_all's range
+    nu0, phi0 = float(rng.random() * 0.99), float(rng.random() * 0.99)
+    with torch.cuda.stream(stream):
+        b = PB.make_batch(w.newicks, w.rows, w.Q, w.leaf_order, compat=False, nu=nu0, phi=phi0,
+                          d=[d0], clamp=False, ultrametric=True, device=dev, stream=stream,
+                          trees=trees)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        t0 = time.perf_counter()
+        e0.record(stream)
+        r = b.run_em(max_iters=1000, chunk=4)[0]
+        e1.record(stream)
+        stream.synchronize()
+        wall = time.perf_counter() - t0
+        ms = e0.elapsed_time(e1)
+        b.e_step()
+        ms_m = _timed(lambda: b.mstep(), stream, max(3, min(args.steps, 10)))
+    b.check_device_error()
+    t = trees[0]
+    paths = []
+    for leaf in range(t.num_leaves):
+        x, acc = leaf, 0.0
+        while t.parent[x] >= 0:
+            acc += r.branch_lengths[x]
+            x = t.parent[x]
+        paths.append(acc)
+    ds = b.datasets[0]
+    line = {"metric": METRIC, "mode": "ultra250", "n_gpus": 1, "dtype": "f64 heights, f32 cores",
+            "data": "synthetic",
+            "config": {"workload": "ultra250", "leaves": t.num_leaves, "sites": ds.n_sites,
+                       "nodes": N_, "model": "exact (EM_solver)", "ultra_constr": True},
+            "value": r.iterations / (ms / 1e3), "unit": "EM iters/s",
+            "em_iterations": r.iterations, "em_seconds": ms / 1e3, "wall_seconds": wall,
+            "ultrametric_mstep_ms": ms_m, "llh": r.llh, "status": r.status,
+            "root_to_leaf_spread": float(np.ptp(paths))}
+    if not args.no_cpu:
+        from oracle import pmm_oracle as O
+        tr = O.parse_tree(w.newicks[0], w.leaf_order)
+        enc = O.recode([w.rows[c] for c in w.leaf_order], w.Q, compat=False)
+        prob = O.Problem(tr, enc, False)
+        t0 = time.perf_counter()
+        O.em_exact(prob, d0, nu0, phi0, max_iters=3, stop=-1.0, ultra=True)
+        dt = time.perf_counter() - t0
+        line["cpu_baseline"] = {"value": 3 / dt, "unit": "EM iters/s", "cores": 1, "kind": "port",
+                                "sample": "the same tree and start, 3 EM iterations of the "
+                                          "oracle's ultrametric EM (NumPy FP64)"}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -451,7 +520,7 @@ def main():
     ap.add_argument("--trees", type=int, default=512,
                     help="use the first N candidates (smaller cases for profiling)")
     ap.add_argument("--workload", default="nni512",
-                    choices=["nni512", "fixed250", "grad4096", "large50k"],
+                    choices=["nni512", "fixed250", "grad4096", "large50k", "ultra250"],
                     help="nni512 (the default bench line) or one of the other configurations")
     ap.add_argument("--passes-only", action="store_true",
                     help="one inside and one outside pass of --trees candidates (profiling)")
@@ -468,6 +537,8 @@ def main():
         return run_reference(args)
     if args.serving:
         return run_serving(args)
+    if args.workload == "ultra250":
+        return run_ultra(args)
     if args.workload != "nni512":
         return run_workload(args)
     if args.passes_only:

@@ -73,7 +73,6 @@ constexpr int kChunk = LAML_CHUNK;   // states loaded ahead per step of a state 
 #endif
 constexpr int kMstepStage = 2048;    // branches of a tree staged in shared memory by the M-step
 constexpr int kOStash = 24;          // words per thread the outside item parks in shared memory
-static_assert(kItemsBlock <= kBlock, "the outside item's shared-memory stash has kBlock columns");
 
 // ---------------------------------------------------------------------------
 // small helpers
@@ -930,9 +929,106 @@ __device__ __forceinline__ void outside_states(const float* __restrict__ urow, f
     B.sumx = sb; B.dot = db; B.mx = mb;
 }
 
-template <int G>
+// ---------------------------------------------------------------------------
+// Per-thread asynchronous staging of the inside state loop (wide levels).  Each
+// thread copies its own coming slots of the rows it reads (cp.async, 4 bytes
+// each, into its own column of shared memory: word w of thread t at
+// sm[w * S + t], S = block size) kAsStages - 1 chunks of kAsChunk slots
+// ahead of the chunk it computes, so the memory latency of a slot is paid
+// once per item rather than once per chunk, without holding the data in
+// flight in registers.  No thread reads another's column, so the only
+// synchronisation is the thread's own cp.async.wait_group.
+// ---------------------------------------------------------------------------
+#ifndef LAML_AS_CHUNK
+#define LAML_AS_CHUNK 4
+#endif
+#ifndef LAML_AS_STAGES
+#define LAML_AS_STAGES 4
+#endif
+constexpr int kAsChunk = LAML_AS_CHUNK;
+constexpr int kAsStages = LAML_AS_STAGES;
+static_assert(kAsStages >= 2, "at least one chunk in flight");
+
+__device__ __forceinline__ void cp_async4(float* dst, const float* src) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n"
+                 :: "r"((uint32_t)__cvta_generic_to_shared(dst)), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() {
+    asm volatile("cp.async.commit_group;\n" ::: "memory");
+}
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+    asm volatile("cp.async.wait_group %0;\n" :: "n"(N) : "memory");
+}
+
+// the rows of slots j0 .. j0 + kAsChunk - 1 (those below C) into one stage
+// of NR words per slot; row r is skipped when it is a leaf's (computed)
+template <int G, int NR>
+__device__ __forceinline__ void as_issue(float* st, int S, int j0, int C,
+                                         const float* const (&rows)[NR], const bool (&live)[NR]) {
+#pragma unroll
+    for (int k = 0; k < kAsChunk; ++k) {
+        const int j = j0 + k;
+        if (j < C) {
+#pragma unroll
+            for (int r = 0; r < NR; ++r)
+                if (live[r]) cp_async4(st + (k * NR + r) * S, rows[r] + j * G);
+        }
+    }
+    cp_async_commit();   // every call commits a group, so wait counts stay uniform
+}
+
+template <int G, bool VL, bool WL>
+__device__ __forceinline__ void inside_states_as(const Child& cv, const Child& cw,
+                                                 const float4& bv, const float4& bw,
+                                                 const float* __restrict__ qrow,
+                                                 float* __restrict__ row, int C, float& dot,
+                                                 float& mx, float* sm, int S) {
+    constexpr int NR = 2, per = kAsChunk * NR;
+    const float* const rows[NR] = {cv.row, cw.row};
+    const bool live[NR] = {!VL, !WL};
+    const float cstv = cv.code == -1 ? cv.ephi : 0.f, cstw = cw.code == -1 ? cw.ephi : 0.f;
+    const float kv = bv.w * cv.ss, kw = bw.w * cw.ss;
+    const int nch = (C - 2 + kAsChunk - 1) / kAsChunk;
+#pragma unroll
+    for (int c = 0; c < kAsStages - 1; ++c) {
+        if (c < nch) as_issue<G, NR>(sm + (c % kAsStages) * per * S, S, 2 + c * kAsChunk, C, rows, live);
+        else cp_async_commit();
+    }
+    for (int ch = 0; ch < nch; ++ch) {
+        cp_async_wait<kAsStages - 2>();
+        const float* st = sm + (ch % kAsStages) * per * S;
+        const int j0 = 2 + ch * kAsChunk;
+#pragma unroll
+        for (int k = 0; k < kAsChunk; ++k) {
+            const int j = j0 + k;
+            if (j < C) {
+                const float av = VL ? (cv.code == j ? cv.e1 : cstv) : st[(k * NR) * S] * cv.f;
+                const float aw = WL ? (cw.code == j ? cw.e1 : cstw) : st[(k * NR + 1) * S] * cw.f;
+                const float x = fmaf(bv.z, av, kv) * fmaf(bw.z, aw, kw);
+                __stcg(row + j * G, x);
+                dot = fmaf(__ldg(qrow + j * G), x, dot);
+                mx = fmaxf(mx, x);
+            }
+        }
+        const int nx = ch + kAsStages - 1;
+        if (nx < nch) as_issue<G, NR>(sm + (nx % kAsStages) * per * S, S, 2 + nx * kAsChunk, C, rows, live);
+        else cp_async_commit();
+    }
+}
+
+// shared-memory words per thread of the wide-level item kernels: the inside
+// item's staging ring, the outside item's stash (its state loop reads global
+// memory directly: staging it doubled the load/store unit's work per element
+// and measured slower)
+template <int KIND>
+constexpr int as_words() {
+    return KIND == 1 ? kOStash : kAsStages * kAsChunk * 2;
+}
+
+template <int G, bool AS = false>
 __device__ void inside_item_d(const laml_batch& b, const ItemDesc& d, int lane,
-                              bool respect_status) {
+                              bool respect_status, float* sm = nullptr) {
     SiteCtx s;
     GroupCtx gc;
     if (!site_ctx_d<G>(b, d, lane, respect_status, s, gc)) return;
@@ -959,11 +1055,22 @@ __device__ void inside_item_d(const laml_batch& b, const ItemDesc& d, int lane,
     __stcg(row, s0);
     __stcg(row + G, ss);
     float mx = fmaxf(s0, ss), dot = 0.f;
-    switch ((cv.row ? 0 : 1) | (cw.row ? 0 : 2)) {   // warp-uniform: items are sorted by it
-        case 0: inside_states<G, false, false>(cv, cw, bv, bw, s.qrow, row, s.C, dot, mx); break;
-        case 1: inside_states<G, true, false>(cv, cw, bv, bw, s.qrow, row, s.C, dot, mx); break;
-        case 2: inside_states<G, false, true>(cv, cw, bv, bw, s.qrow, row, s.C, dot, mx); break;
-        default: inside_states<G, true, true>(cv, cw, bv, bw, s.qrow, row, s.C, dot, mx); break;
+    if constexpr (AS) {
+        float* tsm = sm + threadIdx.x;
+        constexpr int S = kItemsBlock;   // k_items runs kItemsBlock threads a block
+        switch ((cv.row ? 0 : 1) | (cw.row ? 0 : 2)) {   // warp-uniform: items are sorted by it
+            case 0: inside_states_as<G, false, false>(cv, cw, bv, bw, s.qrow, row, s.C, dot, mx, tsm, S); break;
+            case 1: inside_states_as<G, true, false>(cv, cw, bv, bw, s.qrow, row, s.C, dot, mx, tsm, S); break;
+            case 2: inside_states_as<G, false, true>(cv, cw, bv, bw, s.qrow, row, s.C, dot, mx, tsm, S); break;
+            default: inside_states<G, true, true>(cv, cw, bv, bw, s.qrow, row, s.C, dot, mx); break;
+        }
+    } else {
+        switch ((cv.row ? 0 : 1) | (cw.row ? 0 : 2)) {   // warp-uniform: items are sorted by it
+            case 0: inside_states<G, false, false>(cv, cw, bv, bw, s.qrow, row, s.C, dot, mx); break;
+            case 1: inside_states<G, true, false>(cv, cw, bv, bw, s.qrow, row, s.C, dot, mx); break;
+            case 2: inside_states<G, false, true>(cv, cw, bv, bw, s.qrow, row, s.C, dot, mx); break;
+            default: inside_states<G, true, true>(cv, cw, bv, bw, s.qrow, row, s.C, dot, mx); break;
+        }
     }
     const int h = scale_exp(mx);
     const float f = pow2i(-h);
@@ -976,9 +1083,9 @@ __device__ void inside_item_d(const laml_batch& b, const ItemDesc& d, int lane,
         root_site_llh(b, s.tree, s.site, root_edge_logs(b, s.tree), s0 * f, dot * f, ss * f, X);
 }
 
-template <int G>
+template <int G, bool AS = false>
 __device__ void outside_item_d(const laml_batch& b, const ItemDesc& d, int lane, bool act,
-                               bool want_post) {
+                               bool want_post, float* sm = nullptr) {
     float cv_[8] = {0, 0, 0, 0, 0, 0, 0, 0}, cw_[8] = {0, 0, 0, 0, 0, 0, 0, 0};
     SiteCtx s;
     GroupCtx gc;
@@ -1020,50 +1127,59 @@ __device__ void outside_item_d(const laml_batch& b, const ItemDesc& d, int lane,
         B.sumx = B.dot = B.mx = 0.f;
         A.orow = cv.row ? b.out_part + (int64_t)d.v_ref * 8 + s.goff + lane : nullptr;
         B.orow = cw.row ? b.out_part + (int64_t)d.w_ref * 8 + s.goff + lane : nullptr;
-        // what child_finish needs after the state loop waits in shared memory
-        // (one column per thread; read back through volatile loads, so the
-        // values do not stay live in registers across the loop, which
-        // otherwise spills at this kernel's 80-register budget)
-        __shared__ float ostash[kOStash * kBlock];
-        {
-            float* sp = ostash + threadIdx.x;
-            sp[0 * kBlock] = cv.s0; sp[1 * kBlock] = cv.ss; sp[2 * kBlock] = cv.D;
-            sp[3 * kBlock] = __int_as_float(cv.X); sp[4 * kBlock] = __int_as_float(cv.code);
-            sp[5 * kBlock] = cw.s0; sp[6 * kBlock] = cw.ss; sp[7 * kBlock] = cw.D;
-            sp[8 * kBlock] = __int_as_float(cw.X); sp[9 * kBlock] = __int_as_float(cw.code);
-            sp[10 * kBlock] = bv.x; sp[11 * kBlock] = bv.y; sp[12 * kBlock] = bv.w;
-            sp[13 * kBlock] = bw.x; sp[14 * kBlock] = bw.y; sp[15 * kBlock] = bw.w;
-            sp[16 * kBlock] = A.x0; sp[17 * kBlock] = A.xs; sp[18 * kBlock] = __int_as_float(A.X);
-            sp[19 * kBlock] = B.x0; sp[20 * kBlock] = B.xs; sp[21 * kBlock] = __int_as_float(B.X);
-            sp[22 * kBlock] = bv.z; sp[23 * kBlock] = bw.z;
-        }
-        switch ((cv.row ? 0 : 1) | (cw.row ? 0 : 2)) {   // warp-uniform: items are sorted by it
-            case 0: outside_states<G, false, false>(urow, fo, cv, cw, bv, bw, s.qrow, s.C, A, B); break;
-            case 1: outside_states<G, true, false>(urow, fo, cv, cw, bv, bw, s.qrow, s.C, A, B); break;
-            case 2: outside_states<G, false, true>(urow, fo, cv, cw, bv, bw, s.qrow, s.C, A, B); break;
-            default: outside_states<G, true, true>(urow, fo, cv, cw, bv, bw, s.qrow, s.C, A, B); break;
-        }
-        const volatile float* vp = ostash + threadIdx.x;
-        Child cv2, cw2;   // child_finish reads row only as "leaf or not"
-        cv2.s0 = vp[0 * kBlock]; cv2.ss = vp[1 * kBlock]; cv2.D = vp[2 * kBlock];
-        cv2.X = __float_as_int(vp[3 * kBlock]); cv2.code = __float_as_int(vp[4 * kBlock]);
-        cv2.row = (d.flags & 1) ? nullptr : b.in_part;
-        cw2.s0 = vp[5 * kBlock]; cw2.ss = vp[6 * kBlock]; cw2.D = vp[7 * kBlock];
-        cw2.X = __float_as_int(vp[8 * kBlock]); cw2.code = __float_as_int(vp[9 * kBlock]);
-        cw2.row = (d.flags & 2) ? nullptr : b.in_part;
-        const float4 bv2 = make_float4(vp[10 * kBlock], vp[11 * kBlock], vp[22 * kBlock],
-                                       vp[12 * kBlock]);
-        const float4 bw2 = make_float4(vp[13 * kBlock], vp[14 * kBlock], vp[23 * kBlock],
-                                       vp[15 * kBlock]);
-        A.x0 = vp[16 * kBlock]; A.xs = vp[17 * kBlock]; A.X = __float_as_int(vp[18 * kBlock]);
-        B.x0 = vp[19 * kBlock]; B.xs = vp[20 * kBlock]; B.X = __float_as_int(vp[21 * kBlock]);
-        A.orow = (d.flags & 1) ? nullptr : b.out_part + (int64_t)d.v_ref * 8 + s.goff + lane;
-        B.orow = (d.flags & 2) ? nullptr : b.out_part + (int64_t)d.w_ref * 8 + s.goff + lane;
         const int64_t t = __ldg(b.tr_site_base + s.tree) + s.site;
-        const float lroot = __ldcg(b.root_lr + t);
-        const int xroot = __ldcg(b.root_x + t);
-        child_finish<G>(b, s, d.v, cv2, bv2, A, want_post, lroot, xroot, cv_);
-        child_finish<G>(b, s, d.w, cw2, bw2, B, want_post, lroot, xroot, cw_);
+        if constexpr (AS) {
+            // what child_finish needs after the state loop waits in this
+            // thread's shared-memory column, read back through volatile loads,
+            // so it does not stay live in registers across the loop (which
+            // otherwise spills at this kernel's 80-register budget)
+            constexpr int S = kItemsBlock;   // k_items runs kItemsBlock threads a block
+            float* sp = sm + threadIdx.x;
+            sp[0 * S] = cv.s0; sp[1 * S] = cv.ss; sp[2 * S] = cv.D;
+            sp[3 * S] = __int_as_float(cv.X); sp[4 * S] = __int_as_float(cv.code);
+            sp[5 * S] = cw.s0; sp[6 * S] = cw.ss; sp[7 * S] = cw.D;
+            sp[8 * S] = __int_as_float(cw.X); sp[9 * S] = __int_as_float(cw.code);
+            sp[10 * S] = bv.x; sp[11 * S] = bv.y; sp[12 * S] = bv.w;
+            sp[13 * S] = bw.x; sp[14 * S] = bw.y; sp[15 * S] = bw.w;
+            sp[16 * S] = A.x0; sp[17 * S] = A.xs; sp[18 * S] = __int_as_float(A.X);
+            sp[19 * S] = B.x0; sp[20 * S] = B.xs; sp[21 * S] = __int_as_float(B.X);
+            sp[22 * S] = bv.z; sp[23 * S] = bw.z;
+            switch ((cv.row ? 0 : 1) | (cw.row ? 0 : 2)) {   // warp-uniform: items are sorted by it
+                case 0: outside_states<G, false, false>(urow, fo, cv, cw, bv, bw, s.qrow, s.C, A, B); break;
+                case 1: outside_states<G, true, false>(urow, fo, cv, cw, bv, bw, s.qrow, s.C, A, B); break;
+                case 2: outside_states<G, false, true>(urow, fo, cv, cw, bv, bw, s.qrow, s.C, A, B); break;
+                default: outside_states<G, true, true>(urow, fo, cv, cw, bv, bw, s.qrow, s.C, A, B); break;
+            }
+            const volatile float* vp = sp;
+            Child cv2, cw2;   // child_finish reads row only as "leaf or not"
+            cv2.s0 = vp[0 * S]; cv2.ss = vp[1 * S]; cv2.D = vp[2 * S];
+            cv2.X = __float_as_int(vp[3 * S]); cv2.code = __float_as_int(vp[4 * S]);
+            cv2.row = (d.flags & 1) ? nullptr : b.in_part;
+            cw2.s0 = vp[5 * S]; cw2.ss = vp[6 * S]; cw2.D = vp[7 * S];
+            cw2.X = __float_as_int(vp[8 * S]); cw2.code = __float_as_int(vp[9 * S]);
+            cw2.row = (d.flags & 2) ? nullptr : b.in_part;
+            const float4 bv2 = make_float4(vp[10 * S], vp[11 * S], vp[22 * S], vp[12 * S]);
+            const float4 bw2 = make_float4(vp[13 * S], vp[14 * S], vp[23 * S], vp[15 * S]);
+            A.x0 = vp[16 * S]; A.xs = vp[17 * S]; A.X = __float_as_int(vp[18 * S]);
+            B.x0 = vp[19 * S]; B.xs = vp[20 * S]; B.X = __float_as_int(vp[21 * S]);
+            A.orow = (d.flags & 1) ? nullptr : b.out_part + (int64_t)d.v_ref * 8 + s.goff + lane;
+            B.orow = (d.flags & 2) ? nullptr : b.out_part + (int64_t)d.w_ref * 8 + s.goff + lane;
+            const float lroot = __ldcg(b.root_lr + t);
+            const int xroot = __ldcg(b.root_x + t);
+            child_finish<G>(b, s, d.v, cv2, bv2, A, want_post, lroot, xroot, cv_);
+            child_finish<G>(b, s, d.w, cw2, bw2, B, want_post, lroot, xroot, cw_);
+        } else {
+            switch ((cv.row ? 0 : 1) | (cw.row ? 0 : 2)) {   // warp-uniform: items are sorted by it
+                case 0: outside_states<G, false, false>(urow, fo, cv, cw, bv, bw, s.qrow, s.C, A, B); break;
+                case 1: outside_states<G, true, false>(urow, fo, cv, cw, bv, bw, s.qrow, s.C, A, B); break;
+                case 2: outside_states<G, false, true>(urow, fo, cv, cw, bv, bw, s.qrow, s.C, A, B); break;
+                default: outside_states<G, true, true>(urow, fo, cv, cw, bv, bw, s.qrow, s.C, A, B); break;
+            }
+            const float lroot = __ldcg(b.root_lr + t);
+            const int xroot = __ldcg(b.root_x + t);
+            child_finish<G>(b, s, d.v, cv, bv, A, want_post, lroot, xroot, cv_);
+            child_finish<G>(b, s, d.w, cw, bw, B, want_post, lroot, xroot, cw_);
+        }
     }
 #pragma unroll
     for (int off = G / 2; off > 0; off >>= 1) {
@@ -1539,6 +1655,7 @@ constexpr int kRaw = 7;   // gradient of the barrier objective in the height (du
 constexpr int kA = 8, kB = 9, kC = 10;   // objective coefficients of the node's branch
 constexpr int kIE = 11, kIEN = 12;       // 1 / expm1(d), 1 / expm1(nu d) at the current d
 constexpr int kRL = 13, kRH = 14;        // 1 / (d - dmin), 1 / (dmax - d)
+constexpr int kStat = 15;   // root: Newton steps of the last solve; node 0: line-search passes
 constexpr int kSlots = LAML_UWORK_SLOTS;
 static_assert(kSlots >= 15, "nd_uwork slots");
 constexpr double kTheta = 0.1;        // pull of the start point toward its interval's middle
@@ -1684,6 +1801,7 @@ __device__ __noinline__ bool ultra_dstep(const laml_batch& b, int p, Team& T, do
     const double m = mF.x;
     const double gap_tol = kGapRel * (fabs(mF.y) + 1.0);
     double t = 1.0;
+    int n_newton = 0, n_line = 0;
 
     for (int outer = 0; outer < kOuterMax && m > 0.0; ++outer) {
         double lam_prev = INFINITY;
@@ -1779,6 +1897,7 @@ __device__ __noinline__ bool ultra_dstep(const laml_batch& b, int p, Team& T, do
                 T.sync();
             }
             const double lam2 = T.sum2(lam, 0.0).x;
+            ++n_newton;
             if (!(lam2 * 0.5 > kNewtonTol)) break;
             // quadratic phase without progress: the rounding floor of this t
             if (lam2 * 0.5 < 1e-2 && lam2 > 0.25 * lam_prev) break;
@@ -1810,6 +1929,7 @@ __device__ __noinline__ bool ultra_dstep(const laml_batch& b, int p, Team& T, do
                     dphi += t * df + log1p32(s * at(x, kRL)) + log1p32(-s * at(x, kRH));
                 }
                 dphi = T.sum2(dphi, 0.0).x;
+                ++n_line;
                 if (dphi >= 0.25 * alpha * lam2) {
                     ok = true;
                     break;
@@ -1826,6 +1946,10 @@ __device__ __noinline__ bool ultra_dstep(const laml_batch& b, int p, Team& T, do
     }
 
     // 4. branch lengths from the heights; the root's branch alone
+    if (T.leader()) {
+        at(root, kStat) = (double)n_newton;
+        at(0, kStat) = (double)n_line;
+    }
     for (int x = T.tid(); x < N; x += T.size()) {
         if (x == root) {
             if (!freeb(x)) continue;
@@ -2628,10 +2752,11 @@ __global__ void __launch_bounds__(kWWarps * 32) k_items_w(laml_batch b, const in
 // ---------------------------------------------------------------------------
 // kernels
 // ---------------------------------------------------------------------------
-template <int G, int KIND>
+template <int G, int KIND, bool AS = false>
 __device__ __forceinline__ void for_items(const laml_batch& b, const int32_t* items, int64_t n,
                                           int gwarp, int nwarps, bool want_post,
-                                          bool respect_status, const int32_t* desc = nullptr) {
+                                          bool respect_status, const int32_t* desc = nullptr,
+                                          float* sm = nullptr) {
     constexpr int kind = KIND;
     if constexpr (KIND <= 1) {
         if (narrow_level(n)) {   // one item per warp: the shortest latency per item
@@ -2653,9 +2778,9 @@ __device__ __forceinline__ void for_items(const laml_batch& b, const int32_t* it
         if constexpr (KIND <= 1 || KIND == 5) {   // descriptor-driven inside / outside
             const ItemDesc d = load_desc(desc, act ? it : 0);
             if constexpr (KIND == 0) {
-                if (act) inside_item_d<G>(b, d, lane, respect_status);
+                if (act) inside_item_d<G, AS>(b, d, lane, respect_status, sm);
             } else if constexpr (KIND == 1) {
-                outside_item_d<G>(b, d, lane, act, want_post);
+                outside_item_d<G, AS>(b, d, lane, act, want_post, sm);
             } else {
                 outside_root_item_d<G>(b, d, lane, act, want_post);
             }
@@ -2677,7 +2802,13 @@ __global__ void __launch_bounds__(kItemsBlock, KIND == 1 ? LAML_MINB_OUT : LAML_
                                                    const int32_t* desc) {
     const int gwarp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int nwarps = (gridDim.x * blockDim.x) >> 5;
-    for_items<G, KIND>(b, items, n, gwarp, nwarps, want_post != 0, respect_status != 0, desc);
+    if constexpr (KIND <= 1) {   // wide levels stage their state loops (dynamic shared memory)
+        extern __shared__ float ksm[];
+        for_items<G, KIND, true>(b, items, n, gwarp, nwarps, want_post != 0, respect_status != 0,
+                                 desc, ksm);
+    } else {
+        for_items<G, KIND>(b, items, n, gwarp, nwarps, want_post != 0, respect_status != 0, desc);
+    }
 }
 
 // M-step, one block per tree; with skip_big the trees above kClusterNodes
@@ -2969,9 +3100,11 @@ int launch_items(const laml_batch& b, const int32_t* items, int64_t n, int kind,
     int64_t blocks = (n + ipb - 1) / ipb;
     const int64_t cap = (int64_t)num_sms() * 16;
     if (blocks > cap) blocks = cap;
+    const size_t sm0 = sizeof(float) * as_words<0>() * kItemsBlock;
+    const size_t sm1 = sizeof(float) * as_words<1>() * kItemsBlock;
     switch (kind) {
-        case 0: k_items<G, 0><<<(unsigned)blocks, kItemsBlock, 0, st>>>(b, items, n, want_post, respect_status, desc); break;
-        case 1: k_items<G, 1><<<(unsigned)blocks, kItemsBlock, 0, st>>>(b, items, n, want_post, respect_status, desc); break;
+        case 0: k_items<G, 0><<<(unsigned)blocks, kItemsBlock, sm0, st>>>(b, items, n, want_post, respect_status, desc); break;
+        case 1: k_items<G, 1><<<(unsigned)blocks, kItemsBlock, sm1, st>>>(b, items, n, want_post, respect_status, desc); break;
         case 2: k_items<G, 2><<<(unsigned)blocks, kItemsBlock, 0, st>>>(b, items, n, want_post, respect_status, desc); break;
         case 3: k_items<G, 3><<<(unsigned)blocks, kItemsBlock, 0, st>>>(b, items, n, want_post, respect_status, desc); break;
         case 5: k_items<G, 5><<<(unsigned)blocks, kItemsBlock, 0, st>>>(b, items, n, want_post, respect_status, desc); break;
