@@ -1665,6 +1665,17 @@ constexpr double kNewtonTol = 1e-6;   // centred when lambda^2 / 2 is below this
 constexpr int kOuterMax = 30, kNewtonMax = 60, kLineMax = 60;
 
 __device__ __forceinline__ double rcp32(double x) { return (double)(1.f / (float)x); }
+// 1 / x for a positive normal x to ~1e-14: an FP32 seed of the mantissa (the
+// binary exponent split off, so no range is lost) and one FP64 Newton step.
+// The level passes of the elimination divide on their critical path, where
+// GB300's narrow FP64 pipe makes a full FP64 division a long dependent chain.
+__device__ __forceinline__ double rcp64(double x) {
+    int e;
+    const double m = frexp(x, &e);   // x = m 2^e, m in [0.5, 1)
+    double r = (double)(1.f / (float)m);
+    r = r * fma(-m, r, 2.0);
+    return ldexp(r, -e);
+}
 __device__ __forceinline__ double log1p32(double x) { return (double)log1pf((float)x); }
 __device__ __forceinline__ double expm132(double x) { return (double)expm1f((float)x); }
 __device__ __forceinline__ double log1mexp32(double x) {   // log(1 - e^{-x}), x > 0
@@ -1672,9 +1683,14 @@ __device__ __forceinline__ double log1mexp32(double x) {   // log(1 - e^{-x}), x
 }
 }  // namespace ultra
 
-template <class Team>
+// SH: the eight slots threads exchange (kP .. kRaw) live slot-major in
+// shared memory (hot[k * N + v]); the per-branch terms only their owner
+// thread touches stay in nd_uwork.  Each level of the elimination is a chain
+// of dependent loads of these slots, which shared memory serves in tens of
+// cycles instead of a round trip to L2.
+template <class Team, bool SH>
 __device__ __noinline__ bool ultra_dstep(const laml_batch& b, int p, Team& T, double nu,
-                                         bool use_s, float* Dd) {
+                                         bool use_s, float* Dd, double* hot) {
     using namespace ultra;
     const int N = __ldg(b.tr_nodes + p), base = __ldg(b.tr_node_base + p);
     const int root = __ldg(b.tr_root + p) - base;
@@ -1684,7 +1700,10 @@ __device__ __noinline__ bool ultra_dstep(const laml_batch& b, int p, Team& T, do
     const int32_t* ids = ord + L + 2;
     double* U = b.nd_uwork + (int64_t)kSlots * base;
     const double dlo = kDmin, dhi = kDmax;
-    auto at = [&](int v, int k) -> double& { return U[(int64_t)kSlots * v + k]; };
+    auto at = [&](int v, int k) -> double& {
+        if (SH && k <= kRaw) return hot[(int64_t)k * N + v];
+        return U[(int64_t)kSlots * v + k];
+    };
     auto leaf = [&](int v) { return __ldg(b.nd_c0 + base + v) < 0; };
     auto c0_ = [&](int v) { return __ldg(b.nd_c0 + base + v) - base; };
     auto c1_ = [&](int v) { return __ldg(b.nd_c1 + base + v) - base; };
@@ -1860,9 +1879,9 @@ __device__ __noinline__ bool ultra_dstep(const laml_batch& b, int p, Team& T, do
                         if (at(c, kPin) != 0.0) {
                             E += Wc;
                         } else if (freeb(c)) {
-                            const double Ec = at(c, kE), D = Wc + Ec;
-                            E += Wc * (Ec / D);
-                            R += Wc * (at(c, kR) / D);
+                            const double Ec = at(c, kE), iD = rcp64(Wc + Ec);
+                            E += Wc * (Ec * iD);
+                            R += Wc * (at(c, kR) * iD);
                         } else {   // fixed branch: the child's height moves with this one
                             E += at(c, kE);
                             R += at(c, kR);
@@ -1884,12 +1903,12 @@ __device__ __noinline__ bool ultra_dstep(const laml_batch& b, int p, Team& T, do
                         del = 0.0;
                     } else if (x == root) {
                         const double E = at(x, kE);
-                        del = E > 0.0 ? at(x, kR) / E : 0.0;
+                        del = E > 0.0 ? at(x, kR) * rcp64(E) : 0.0;
                     } else if (!freeb(x)) {
                         del = at(par(x), kDel);
                     } else {
                         const double W = at(x, kW);
-                        del = (at(x, kR) + W * at(par(x), kDel)) / (W + at(x, kE));
+                        del = (at(x, kR) + W * at(par(x), kDel)) * rcp64(W + at(x, kE));
                     }
                     at(x, kDel) = del;
                     lam += at(x, kRaw) * del;
@@ -1909,8 +1928,8 @@ __device__ __noinline__ bool ultra_dstep(const laml_batch& b, int p, Team& T, do
                 const int u = par(x);
                 const double d = at(u, kP) - at(x, kP);
                 const double s = at(u, kDel) - at(x, kDel);
-                if (s > 0.0) amax = fmin(amax, (dhi - d) / s);
-                else if (s < 0.0) amax = fmin(amax, (d - dlo) / -s);
+                if (s > 0.0) amax = fmin(amax, (dhi - d) * rcp64(s));
+                else if (s < 0.0) amax = fmin(amax, (d - dlo) * rcp64(-s));
             }
             amax = T.mind(amax);
             double alpha = fmin(1.0, 0.99 * amax);
@@ -1969,7 +1988,7 @@ __device__ __noinline__ bool ultra_dstep(const laml_batch& b, int p, Team& T, do
 
 template <class Team>
 __device__ void mstep_tree(const laml_batch& b, int p, int rounds, Team& T, float4* s_cnt,
-                           float* s_d, int flags) {
+                           float* s_d, int flags, double* usm = nullptr, int ucap = 0) {
     const bool polish = (flags & LAML_MSTEP_FP64_POLISH) != 0;
     const bool ultra = (flags & LAML_MSTEP_ULTRAMETRIC) != 0 && !b.compat;
     if (__ldcg(b.tr_status + p) != LAML_TREE_ACTIVE) return;
@@ -2054,7 +2073,10 @@ __device__ void mstep_tree(const laml_batch& b, int p, int rounds, Team& T, floa
         if (ultra) {
             // EM_solver.Mstep returns "d_infeasible" before it places any
             // parameter (EM_solver.py:419-420): the tree keeps d, nu and phi
-            if (!ultra_dstep(b, p, T, nu, use_s, Dd)) {
+            const bool ok = (usm && N <= ucap)
+                                ? ultra_dstep<Team, true>(b, p, T, nu, use_s, Dd, usm)
+                                : ultra_dstep<Team, false>(b, p, T, nu, use_s, Dd, nullptr);
+            if (!ok) {
                 if (T.leader()) b.tr_status[p] = LAML_TREE_INFEASIBLE;
                 T.sync();
                 return;
@@ -2814,14 +2836,15 @@ __global__ void __launch_bounds__(kItemsBlock, KIND == 1 ? LAML_MINB_OUT : LAML_
 // M-step, one block per tree; with skip_big the trees above kClusterNodes
 // nodes are left to k_mstep_cluster
 __global__ void __launch_bounds__(kBlock, 4) k_mstep(laml_batch b, int rounds, int flags,
-                                                    int skip_big) {
+                                                    int skip_big, int ucap) {
     __shared__ double2 sh[kBlock / 32];
     __shared__ float4 s_cnt[kMstepStage];
     __shared__ float s_d[kMstepStage];
+    extern __shared__ double usm[];   // ultrametric solve: 8 slots for trees up to ucap nodes
     BlockTeam T{sh};
     for (int p = blockIdx.x; p < b.n_trees; p += gridDim.x) {
         if (skip_big && __ldg(b.tr_nodes + p) > kClusterNodes) continue;
-        mstep_tree(b, p, rounds, T, s_cnt, s_d, flags);
+        mstep_tree(b, p, rounds, T, s_cnt, s_d, flags, ucap > 0 ? usm : nullptr, ucap);
     }
 }
 
@@ -3167,9 +3190,25 @@ int outside_t(const laml_batch& b, int flags, cudaStream_t st, const Levels& L) 
 
 // the M-step launches: every tree up to kClusterNodes nodes in k_mstep, the
 // larger ones (when the batch may hold any) in k_mstep_cluster
+constexpr int kUltraSmemNodes = 2816;   // 8 FP64 slots a node: 176 KB beside k_mstep's 41 KB
+
 int launch_mstep(const laml_batch& b, int rounds, int flags, cudaStream_t st) {
     const bool big = b.max_tree_nodes <= 0 || b.max_tree_nodes > kClusterNodes;
-    k_mstep<<<b.n_trees, kBlock, 0, st>>>(b, rounds, flags, big ? 1 : 0);
+    int ucap = 0;
+    size_t usmem = 0;
+    if ((flags & LAML_MSTEP_ULTRAMETRIC) && !b.compat) {
+        ucap = b.max_tree_nodes > 0 ? std::min(b.max_tree_nodes, kUltraSmemNodes) : kUltraSmemNodes;
+        usmem = sizeof(double) * 8 * (size_t)ucap;
+        static bool attr_set = false;
+        if (!attr_set) {
+            const int rc = check(cudaFuncSetAttribute(k_mstep, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                      (int)(sizeof(double) * 8 * kUltraSmemNodes)),
+                                 "k_mstep shared memory limit");
+            if (rc) return rc;
+            attr_set = true;
+        }
+    }
+    k_mstep<<<b.n_trees, kBlock, usmem, st>>>(b, rounds, flags, big ? 1 : 0, ucap);
     int rc = check(cudaGetLastError(), "k_mstep");
     if (rc || !big) return rc;
     const int clusters = std::max(1, std::min(b.n_trees, num_sms() / kMstepCluster));
