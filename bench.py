@@ -42,7 +42,7 @@ METRIC = "EM iters/s & node-site updates/s, batched+served vs plain GPU; p50/p99
 # batch (G = 8): ncu dram__bytes_read.sum + dram__bytes_write.sum summed over
 # one pass of the first 128 candidates (`--passes-only --trees 128`), times 4
 # -- the full batch holds 4x the same-shaped rows -- over the pass's launches
-TRAFFIC_PER_LAUNCH = {"outside": 185.1e6, "inside": 134.6e6}
+TRAFFIC_PER_LAUNCH = {"outside": 168.0e6, "inside": 119.6e6}
 UNIT = "tree-EM-iters/s"
 WORKLOAD = "nni512"
 
