@@ -912,21 +912,32 @@ extern "C" int laml_plan_fill(const laml_plan_input* in, laml_plan_output* o) {
         }
     }, 8);
     // level buckets: inside by height, outside by the depth of the internal
-    // parent; within a level, trees in order and nodes ascending.  Per-tree
-    // level counts, a prefix over (level, tree), then a parallel scatter.
+    // parent; within a level, nodes grouped by which of their children are
+    // leaves (key 0..3: consecutive items -- the items of one warp -- then
+    // take the same specialised state loop), then trees in order and nodes
+    // ascending.  Per-(tree, level, key) counts, a prefix over (level, key,
+    // tree), then a parallel scatter: the order a stable sort by key of the
+    // tree-major level lists gives, without a sort pass.
     const int NL[2] = {H, D};
+    constexpr int NK = 4;
     std::vector<int64_t> lcnt[2];
-    for (int s2 = 0; s2 < 2; ++s2) lcnt[s2].assign((size_t)T * (NL[s2] + 1), 0);
+    for (int s2 = 0; s2 < 2; ++s2) lcnt[s2].assign((size_t)T * (NL[s2] + 1) * NK, 0);
     auto level_of = [&](const TreeLevels& L, int u, int side) {
         return side == 0 ? L.height[u] : L.depth[u] + 1;
+    };
+    auto key_of = [&](const int32_t* c0, const int32_t* c1, int u) {
+        return (c0[c0[u]] < 0 ? 1 : 0) | (c0[c1[u]] < 0 ? 2 : 0);
     };
     parallel_for(T, [&](int64_t a, int64_t e) {
         for (int64_t p = a; p < e; ++p) {
             const int N = in->tree_nodes[p], n = in->tree_leaves[p];
+            const int64_t nb = S.node_base[p];
+            const int32_t* c0 = in->child0 + nb;
+            const int32_t* c1 = in->child1 + nb;
             const TreeLevels& L = S.lv[p];
             for (int side = 0; side < 2; ++side) {
-                int64_t* c = lcnt[side].data() + (size_t)p * (NL[side] + 1);
-                for (int u = n; u < N; ++u) ++c[level_of(L, u, side)];
+                int64_t* c = lcnt[side].data() + (size_t)p * (NL[side] + 1) * NK;
+                for (int u = n; u < N; ++u) ++c[level_of(L, u, side) * NK + key_of(c0, c1, u)];
             }
         }
     }, 8);
@@ -938,12 +949,13 @@ extern "C" int laml_plan_fill(const laml_plan_input* in, laml_plan_output* o) {
         int64_t acc = 0;
         for (int l = 0; l <= nl; ++l) {
             lstart[side][l] = acc;
-            for (int p = 0; p < T; ++p) {
-                int64_t& c = lcnt[side][(size_t)p * (nl + 1) + l];
-                const int64_t x = c;
-                c = acc;          // becomes the tree's first slot in the level
-                acc += x;
-            }
+            for (int k = 0; k < NK; ++k)
+                for (int p = 0; p < T; ++p) {
+                    int64_t& c = lcnt[side][((size_t)p * (nl + 1) + l) * NK + k];
+                    const int64_t x = c;
+                    c = acc;          // becomes the tree's first slot of (level, key)
+                    acc += x;
+                }
         }
         lstart[side][nl + 1] = acc;
         lnodes[side].assign(acc, 0);
@@ -952,34 +964,17 @@ extern "C" int laml_plan_fill(const laml_plan_input* in, laml_plan_output* o) {
         for (int64_t p = a; p < e; ++p) {
             const int N = in->tree_nodes[p], n = in->tree_leaves[p];
             const int64_t nb = S.node_base[p];
+            const int32_t* c0 = in->child0 + nb;
+            const int32_t* c1 = in->child1 + nb;
             const TreeLevels& L = S.lv[p];
             for (int side = 0; side < 2; ++side) {
-                int64_t* c = lcnt[side].data() + (size_t)p * (NL[side] + 1);
-                for (int u = n; u < N; ++u) lnodes[side][c[level_of(L, u, side)]++] = (int32_t)(nb + u);
+                int64_t* c = lcnt[side].data() + (size_t)p * (NL[side] + 1) * NK;
+                for (int u = n; u < N; ++u)
+                    lnodes[side][c[level_of(L, u, side) * NK + key_of(c0, c1, u)]++] =
+                        (int32_t)(nb + u);
             }
         }
     }, 8);
-    // within a level, nodes grouped (stably) by which of their children are
-    // leaves: consecutive items -- the items of one warp -- then take the same
-    // specialised state loop
-    auto leaf_key = [&](int32_t g) {
-        return (o->nd_c0[o->nd_c0[g]] < 0 ? 1 : 0) | (o->nd_c0[o->nd_c1[g]] < 0 ? 2 : 0);
-    };
-    for (int side = 0; side < 2; ++side) {
-        parallel_for(NL[side] + 1, [&](int64_t a, int64_t e) {
-            std::vector<int32_t> tmp;
-            for (int64_t l = a; l < e; ++l) {   // a counting sort on the 4 keys
-                int32_t* first = lnodes[side].data() + lstart[side][l];
-                const int64_t cnt = lstart[side][l + 1] - lstart[side][l];
-                int64_t at[5] = {0, 0, 0, 0, 0};
-                for (int64_t x = 0; x < cnt; ++x) ++at[leaf_key(first[x]) + 1];
-                for (int k = 1; k < 5; ++k) at[k] += at[k - 1];
-                tmp.resize((size_t)cnt);
-                for (int64_t x = 0; x < cnt; ++x) tmp[at[leaf_key(first[x])]++] = first[x];
-                std::copy(tmp.begin(), tmp.end(), first);
-            }
-        }, 2);
-    }
     // items, group-major within a level (groups are sorted by state count)
     bool uniform = true;
     for (int p = 0; p < T; ++p) uniform = uniform && in->ds_groups[in->tree_dataset[p]] == maxNG;
