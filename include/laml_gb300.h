@@ -73,6 +73,30 @@ int laml_newick_encode_batch(int32_t n_trees, const char* const* newicks,
                              int32_t* parent, int32_t* child0, int32_t* child1,
                              double* branch_length, uint8_t* has_length);
 
+/* NNI candidates of one binary tree without writing or parsing newick.
+ * Topology_search's move (laml_libs/Topology_search.py:242-322,
+ * Topology_search_parallel.py:65-130) trades u's child `u_child` with u's
+ * sibling w; treeswift's child lists then read u: (u's other child, w) and
+ * v = parent(u): (u, u_child).  Moves are taken in order on one tree whose
+ * child lists each swap-and-undo leaves reading u: (u's other child,
+ * u_child), v: (u, w) -- the order the search's own listing leaves its tree
+ * object in -- and every later candidate's numbering follows from that
+ * state.  Each candidate is written in the numbering
+ * laml_newick_encode gives the newick Topology_search writes for it: leaves
+ * keep their ids (the input's leaf order), internal nodes are renumbered in
+ * treeswift preorder of the new tree, child0/child1 in networkx successor
+ * order; every node keeps its own branch length.  Input: the tree as
+ * laml_newick_encode wrote it; moves[2 * n_moves] = (u, u_child) pairs of
+ * node ids (u internal, not the root).  Outputs hold n_moves * n_nodes
+ * entries, candidate m at offset m * n_nodes.  n_threads = 0: all host
+ * threads. */
+int laml_nni_candidates(int32_t n_nodes, int32_t n_leaves, const int32_t* parent,
+                        const int32_t* child0, const int32_t* child1,
+                        const double* branch_length, const uint8_t* has_length,
+                        int32_t n_moves, const int32_t* moves, int32_t n_threads,
+                        int32_t* out_parent, int32_t* out_child0, int32_t* out_child1,
+                        double* out_length, uint8_t* out_has_length);
+
 /* Site layout of a character matrix for the device kernels.
  * chars: n_leaves x n_sites int32 in leaf order (LAML_CHAR_* or >= 0 raw
  * states); priors as CSR over sites: prior_ptr[n_sites+1], prior_state[],

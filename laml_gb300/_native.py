@@ -105,6 +105,8 @@ EXPORTS = {
     "laml_plan_measure": (i32, [P(PlanInput), P(PlanSizes)]),
     "laml_plan_fill": (i32, [P(PlanInput), P(PlanOutput)]),
     "laml_ultra_order": (i32, [vp, i32, vp, i64, P(i64)]),
+    "laml_nni_candidates": (i32, [i32, i32, vp, vp, vp, vp, vp, i32, vp, i32, vp, vp, vp, vp,
+                                  vp]),
     "laml_supported_group_sites": (i32, []),
     "laml_plan_descriptors": (i32, [P(Batch), vp, vp, vp, vp]),
     "laml_branch_terms": (i32, [P(Batch), vp]),

@@ -1174,3 +1174,108 @@ extern "C" int laml_ultra_order(const int32_t* parent, int32_t n_nodes, int32_t*
     if (written) *written = (int64_t)N + L + 2;
     return LAML_OK;
 }
+
+// NNI candidates of one encoded tree, renumbered as the encoder numbers the
+// newick of each swapped tree.  The search lists its moves on ONE tree object,
+// swapping and swapping back in turn (Topology_search_parallel.py:114-129);
+// treeswift appends on add_child, so a swap and its undo leave the topology
+// as it was but u's children reading (u's other child, u_child) and v's
+// reading (u, w).  Every later candidate's newick -- and so its preorder
+// numbering -- sees those orders: the child orders are state, replayed move
+// by move (each thread replays the moves before its chunk, O(1) each).
+extern "C" int laml_nni_candidates(int32_t n_nodes, int32_t n_leaves, const int32_t* parent,
+                                   const int32_t* child0, const int32_t* child1,
+                                   const double* branch_length, const uint8_t* has_length,
+                                   int32_t n_moves, const int32_t* moves, int32_t n_threads,
+                                   int32_t* out_parent, int32_t* out_child0,
+                                   int32_t* out_child1, double* out_length,
+                                   uint8_t* out_has_length) {
+    const int N = n_nodes, n = n_leaves;
+    if (N < 3 || n < 2 || n >= N || n_moves < 0 || !parent || !child0 || !child1 ||
+        !branch_length || !has_length || (n_moves > 0 && (!moves || !out_parent || !out_child0 ||
+                                                          !out_child1 || !out_length ||
+                                                          !out_has_length))) {
+        set_error("laml_nni_candidates: bad argument");
+        return LAML_ERR_ARG;
+    }
+    int root = -1;
+    for (int x = 0; x < N; ++x) {
+        const bool internal = child0[x] >= 0;
+        if ((x < n) == internal || (internal && (child1[x] < 0 || child0[x] >= N || child1[x] >= N))) {
+            set_error("laml_nni_candidates: leaves must be 0..n-1 and internal nodes binary");
+            return LAML_ERR_ARG;
+        }
+        if (parent[x] < 0) {
+            if (root >= 0) { set_error("laml_nni_candidates: more than one root"); return LAML_ERR_ARG; }
+            root = x;
+        }
+    }
+    if (root < 0) { set_error("laml_nni_candidates: no root"); return LAML_ERR_ARG; }
+    for (int m = 0; m < n_moves; ++m) {
+        const int u = moves[2 * m], uc = moves[2 * m + 1];
+        if (u < n || u >= N || u == root || uc < 0 || uc >= N || parent[uc] != u) {
+            set_error("laml_nni_candidates: move " + std::to_string(m) +
+                      " is not (internal non-root u, a child of u)");
+            return LAML_ERR_ARG;
+        }
+    }
+    auto other = [&](int x, int c) { return child0[x] == c ? child1[x] : child0[x]; };
+    const int hw = (int)std::max(1u, std::thread::hardware_concurrency());
+    const int nt = std::max(1, std::min(n_threads > 0 ? n_threads : hw, std::max(1, n_moves / 16)));
+    const int chunk = (n_moves + nt - 1) / std::max(1, nt);
+    auto work = [&](int t) {
+        const int m0 = t * chunk, m1 = std::min(n_moves, m0 + chunk);
+        if (m0 >= m1) return;
+        // newick order (first, second) of every internal node, as the tree
+        // object reads it before move m0
+        std::vector<int32_t> fst(child1, child1 + N), snd(child0, child0 + N);
+        auto undo_state = [&](int m) {
+            const int u = moves[2 * m], uc = moves[2 * m + 1], v = parent[u];
+            fst[u] = other(u, uc); snd[u] = uc;
+            fst[v] = u; snd[v] = other(v, u);
+        };
+        for (int m = 0; m < m0; ++m) undo_state(m);
+        std::vector<int32_t> id(N), st;
+        st.reserve(64);
+        for (int m = m0; m < m1; ++m) {
+            const int u = moves[2 * m], uc = moves[2 * m + 1];
+            const int v = parent[u], w = other(v, u), keep = other(u, uc);
+            auto first = [&](int x) { return x == u ? keep : (x == v ? u : fst[x]); };
+            auto second = [&](int x) { return x == u ? w : (x == v ? uc : snd[x]); };
+            // treeswift preorder: the first newick child is pushed first, so
+            // the second is visited first
+            int nxt = n;
+            st.clear();
+            st.push_back(root);
+            while (!st.empty()) {
+                const int x = st.back();
+                st.pop_back();
+                if (x < n) { id[x] = x; continue; }
+                id[x] = nxt++;
+                st.push_back(first(x));
+                st.push_back(second(x));
+            }
+            const int64_t o = (int64_t)m * N;
+            int32_t* P = out_parent + o; int32_t* A = out_child0 + o; int32_t* B = out_child1 + o;
+            double* D = out_length + o; uint8_t* H = out_has_length + o;
+            P[id[root]] = -1;
+            for (int x = 0; x < N; ++x) {
+                const int i = id[x];
+                D[i] = branch_length[x];
+                H[i] = has_length[x];
+                if (x < n) { A[i] = -1; B[i] = -1; continue; }
+                const int f = id[first(x)], s2 = id[second(x)];
+                A[i] = s2;   // networkx successor order = reversed newick order
+                B[i] = f;
+                P[f] = i;
+                P[s2] = i;
+            }
+            undo_state(m);
+        }
+    };
+    std::vector<std::thread> th;
+    for (int t = 1; t < nt; ++t) th.emplace_back(work, t);
+    work(0);
+    for (auto& x : th) x.join();
+    return LAML_OK;
+}

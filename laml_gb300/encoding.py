@@ -201,6 +201,29 @@ def encode_dataset(chars: np.ndarray, Q, compat: bool = True, group_sites: int =
                           smap[:sptr[-1]].copy(), compat)
 
 
+def nni_candidates(tree: EncodedTree, moves) -> List[EncodedTree]:
+    """laml_nni_candidates: one EncodedTree per (u, u_child) move of
+    ``tree`` (node ids), numbered as encoding the swapped tree's newick would
+    number it; the candidates are views into shared arrays and carry no
+    labels."""
+    mv = np.ascontiguousarray(np.asarray(moves, np.int32).reshape(-1, 2))
+    M, Nn = mv.shape[0], tree.num_nodes
+    par = np.empty((M, Nn), np.int32)
+    c0 = np.empty((M, Nn), np.int32)
+    c1 = np.empty((M, Nn), np.int32)
+    bl = np.empty((M, Nn), np.float64)
+    has = np.empty((M, Nn), np.uint8)
+    src = [np.ascontiguousarray(a, t) for a, t in
+           ((tree.parent, np.int32), (tree.child0, np.int32), (tree.child1, np.int32),
+            (tree.branch_length, np.float64), (tree.has_length, np.uint8))]
+    N.check(N.lib().laml_nni_candidates(Nn, tree.num_leaves, *[a.ctypes.data for a in src], M,
+                                        mv.ctypes.data, 0, par.ctypes.data, c0.ctypes.data,
+                                        c1.ctypes.data, bl.ctypes.data, has.ctypes.data))
+    hb = has.astype(bool)
+    return [EncodedTree(Nn, tree.num_leaves, par[m], c0[m], c1[m], bl[m], hb[m], None)
+            for m in range(M)]
+
+
 def plan_batch(trees: Sequence[EncodedTree], tree_ds: Sequence[int],
                datasets: Sequence[EncodedDataset], host_desc: bool = True):
     """Level schedule + buffer offsets of a batch (laml_plan_*).  Returns

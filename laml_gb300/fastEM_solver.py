@@ -332,31 +332,40 @@ class CandidateScore:
     @property
     def newicks(self):
         if self._newicks is None:
+            topos = self._topos() if callable(self._topos) else self._topos
             self._newicks = [write_newick(encode_newick(nw, self._leaf_order), d)
-                             for nw, d in zip(self._topos, self._lengths)]
+                             for nw, d in zip(topos, self._lengths)]
         return self._newicks
 
 
 def score_candidate_batch(candidates, strategies, data, prior, params, group_sites=8,
-                          device="cuda"):
+                          device="cuda", trees=None):
     """fastEM_solver(treeList, data, prior, params).score_tree(strategy) for
     many candidates at once (each a treeList over the same leaves), as one
     batched EM on the device.  Per tree: missing lengths drawn U(0.01, 0.5) in
     node order (fastEM_solver.py:95-126, candidates in order), nu, phi start
     at the strategy's fixed values or 0.5 (320-321) and are optimised
-    (323-324), every branch fixed when ``fixed_brlen`` is given (310-316)."""
+    (323-324), every branch fixed when ``fixed_brlen`` is given (310-316).
+    ``trees``: the candidates already encoded (one tree each, numbered in
+    data['ordered_leaf_labels'] order, e.g. by laml_nni_candidates); each
+    candidate is then a callable giving its newick list when it is needed."""
     from .encoding import encode_newick_batch
     lo = data.get("ordered_leaf_labels")
     leaf_order = list(lo[0]) if lo else None
-    flat, owner = [], []
-    for ci, topos in enumerate(candidates):
-        for nw in topos:
-            flat.append(nw)
-            owner.append(ci)
-    if leaf_order is None:
-        first = encode_newick(flat[0])
-        leaf_order = first.labels[:first.num_leaves]
-    trees = encode_newick_batch(flat, leaf_order)
+    if trees is not None:
+        if leaf_order is None:
+            raise ValueError("encoded candidates need data['ordered_leaf_labels']")
+        owner = list(range(len(trees)))
+    else:
+        flat, owner = [], []
+        for ci, topos in enumerate(candidates):
+            for nw in topos:
+                flat.append(nw)
+                owner.append(ci)
+        if leaf_order is None:
+            first = encode_newick(flat[0])
+            leaf_order = first.labels[:first.num_leaves]
+        trees = encode_newick_batch(flat, leaf_order)
     mat = char_matrix([data["charMtrx"][c] for c in leaf_order])
     ds = encode_dataset(mat, prior["Q"], compat=True, group_sites=group_sites)
     d, masks, nus, phis = [], [], [], []
@@ -378,8 +387,9 @@ def score_candidate_batch(candidates, strategies, data, prior, params, group_sit
     out = []
     k = 0
     for ci, topos in enumerate(candidates):
-        rs = res[k:k + len(topos)]
-        k += len(topos)
+        ntree = 1 if callable(topos) else len(topos)
+        rs = res[k:k + ntree]
+        k += ntree
         out.append(CandidateScore(rs[-1].llh, {'phi': rs[-1].phi, 'nu': rs[-1].nu}, topos,
                                   [r.branch_lengths for r in rs], leaf_order))
     return out

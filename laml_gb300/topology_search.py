@@ -35,6 +35,23 @@ DEFAULT_STRATEGY = {'resolve_search_only': False, 'only_marked': False, 'ultra_c
 CHKPT_FREQ = 10                                   # laml_libs/core_constants.py:9
 
 
+def encoded_ids(tree: Tree, leaf_index) -> dict:
+    """id(node) -> the node's id in laml_newick_encode's numbering of
+    tree.newick(): leaves by ``leaf_index`` (label -> position), internal
+    nodes in treeswift preorder (the traversal Tree.traverse_preorder
+    makes).  None when the root is unifurcating (the encoder drops it)."""
+    if len(tree.root.child_nodes()) == 1:
+        return None
+    out, nxt = {}, len(leaf_index)
+    for node in tree.traverse_preorder():
+        if node.is_leaf():
+            out[id(node)] = leaf_index[node.label]
+        else:
+            out[id(node)] = nxt
+            nxt += 1
+    return out
+
+
 class Topology_search:
     def __init__(self, treeTopoList, solver, data={}, prior={}, params={}, T_cooldown=20,
                  alpha_cooldown=0.9):
@@ -263,13 +280,18 @@ class Topology_search_batched(Topology_search):
     """Topology_search_parallel's listing of every NNI move, scored in device
     batches of ``batch_size`` through one batched EM."""
 
-    def __init__(self, *a, batch_size: int = 512, group_sites: int = 8, device="cuda", **k):
+    def __init__(self, *a, batch_size: int = 512, group_sites: int = 8, device="cuda",
+                 native: bool = True, **k):
         super().__init__(*a, **k)
         self.batch_size = batch_size
         self.group_sites = group_sites
         self.device = device
+        self.native = native   # False: one newick per candidate, as the reference lists them
 
     def list_all_nni(self, strategy, only_marked=False):
+        fast = self._list_all_nni_native(strategy, only_marked)
+        if fast is not None:
+            return fast
         moves = []
         for u in self._branches(only_marked):
             v = u.get_parent()
@@ -283,16 +305,84 @@ class Topology_search_batched(Topology_search):
                 self._unswap(u, v, u_child, w)
         return moves
 
+    def _list_all_nni_native(self, strategy, only_marked):
+        """list_all_nni for one tree with the leaf order given: the same moves
+        in the same order with the same random draws, the candidates built by
+        laml_nni_candidates instead of a newick per move.  The tree object
+        gets the child orders each swap-and-undo of the reference's listing
+        leaves (Topology_search_parallel.py:114-129) as the moves are taken,
+        so every u.child_nodes() copy that is shuffled reads as it would
+        there.  The strategy keeps what the batched fastEM scorer reads:
+        fastEM fixes every branch whenever fixed_brlen is given
+        (fastEM_solver.py:310-316), so its leaf-anchored contents are not
+        built.  Returns None when the newick path must run."""
+        from .encoding import encode_newick, nni_candidates
+        lo = self.data.get("ordered_leaf_labels")
+        if not self.native or len(self.treeList_obj) != 1 or not lo:
+            return None
+        tree = self.treeList_obj[0]
+        leaf_order = list(lo[0])
+        leaf_index = {c: i for i, c in enumerate(leaf_order)}
+        ids = encoded_ids(tree, leaf_index)
+        if ids is None:
+            return None
+        start = encode_newick(tree.newick(), leaf_order)
+        snapshot = [(x, list(x.children)) for x in tree.traverse_preorder() if x.children]
+        meta, pairs, sts = [], [], []
+        for u in self._branches(only_marked):
+            v = u.get_parent()
+            w = next(x for x in v.child_nodes() if x is not u)
+            st = deepcopy(strategy)
+            st['fixed_brlen'] = None
+            st['nodes_to_recompute'] = None
+            if strategy['local_brlen_opt']:
+                st['fixed_nu'] = self.params['nu']
+                st['fixed_phi'] = self.params['phi']
+                st['fixed_brlen'] = [{}]   # set: fastEM then fixes every branch
+            u_children = u.child_nodes()
+            _random.shuffle(u_children)
+            for u_child in u_children:
+                meta.append((u, v, u_child, w))
+                pairs.append((ids[id(u)], ids[id(u_child)]))
+                sts.append(st)
+                keep = next(x for x in u.children if x is not u_child)
+                u.children = [keep, u_child]   # what the swap and its undo leave
+                v.children = [u, w]
+        if not pairs:
+            return []
+        cands = nni_candidates(start, pairs)
+        final = [(x, list(x.children)) for x, _ in snapshot]
+
+        def newick_of(m):
+            # the tree object as it read when move m was listed, swapped
+            for x, ch in snapshot:
+                x.children = list(ch)
+            for (u, v, uc, w) in meta[:m]:
+                u.children = [next(x for x in u.children if x is not uc), uc]
+                v.children = [u, w]
+            u, v, uc, w = meta[m]
+            self._swap(u, v, uc, w)
+            nw = tree.newick()
+            self._unswap(u, v, uc, w)
+            for x, ch in final:
+                x.children = list(ch)
+            return [nw]
+        return [(None, st, mv, cand, (lambda m=m: newick_of(m)))
+                for m, (st, mv, cand) in enumerate(zip(sts, meta, cands))]
+
     def single_nni(self, curr_score, nni_iter, strategy, only_marked=False, verbose=False):
         from .fastEM_solver import score_candidate_batch
         moves = self.list_all_nni(strategy, only_marked=only_marked)
         checked = 0
         for start in range(0, len(moves), self.batch_size):
             chunk = moves[start:start + self.batch_size]
-            results = score_candidate_batch([m[0] for m in chunk], [m[1] for m in chunk],
-                                            self.data, self.prior, self.params,
-                                            group_sites=self.group_sites, device=self.device)
-            for (topos, st, cache), res in zip(chunk, results):
+            native = len(chunk) > 0 and chunk[0][0] is None
+            extra = {"trees": [m[3] for m in chunk]} if native else {}
+            results = score_candidate_batch(
+                [m[4] if native else m[0] for m in chunk], [m[1] for m in chunk], self.data,
+                self.prior, self.params, group_sites=self.group_sites, device=self.device,
+                **extra)
+            for res in results:
                 checked += 1
                 if self.__accept_proposal__(curr_score, res.score, nni_iter):
                     self.treeTopoList = res.newicks

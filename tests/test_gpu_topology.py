@@ -81,3 +81,25 @@ def test_nni_search_reaches_brute_force_optimum(start, batched):
     s = cls([start], fastEM_solver, data=data, prior=prior, params=params)
     trees, score, best_params = s.search(maxiter=200, nreps=10, verbose=False)
     assert -score == pytest.approx(nllh_bf, abs=5e-5)
+
+
+def test_batched_search_native_listing_equals_newick_listing():
+    """The batched NNI search on a 60-leaf tree, candidates built by
+    laml_nni_candidates against one newick per candidate: the same random
+    draws, the same scores bit for bit, the same accepted trees."""
+    from copy import deepcopy
+    from laml_gb300 import synth
+    w = synth.pmm_workload(60, 12, 3, 8, 0.5, 0.1, 0.1, seed=5)
+    data = {"charMtrx": w.rows, "ordered_leaf_labels": [w.leaf_order]}
+    out = []
+    for native in (True, False):
+        random.seed(11)
+        s = TS.Topology_search_batched([w.newicks[0]], fastEM_solver, data=data,
+                                       prior={"Q": w.Q}, params={"nu": 0.1, "phi": 0.1},
+                                       batch_size=64, native=native)
+        strategy = deepcopy(TS.DEFAULT_STRATEGY)
+        trees, score, params = s.search(maxiter=3, nreps=1, strategy=strategy)
+        out.append((trees, score, params))
+    assert out[0][1] == out[1][1]
+    assert out[0][0] == out[1][0]
+    assert out[0][2] == out[1][2]

@@ -128,3 +128,88 @@ def test_search_finds_target_with_stand_in_scorer(batched, monkeypatch):
         s = TS.Topology_search([start], _FakeSolver, params={'nu': .1, 'phi': .1})
     trees, score, params = s.search(maxiter=200, nreps=3, strategy=strat)
     assert score == len(_FakeSolver.clades(_FakeSolver.target))
+
+
+@pytest.mark.parametrize("seed", [0, 1, 2])
+def test_nni_candidates_equal_encoded_newicks(seed):
+    """laml_nni_candidates against the search's own path: swap the Python
+    tree, write its newick, encode it.  Every array equal, for every move."""
+    import numpy as np
+    from laml_gb300 import synth
+    from laml_gb300.encoding import encode_newick, nni_candidates
+    from laml_gb300.topology_search import Topology_search, encoded_ids
+    from laml_gb300.tree import read_tree_newick
+    w = synth.pmm_workload(40, 5, 3, 6, 0.5, 0.1, 0.1, seed=seed)
+    tree = read_tree_newick(w.newicks[0])
+    leaf_index = {c: i for i, c in enumerate(w.leaf_order)}
+    ids = encoded_ids(tree, leaf_index)
+    et = encode_newick(tree.newick(), w.leaf_order)
+    moves, ref = [], []
+    for u in tree.traverse_preorder():
+        if u.is_leaf() or u.get_parent() is None:
+            continue
+        v = u.get_parent()
+        wn = next(x for x in v.child_nodes() if x is not u)
+        for uc in list(u.child_nodes()):
+            Topology_search._swap(u, v, uc, wn)
+            ref.append(encode_newick(tree.newick(), w.leaf_order))
+            Topology_search._unswap(u, v, uc, wn)
+            moves.append((ids[id(u)], ids[id(uc)]))
+    assert len(moves) == 2 * (et.num_nodes - et.num_leaves - 1)
+    cands = nni_candidates(et, moves)
+    for c, r in zip(cands, ref):
+        for a in ("parent", "child0", "child1", "branch_length", "has_length"):
+            np.testing.assert_array_equal(getattr(c, a), getattr(r, a), err_msg=a)
+
+
+def test_nni_candidates_rejects_bad_moves():
+    import numpy as np
+    from laml_gb300 import _native as N
+    from laml_gb300.encoding import encode_newick, nni_candidates
+    et = encode_newick("((a:1,b:1):1,(c:1,d:1):1):0.5;", ["a", "b", "c", "d"])
+    root = et.root
+    with pytest.raises(N.LamlError):
+        nni_candidates(et, [(root, int(et.child0[root]))])   # u may not be the root
+    with pytest.raises(N.LamlError):
+        nni_candidates(et, [(0, 1)])                          # u must be internal
+    u = int(et.child0[root])
+    with pytest.raises(N.LamlError):
+        nni_candidates(et, [(u, 0 if et.parent[0] != u else 2)])   # not a child of u
+
+
+@pytest.mark.parametrize("seed", [3, 4])
+def test_native_nni_listing_equals_newick_listing(seed):
+    """Topology_search_batched.list_all_nni, native (leaf order given) against
+    the newick path under the same random seed: the same moves in the same
+    order, candidates encoded identically, each candidate's listing-time
+    newick rebuilt exactly, and the tree object left with the same child
+    orders (the next round's listing reads them)."""
+    import copy
+    import numpy as np
+    from laml_gb300 import synth
+    from laml_gb300.encoding import encode_newick_batch
+    w = synth.pmm_workload(30, 5, 3, 6, 0.5, 0.1, 0.1, seed=seed)
+    strat = dict(TS.DEFAULT_STRATEGY)
+    prior = {"Q": w.Q}
+    with_order = {"charMtrx": w.rows, "ordered_leaf_labels": [w.leaf_order]}
+    without = {"charMtrx": w.rows}
+    a = TS.Topology_search_batched([w.newicks[0]], None, data=with_order, prior=prior,
+                                   params={"nu": .1, "phi": .2})
+    b = TS.Topology_search_batched([w.newicks[0]], None, data=without, prior=prior,
+                                   params={"nu": .1, "phi": .2})
+    for _ in range(2):   # two rounds: the second starts from the mutated child orders
+        random.seed(seed)
+        na = a.list_all_nni(strat)
+        random.seed(seed)
+        nb = b.list_all_nni(strat)
+        assert len(na) == len(nb)
+        ref = encode_newick_batch([m[0][0] for m in nb], w.leaf_order)
+        for k, (x, y) in enumerate(zip(na, nb)):
+            assert [n.label for n in x[2]] == [n.label for n in y[2]]
+            assert x[1]['fixed_nu'] == y[1]['fixed_nu'] and x[1]['fixed_phi'] == y[1]['fixed_phi']
+            assert (x[1]['fixed_brlen'] is None) == (y[1]['fixed_brlen'] is None)
+            for f in ("parent", "child0", "child1", "branch_length", "has_length"):
+                np.testing.assert_array_equal(getattr(x[3], f), getattr(ref[k], f), err_msg=f)
+        for k in (0, len(na) // 2, len(na) - 1):
+            assert na[k][4]() == nb[k][0]
+        assert a.treeList_obj[0].newick() == b.treeList_obj[0].newick()
