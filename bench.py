@@ -675,9 +675,12 @@ def main():
     if rank == 0 and not args.no_cpu:
         try:
             v, cores = cpu_sample_port(w, 16, 1)
+            v1, _ = cpu_sample_port(w, 1, 1)   # one tree runs on one core
             cpu = {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
+                   "value_1core": v1,
                    "sample": "16 of the 512 candidates x 1 EM iteration, FP64 C restatement "
-                             "of the fastEM path, one tree per core"}
+                             "of the fastEM path, one tree per core; value_1core: one "
+                             "candidate x 1 EM iteration on one core"}
         except Exception as ex:  # the baseline is reported, never required
             cpu = {"value": None, "unit": UNIT, "cores": 0, "kind": "port",
                    "sample": f"unavailable: {ex}"}
