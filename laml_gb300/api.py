@@ -38,21 +38,64 @@ def score_candidates(newicks: Sequence[str], rows: dict, Q, leaf_order: Sequence
                      compat: bool = True, group_sites: int = 8, nu: float = 0.5,
                      phi: float = 0.5, rounds: int = MSTEP_ROUNDS, max_iters: int = 100000,
                      fix_nu=None, fix_phi=None, masks=None, device="cuda", chunk: int = 4,
-                     rng: Optional[random.Random] = None) -> ScoreResult:
+                     rng: Optional[random.Random] = None,
+                     pipeline: Optional[int] = None) -> ScoreResult:
+    """``pipeline`` parts: the candidates are cut into that many contiguous
+    parts, each its own device batch on its own stream; a worker thread
+    parses, plans and uploads part k+1 while part k iterates, so the host
+    work of all parts but the first overlaps the device.  Each tree's EM is
+    independent of the others in its batch, so the parts give each tree the
+    result it has in one batch (up to FP32 summation order when a level's
+    width crosses the wide/narrow rule).  Default: 2 parts from 256
+    candidates on, else 1."""
+    import threading
+    from concurrent.futures import ThreadPoolExecutor
+
     ds = dataset_from_rows(rows, Q, leaf_order, compat, group_sites)
-    trees = encode_newick_batch(newicks, leaf_order)
     rng = rng if rng is not None else random
-    d = []
-    for t in trees:
-        x = t.branch_length.copy()
-        if not t.has_length.all():
-            # fastEM_solver.parse_tree draws U(0.01, 0.5): leaves first, then internal nodes
-            for i in np.flatnonzero(~t.has_length):
-                x[i] = rng.uniform(0.01, 0.5)
-        d.append(x)
-    b = make_batch(newicks, rows, Q, leaf_order, compat=compat, group_sites=group_sites, nu=nu,
-                   phi=phi, d=d, mask=masks, fix_nu=fix_nu, fix_phi=fix_phi, device=device,
-                   trees=trees, dataset=ds)
-    res = b.run_em(rounds=rounds, max_iters=max_iters, chunk=chunk)
-    d2h = b.last_d2h_bytes
-    return ScoreResult(res, b.h2d_bytes, d2h)
+    T = len(newicks)
+    parts = pipeline if pipeline is not None else (2 if T >= 256 else 1)
+    parts = max(1, min(int(parts), T))
+    bounds = [T * k // parts for k in range(parts + 1)]
+    dev = torch.device(device)
+    if dev.type == "cuda" and dev.index is None:   # the worker thread needs the index
+        dev = torch.device("cuda", torch.cuda.current_device())
+
+    def prep(k):
+        lo, hi = bounds[k], bounds[k + 1]
+        nws = list(newicks[lo:hi])
+        trees = encode_newick_batch(nws, leaf_order)
+        d = []
+        for t in trees:
+            x = t.branch_length.copy()
+            if not t.has_length.all():
+                # fastEM_solver.parse_tree draws U(0.01, 0.5): leaves first, then internal nodes
+                for i in np.flatnonzero(~t.has_length):
+                    x[i] = rng.uniform(0.01, 0.5)
+            d.append(x)
+        sub = lambda a: None if a is None else (a[lo:hi] if not np.isscalar(a) else a)  # noqa: E731
+        if dev.type == "cuda" and threading.current_thread() is not threading.main_thread():
+            torch.cuda.set_device(dev)
+        st = torch.cuda.Stream(dev) if (parts > 1 and dev.type == "cuda") else None
+        b = make_batch(nws, rows, Q, leaf_order, compat=compat, group_sites=group_sites, nu=nu,
+                       phi=phi, d=d, mask=sub(masks), fix_nu=sub(fix_nu), fix_phi=sub(fix_phi),
+                       device=device, trees=trees, dataset=ds, stream=st)
+        return b, st
+
+    res, h2d, d2h = [], 0, 0
+    if parts == 1:
+        b, _ = prep(0)
+        res = b.run_em(rounds=rounds, max_iters=max_iters, chunk=chunk)
+        return ScoreResult(res, b.h2d_bytes, b.last_d2h_bytes)
+    with ThreadPoolExecutor(1) as ex:
+        fut = ex.submit(prep, 0)
+        for k in range(parts):
+            b, st = fut.result()
+            if k + 1 < parts:
+                fut = ex.submit(prep, k + 1)
+            with torch.cuda.stream(st):
+                res += b.run_em(rounds=rounds, max_iters=max_iters, chunk=chunk)
+            h2d += b.h2d_bytes
+            d2h += b.last_d2h_bytes
+            del b
+    return ScoreResult(res, h2d, d2h)

@@ -375,3 +375,21 @@ def test_em_through_root_branch_blowup(n, K, nu0, phi0, seed, loose):
         else:
             assert r.llh == pytest.approx(llh[0], rel=1e-5)
             assert r.nu == pytest.approx(nu[0], rel=1e-3)
+
+
+def test_score_candidates_pipeline_parts_agree():
+    """api.score_candidates in 3 pipelined parts (worker-thread preparation,
+    one stream per part) against one batch: every tree's EM is independent,
+    so results agree to FP32 summation order."""
+    import random as _r
+    from laml_gb300.api import score_candidates
+    w = synth.pmm_workload(150, 16, 3, 10, 0.5, 0.1, 0.15, seed=4, n_trees=40, nni=True)
+    one = score_candidates(w.newicks, w.rows, w.Q, w.leaf_order, rng=_r.Random(5), pipeline=1)
+    three = score_candidates(w.newicks, w.rows, w.Q, w.leaf_order, rng=_r.Random(5), pipeline=3)
+    assert len(one.results) == len(three.results) == 40
+    for a, b in zip(one.results, three.results):
+        assert b.llh == pytest.approx(a.llh, rel=1e-9)
+        assert abs(a.iterations - b.iterations) <= 1
+        if a.iterations == b.iterations:
+            np.testing.assert_allclose(b.branch_lengths, a.branch_lengths, rtol=1e-5, atol=1e-8)
+    assert three.h2d_bytes > 0 and three.d2h_bytes > 0
