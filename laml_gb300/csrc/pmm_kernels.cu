@@ -1623,17 +1623,21 @@ struct ClusterTeam {
 // constant).  The root's own branch is in no equality of a single tree and
 // is solved alone.
 //
-// Method: log-barrier interior point on the bounds.  The Newton system of
-// the heights is a weighted tree Laplacian (edge weight W_x = -phi''_x),
+// Method: a primal-dual interior point (Mehrotra predictor-corrector,
+// section 4a below) on the bounds; if it has not converged in kPdMax
+// iterations, a log-barrier interior point continues from its point.  Both
+// solve, per iteration, the Newton system of the heights: a weighted tree
+// Laplacian (edge weight W_x),
 // solved exactly by eliminating nodes from the deepest level up and
 // substituting back down, one depth level (nd_uorder) per team sync; a
 // node's reduced diagonal is kept as the sum of positive terms
 // W_c E_c / (W_c + E_c), which loses nothing to cancellation however large
-// the weights grow.  A backtracking line search tests the barrier
-// objective's change summed branch by branch from log1p/expm1 differences,
-// so no difference of large totals is taken.  Heights, branch lengths, the
-// elimination and every sum are FP64; the transcendental and reciprocal
-// cores (expm1, log1p, 1/x of values formed in FP64) run in FP32, since
+// the weights grow.  In the barrier phase a backtracking line search tests
+// the barrier objective's change summed branch by branch from log1p/expm1
+// differences, so no difference of large totals is taken.  Heights, branch
+// lengths, the elimination and every sum are FP64; in the barrier phase the
+// transcendental and reciprocal cores (expm1, log1p, 1/x of values formed in
+// FP64) run in FP32, since
 // GB300's FP64 pipe is narrow and each enters only a gradient, a weight or a
 // line-search term at FP32 relative precision (the solution moves by ~1e-7
 // relative).  Centring ends when lambda^2 / 2 < 1e-6 or, in the quadratic
@@ -1663,6 +1667,13 @@ constexpr double kMu = 20.0;          // barrier weight growth per centring
 constexpr double kGapRel = 1e-10;     // objective suboptimality m / t, relative
 constexpr double kNewtonTol = 1e-6;   // centred when lambda^2 / 2 is below this
 constexpr int kOuterMax = 30, kNewtonMax = 60, kLineMax = 60;
+// primal-dual phase (slots 11..14 hold z_lo, z_hi, the predictor's branch
+// step and f'(d) while it runs; the barrier phase reuses them)
+constexpr int kZL = 11, kZH = 12, kAD = 13, kF1 = 14;
+constexpr int kPdMax = 60;            // iterations before the barrier phase takes over
+constexpr double kPdMu = 1e-13;       // mean complementarity, relative to 1 + max a
+constexpr double kPdMove = 1e-9;      // largest branch move of the last step, relative to 1 + d
+constexpr double kPdFloor = 1e-14;    // smallest slack to a bound, relative to 1 + d
 
 __device__ __forceinline__ double rcp32(double x) { return (double)(1.f / (float)x); }
 // 1 / x for a positive normal x to ~1e-14: an FP32 seed of the mantissa (the
@@ -1822,7 +1833,250 @@ __device__ __noinline__ bool ultra_dstep(const laml_batch& b, int p, Team& T, do
     double t = 1.0;
     int n_newton = 0, n_line = 0;
 
-    for (int outer = 0; outer < kOuterMax && m > 0.0; ++outer) {
+    // the tree system's elimination, deepest level first, and substitution,
+    // root first (the latter returns this thread's share of gradient . step)
+    auto eliminate = [&]() {
+        for (int l = L - 1; l >= 0; --l) {
+            for (int k = __ldg(off + l) + T.tid(); k < __ldg(off + l + 1); k += T.size()) {
+                const int u = __ldg(ids + k);
+                if (leaf(u)) continue;
+                const int cs[2] = {c0_(u), c1_(u)};
+                double raw = at(cs[0], kG) + at(cs[1], kG) - (u == root ? 0.0 : at(u, kG));
+                at(u, kRaw) = raw;
+                if (at(u, kPin) != 0.0) {
+                    at(u, kE) = 0.0;
+                    at(u, kR) = 0.0;
+                    continue;
+                }
+                double E = 0.0, R = raw;
+                for (int i = 0; i < 2; ++i) {
+                    const int c = cs[i];
+                    const double Wc = at(c, kW);
+                    if (at(c, kPin) != 0.0) {
+                        E += Wc;
+                    } else if (freeb(c)) {
+                        const double Ec = at(c, kE), iD = rcp64(Wc + Ec);
+                        E += Wc * (Ec * iD);
+                        R += Wc * (at(c, kR) * iD);
+                    } else {   // fixed branch: the child's height moves with this one
+                        E += at(c, kE);
+                        R += at(c, kR);
+                    }
+                }
+                at(u, kE) = E;
+                at(u, kR) = R;
+            }
+            T.sync();
+        }
+    };
+    auto substitute = [&]() -> double {
+        double lam = 0.0;
+        for (int l = 0; l < L; ++l) {
+            for (int k = __ldg(off + l) + T.tid(); k < __ldg(off + l + 1); k += T.size()) {
+                const int x = __ldg(ids + k);
+                if (leaf(x)) continue;
+                double del;
+                if (at(x, kPin) != 0.0) {
+                    del = 0.0;
+                } else if (x == root) {
+                    const double E = at(x, kE);
+                    del = E > 0.0 ? at(x, kR) * rcp64(E) : 0.0;
+                } else if (!freeb(x)) {
+                    del = at(par(x), kDel);
+                } else {
+                    const double W = at(x, kW);
+                    del = (at(x, kR) + W * at(par(x), kDel)) * rcp64(W + at(x, kE));
+                }
+                at(x, kDel) = del;
+                lam += at(x, kRaw) * del;
+            }
+            T.sync();
+        }
+        return lam;
+    };
+
+    // 4a. primal-dual interior point (Mehrotra predictor-corrector) on the
+    //     same tree system: duals z_lo, z_hi of every active branch's
+    //     bounds; each iteration solves the system twice (predictor with
+    //     complementarity target 0, corrector with sigma mu and the
+    //     predictor's second-order term) and steps 99% of the way to the
+    //     nearest bound.  FP64 throughout: it takes ~16 passes of
+    //     transcendentals where the barrier phase takes hundreds.  Done when
+    //     the mean complementarity is below kPdMu (1 + max a) and the last
+    //     step moved no branch by more than kPdMove (1 + d); otherwise the
+    //     barrier phase below continues from the point reached.
+    bool pd_done = !(m > 0.0);
+    if (!pd_done) {
+        auto derivs = [&](int x, double d, double& g, double& h) {
+            const double a = at(x, kA), bb = at(x, kB), c = at(x, kC);
+            g = -a;
+            h = 0.0;
+            if (bb > 0.0) {
+                const double e = expm1(d);
+                g += bb / e;
+                h -= bb * (e + 1.0) / (e * e);
+            }
+            if (c > 0.0) {
+                const double e = expm1(nu * d);
+                g += c * nu / e;
+                h -= c * nu * nu * (e + 1.0) / (e * e);
+            }
+        };
+        auto bdist = [&](int x, double& d, double& slo, double& shi) {
+            d = at(par(x), kP) - at(x, kP);
+            slo = d - dlo;
+            shi = dhi - d;
+        };
+        // starting duals: z = mu0 / s, mu0 the mean |f'| times the distance
+        // to the nearer bound
+        double s_loc = 0.0, na = 0.0;
+        for (int x = T.tid(); x < N; x += T.size()) {
+            if (!active(x)) continue;
+            double d, slo, shi, g, h;
+            bdist(x, d, slo, shi);
+            derivs(x, d, g, h);
+            s_loc += fabs(g) * fmin(slo, shi);
+            na = fmax(na, at(x, kA));
+        }
+        const double mu0 = fmax(1e-8, T.sum2(s_loc, 0.0).x / (0.5 * m));
+        const double scale = 1.0 - T.mind(-na);
+        for (int x = T.tid(); x < N; x += T.size()) {
+            if (!active(x)) continue;
+            double d, slo, shi;
+            bdist(x, d, slo, shi);
+            at(x, kZL) = mu0 / slo;
+            at(x, kZH) = mu0 / shi;
+        }
+        T.sync();
+        double move = INFINITY;
+        for (int it = 0; it < kPdMax; ++it) {
+            // (i) f', the weights -f'' + z_lo/s_lo + z_hi/s_hi, the
+            //     predictor's right-hand sides f', and mu
+            double mu_loc = 0.0, smin = INFINITY;
+            for (int x = T.tid(); x < N; x += T.size()) {
+                if (x == root) continue;
+                if (!active(x)) {
+                    at(x, kW) = 0.0;
+                    at(x, kG) = 0.0;
+                    continue;
+                }
+                double d, slo, shi, g, h;
+                bdist(x, d, slo, shi);
+                smin = fmin(smin, fmin(slo, shi) / (1.0 + d));
+                derivs(x, d, g, h);
+                const double zl = at(x, kZL), zh = at(x, kZH);
+                at(x, kF1) = g;
+                at(x, kW) = -h + zl / slo + zh / shi;
+                at(x, kG) = g;
+                mu_loc += zl * slo + zh * shi;
+            }
+            const double mu = T.sum2(mu_loc, 0.0).x / m;   // also orders the writes
+            smin = T.mind(smin);
+            ++n_newton;
+            // done: complementarity small and either nothing moves any more
+            // or a branch sits at its bound to the heights' rounding (its
+            // slack would next round to zero)
+            if (it > 0 && mu < kPdMu * scale && (move < kPdMove || smin < kPdFloor)) {
+                pd_done = true;
+                break;
+            }
+            if (!isfinite(mu)) break;   // not expected; the barrier phase takes over
+            // (ii) predictor: solve, keep each branch's step, longest steps
+            eliminate();
+            substitute();
+            auto zsteps = [&](int x, double dd, double slo, double shi, double tlo, double thi,
+                              double& dzl, double& dzh) {
+                const double zl = at(x, kZL), zh = at(x, kZH);
+                dzl = (tlo - zl * slo - zl * dd) / slo;
+                dzh = (thi - zh * shi + zh * dd) / shi;
+            };
+            auto limits = [&](int x, double dd, double slo, double shi, double dzl, double dzh,
+                              double& ap, double& ad) {
+                if (dd < 0.0) ap = fmin(ap, slo / -dd);
+                if (dd > 0.0) ap = fmin(ap, shi / dd);
+                if (dzl < 0.0) ad = fmin(ad, at(x, kZL) / -dzl);
+                if (dzh < 0.0) ad = fmin(ad, at(x, kZH) / -dzh);
+            };
+            double ap = INFINITY, ad = INFINITY;
+            for (int x = T.tid(); x < N; x += T.size()) {
+                if (!active(x)) continue;
+                double d, slo, shi, dzl, dzh;
+                bdist(x, d, slo, shi);
+                const double dd = at(par(x), kDel) - at(x, kDel);
+                at(x, kAD) = dd;
+                zsteps(x, dd, slo, shi, 0.0, 0.0, dzl, dzh);
+                limits(x, dd, slo, shi, dzl, dzh, ap, ad);
+            }
+            ap = fmin(1.0, T.mind(ap));
+            ad = fmin(1.0, T.mind(ad));
+            // (iii) mu after the predictor's step; sigma = (mu_aff / mu)^3
+            double maff = 0.0;
+            for (int x = T.tid(); x < N; x += T.size()) {
+                if (!active(x)) continue;
+                double d, slo, shi, dzl, dzh;
+                bdist(x, d, slo, shi);
+                const double dd = at(x, kAD);
+                zsteps(x, dd, slo, shi, 0.0, 0.0, dzl, dzh);
+                maff += (at(x, kZL) + ad * dzl) * (slo + ap * dd) +
+                        (at(x, kZH) + ad * dzh) * (shi - ap * dd);
+            }
+            maff = T.sum2(maff, 0.0).x / m;
+            const double r = maff / mu, sigma = fmin(1.0, r * r * r);
+            // (iv) corrector: complementarity targets sigma mu less the
+            //      predictor's second-order term
+            auto targets = [&](int x, double slo, double shi, double& tlo, double& thi) {
+                const double dd = at(x, kAD);
+                double dzl, dzh;
+                zsteps(x, dd, slo, shi, 0.0, 0.0, dzl, dzh);
+                tlo = sigma * mu - dd * dzl;
+                thi = sigma * mu + dd * dzh;
+            };
+            for (int x = T.tid(); x < N; x += T.size()) {
+                if (!active(x)) continue;
+                double d, slo, shi, tlo, thi;
+                bdist(x, d, slo, shi);
+                targets(x, slo, shi, tlo, thi);
+                at(x, kG) = at(x, kF1) + tlo / slo - thi / shi;
+            }
+            T.sync();
+            eliminate();
+            substitute();
+            // (v) one step length for heights and duals, 99% of the way to
+            //     the nearest bound
+            ap = INFINITY;
+            ad = INFINITY;
+            for (int x = T.tid(); x < N; x += T.size()) {
+                if (!active(x)) continue;
+                double d, slo, shi, tlo, thi, dzl, dzh;
+                bdist(x, d, slo, shi);
+                targets(x, slo, shi, tlo, thi);
+                const double dd = at(par(x), kDel) - at(x, kDel);
+                zsteps(x, dd, slo, shi, tlo, thi, dzl, dzh);
+                limits(x, dd, slo, shi, dzl, dzh, ap, ad);
+            }
+            const double al = fmin(1.0, 0.99 * fmin(T.mind(ap), T.mind(ad)));
+            if (!(al > 0.0)) break;   // no step: the barrier phase takes over
+            // (vi) duals and the largest move, then the heights
+            double mv = 0.0;
+            for (int x = T.tid(); x < N; x += T.size()) {
+                if (!active(x)) continue;
+                double d, slo, shi, tlo, thi, dzl, dzh;
+                bdist(x, d, slo, shi);
+                targets(x, slo, shi, tlo, thi);
+                const double dd = at(par(x), kDel) - at(x, kDel);
+                zsteps(x, dd, slo, shi, tlo, thi, dzl, dzh);
+                at(x, kZL) += al * dzl;
+                at(x, kZH) += al * dzh;
+                mv = fmax(mv, fabs(al * dd) / (1.0 + d));
+            }
+            move = -T.mind(-mv);   // every thread has read the heights
+            for (int x = T.tid(); x < N; x += T.size())
+                if (!leaf(x) && at(x, kPin) == 0.0) at(x, kP) += al * at(x, kDel);
+            T.sync();
+        }
+    }
+
+    for (int outer = 0; outer < kOuterMax && !pd_done; ++outer) {
         double lam_prev = INFINITY;
         for (int it = 0; it < kNewtonMax; ++it) {
             // (a) slope and weight of every branch in the barrier objective
@@ -1859,62 +2113,8 @@ __device__ __noinline__ bool ultra_dstep(const laml_batch& b, int p, Team& T, do
                 at(x, kRH) = rh;
             }
             T.sync();
-            // (b) elimination, deepest level first
-            for (int l = L - 1; l >= 0; --l) {
-                for (int k = __ldg(off + l) + T.tid(); k < __ldg(off + l + 1); k += T.size()) {
-                    const int u = __ldg(ids + k);
-                    if (leaf(u)) continue;
-                    const int cs[2] = {c0_(u), c1_(u)};
-                    double raw = at(cs[0], kG) + at(cs[1], kG) - (u == root ? 0.0 : at(u, kG));
-                    at(u, kRaw) = raw;
-                    if (at(u, kPin) != 0.0) {
-                        at(u, kE) = 0.0;
-                        at(u, kR) = 0.0;
-                        continue;
-                    }
-                    double E = 0.0, R = raw;
-                    for (int i = 0; i < 2; ++i) {
-                        const int c = cs[i];
-                        const double Wc = at(c, kW);
-                        if (at(c, kPin) != 0.0) {
-                            E += Wc;
-                        } else if (freeb(c)) {
-                            const double Ec = at(c, kE), iD = rcp64(Wc + Ec);
-                            E += Wc * (Ec * iD);
-                            R += Wc * (at(c, kR) * iD);
-                        } else {   // fixed branch: the child's height moves with this one
-                            E += at(c, kE);
-                            R += at(c, kR);
-                        }
-                    }
-                    at(u, kE) = E;
-                    at(u, kR) = R;
-                }
-                T.sync();
-            }
-            // (c) substitution, root first; lambda^2 = gradient . step
-            double lam = 0.0;
-            for (int l = 0; l < L; ++l) {
-                for (int k = __ldg(off + l) + T.tid(); k < __ldg(off + l + 1); k += T.size()) {
-                    const int x = __ldg(ids + k);
-                    if (leaf(x)) continue;
-                    double del;
-                    if (at(x, kPin) != 0.0) {
-                        del = 0.0;
-                    } else if (x == root) {
-                        const double E = at(x, kE);
-                        del = E > 0.0 ? at(x, kR) * rcp64(E) : 0.0;
-                    } else if (!freeb(x)) {
-                        del = at(par(x), kDel);
-                    } else {
-                        const double W = at(x, kW);
-                        del = (at(x, kR) + W * at(par(x), kDel)) * rcp64(W + at(x, kE));
-                    }
-                    at(x, kDel) = del;
-                    lam += at(x, kRaw) * del;
-                }
-                T.sync();
-            }
+            eliminate();
+            const double lam = substitute();
             const double lam2 = T.sum2(lam, 0.0).x;
             ++n_newton;
             if (!(lam2 * 0.5 > kNewtonTol)) break;
