@@ -365,6 +365,10 @@ int laml_gradient(const laml_batch* b, double* grad_d, double* grad_nu_phi, void
  * gets LAML_TREE_INFEASIBLE.  Ignored in compat mode (the fastEM path has no
  * such constraint). */
 #define LAML_MSTEP_ULTRAMETRIC 2
+/* With LAML_MSTEP_ULTRAMETRIC: solve with the log-barrier method alone (the
+ * primal-dual method's fallback) instead of the primal-dual method first --
+ * slower, kept selectable so both stay checked. */
+#define LAML_MSTEP_ULTRA_BARRIER 4
 /* doubles per node of laml_batch.nd_uwork */
 #define LAML_UWORK_SLOTS 16
 

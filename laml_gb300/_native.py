@@ -19,7 +19,7 @@ ERRORS = {-1: "LAML_ERR_ARG", -2: "LAML_ERR_CUDA", -3: "LAML_ERR_PARSE", -4: "LA
           -5: "LAML_ERR_TIMEOUT", -6: "LAML_ERR_NOT_BINARY", -7: "LAML_ERR_LEAF"}
 TREE_ACTIVE, TREE_CONVERGED, TREE_NAN, TREE_MAXITER, TREE_INFEASIBLE = 0, 1, 2, 3, 4
 MODE_LINEAR, MODE_LOG = 0, 1
-MSTEP_FP64_POLISH, MSTEP_ULTRAMETRIC = 1, 2
+MSTEP_FP64_POLISH, MSTEP_ULTRAMETRIC, MSTEP_ULTRA_BARRIER = 1, 2, 4
 UWORK_SLOTS = 16   # LAML_UWORK_SLOTS: doubles per node of nd_uwork
 OUT_POSTERIORS, OUT_TRUE_ROOT = 1, 2
 

@@ -1701,7 +1701,7 @@ __device__ __forceinline__ double log1mexp32(double x) {   // log(1 - e^{-x}), x
 // cycles instead of a round trip to L2.
 template <class Team, bool SH>
 __device__ __noinline__ bool ultra_dstep(const laml_batch& b, int p, Team& T, double nu,
-                                         bool use_s, float* Dd, double* hot) {
+                                         bool use_s, float* Dd, double* hot, bool pd) {
     using namespace ultra;
     const int N = __ldg(b.tr_nodes + p), base = __ldg(b.tr_node_base + p);
     const int root = __ldg(b.tr_root + p) - base;
@@ -1906,7 +1906,7 @@ __device__ __noinline__ bool ultra_dstep(const laml_batch& b, int p, Team& T, do
     //     step moved no branch by more than kPdMove (1 + d); otherwise the
     //     barrier phase below continues from the point reached.
     bool pd_done = !(m > 0.0);
-    if (!pd_done) {
+    if (!pd_done && pd) {
         auto derivs = [&](int x, double d, double& g, double& h) {
             const double a = at(x, kA), bb = at(x, kB), c = at(x, kC);
             g = -a;
@@ -2191,6 +2191,7 @@ __device__ void mstep_tree(const laml_batch& b, int p, int rounds, Team& T, floa
                            float* s_d, int flags, double* usm = nullptr, int ucap = 0) {
     const bool polish = (flags & LAML_MSTEP_FP64_POLISH) != 0;
     const bool ultra = (flags & LAML_MSTEP_ULTRAMETRIC) != 0 && !b.compat;
+    const bool upd = (flags & LAML_MSTEP_ULTRA_BARRIER) == 0;   // primal-dual phase first
     if (__ldcg(b.tr_status + p) != LAML_TREE_ACTIVE) return;
     const int N = __ldg(b.tr_nodes + p), n = __ldg(b.tr_leaves + p), base = __ldg(b.tr_node_base + p);
     const int ds = __ldg(b.tr_ds + p), NG = __ldg(b.ds_groups + ds), K = __ldg(b.ds_sites + ds);
@@ -2274,8 +2275,8 @@ __device__ void mstep_tree(const laml_batch& b, int p, int rounds, Team& T, floa
             // EM_solver.Mstep returns "d_infeasible" before it places any
             // parameter (EM_solver.py:419-420): the tree keeps d, nu and phi
             const bool ok = (usm && N <= ucap)
-                                ? ultra_dstep<Team, true>(b, p, T, nu, use_s, Dd, usm)
-                                : ultra_dstep<Team, false>(b, p, T, nu, use_s, Dd, nullptr);
+                                ? ultra_dstep<Team, true>(b, p, T, nu, use_s, Dd, usm, upd)
+                                : ultra_dstep<Team, false>(b, p, T, nu, use_s, Dd, nullptr, upd);
             if (!ok) {
                 if (T.leader()) b.tr_status[p] = LAML_TREE_INFEASIBLE;
                 T.sync();

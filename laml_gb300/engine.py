@@ -265,7 +265,8 @@ class DeviceBatch:
 
     def _mflags(self, polish):
         return ((N.MSTEP_FP64_POLISH if self._polish(polish) else 0) |
-                (N.MSTEP_ULTRAMETRIC if self.ultrametric else 0))
+                (N.MSTEP_ULTRAMETRIC if self.ultrametric else 0) |
+                (N.MSTEP_ULTRA_BARRIER if getattr(self, "ultra_barrier", False) else 0))
 
     def mstep(self, rounds=MSTEP_ROUNDS, polish=None):
         N.check(N.lib().laml_mstep(C.byref(self.b), rounds, self._mflags(polish), self._s()))

@@ -247,3 +247,36 @@ def test_topology_search_ultrametric_em_solver():
     strategy["ultra_constr"] = True
     _, max_score, _ = search.search(maxiter=200, verbose=False, strategy=strategy, nreps=1)
     assert round(-max_score - case["nllh_bf"], 4) == 0
+
+
+@pytest.mark.parametrize("n,K,seed,nu,fixed", [CASES[1], CASES[4]])
+def test_ultrametric_barrier_only_matches_primal_dual(n, K, seed, nu, fixed):
+    """LAML_MSTEP_ULTRA_BARRIER: the log-barrier method alone (the
+    primal-dual method's fallback) solves the same M-step: against the oracle
+    on the device's counts and against the primal-dual solution."""
+    w = synth.pmm_workload(n, K, 3, 12, 0.5, 0.1, 0.15, seed=seed)
+    rng = np.random.default_rng(seed)
+    tr = O.parse_tree(w.newicks[0], w.leaf_order)
+    N_ = len(tr.parent)
+    d0 = _start(tr.parent, rng)
+    mask = rng.random(N_) >= fixed
+    if fixed > 0:
+        d0 = np.where(mask, d0, _ultrametric_lengths(tr, rng))
+    out = []
+    for barrier in (False, True):
+        b = PB.make_batch(w.newicks, w.rows, w.Q, w.leaf_order, compat=False, nu=nu,
+                          phi=0.15, d=[d0], mask=[mask], clamp=False, ultrametric=True,
+                          fix_nu=True, fix_phi=True)
+        b.ultra_barrier = barrier
+        b.e_step()
+        b.mstep()
+        torch.cuda.synchronize()
+        out.append((b.results()[0], b.work["nd_cnt"].cpu().numpy().reshape(-1, 6)[:N_, :5]))
+    (rp, Sp), (rb, Sb) = out
+    np.testing.assert_array_equal(Sp, Sb)   # the same E-step
+    od, ok = O.ultrametric_d(Sb, nu, d0, mask, tr)
+    assert ok
+    np.testing.assert_allclose(rb.branch_lengths, od, rtol=3e-6, atol=1e-7)
+    np.testing.assert_allclose(rb.branch_lengths, rp.branch_lengths, rtol=3e-6, atol=1e-7)
+    p = _paths(tr.parent, tr.num_leaves, rb.branch_lengths)
+    assert np.ptp(p) <= 1e-9 * np.max(p)
