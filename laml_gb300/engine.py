@@ -86,7 +86,9 @@ class DeviceBatch:
     ``nu``, ``phi``: per-tree starting values; ``mask``: per-tree bool arrays
     (True = branch length optimised); ``fix_nu`` / ``fix_phi``: per-tree flags;
     ``ultrametric``: exact model only -- every M-step solves the branch
-    lengths under EM_solver's ultrametric equalities (EM_solver.py:53-89).
+    lengths under EM_solver's ultrametric equalities (EM_solver.py:53-89),
+    by the primal-dual method (set the attribute ``ultra_barrier`` to use the
+    log-barrier method alone).
     """
 
     def __init__(self, datasets: Sequence[EncodedDataset], trees: Sequence[EncodedTree],
