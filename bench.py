@@ -567,6 +567,7 @@ def main():
                           nu=0.5, phi=0.5, device=dev, stream=stream)
         b.branch_terms()
         b.inside(update_em=True)
+    llh_start = b.work["tr_llh"].cpu().numpy().copy()
     T = b.T
     nodes = b.sizes["n_nodes"]
     K = b.datasets[0].n_sites
@@ -685,6 +686,20 @@ def main():
             cpu = {"value": None, "unit": UNIT, "cores": 0, "kind": "port",
                    "sample": f"unavailable: {ex}"}
 
+    # parity: every candidate's log-likelihood at the starting parameters
+    # against the FP64 C restatement (not timed)
+    parity = None
+    if rank == 0 and not args.no_cpu:
+        try:
+            from oracle import cpu_port
+            ref = cpu_port.loglik(w.newicks, w.rows, w.Q, w.leaf_order, 0.5, 0.5)
+            rel = np.abs(llh_start / ref - 1.0)
+            parity = {"max_rel_err_llh": float(rel.max()), "trees": int(len(ref)),
+                      "tolerance": 1e-6, "oracle": "FP64 C restatement of the fastEM path",
+                      "at": "starting parameters nu = phi = 0.5, newick branch lengths"}
+        except Exception as ex:  # reported, never required
+            parity = {"max_rel_err_llh": None, "error": str(ex)}
+
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
@@ -711,6 +726,7 @@ def main():
             "path": args.path,
             "wall_s_timed": t1 - t0,
             "llh_mean": float(np.mean(llh_now)),
+            "parity": parity,
         }
         print(json.dumps(line), flush=True)
     if world > 1:

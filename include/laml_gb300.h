@@ -285,6 +285,10 @@ typedef struct laml_batch {
      * nd_uwork [LAML_UWORK_SLOTS * n_nodes] -- FP64 scratch of the solve. */
     const int32_t* nd_uorder;
     double* nd_uwork;
+    /* the plan's part_floats and scalar_len (laml_plan_sizes): the sizes of
+     * in_part and of in_x / in_h / in_dot; laml_inside_noalloc refuses a
+     * batch without them */
+    int64_t plan_part_floats, plan_scalar_len;
 } laml_batch;
 
 /* A tree's partials are FP32 values with power-of-two exponents (linear)
@@ -369,8 +373,13 @@ int laml_gradient(const laml_batch* b, double* grad_d, double* grad_nu_phi, void
  * primal-dual method's fallback) instead of the primal-dual method first --
  * slower, kept selectable so both stay checked. */
 #define LAML_MSTEP_ULTRA_BARRIER 4
+/* With LAML_MSTEP_ULTRAMETRIC: stop the primal-dual method after 3 iterations
+ * and let the log-barrier method continue from the point it reached (the
+ * fallback the solve takes when the primal-dual method has not converged in
+ * 60 iterations), so that path stays checked. */
+#define LAML_MSTEP_ULTRA_PD_SHORT 8
 /* doubles per node of laml_batch.nd_uwork */
-#define LAML_UWORK_SLOTS 16
+#define LAML_UWORK_SLOTS 17
 
 /* M-step of every active tree: compat maximises the fastEM objective
  * (fast_em/laml.py:62-78) by `rounds` coordinate-ascent rounds; exact follows
@@ -404,9 +413,14 @@ int laml_em_run_levels(const laml_batch* b, int32_t iters, int32_t rounds, doubl
  * every GPU which loads the library holds until the process exits; the caller
  * passes the batch's plan sizes (laml_plan_sizes.part_floats / scalar_len) and
  * a batch whose 4 * part_floats + 12 * scalar_len bytes (plus alignment)
- * exceed 32 MiB is rejected with LAML_ERR_ARG.  The first call on each device
+ * exceed 32 MiB is rejected with LAML_ERR_ARG, and so are sizes below the
+ * batch's own plan sizes (laml_batch.plan_part_floats / plan_scalar_len,
+ * which must be filled).  The first call on each device
  * looks up the array's device address (cudaGetSymbolAddress) with that device
- * current; make that first call before any stream capture.  Every call shares
+ * current; make that first call before any stream capture.  The address is
+ * kept for the life of the process: it does not survive cudaDeviceReset (or
+ * any other teardown of the device's primary context) in the same process,
+ * after which this entry point must not be called on that device.  Every call shares
  * the one array: calls whose work overlaps on the GPU race and must be
  * serialised by the caller (one stream, or events).  Nothing in the array has
  * to start at zero: the pass writes every word it reads. */

@@ -20,7 +20,8 @@ ERRORS = {-1: "LAML_ERR_ARG", -2: "LAML_ERR_CUDA", -3: "LAML_ERR_PARSE", -4: "LA
 TREE_ACTIVE, TREE_CONVERGED, TREE_NAN, TREE_MAXITER, TREE_INFEASIBLE = 0, 1, 2, 3, 4
 MODE_LINEAR, MODE_LOG = 0, 1
 MSTEP_FP64_POLISH, MSTEP_ULTRAMETRIC, MSTEP_ULTRA_BARRIER = 1, 2, 4
-UWORK_SLOTS = 16   # LAML_UWORK_SLOTS: doubles per node of nd_uwork
+MSTEP_ULTRA_PD_SHORT = 8
+UWORK_SLOTS = 17   # LAML_UWORK_SLOTS: doubles per node of nd_uwork
 OUT_POSTERIORS, OUT_TRUE_ROOT = 1, 2
 
 
@@ -86,6 +87,7 @@ BATCH_FIELDS = [
     ("h_in_level_off", vp), ("h_out_level_off", vp),
     ("barrier", vp), ("error", vp), ("max_states", i32), ("max_tree_nodes", i32),
     ("tr_leaf", vp), ("nd_uorder", vp), ("nd_uwork", vp),
+    ("plan_part_floats", i64), ("plan_scalar_len", i64),
 ]
 
 

@@ -1660,8 +1660,9 @@ constexpr int kA = 8, kB = 9, kC = 10;   // objective coefficients of the node's
 constexpr int kIE = 11, kIEN = 12;       // 1 / expm1(d), 1 / expm1(nu d) at the current d
 constexpr int kRL = 13, kRH = 14;        // 1 / (d - dmin), 1 / (dmax - d)
 constexpr int kStat = 15;   // root: Newton steps of the last solve; node 0: line-search passes
+constexpr int kBak = 16;    // the primal-dual phase's last heights with every slack positive
 constexpr int kSlots = LAML_UWORK_SLOTS;
-static_assert(kSlots >= 15, "nd_uwork slots");
+static_assert(kSlots >= 17, "nd_uwork slots");
 constexpr double kTheta = 0.1;        // pull of the start point toward its interval's middle
 constexpr double kMu = 20.0;          // barrier weight growth per centring
 constexpr double kGapRel = 1e-10;     // objective suboptimality m / t, relative
@@ -1671,6 +1672,7 @@ constexpr int kOuterMax = 30, kNewtonMax = 60, kLineMax = 60;
 // step and f'(d) while it runs; the barrier phase reuses them)
 constexpr int kZL = 11, kZH = 12, kAD = 13, kF1 = 14;
 constexpr int kPdMax = 60;            // iterations before the barrier phase takes over
+constexpr int kPdShort = 3;           // the same with LAML_MSTEP_ULTRA_PD_SHORT
 constexpr double kPdMu = 1e-13;       // mean complementarity, relative to 1 + max a
 constexpr double kPdMove = 1e-9;      // largest branch move of the last step, relative to 1 + d
 constexpr double kPdFloor = 1e-14;    // smallest slack to a bound, relative to 1 + d
@@ -1699,9 +1701,13 @@ __device__ __forceinline__ double log1mexp32(double x) {   // log(1 - e^{-x}), x
 // thread touches stay in nd_uwork.  Each level of the elimination is a chain
 // of dependent loads of these slots, which shared memory serves in tens of
 // cycles instead of a round trip to L2.
+// Returns kUltraOk, kUltraInfeasible (the constraints admit no lengths in
+// [dmin, dmax]) or kUltraNaN (a height is not finite: nothing is written).
+// pd_iters: iterations of the primal-dual phase (0: the barrier phase alone).
+constexpr int kUltraOk = 0, kUltraInfeasible = 1, kUltraNaN = 2;
 template <class Team, bool SH>
-__device__ __noinline__ bool ultra_dstep(const laml_batch& b, int p, Team& T, double nu,
-                                         bool use_s, float* Dd, double* hot, bool pd) {
+__device__ __noinline__ int ultra_dstep(const laml_batch& b, int p, Team& T, double nu,
+                                        bool use_s, float* Dd, double* hot, int pd_iters) {
     using namespace ultra;
     const int N = __ldg(b.tr_nodes + p), base = __ldg(b.tr_node_base + p);
     const int root = __ldg(b.tr_root + p) - base;
@@ -1789,7 +1795,7 @@ __device__ __noinline__ bool ultra_dstep(const laml_batch& b, int p, Team& T, do
         }
         T.sync();
     }
-    if (T.maxi(bad)) return false;
+    if (T.maxi(bad)) return kUltraInfeasible;
 
     // 2. strictly feasible start, top-down: each height the warm start
     //    clamped to what its parent's height leaves, pulled kTheta toward the
@@ -1906,7 +1912,7 @@ __device__ __noinline__ bool ultra_dstep(const laml_batch& b, int p, Team& T, do
     //     step moved no branch by more than kPdMove (1 + d); otherwise the
     //     barrier phase below continues from the point reached.
     bool pd_done = !(m > 0.0);
-    if (!pd_done && pd) {
+    if (!pd_done && pd_iters > 0) {
         auto derivs = [&](int x, double d, double& g, double& h) {
             const double a = at(x, kA), bb = at(x, kB), c = at(x, kC);
             g = -a;
@@ -1949,10 +1955,16 @@ __device__ __noinline__ bool ultra_dstep(const laml_batch& b, int p, Team& T, do
         }
         T.sync();
         double move = INFINITY;
-        for (int it = 0; it < kPdMax; ++it) {
+        for (int it = 0; it < pd_iters; ++it) {
             // (i) f', the weights -f'' + z_lo/s_lo + z_hi/s_hi, the
-            //     predictor's right-hand sides f', and mu
+            //     predictor's right-hand sides f', and mu.  The heights of a
+            //     branch move separately, so its length can round onto or
+            //     past a bound although the step stopped 99% of the way
+            //     there: then the phase ends at the heights of the previous
+            //     iteration (kBak, every slack positive there) and the
+            //     barrier phase continues from them
             double mu_loc = 0.0, smin = INFINITY;
+            int lost = 0;
             for (int x = T.tid(); x < N; x += T.size()) {
                 if (x == root) continue;
                 if (!active(x)) {
@@ -1962,6 +1974,10 @@ __device__ __noinline__ bool ultra_dstep(const laml_batch& b, int p, Team& T, do
                 }
                 double d, slo, shi, g, h;
                 bdist(x, d, slo, shi);
+                if (!(slo > 0.0 && shi > 0.0)) {   // also NaN
+                    lost = 1;
+                    continue;
+                }
                 smin = fmin(smin, fmin(slo, shi) / (1.0 + d));
                 derivs(x, d, g, h);
                 const double zl = at(x, kZL), zh = at(x, kZH);
@@ -1969,6 +1985,12 @@ __device__ __noinline__ bool ultra_dstep(const laml_batch& b, int p, Team& T, do
                 at(x, kW) = -h + zl / slo + zh / shi;
                 at(x, kG) = g;
                 mu_loc += zl * slo + zh * shi;
+            }
+            if (T.maxi(lost)) {   // it > 0: the start point is strictly feasible
+                for (int x = T.tid(); x < N; x += T.size())
+                    if (!leaf(x) && at(x, kPin) == 0.0) at(x, kP) = at(x, kBak);
+                T.sync();
+                break;
             }
             const double mu = T.sum2(mu_loc, 0.0).x / m;   // also orders the writes
             smin = T.mind(smin);
@@ -2071,7 +2093,10 @@ __device__ __noinline__ bool ultra_dstep(const laml_batch& b, int p, Team& T, do
             }
             move = -T.mind(-mv);   // every thread has read the heights
             for (int x = T.tid(); x < N; x += T.size())
-                if (!leaf(x) && at(x, kPin) == 0.0) at(x, kP) += al * at(x, kDel);
+                if (!leaf(x) && at(x, kPin) == 0.0) {
+                    at(x, kBak) = at(x, kP);
+                    at(x, kP) += al * at(x, kDel);
+                }
             T.sync();
         }
     }
@@ -2164,7 +2189,13 @@ __device__ __noinline__ bool ultra_dstep(const laml_batch& b, int p, Team& T, do
         t *= kMu;
     }
 
-    // 4. branch lengths from the heights; the root's branch alone
+    // 4. branch lengths from the heights; the root's branch alone.  A height
+    //    that is not finite (not expected) ends the solve with nothing
+    //    written, instead of clamping a NaN length onto a bound
+    int nonfinite = 0;
+    for (int x = T.tid(); x < N; x += T.size())
+        if (!isfinite(at(x, kP))) nonfinite = 1;
+    if (T.maxi(nonfinite)) return kUltraNaN;
     if (T.leader()) {
         at(root, kStat) = (double)n_newton;
         at(0, kStat) = (double)n_line;
@@ -2183,7 +2214,7 @@ __device__ __noinline__ bool ultra_dstep(const laml_batch& b, int p, Team& T, do
         }
     }
     T.sync();
-    return true;
+    return kUltraOk;
 }
 
 template <class Team>
@@ -2191,7 +2222,10 @@ __device__ void mstep_tree(const laml_batch& b, int p, int rounds, Team& T, floa
                            float* s_d, int flags, double* usm = nullptr, int ucap = 0) {
     const bool polish = (flags & LAML_MSTEP_FP64_POLISH) != 0;
     const bool ultra = (flags & LAML_MSTEP_ULTRAMETRIC) != 0 && !b.compat;
-    const bool upd = (flags & LAML_MSTEP_ULTRA_BARRIER) == 0;   // primal-dual phase first
+    // primal-dual phase first (capped at kPdShort iterations to test the
+    // barrier phase's continuation from its point)
+    const int upd = (flags & LAML_MSTEP_ULTRA_BARRIER) ? 0
+                    : (flags & LAML_MSTEP_ULTRA_PD_SHORT) ? ultra::kPdShort : ultra::kPdMax;
     if (__ldcg(b.tr_status + p) != LAML_TREE_ACTIVE) return;
     const int N = __ldg(b.tr_nodes + p), n = __ldg(b.tr_leaves + p), base = __ldg(b.tr_node_base + p);
     const int ds = __ldg(b.tr_ds + p), NG = __ldg(b.ds_groups + ds), K = __ldg(b.ds_sites + ds);
@@ -2274,11 +2308,12 @@ __device__ void mstep_tree(const laml_batch& b, int p, int rounds, Team& T, floa
         if (ultra) {
             // EM_solver.Mstep returns "d_infeasible" before it places any
             // parameter (EM_solver.py:419-420): the tree keeps d, nu and phi
-            const bool ok = (usm && N <= ucap)
-                                ? ultra_dstep<Team, true>(b, p, T, nu, use_s, Dd, usm, upd)
-                                : ultra_dstep<Team, false>(b, p, T, nu, use_s, Dd, nullptr, upd);
-            if (!ok) {
-                if (T.leader()) b.tr_status[p] = LAML_TREE_INFEASIBLE;
+            const int us = (usm && N <= ucap)
+                               ? ultra_dstep<Team, true>(b, p, T, nu, use_s, Dd, usm, upd)
+                               : ultra_dstep<Team, false>(b, p, T, nu, use_s, Dd, nullptr, upd);
+            if (us != kUltraOk) {
+                if (T.leader())
+                    b.tr_status[p] = us == kUltraNaN ? LAML_TREE_NAN : LAML_TREE_INFEASIBLE;
                 T.sync();
                 return;
             }
@@ -3684,6 +3719,16 @@ extern "C" int laml_inside_noalloc(const laml_batch* b, int64_t part_floats, int
     if (rc) return rc;
     if (part_floats < 0 || scalar_len < 0) {
         laml::set_error("laml_inside_noalloc: negative size");
+        return LAML_ERR_ARG;
+    }
+    // the level kernels write at the plan's row offsets: sizes below the
+    // plan's would put those writes past the carve-outs below
+    if (b->plan_part_floats <= 0 || part_floats < b->plan_part_floats ||
+        scalar_len < b->plan_scalar_len) {
+        laml::set_error("laml_inside_noalloc: part_floats / scalar_len must be at least the "
+                        "batch's plan sizes (laml_batch.plan_part_floats = " +
+                        std::to_string(b->plan_part_floats) + ", plan_scalar_len = " +
+                        std::to_string(b->plan_scalar_len) + ")");
         return LAML_ERR_ARG;
     }
     const size_t need = align256((size_t)part_floats * sizeof(float)) +

@@ -105,6 +105,10 @@ class DeviceBatch:
             raise ValueError("the ultrametric M-step belongs to the exact model (compat=False)")
         self.T, self.compat, self.G = T, compat, G
         self.ultrametric = bool(ultrametric)
+        # select the ultrametric M-step's log-barrier method alone
+        self.ultra_barrier = False
+        # cap its primal-dual phase at 3 iterations (the barrier phase continues)
+        self.ultra_pd_short = False
         self.device = torch.device(device)
         self.stream = stream
         self.trees = list(trees)
@@ -211,6 +215,8 @@ class DeviceBatch:
         b.max_states = int(max(int(np.max(x.group_C)) for x in datasets))
         # the largest tree: whether the M-step needs its cluster kernel
         b.max_tree_nodes = int(max(t.num_nodes for t in trees))
+        b.plan_part_floats = int(sizes["part_floats"])
+        b.plan_scalar_len = int(sizes["scalar_len"])
         for name, _ in N.BATCH_FIELDS:
             if name in v:
                 setattr(b, name, v[name].data_ptr())
@@ -268,7 +274,8 @@ class DeviceBatch:
     def _mflags(self, polish):
         return ((N.MSTEP_FP64_POLISH if self._polish(polish) else 0) |
                 (N.MSTEP_ULTRAMETRIC if self.ultrametric else 0) |
-                (N.MSTEP_ULTRA_BARRIER if getattr(self, "ultra_barrier", False) else 0))
+                (N.MSTEP_ULTRA_BARRIER if self.ultra_barrier else 0) |
+                (N.MSTEP_ULTRA_PD_SHORT if self.ultra_pd_short else 0))
 
     def mstep(self, rounds=MSTEP_ROUNDS, polish=None):
         N.check(N.lib().laml_mstep(C.byref(self.b), rounds, self._mflags(polish), self._s()))

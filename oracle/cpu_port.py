@@ -43,15 +43,18 @@ def lib():
         L.ora_em.argtypes = [C.POINTER(OraTree), C.c_int, C.c_int, C.c_int]
         L.ora_loglik.restype = None
         L.ora_loglik.argtypes = [C.POINTER(OraTree), C.c_int]
+        L.ora_site_loglik.restype = None
+        L.ora_site_loglik.argtypes = [C.POINTER(OraTree), C.c_void_p]
         L.ora_num_threads.restype = C.c_int
         _lib = L
     return _lib
 
 
-def _prepare(newicks, rows, Q, leaf_order, nu, phi):
+def _prepare(newicks, rows, Q, leaf_order, nu, phi, ds=None, enc=None):
     keep = []
     trees = (OraTree * len(newicks))()
-    enc = O.recode([rows[c] for c in leaf_order], Q, compat=True)
+    if enc is None:
+        enc = O.recode([rows[c] for c in leaf_order], Q, compat=True)
     chars = np.ascontiguousarray(enc.chars, np.int32)
     kc = np.ascontiguousarray(enc.k, np.int32)
     q = np.ascontiguousarray(enc.q, np.float64)
@@ -61,7 +64,7 @@ def _prepare(newicks, rows, Q, leaf_order, nu, phi):
         c0 = np.array([c[0] if c else -1 for c in tr.children], np.int32)
         c1 = np.array([c[1] if c else -1 for c in tr.children], np.int32)
         par = tr.parent.astype(np.int32)
-        d = tr.branch_lengths.astype(np.float64).copy()
+        d = (tr.branch_lengths if ds is None else ds[i]).astype(np.float64).copy()
         keep += [c0, c1, par, d]
         trees[i] = OraTree(len(par), tr.num_leaves, chars.shape[1], c0.ctypes.data,
                            c1.ctypes.data, par.ctypes.data, chars.ctypes.data, kc.ctypes.data,
@@ -77,6 +80,27 @@ def em(newicks, rows, Q, leaf_order, nu=0.5, phi=0.5, iters=1, rounds=4):
                                 shape=(trees[i].N,)).copy() for i in range(len(newicks))]
     return ([trees[i].llh for i in range(len(newicks))], [trees[i].nu for i in range(len(newicks))],
             [trees[i].phi for i in range(len(newicks))], ds, t)
+
+
+def loglik(newicks, rows, Q, leaf_order, nu, phi, ds=None):
+    """fastEM log-likelihood of every tree at (d, nu, phi), one tree per core;
+    ``ds``: branch lengths per tree in the parse_tree numbering (default: the
+    newick's)."""
+    trees, keep = _prepare(newicks, rows, Q, leaf_order, nu, phi, ds)
+    lib().ora_loglik(trees, len(newicks))
+    return np.array([trees[i].llh for i in range(len(newicks))])
+
+
+def site_loglik(newick, rows, Q, leaf_order, nu, phi, d=None, enc=None):
+    """Per-site fastEM log-likelihood of one tree (original site order), sites
+    in parallel: the form that fits 50,000-leaf x 300-site trees."""
+    if enc is None:
+        enc = O.recode([rows[c] for c in leaf_order], Q, compat=True)
+    trees, keep = _prepare([newick], rows, Q, leaf_order, nu, phi,
+                           None if d is None else [np.asarray(d)], enc)
+    out = np.zeros(enc.chars.shape[1])
+    lib().ora_site_loglik(trees, out.ctypes.data)
+    return out
 
 
 def em_throughput(workload, n_trees, iters):

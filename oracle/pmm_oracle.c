@@ -304,6 +304,90 @@ void ora_loglik(ora_tree* trees, int n_trees) {
     }
 }
 
+/* Per-site log-likelihood of one tree, sites in parallel (one site's column
+ * of inside rows at a time per thread: N * (k_c + 2) doubles), so trees too
+ * large for ora_loglik's whole-tree rows (50,000 leaves x 300 sites) fit.
+ * Same arithmetic as inside() restricted to site c: leaf rows
+ * (calculations.py:278-334), edge-inside (calculations.py:47-91) summed over
+ * the two children in postorder (calculations.py:240-251), the root's own
+ * edge from state 0 (calculations.py:270-276). */
+void ora_site_loglik(const ora_tree* T, double* per_site) {
+    int root = -1;
+    for (int v = 0; v < T->N; ++v)
+        if (T->parent[v] < 0) root = v;
+#pragma omp parallel
+    {
+        int kmax = 0;
+        for (int c = 0; c < T->K; ++c) if (T->kc[c] > kmax) kmax = T->kc[c];
+        const int Rm = kmax + 2;
+        double* col = (double*)malloc(sizeof(double) * (size_t)T->N * Rm);
+        double* e = (double*)malloc(sizeof(double) * 2 * Rm);
+        double* lq = (double*)malloc(sizeof(double) * Rm);
+        double *t1 = (double*)malloc(sizeof(double) * T->N), *t2 = (double*)malloc(sizeof(double) * T->N);
+        double *t3 = (double*)malloc(sizeof(double) * T->N), *a0 = (double*)malloc(sizeof(double) * T->N);
+        for (int v = 0; v < T->N; ++v) {
+            double d = T->d[v], nd = d * T->nu;
+            t1[v] = -nd;
+            t2[v] = nd < EPS ? log(EPS) : log(-expm1(-nd));
+            t3[v] = d < EPS ? log(EPS) : log(-expm1(-d));
+            a0[v] = -d * (1.0 + T->nu);
+        }
+        const double e1 = log(fmax(1.0 - T->phi, EPS)), ep = log(fmax(T->phi, EPS));
+#pragma omp for schedule(dynamic, 1)
+        for (int c = 0; c < T->K; ++c) {
+            const int k = T->kc[c], R = k + 2, s = k + 1;
+            for (int a = 1; a <= k; ++a) {
+                double qv = T->q[c * T->kmax + a - 1];
+                lq[a] = qv > 0 ? log(qv) : -INFINITY;
+            }
+            for (int v = 0; v < T->n; ++v) {
+                const int ch = T->chars[(size_t)v * T->K + c];
+                double* x = col + (size_t)v * R;
+                for (int a = 0; a <= k; ++a) x[a] = (a == ch) ? e1 : (ch == -1 ? ep : -INFINITY);
+                x[s] = ch == -1 ? 0.0 : log(EPS);
+            }
+            /* children before parents: internal ids grow down the tree */
+            for (int u = T->N - 1; u >= T->n; --u) {
+                const int kids[2] = {T->c0[u], T->c1[u]};
+                for (int z = 0; z < 2; ++z) {
+                    const int v = kids[z];
+                    const double* x = col + (size_t)v * R;
+                    double* ev = e + z * Rm;
+                    double m = a0[v] + x[0];
+                    for (int a = 1; a <= k; ++a) {
+                        double y = t1[v] + lq[a] + t3[v] + x[a];
+                        if (y > m) m = y;
+                    }
+                    if (t2[v] + x[s] > m) m = t2[v] + x[s];
+                    if (m == -INFINITY) {
+                        ev[0] = -INFINITY;
+                    } else {
+                        double sum = exp(a0[v] + x[0] - m) + exp(t2[v] + x[s] - m);
+                        for (int a = 1; a <= k; ++a) sum += exp(t1[v] + lq[a] + t3[v] + x[a] - m);
+                        ev[0] = m + log(sum);
+                    }
+                    for (int a = 1; a <= k; ++a) ev[a] = lse2(t1[v] + x[a], t2[v] + x[s]);
+                    ev[s] = x[s];
+                }
+                double* r = col + (size_t)u * R;
+                for (int j = 0; j < R; ++j) r[j] = e[j] + e[Rm + j];
+            }
+            /* the root's own edge, from a progenitor in state 0 */
+            const double* x = col + (size_t)root * R;
+            double m = a0[root] + x[0];
+            for (int a = 1; a <= k; ++a) {
+                double y = t1[root] + lq[a] + t3[root] + x[a];
+                if (y > m) m = y;
+            }
+            if (t2[root] + x[s] > m) m = t2[root] + x[s];
+            double sum = exp(a0[root] + x[0] - m) + exp(t2[root] + x[s] - m);
+            for (int a = 1; a <= k; ++a) sum += exp(t1[root] + lq[a] + t3[root] + x[a] - m);
+            per_site[c] = m + log(sum);
+        }
+        free(col); free(e); free(lq); free(t1); free(t2); free(t3); free(a0);
+    }
+}
+
 /* `iters` EM iterations per tree (E-step, M-step, log-likelihood), with the
  * starting inside pass outside the timed part.  Returns the seconds spent in
  * the iterations (max over threads = wall time of the parallel region). */

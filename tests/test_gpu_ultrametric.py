@@ -249,11 +249,14 @@ def test_topology_search_ultrametric_em_solver():
     assert round(-max_score - case["nllh_bf"], 4) == 0
 
 
+@pytest.mark.parametrize("mode", ["barrier", "pd_short"])
 @pytest.mark.parametrize("n,K,seed,nu,fixed", [CASES[1], CASES[4]])
-def test_ultrametric_barrier_only_matches_primal_dual(n, K, seed, nu, fixed):
-    """LAML_MSTEP_ULTRA_BARRIER: the log-barrier method alone (the
-    primal-dual method's fallback) solves the same M-step: against the oracle
-    on the device's counts and against the primal-dual solution."""
+def test_ultrametric_barrier_only_matches_primal_dual(n, K, seed, nu, fixed, mode):
+    """The primal-dual method's fallback solves the same M-step, against the
+    oracle on the device's counts and against the primal-dual solution:
+    LAML_MSTEP_ULTRA_BARRIER (the log-barrier method alone) and
+    LAML_MSTEP_ULTRA_PD_SHORT (3 primal-dual iterations, then the barrier
+    method from the near-boundary point they reach)."""
     w = synth.pmm_workload(n, K, 3, 12, 0.5, 0.1, 0.15, seed=seed)
     rng = np.random.default_rng(seed)
     tr = O.parse_tree(w.newicks[0], w.leaf_order)
@@ -267,7 +270,8 @@ def test_ultrametric_barrier_only_matches_primal_dual(n, K, seed, nu, fixed):
         b = PB.make_batch(w.newicks, w.rows, w.Q, w.leaf_order, compat=False, nu=nu,
                           phi=0.15, d=[d0], mask=[mask], clamp=False, ultrametric=True,
                           fix_nu=True, fix_phi=True)
-        b.ultra_barrier = barrier
+        b.ultra_barrier = barrier and mode == "barrier"
+        b.ultra_pd_short = barrier and mode == "pd_short"
         b.e_step()
         b.mstep()
         torch.cuda.synchronize()

@@ -44,3 +44,22 @@ def test_c_port_large_tree_root_row():
     assert r.trace[1] > r.trace[0] and r.trace[2] > r.trace[1]
     assert abs(llh[0] / r.llh - 1) < 1e-12
     np.testing.assert_allclose(ds[0], r.d, rtol=1e-10)
+
+
+def test_c_port_loglik_forms_match_numpy_oracle():
+    """The whole-tree (ora_loglik) and per-site (ora_site_loglik) forms of the
+    C restatement give the NumPy oracle's per-site and total log-likelihood."""
+    w = synth.pmm_workload(60, 17, 3, 14, 0.5, 0.1, 0.15, seed=7, n_trees=3)
+    enc = O.recode([w.rows[c] for c in w.leaf_order], w.Q, True)
+    ll = cpu_port.loglik(w.newicks, w.rows, w.Q, w.leaf_order, 0.13, 0.21)
+    for i in range(3):
+        tr = O.parse_tree(w.newicks[i], w.leaf_order)
+        d = tr.branch_lengths * (1.0 + 0.1 * i)
+        ref, ref_site = O.log_likelihood(O.Problem(tr, enc, True), d, 0.13, 0.21)
+        site = cpu_port.site_loglik(w.newicks[i], w.rows, w.Q, w.leaf_order, 0.13, 0.21, d=d,
+                                    enc=enc)
+        np.testing.assert_allclose(site, ref_site, rtol=1e-12)
+        assert abs(site.sum() / ref - 1) < 1e-12
+        if i == 0:
+            assert abs(ll[0] / O.log_likelihood(O.Problem(tr, enc, True), tr.branch_lengths,
+                                                0.13, 0.21)[0] - 1) < 1e-12

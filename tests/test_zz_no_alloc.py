@@ -54,3 +54,9 @@ def test_inside_noalloc_rejects_oversized_batches():
                                  C.c_void_p(torch.cuda.current_stream().cuda_stream))
     assert rc == N.LAML_OK - 1   # LAML_ERR_ARG
     assert b"fixed scratch" in lib.laml_last_error()
+    # sizes below the batch's own plan are refused before any launch (the
+    # level kernels write at the plan's offsets)
+    rc = lib.laml_inside_noalloc(C.byref(b.b), b.sizes["part_floats"] - 8, b.sizes["scalar_len"],
+                                 C.c_void_p(torch.cuda.current_stream().cuda_stream))
+    assert rc == N.LAML_OK - 1
+    assert b"plan sizes" in lib.laml_last_error()
