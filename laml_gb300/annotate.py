@@ -56,12 +56,12 @@ def az_labels(et, rows: Sequence[Sequence]):
     lab = [[None] * K for _ in range(N)]
     order = []
     st = [et.root]
-    while st:
+    while st:   # treeswift's preorder: the last child in newick order (child0) first
         u = st.pop()
         order.append(u)
         if et.child0[u] >= 0:
-            st.append(int(et.child0[u]))
             st.append(int(et.child1[u]))
+            st.append(int(et.child0[u]))
     for u in reversed(order):
         if u < n:
             for c in range(K):
@@ -77,23 +77,16 @@ def az_labels(et, rows: Sequence[Sequence]):
     return lab, order
 
 
-def annotate(newick: str, char_mtrx: Dict[str, list], Q: List[dict], nu: float, phi: float,
-             leaf_order: Sequence[str] = None, device="cuda"):
-    """Returns (annotated newick, [(label, posterior string)]) in the
-    runner's order: a new root 'I0' above the tree (runner.py:396-405),
-    unlabelled or duplicate labels replaced by I<k> in preorder, branch
-    lengths = round(S1 + S2 + S4, 3)."""
-    et = encode_newick(newick, leaf_order)
-    rows = [char_mtrx[et.labels[i]] for i in range(et.num_leaves)]
-    ds = encode_dataset(char_matrix(rows, exact=True), Q, compat=False)
-    b = DeviceBatch([ds], [et], [0], [et.branch_length], [nu], [phi], compat=False,
-                    want_post=True, device=device)
-    b.e_step(want_post=True)
-    cnt, _ = b.counts_from_partials()
-    p0, p1 = b.posteriors(0)
+def annotation_lines(et, rows: Sequence[Sequence], Q: List[dict], p0, p1, mut):
+    """The runner's annotation output (runner.py:391-430) from per-node
+    posteriors: ``p0`` = P(v = 0 | D), ``p1`` = P(v = silenced | D) as [N, K]
+    probabilities (original site order), ``mut`` = the expected mutations on
+    each node's branch (S1 + S2 + S4 summed over sites).  Returns (annotated
+    newick, [(label, posterior string)]) in the runner's order: a new root
+    'I0' above the tree (runner.py:396-405), unlabelled or repeated labels
+    replaced by I<k> in preorder, branch lengths = round(mut, 3)."""
     lab, order = az_labels(et, rows)
     K = len(rows[0])
-    # labels: the new root is I0; others keep theirs unless unnamed ("node_k") or repeated
     names = {}
     seen = set()
     idx = 1
@@ -104,7 +97,7 @@ def annotate(newick: str, char_mtrx: Dict[str, list], Q: List[dict], nu: float, 
             idx += 1
         seen.add(nm)
         names[u] = nm
-    mut = np.round(cnt[:, 1] + cnt[:, 2] + cnt[:, 4], 3)
+    mut = np.round(np.asarray(mut, np.float64), 3)
     parent = {int(et.child0[u]): u for u in order if et.child0[u] >= 0}
     parent.update({int(et.child1[u]): u for u in order if et.child0[u] >= 0})
     # alpha of '?' nodes inherits the parent's when the parent is not 'z'
@@ -115,12 +108,23 @@ def annotate(newick: str, char_mtrx: Dict[str, list], Q: List[dict], nu: float, 
                 if lab[u][c] == "?" and lab[pu][c] != "z":
                     lab[u][c] = lab[pu][c]
 
-    def nwk(u):
-        if et.child0[u] < 0:
-            return f"{names[u]}:{mut[u]}"
-        return f"({nwk(int(et.child1[u]))},{nwk(int(et.child0[u]))}){names[u]}:{mut[u]}"
+    def length(x):   # the tree writer prints an integral length without ".0"
+        x = float(x)
+        return str(int(x)) if x.is_integer() else str(x)
 
-    tree_line = "(" + nwk(et.root) + ")I0;"
+    out = []   # newick, children in newick order (child1, then child0); no recursion
+    st = [(et.root, 0)]
+    while st:
+        u, k = st.pop()
+        if et.child0[u] >= 0 and k < 2:
+            out.append("(" if k == 0 else ",")
+            st.append((u, k + 1))
+            st.append((int(et.child1[u] if k == 0 else et.child0[u]), 0))
+            continue
+        if et.child0[u] >= 0:
+            out.append(")")
+        out.append(f"{names[u]}:{length(mut[u])}")
+    tree_line = "(" + "".join(out) + ")I0;"
     lines = [("I0", ",".join(["0"] * K))]
     for u in order:
         parts = []
@@ -131,3 +135,20 @@ def annotate(newick: str, char_mtrx: Dict[str, list], Q: List[dict], nu: float, 
             parts.append(format_posterior(a0, a1, aa, str(lab[u][c]), Q[c]))
         lines.append((names[u], ",".join(parts)))
     return tree_line, lines
+
+
+def annotate(newick: str, char_mtrx: Dict[str, list], Q: List[dict], nu: float, phi: float,
+             leaf_order: Sequence[str] = None, device="cuda", branch_lengths=None):
+    """The exact-model E-step on the GPU at (the tree's branch lengths, or
+    ``branch_lengths`` in the encoder's node order, nu, phi), then
+    ``annotation_lines``."""
+    et = encode_newick(newick, leaf_order)
+    rows = [char_mtrx[et.labels[i]] for i in range(et.num_leaves)]
+    ds = encode_dataset(char_matrix(rows, exact=True), Q, compat=False)
+    d = et.branch_length if branch_lengths is None else np.asarray(branch_lengths, np.float64)
+    b = DeviceBatch([ds], [et], [0], [d], [nu], [phi], compat=False,
+                    want_post=True, device=device)
+    b.e_step(want_post=True)
+    cnt, _ = b.counts_from_partials()
+    p0, p1 = b.posteriors(0)
+    return annotation_lines(et, rows, Q, p0, p1, cnt[:, 1] + cnt[:, 2] + cnt[:, 4])

@@ -1,5 +1,7 @@
 """Input formats feeding the encoder: the reference's character-matrix and
-prior readers (laml_libs/sequence_lib.py:100-363) and writer (78-92).
+prior readers (laml_libs/sequence_lib.py:100-363) and writer (78-92), and
+the collapsing of identical sequences before a run with their return as
+polytomies after it (dedup / add_dup, sequence_lib.py:10-76).
 
 ``read_sequences`` returns (charMtrx, site_names) with charMtrx =
 {cell: [int | '?']}; ``read_priors`` returns Q = [{state: prob}] per site
@@ -10,9 +12,13 @@ site names, or a pickled {site: {state: prob}} dict where state 0 gets prior
 from __future__ import annotations
 
 import pickle
+from collections import defaultdict
 from typing import Dict, List, Optional, Sequence, Tuple
 
+from .tree import Node, Tree, read_tree_newick
+
 RECOGNIZED_MISSING = {"-", "?", "-1"}   # sequence_lib.py:8
+DMIN = 0.005   # laml_libs/core_constants.py: dmin
 
 
 def _is_missing(seen, x):
@@ -96,3 +102,77 @@ def write_sequences(char_mtrx: dict, nsites: int, path: str, delimiter: str = ",
         f.write("cell" + "".join(delimiter + "r" + str(i) for i in range(nsites)) + "\n")
         for cell, seq in char_mtrx.items():
             f.write(cell + "".join(delimiter + str(x) for x in seq) + "\n")
+
+
+def _without_leaves(tree: Tree, labels) -> Tree:
+    """A copy of ``tree`` without the leaves named in ``labels``: internal
+    nodes left without children go too, and nodes left with one child are
+    suppressed (their edge length added to the child's), as treeswift's
+    extract_tree_without(labels, suppress_unifurcations=True) leaves it."""
+    drop = set(labels)
+    new = {}
+    for v in tree.traverse_postorder():   # children before parents
+        if v.is_leaf():
+            if v.label in drop:
+                continue
+        else:
+            kids = [new[c] for c in v.children if c in new]
+            if not kids:
+                continue
+        c = Node(v.label, v.edge_length)
+        if not v.is_leaf():
+            for k in (new[x] for x in v.children if x in new):
+                c.add_child(k)
+        new[v] = c
+    if tree.root not in new:
+        return Tree(Node())
+    out = Tree(new[tree.root])
+    out.suppress_unifurcations()
+    return out
+
+
+def dedup(char_mtrx: Dict[str, list], input_tree_strings: Sequence[str]):
+    """sequence_lib.dedup (sequence_lib.py:10-53): cells with identical
+    sequences are grouped (first-seen order); the first cell of each group
+    represents it and the others are pruned from every tree.  Returns
+    (has_dup, dup_map {representative: [others]}, char_mtrx -- returned
+    whole, as the reference does -- and the pruned newick strings)."""
+    seq_to_taxa = defaultdict(list)
+    for taxon, seq in char_mtrx.items():
+        seq_to_taxa[tuple(seq)].append(taxon)
+    if len(seq_to_taxa) == len(char_mtrx):
+        return False, {}, char_mtrx, list(input_tree_strings)
+    dup_map = {g[0]: g[1:] for g in seq_to_taxa.values() if len(g) > 1}
+    out = []
+    for s in input_tree_strings:
+        t = read_tree_newick(s)
+        for rep in dup_map:
+            t = _without_leaves(t, dup_map[rep])
+        out.append(t.newick())
+    return True, dup_map, char_mtrx, out
+
+
+def add_dup(input_tree_strings: Sequence[str], dup_map: Dict[str, List[str]]) -> List[str]:
+    """sequence_lib.add_dup (sequence_lib.py:55-76): each representative
+    leaf is replaced by a node "node_dummy_<rep>" carrying the leaf's edge
+    length (appended as its parent's last child), under which the leaf and
+    its duplicates hang with length dmin."""
+    out = []
+    for s in input_tree_strings:
+        t = read_tree_newick(s)
+        leaves = {v.label: v for v in t.traverse_leaves()}
+        for rep, dups in dup_map.items():
+            node = leaves.get(rep)
+            if node is None:
+                continue
+            p = node.get_parent()
+            dummy = Node(None, node.edge_length)
+            p.remove_child(node)
+            p.add_child(dummy)
+            node.edge_length = DMIN
+            dummy.add_child(node)
+            dummy.label = f"node_dummy_{rep}"
+            for taxon in dups:
+                dummy.add_child(Node(taxon, DMIN))
+        out.append(t.newick())
+    return out

@@ -11,7 +11,8 @@ out every known-answer case: the literal ``Q``, ``T``, ``msa``, ``phi``,
 ``__test_outllh__`` call (the reduced-tree outside identity tests); from
 unit_tests_TopoSearch.py the ultrametric brute-force case with its
 pre-computed optimum.  It also
-copies the small data fixtures those tests load (test_EM/test1 and test4).
+copies the small data fixtures those tests load (test_EM/test1 and test4)
+and the example1 inputs with the runner's outputs for them (example1/).
 Nothing here imports or runs reference code.
 """
 import ast
@@ -144,9 +145,20 @@ def main(ref):
     for f in ("test1.tre", "test1_charMtrx.txt", "test4.tre", "test4_charMtrx.txt",
               "test4_prior.csv"):
         shutil.copyfile(os.path.join(td, f), os.path.join(HERE, f))
+    # examples/example1 (inputs) and examples/out_example1 (the runner's
+    # outputs for them: scaled trees, parameters, posterior annotations)
+    ex = os.path.join(HERE, "example1")
+    os.makedirs(ex, exist_ok=True)
+    for sub, f in (("example1", "character_matrix.csv"), ("example1", "priors.csv"),
+                   ("out_example1", "example1_trees.nwk"),
+                   ("out_example1", "example1_params.txt"),
+                   ("out_example1", "example1_annotations.txt")):
+        shutil.copyfile(os.path.join(ref, "examples", sub, f), os.path.join(ex, f))
     print(f"{len(llh)} likelihood cases, {len(outside)} outside cases, "
           f"{len(ultra)} ultrametric brute-force cases")
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2:
+        sys.exit("usage: python tests/golden/make_golden.py <path of the LAML checkout>")
+    main(sys.argv[1])
