@@ -289,6 +289,11 @@ typedef struct laml_batch {
      * in_part and of in_x / in_h / in_dot; laml_inside_noalloc refuses a
      * batch without them */
     int64_t plan_part_floats, plan_scalar_len;
+    /* [2T] or NULL: per tree, the '?' entry count and the site count the
+     * M-step uses for phi and for the exact model's count normalisation in
+     * place of its dataset's -- the totals over all ranks when the tree's
+     * sites are split across ranks and cnt_part holds the reduced counts */
+    const double* tr_mstats;
 } laml_batch;
 
 /* A tree's partials are FP32 values with power-of-two exponents (linear)

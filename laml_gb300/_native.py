@@ -87,7 +87,7 @@ BATCH_FIELDS = [
     ("h_in_level_off", vp), ("h_out_level_off", vp),
     ("barrier", vp), ("error", vp), ("max_states", i32), ("max_tree_nodes", i32),
     ("tr_leaf", vp), ("nd_uorder", vp), ("nd_uwork", vp),
-    ("plan_part_floats", i64), ("plan_scalar_len", i64),
+    ("plan_part_floats", i64), ("plan_scalar_len", i64), ("tr_mstats", vp),
 ]
 
 

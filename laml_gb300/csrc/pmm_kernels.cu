@@ -2228,7 +2228,9 @@ __device__ void mstep_tree(const laml_batch& b, int p, int rounds, Team& T, floa
                     : (flags & LAML_MSTEP_ULTRA_PD_SHORT) ? ultra::kPdShort : ultra::kPdMax;
     if (__ldcg(b.tr_status + p) != LAML_TREE_ACTIVE) return;
     const int N = __ldg(b.tr_nodes + p), n = __ldg(b.tr_leaves + p), base = __ldg(b.tr_node_base + p);
-    const int ds = __ldg(b.tr_ds + p), NG = __ldg(b.ds_groups + ds), K = __ldg(b.ds_sites + ds);
+    const int ds = __ldg(b.tr_ds + p), NG = __ldg(b.ds_groups + ds);
+    // the whole tree's sites and '?' entries (all ranks' when its sites are split)
+    const int K = b.tr_mstats ? (int)__ldg(b.tr_mstats + 2 * p + 1) : __ldg(b.ds_sites + ds);
     const int64_t cb = __ldg(b.tr_cnt_base + p);
     const bool compat = b.compat != 0;
     const uint8_t fix = __ldg(b.tr_fix + p);
@@ -2283,7 +2285,8 @@ __device__ void mstep_tree(const laml_batch& b, int p, int rounds, Team& T, floa
     }
     // 2. phi (fast_em/laml.py:77 stationary point; EM_solver.py:318-326)
     if (!(fix & 2)) {
-        const double M = __ldg(b.ds_missing + ds), total = (double)n * K;
+        const double M = b.tr_mstats ? __ldg(b.tr_mstats + 2 * p) : __ldg(b.ds_missing + ds);
+        const double total = (double)n * K;
         if (compat) {
             // stationary point of R log(1 - phi) + B log(phi); with B <= 0
             // (leaf silencing explains every '?') the objective decreases in
