@@ -34,6 +34,7 @@
 #include <cfloat>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <string>
 #include <vector>
 
@@ -3011,6 +3012,387 @@ __global__ void __launch_bounds__(kWWarps * 32) k_items_w(laml_batch b, const in
 }
 
 // ---------------------------------------------------------------------------
+// Bulk-staged wide levels (inside, and outside below the roots; linear
+// partials).  The item mapping of the wide kernels -- G sites x 32 / G items
+// per warp, one thread per (item, site) -- with the partial rows a thread
+// reads arriving in shared memory from the bulk-copy engine.  Each warp runs
+// a ring of kSStages stages; a stage holds kSChunk state slots of every row
+// of the warp's 32 / G items (one cp.async.bulk per row and chunk, issued by
+// the item's first lane, completion counted on the stage's mbarrier), and is
+// refilled as soon as the warp has consumed it.  So up to kSStages chunks of
+// rows are in flight per warp whatever the items' state counts, the
+// load/store unit reads only shared memory for them, and no register holds
+// a load in flight.  A warp takes every nw-th slab (32 / G consecutive
+// items) of the level; each slab's descriptors are read two slabs ahead and
+// its scalars one slab ahead.  Every thread's arithmetic is the direct wide
+// kernels', in the same order, so the results are bitwise equal.
+// ---------------------------------------------------------------------------
+constexpr int kSWarps = 4;    // warps per block
+constexpr int kSChunk = 16;   // state slots of a row per stage
+constexpr int kSStages = 4;   // stages per warp
+
+template <int G, int NR>
+struct SGeom {
+    static constexpr int P = 32 / G;                 // items per warp
+    static constexpr int row = kSChunk * G;          // floats of one row's chunk
+    static constexpr int item = NR * row + G;        // + G floats: items start G banks apart
+    static constexpr int stage = P * item;
+    static constexpr size_t warp_bytes = (size_t)kSStages * stage * sizeof(float);
+    static constexpr size_t block_bytes = kSWarps * (warp_bytes + kSStages * sizeof(uint64_t));
+};
+
+// one thread's item of a slab: descriptor, site, the group's slot count and
+// the scalars its state loop needs (internal children's slots 0 and 1 come
+// from the first stage)
+struct SItem {
+    ItemDesc d;
+    SiteCtx s;
+    GroupCtx gc;
+    int Cg;                    // slots of each of the item's rows (the group's)
+    bool valid, live, staged;  // it < n; a real site of an active tree; rows staged
+    bool logm;                 // the tree keeps log partials (per-lane global path)
+    Child cv, cw;
+    float4 bv, bw;
+    float fo, lroot;           // outside: 2^-h of the parent's outside row; site likelihood mantissa
+    int Xo, xroot;
+};
+
+template <int G>
+__device__ __forceinline__ Child s_child(const laml_batch& b, bool leaf, int ref, int srow,
+                                         const SiteCtx& s, const GroupCtx& gc, const Leaf& L) {
+    Child c;
+    c.e1 = L.e1;
+    c.ephi = L.ephi;
+    if (leaf) {
+        const int code = __ldg(b.codes + gc.code_base + (int64_t)ref * gc.kpad + s.site);
+        c.row = nullptr;
+        c.f = 1.f;
+        c.X = 0;
+        c.code = code;
+        c.s0 = code == 0 ? L.e1 : (code == -1 ? L.ephi : 0.f);
+        c.ss = code < 0 ? 1.f : L.es;
+        c.D = code >= 2 ? __ldg(s.qrow + code * G) * L.e1 : (code == -1 ? L.ephi * s.sumq : 0.f);
+    } else {
+        const int64_t si = (int64_t)srow + s.site;
+        c.f = pow2i(-__ldcg(b.in_h + si));
+        c.X = __ldcg(b.in_x + si);
+        c.D = __ldcg(b.in_dot + si);
+        c.row = b.in_part;   // marks an internal child; its slots come from the stages
+        c.code = 0;
+        c.s0 = c.ss = 0.f;
+    }
+    return c;
+}
+
+template <int G, int KIND>
+__device__ __forceinline__ void s_load(const laml_batch& b, const ItemDesc& d, bool valid,
+                                       int lane, bool respect_status, SItem& t) {
+    const bool rs = KIND == 1 || respect_status;
+    t.d = d;
+    t.valid = valid;
+    t.live = valid && site_ctx_d<G>(b, d, lane, rs, t.s, t.gc);
+    t.Cg = valid ? __ldg(b.group_C + d.gd) : 0;
+    const bool active = valid && (!rs || __ldcg(b.tr_status + d.tree) == LAML_TREE_ACTIVE);
+    t.logm = valid && tree_log(b, d.tree);
+    t.staged = active && !t.logm;
+    if (!(t.live && t.staged)) return;
+    const Leaf L = leaf_params(b, t.s.tree);
+    t.cv = s_child<G>(b, d.flags & 1, d.v_ref, d.v_srow, t.s, t.gc, L);
+    t.cw = s_child<G>(b, d.flags & 2, d.w_ref, d.w_srow, t.s, t.gc, L);
+    t.bv = load_bt(b, d.v);
+    t.bw = load_bt(b, d.w);
+    if (KIND == 1) {
+        const int64_t su = (int64_t)d.u_srow + t.s.site;
+        t.fo = pow2i(-__ldcg(b.out_h + su));
+        t.Xo = __ldcg(b.out_x + su);
+        const int64_t ts = __ldg(b.tr_site_base + t.s.tree) + t.s.site;
+        t.lroot = __ldcg(b.root_lr + ts);
+        t.xroot = __ldcg(b.root_x + ts);
+    }
+}
+
+// chunks of a slab: its staged items' largest slot count over kSChunk
+__device__ __forceinline__ int s_chunks(const SItem& t) {
+    const int c = t.staged ? t.Cg : 0;
+    const int m = __reduce_max_sync(kFull, c);
+    return (m + kSChunk - 1) / kSChunk;
+}
+
+// the item's leader lane: arrive on the stage's mbarrier with the bytes of
+// chunk c of the item's rows (0 when it has none) and start their copies
+template <int G, int KIND>
+__device__ __forceinline__ void s_issue(const laml_batch& b, const SItem& t, int c, float* dst,
+                                        uint64_t* bar) {
+    constexpr int R = SGeom<G, 1>::row;
+    const int j0 = c * kSChunk;
+    const int ns = t.staged ? min(kSChunk, t.Cg - j0) : 0;
+    const uint32_t bytes = ns > 0 ? (uint32_t)ns * G * 4u : 0u;
+    const bool uin = KIND == 1, vin = !(t.d.flags & 1), win = !(t.d.flags & 2);
+    const uint32_t tx = bytes ? (uin ? bytes : 0u) + (vin ? bytes : 0u) + (win ? bytes : 0u) : 0u;
+    fence_proxy_async_smem();   // this warp's reads of the stage's last use come first
+    mbar_arrive_tx(bar, tx);
+    if (!tx) return;
+    const int64_t off = (int64_t)t.s.goff + (int64_t)j0 * G;
+    if (uin) bulk_g2s(dst, b.out_part + (int64_t)t.d.u_prow8 * 8 + off, bytes, bar);
+    if (vin) bulk_g2s(dst + (uin ? 1 : 0) * R, b.in_part + (int64_t)t.d.v_ref * 8 + off, bytes, bar);
+    if (win) bulk_g2s(dst + (uin ? 2 : 1) * R, b.in_part + (int64_t)t.d.w_ref * 8 + off, bytes, bar);
+}
+
+template <int G, bool VL, bool WL>
+__device__ __forceinline__ void s_outside_chunk(const float* su, const float* sv, const float* sw,
+                                                int j0, int jlo, int jhi, float fo,
+                                                const Child& cv, const Child& cw,
+                                                const float4& bv, const float4& bw,
+                                                const float* __restrict__ qrow, float pxa,
+                                                float pxb, float* __restrict__ ra,
+                                                float* __restrict__ rb, float& sa, float& da,
+                                                float& ma, float& sb, float& db, float& mb) {
+    const float cstv = cv.code == -1 ? cv.ephi : 0.f, cstw = cw.code == -1 ? cw.ephi : 0.f;
+    const float kv = bv.w * cv.ss, kw = bw.w * cw.ss;
+#pragma unroll 4
+    for (int j = jlo; j < jhi; ++j) {
+        const int k = (j - j0) * G;
+        const float o = su[k] * fo;
+        const float av = VL ? (cv.code == j ? cv.e1 : cstv) : sv[k] * cv.f;
+        const float aw = WL ? (cw.code == j ? cw.e1 : cstw) : sw[k] * cw.f;
+        const float qj = __ldg(qrow + j * G);
+        const float xa = o * fmaf(bw.z, aw, kw);
+        const float xb = o * fmaf(bv.z, av, kv);
+        sa += xa;
+        da = fmaf(xa, av, da);
+        sb += xb;
+        db = fmaf(xb, aw, db);
+        if (!VL) {
+            const float r = fmaf(pxa, qj, bv.z * xa);
+            __stcg(ra + j * G, r);
+            ma = fmaxf(ma, r);
+        }
+        if (!WL) {
+            const float r = fmaf(pxb, qj, bw.z * xb);
+            __stcg(rb + j * G, r);
+            mb = fmaxf(mb, r);
+        }
+    }
+}
+
+template <int G, bool VL, bool WL>
+__device__ __forceinline__ void s_inside_chunk(const float* sv, const float* sw, int j0, int jlo,
+                                               int jhi, const Child& cv, const Child& cw,
+                                               const float4& bv, const float4& bw,
+                                               const float* __restrict__ qrow,
+                                               float* __restrict__ row, float& dot, float& mx) {
+    const float cstv = cv.code == -1 ? cv.ephi : 0.f, cstw = cw.code == -1 ? cw.ephi : 0.f;
+    const float kv = bv.w * cv.ss, kw = bw.w * cw.ss;
+#pragma unroll 4
+    for (int j = jlo; j < jhi; ++j) {
+        const int k = (j - j0) * G;
+        const float av = VL ? (cv.code == j ? cv.e1 : cstv) : sv[k] * cv.f;
+        const float aw = WL ? (cw.code == j ? cw.e1 : cstw) : sw[k] * cw.f;
+        const float x = fmaf(bv.z, av, kv) * fmaf(bw.z, aw, kw);
+        __stcg(row + j * G, x);
+        dot = fmaf(__ldg(qrow + j * G), x, dot);
+        mx = fmaxf(mx, x);
+    }
+}
+
+template <int G, int KIND>
+__global__ void __launch_bounds__(kSWarps * 32) k_items_ws(laml_batch b, const int32_t* desc,
+                                                           int64_t n, int want_post,
+                                                           int respect_status) {
+    constexpr int NR = KIND == 1 ? 3 : 2;
+    using Geo = SGeom<G, NR>;
+    constexpr int P = Geo::P, R = Geo::row;
+    extern __shared__ __align__(128) unsigned char ssm[];
+    const int lane32 = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    const int sub = lane32 / G, l = lane32 % G;
+    const bool leader = l == 0;
+    float* ring = reinterpret_cast<float*>(ssm) + (size_t)wib * kSStages * Geo::stage;
+    uint64_t* bars = reinterpret_cast<uint64_t*>(ssm + kSWarps * Geo::warp_bytes) + wib * kSStages;
+    const int64_t nslab = (n + P - 1) / P;
+    const int64_t nw = (int64_t)gridDim.x * kSWarps;
+    int64_t sc = (int64_t)blockIdx.x * kSWarps + wib;   // this warp's current slab
+    if (sc >= nslab) return;
+    if (lane32 == 0) {
+        for (int k = 0; k < kSStages; ++k) mbar_init(bars + k, P);
+        fence_mbar_init();
+    }
+    __syncwarp();
+    const bool rs = respect_status != 0;
+    auto item_of = [&](int64_t slab) { return slab * P + sub; };
+    SItem cur, nxt;
+    {
+        const int64_t i0 = item_of(sc), i1 = item_of(sc + nw);
+        s_load<G, KIND>(b, load_desc(desc, i0 < n ? i0 : 0), i0 < n, l, rs, cur);
+        s_load<G, KIND>(b, load_desc(desc, i1 < n ? i1 : 0), i1 < n, l, rs, nxt);
+    }
+    int64_t i2 = item_of(sc + 2 * nw);
+    ItemDesc d2 = load_desc(desc, i2 < n ? i2 : 0);   // two slabs ahead
+    int nch_cur = s_chunks(cur), nch_nxt = s_chunks(nxt);
+    int iw = 0, ic = 0;   // next chunk to issue: slab (0 cur, 1 nxt), chunk
+    int qi = 0, qc = 0;   // chunks issued / consumed by this warp
+    auto issue_more = [&]() {
+        while (qi - qc < kSStages) {
+            if (iw == 0 && ic >= nch_cur) {
+                iw = 1;
+                ic = 0;
+            }
+            if (iw == 1 && ic >= nch_nxt) break;   // the rest after the next rotation
+            float* dst = ring + (qi % kSStages) * Geo::stage + sub * Geo::item;
+            uint64_t* bar = bars + (qi % kSStages);
+            if (leader) {
+                if (iw == 0) s_issue<G, KIND>(b, cur, ic, dst, bar);
+                else s_issue<G, KIND>(b, nxt, ic, dst, bar);
+            }
+            ++qi;
+            ++ic;
+        }
+    };
+    for (;;) {
+        float cv_[8] = {0, 0, 0, 0, 0, 0, 0, 0}, cw_[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+        const bool run = cur.live && cur.staged;
+        const int C = run ? cur.s.C : 0;
+        // outside accumulators (A: child v, B: child w) / inside running values
+        ChildOut A, B;
+        float pxa = 0.f, pxb = 0.f;
+        float* row = nullptr;
+        float dot = 0.f, mx = 0.f, s0 = 0.f, ss = 0.f;
+        for (int c = 0; c < nch_cur; ++c) {
+            issue_more();
+            const int stg = qc % kSStages;
+            if (!mbar_wait(b, bars + stg, (uint32_t)(qc / kSStages) & 1u)) {
+                // timed out: wait (bounded) for this warp's other copies, then leave
+                for (int q = qc + 1; q < qi; ++q)
+                    mbar_wait(b, bars + (q % kSStages), (uint32_t)(q / kSStages) & 1u);
+                return;
+            }
+            const float* st = ring + stg * Geo::stage + sub * Geo::item + l;
+            const int j0 = c * kSChunk;
+            if (run && j0 < C) {
+                const float* su = st;
+                const float* sv = st + (KIND == 1 ? R : 0);
+                const float* sw = st + (KIND == 1 ? 2 : 1) * R;
+                Child& cv = cur.cv;
+                Child& cw = cur.cw;
+                const float4 bv = cur.bv, bw = cur.bw;
+                if (c == 0) {   // slots 0 and 1: the item's heads
+                    if (cv.row) { cv.s0 = sv[0] * cv.f; cv.ss = sv[G] * cv.f; }
+                    if (cw.row) { cw.s0 = sw[0] * cw.f; cw.ss = sw[G] * cw.f; }
+                    const float ev0 = bv.x * cv.s0 + bv.y * cv.D + bv.w * cv.ss;
+                    const float ew0 = bw.x * cw.s0 + bw.y * cw.D + bw.w * cw.ss;
+                    if (KIND == 1) {
+                        const float o0 = su[0] * cur.fo, os = su[G] * cur.fo;
+                        A.x0 = o0 * ew0; A.xs = os * cw.ss; A.X = cur.Xo + cw.X;
+                        B.x0 = o0 * ev0; B.xs = os * cv.ss; B.X = cur.Xo + cv.X;
+                        A.sumx = A.dot = A.mx = 0.f;
+                        B.sumx = B.dot = B.mx = 0.f;
+                        const int64_t ro = (int64_t)cur.s.goff + l;
+                        A.orow = cv.row ? b.out_part + (int64_t)cur.d.v_ref * 8 + ro : nullptr;
+                        B.orow = cw.row ? b.out_part + (int64_t)cur.d.w_ref * 8 + ro : nullptr;
+                        pxa = bv.y * A.x0;
+                        pxb = bw.y * B.x0;
+                    } else {
+                        row = b.in_part + (int64_t)cur.d.u_prow8 * 8 + cur.s.goff + l;
+                        s0 = ev0 * ew0;
+                        ss = cv.ss * cw.ss;
+                        __stcg(row, s0);
+                        __stcg(row + G, ss);
+                        mx = fmaxf(s0, ss);
+                        dot = 0.f;
+                    }
+                }
+                const int jlo = max(j0, 2), jhi = min(j0 + kSChunk, C);
+                if (KIND == 1) {
+#define LAML_S_OUT(VL, WL)                                                                     \
+    s_outside_chunk<G, VL, WL>(su, sv, sw, j0, jlo, jhi, cur.fo, cv, cw, bv, bw, cur.s.qrow,  \
+                               pxa, pxb, A.orow, B.orow, A.sumx, A.dot, A.mx, B.sumx, B.dot,  \
+                               B.mx)
+                    switch ((cv.row ? 0 : 1) | (cw.row ? 0 : 2)) {
+                        case 0: LAML_S_OUT(false, false); break;
+                        case 1: LAML_S_OUT(true, false); break;
+                        case 2: LAML_S_OUT(false, true); break;
+                        default: LAML_S_OUT(true, true); break;
+                    }
+#undef LAML_S_OUT
+                } else {
+#define LAML_S_IN(VL, WL) \
+    s_inside_chunk<G, VL, WL>(sv, sw, j0, jlo, jhi, cv, cw, bv, bw, cur.s.qrow, row, dot, mx)
+                    switch ((cv.row ? 0 : 1) | (cw.row ? 0 : 2)) {
+                        case 0: LAML_S_IN(false, false); break;
+                        case 1: LAML_S_IN(true, false); break;
+                        case 2: LAML_S_IN(false, true); break;
+                        default: LAML_S_IN(true, true); break;
+                    }
+#undef LAML_S_IN
+                }
+            }
+            __syncwarp();
+            ++qc;
+        }
+        // finish the slab's items
+        if (KIND == 1) {
+            if (run) {
+                child_finish<G>(b, cur.s, cur.d.v, cur.cv, cur.bv, A, want_post != 0, cur.lroot,
+                                cur.xroot, cv_);
+                child_finish<G>(b, cur.s, cur.d.w, cur.cw, cur.bw, B, want_post != 0, cur.lroot,
+                                cur.xroot, cw_);
+            } else if (cur.live && cur.logm) {
+                float tv[8], tw[8];
+                const ItemDesc dl = cur.d;
+                const SiteCtx sl = cur.s;
+                const GroupCtx gl = cur.gc;
+                outside_log_lane<G>(b, dl, sl, gl, want_post != 0, tv, tw);
+#pragma unroll
+                for (int k = 0; k < 8; ++k) {
+                    cv_[k] = tv[k];
+                    cw_[k] = tw[k];
+                }
+            }
+#pragma unroll
+            for (int off = G / 2; off > 0; off >>= 1) {
+#pragma unroll
+                for (int k = 0; k < 8; ++k) {
+                    cv_[k] += __shfl_xor_sync(kFull, cv_[k], off);
+                    cw_[k] += __shfl_xor_sync(kFull, cw_[k], off);
+                }
+            }
+            if (cur.valid && leader && __ldcg(b.tr_status + cur.d.tree) == LAML_TREE_ACTIVE) {
+                write_counts<G>(b, cur.d.tree, cur.d.v, cur.d.g, cv_);
+                write_counts<G>(b, cur.d.tree, cur.d.w, cur.d.g, cw_);
+            }
+        } else {
+            if (run) {
+                const int h = scale_exp(mx);
+                const float f = pow2i(-h);
+                const int X = cur.cv.X + cur.cw.X + h;
+                const int64_t sr = (int64_t)cur.d.u_srow + cur.s.site;
+                __stcg(b.in_h + sr, h);
+                __stcg(b.in_x + sr, X);
+                __stcg(b.in_dot + sr, dot * f);
+                if (cur.d.flags & 4)
+                    root_site_llh(b, cur.s.tree, cur.s.site, root_edge_logs(b, cur.s.tree),
+                                  s0 * f, dot * f, ss * f, X);
+            } else if (cur.live && cur.logm) {
+                const ItemDesc dl = cur.d;
+                const SiteCtx sl = cur.s;
+                const GroupCtx gl = cur.gc;
+                inside_log_item<G>(b, dl, sl, gl);
+            }
+        }
+        // rotate: next slab's state (loaded a slab ago) becomes current
+        sc += nw;
+        if (sc >= nslab) break;
+        cur = nxt;
+        nch_cur = nch_nxt;
+        s_load<G, KIND>(b, d2, i2 < n, l, rs, nxt);
+        nch_nxt = s_chunks(nxt);
+        i2 = item_of(sc + 2 * nw);
+        d2 = load_desc(desc, i2 < n ? i2 : 0);
+        if (iw == 1) iw = 0;   // the issue position moves with the slab
+        else { iw = 0; ic = 0; }
+    }
+}
+
+// ---------------------------------------------------------------------------
 // kernels
 // ---------------------------------------------------------------------------
 template <int G, int KIND, bool AS = false>
@@ -3346,10 +3728,55 @@ int launch_staged(const laml_batch& b, const int32_t* desc, int64_t n, int want_
     return check(cudaGetLastError(), "k_items_w launch");
 }
 
+// the wide levels' kernel: bulk-staged (default) or direct per-thread loads
+// (LAML_WIDE_KERNEL=direct in the environment, read once)
+bool wide_staged() {
+    static const bool on = [] {
+        const char* e = std::getenv("LAML_WIDE_KERNEL");
+        return !(e && std::string(e) == "direct");
+    }();
+    return on;
+}
+
+template <int G, int KIND>
+int launch_staged_wide(const laml_batch& b, const int32_t* desc, int64_t n, int want_post,
+                       int respect_status, cudaStream_t st) {
+    using Geo = SGeom<G, KIND == 1 ? 3 : 2>;
+    static bool attr_set = false;
+    if (!attr_set) {
+        int rc = check(cudaFuncSetAttribute(k_items_ws<G, KIND>,
+                                            cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                            (int)Geo::block_bytes),
+                       "staged wide kernel shared memory limit");
+        if (rc) return rc;
+        attr_set = true;
+    }
+    static int per_sm = 0;
+    if (!per_sm) {
+        int rc = check(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+                           &per_sm, k_items_ws<G, KIND>, kSWarps * 32, Geo::block_bytes),
+                       "staged wide kernel occupancy");
+        if (rc) return rc;
+        if (per_sm < 1) per_sm = 1;
+    }
+    const int64_t slabs = (n + Geo::P - 1) / Geo::P;
+    int64_t blocks = (slabs + kSWarps - 1) / kSWarps;
+    const int64_t cap = (int64_t)per_sm * num_sms();
+    if (blocks > cap) blocks = cap;
+    k_items_ws<G, KIND><<<(unsigned)blocks, kSWarps * 32, Geo::block_bytes, st>>>(
+        b, desc, n, want_post, respect_status);
+    return check(cudaGetLastError(), "k_items_ws launch");
+}
+
 template <int G>
 int launch_items(const laml_batch& b, const int32_t* items, int64_t n, int kind, int want_post,
                  int respect_status, cudaStream_t st, const int32_t* desc = nullptr) {
     if (n <= 0) return LAML_OK;
+    // wide inside / outside levels below the roots: bulk-staged rows
+    if ((kind == 0 || kind == 1) && !narrow_level(n) && b.max_states > 0 && wide_staged()) {
+        return kind == 0 ? launch_staged_wide<G, 0>(b, desc, n, want_post, respect_status, st)
+                         : launch_staged_wide<G, 1>(b, desc, n, want_post, respect_status, st);
+    }
     // inside / outside below the roots: the staged kernels when the batch
     // states its largest group and the buffers fit in shared memory
     if ((kind == 0 || kind == 1) && narrow_level(n) && b.max_states > 0 &&
