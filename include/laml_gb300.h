@@ -294,6 +294,10 @@ typedef struct laml_batch {
      * place of its dataset's -- the totals over all ranks when the tree's
      * sites are split across ranks and cnt_part holds the reduced counts */
     const double* tr_mstats;
+    /* state slots per stage of the bulk-staged wide level kernels: 8, 16 or
+     * 32 (with 8, 4 or 2 stages per warp); 0 = 16.  A tiling choice only
+     * (laml_gb300/tune.py picks it): results are bitwise the same. */
+    int32_t wide_chunk;
 } laml_batch;
 
 /* A tree's partials are FP32 values with power-of-two exponents (linear)

@@ -88,6 +88,18 @@ __device__ __forceinline__ void prefetch_l2(const void* p, uint32_t bytes) {
     asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(p), "r"(bytes) : "memory");
 }
 
+// Sums of products in the level kernels' shared arithmetic are written with
+// the round-to-nearest intrinsics: the compiler may not fuse them into FMAs
+// on its own, which it could do differently in each kernel that inlines
+// them, so every path (direct, bulk-staged, persistent) rounds alike and
+// their results stay bitwise equal.
+__device__ __forceinline__ float mulr(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ float addr(float a, float b) { return __fadd_rn(a, b); }
+// the transition out of state 0 applied to a child's vector: P00 s0 + Pmut D + Psil ss
+__device__ __forceinline__ float edge0(const float4& bt, float s0, float D, float ss) {
+    return addr(addr(mulr(bt.x, s0), mulr(bt.y, D)), mulr(bt.w, ss));
+}
+
 __device__ __forceinline__ int scale_exp(float m) {
     // exponent h with m * 2^-h in [0.5, 1), clamped so 2^-h stays a normal float
     if (!(m > 0.f)) return 0;
@@ -320,7 +332,7 @@ __device__ __forceinline__ void child_finish(const laml_batch& b, const SiteCtx&
                                              const Child& cv, const float4& bv, ChildOut& o,
                                              bool want_post, float lroot, int xroot, float* cnt) {
     const float out0 = bv.x * o.x0;
-    const float outs = bv.w * (o.x0 + o.sumx) + o.xs;
+    const float outs = addr(mulr(bv.w, addr(o.x0, o.sumx)), o.xs);
     if (o.orow) {
         __stcg(o.orow, out0);
         __stcg(o.orow + G, outs);
@@ -785,7 +797,7 @@ __device__ void root_counts_item(const laml_batch& b, int v, int g, int lane, bo
             const int64_t su = __ldg(b.nd_srow + u) + s.site;
             const float fo = pow2i(-__ldcg(b.out_h + su));
             const float* urow = b.out_part + __ldg(b.nd_prow + u) + s.goff + lane;
-            x0 = __ldcg(urow) * fo * (bw.x * cw.s0 + bw.y * cw.D + bw.w * cw.ss);
+            x0 = __ldcg(urow) * fo * (edge0(bw, cw.s0, cw.D, cw.ss));
             xs = __ldcg(urow + G) * fo * cw.ss;
             Xx = __ldcg(b.out_x + su) + cw.X;
             const float kw = bw.w * cw.ss;
@@ -893,19 +905,19 @@ __device__ __forceinline__ void outside_states(const float* __restrict__ urow, f
     const float pxa = bv.y * A.x0, pxb = bw.y * B.x0;
     float sa = 0.f, da = 0.f, ma = 0.f, sb = 0.f, db = 0.f, mb = 0.f;
     auto step = [&](float o, float av, float aw, float qj, int j) {
-        const float xa = o * fmaf(bw.z, aw, kw);
-        const float xb = o * fmaf(bv.z, av, kv);
-        sa += xa;
+        const float xa = mulr(o, fmaf(bw.z, aw, kw));
+        const float xb = mulr(o, fmaf(bv.z, av, kv));
+        sa = addr(sa, xa);
         da = fmaf(xa, av, da);
-        sb += xb;
+        sb = addr(sb, xb);
         db = fmaf(xb, aw, db);
         if (!VL) {
-            const float r = fmaf(pxa, qj, bv.z * xa);
+            const float r = fmaf(pxa, qj, mulr(bv.z, xa));
             __stcg(ra + j * G, r);
             ma = fmaxf(ma, r);
         }
         if (!WL) {
-            const float r = fmaf(pxb, qj, bw.z * xb);
+            const float r = fmaf(pxb, qj, mulr(bw.z, xb));
             __stcg(rb + j * G, r);
             mb = fmaxf(mb, r);
         }
@@ -1049,8 +1061,8 @@ __device__ void inside_item_d(const laml_batch& b, const ItemDesc& d, int lane,
     const Child cv = load_child_d<G>(b, d.flags & 1, d.v_ref, d.v_srow, s, gc, lane, L);
     const Child cw = load_child_d<G>(b, d.flags & 2, d.w_ref, d.w_srow, s, gc, lane, L);
     const float4 bv = load_bt(b, d.v), bw = load_bt(b, d.w);
-    const float ev0 = bv.x * cv.s0 + bv.y * cv.D + bv.w * cv.ss;
-    const float ew0 = bw.x * cw.s0 + bw.y * cw.D + bw.w * cw.ss;
+    const float ev0 = edge0(bv, cv.s0, cv.D, cv.ss);
+    const float ew0 = edge0(bw, cw.s0, cw.D, cw.ss);
     float* row = b.in_part + (int64_t)d.u_prow8 * 8 + s.goff + lane;
     const float s0 = ev0 * ew0, ss = cv.ss * cw.ss;
     __stcg(row, s0);
@@ -1119,8 +1131,8 @@ __device__ void outside_item_d(const laml_batch& b, const ItemDesc& d, int lane,
         const float fo = pow2i(-__ldcg(b.out_h + su));
         const int Xo = __ldcg(b.out_x + su);
         const float o0 = u0 * fo, os = u1 * fo;
-        const float ev0 = bv.x * cv.s0 + bv.y * cv.D + bv.w * cv.ss;
-        const float ew0 = bw.x * cw.s0 + bw.y * cw.D + bw.w * cw.ss;
+        const float ev0 = edge0(bv, cv.s0, cv.D, cv.ss);
+        const float ew0 = edge0(bw, cw.s0, cw.D, cw.ss);
         ChildOut A, B;   // A: child v (uses E[w]), B: child w (uses E[v])
         A.x0 = o0 * ew0; A.xs = os * cw.ss; A.X = Xo + cw.X;
         B.x0 = o0 * ev0; B.xs = os * cv.ss; B.X = Xo + cv.X;
@@ -1225,8 +1237,8 @@ __device__ void outside_root_item_d(const laml_batch& b, const ItemDesc& d, int 
         const Child cw = load_child_d<G>(b, d.flags & 2, d.w_ref, d.w_srow, s, gc, lane, L);
         const float4 bv = load_bt(b, d.v), bw = load_bt(b, d.w);
         const RootEdge re = root_edge_logs(b, s.tree);
-        const float ev0 = bv.x * cv.s0 + bv.y * cv.D + bv.w * cv.ss;
-        const float ew0 = bw.x * cw.s0 + bw.y * cw.D + bw.w * cw.ss;
+        const float ev0 = edge0(bv, cv.s0, cv.D, cv.ss);
+        const float ew0 = edge0(bw, cw.s0, cw.D, cw.ss);
         const float kv = bv.w * cv.ss, kw = bw.w * cw.ss;
         // largest q_a E[.]_a of each child: the mutated class's share of x
         float ma = 0.f, mb = 0.f;
@@ -1260,17 +1272,17 @@ __device__ void outside_root_item_d(const laml_batch& b, const ItemDesc& d, int 
             const float qj = __ldg(s.qrow + j * G);
             const float xa = ldexpf(fa * (qj * fmaf(bw.z, aw, kw)), ea);
             const float xb = ldexpf(fb * (qj * fmaf(bv.z, av, kv)), eb);
-            A.sumx += xa;
+            A.sumx = addr(A.sumx, xa);
             A.dot = fmaf(xa, av, A.dot);
-            B.sumx += xb;
+            B.sumx = addr(B.sumx, xb);
             B.dot = fmaf(xb, aw, B.dot);
             if (A.orow) {
-                const float r = fmaf(pxa, qj, bv.z * xa);
+                const float r = fmaf(pxa, qj, mulr(bv.z, xa));
                 __stcg(A.orow + j * G, r);
                 A.mx = fmaxf(A.mx, r);
             }
             if (B.orow) {
-                const float r = fmaf(pxb, qj, bw.z * xb);
+                const float r = fmaf(pxb, qj, mulr(bw.z, xb));
                 __stcg(B.orow + j * G, r);
                 B.mx = fmaxf(B.mx, r);
             }
@@ -2758,8 +2770,8 @@ __device__ void inside_w(const laml_batch& b, const WItem& t, const float* buf, 
     }
     if (!VL) { cv.s0 = wrow<STAGED>(rv, 0) * cv.f; cv.ss = wrow<STAGED>(rv, G) * cv.f; }
     if (!WL) { cw.s0 = wrow<STAGED>(rw, 0) * cw.f; cw.ss = wrow<STAGED>(rw, G) * cw.f; }
-    const float ev0 = bv.x * cv.s0 + bv.y * cv.D + bv.w * cv.ss;
-    const float ew0 = bw.x * cw.s0 + bw.y * cw.D + bw.w * cw.ss;
+    const float ev0 = edge0(bv, cv.s0, cv.D, cv.ss);
+    const float ew0 = edge0(bw, cw.s0, cw.D, cw.ss);
     const float kv = bv.w * cv.ss, kw = bw.w * cw.ss;
     const float cstv = cv.code == -1 ? L.ephi : 0.f, cstw = cw.code == -1 ? L.ephi : 0.f;
     float* row = b.in_part + (int64_t)t.u_prow8 * 8 + t.goff + l;
@@ -2830,8 +2842,8 @@ __device__ void outside_w(const laml_batch& b, const WItem& t, const float* buf,
     if (!VL) { cv.s0 = wrow<STAGED>(rv, 0) * cv.f; cv.ss = wrow<STAGED>(rv, G) * cv.f; }
     if (!WL) { cw.s0 = wrow<STAGED>(rw, 0) * cw.f; cw.ss = wrow<STAGED>(rw, G) * cw.f; }
     const float o0 = wrow<STAGED>(ru, 0) * fo, os = wrow<STAGED>(ru, G) * fo;
-    const float ev0 = bv.x * cv.s0 + bv.y * cv.D + bv.w * cv.ss;
-    const float ew0 = bw.x * cw.s0 + bw.y * cw.D + bw.w * cw.ss;
+    const float ev0 = edge0(bv, cv.s0, cv.D, cv.ss);
+    const float ew0 = edge0(bw, cw.s0, cw.D, cw.ss);
     ChildOut A, B;   // A: child v (uses E[w]), B: child w (uses E[v])
     A.x0 = o0 * ew0; A.xs = os * cw.ss; A.X = Xo + cw.X;
     B.x0 = o0 * ev0; B.xs = os * cv.ss; B.X = Xo + cv.X;
@@ -2848,19 +2860,19 @@ __device__ void outside_w(const laml_batch& b, const WItem& t, const float* buf,
         const float av = wval<G, VL, STAGED>(cv, rv, j, cstv);
         const float aw = wval<G, WL, STAGED>(cw, rw, j, cstw);
         const float qj = __ldg(s.qrow + j * G);
-        const float xa = o * fmaf(bw.z, aw, kw);
-        const float xb = o * fmaf(bv.z, av, kv);
-        A.sumx += xa;
+        const float xa = mulr(o, fmaf(bw.z, aw, kw));
+        const float xb = mulr(o, fmaf(bv.z, av, kv));
+        A.sumx = addr(A.sumx, xa);
         A.dot = fmaf(xa, av, A.dot);
-        B.sumx += xb;
+        B.sumx = addr(B.sumx, xb);
         B.dot = fmaf(xb, aw, B.dot);
         if (!VL) {
-            const float r = fmaf(pxa, qj, bv.z * xa);
+            const float r = fmaf(pxa, qj, mulr(bv.z, xa));
             __stcg(A.orow + j * G, r);
             A.mx = fmaxf(A.mx, r);
         }
         if (!WL) {
-            const float r = fmaf(pxb, qj, bw.z * xb);
+            const float r = fmaf(pxb, qj, mulr(bw.z, xb));
             __stcg(B.orow + j * G, r);
             B.mx = fmaxf(B.mx, r);
         }
@@ -3016,10 +3028,10 @@ __global__ void __launch_bounds__(kWWarps * 32) k_items_w(laml_batch b, const in
 // partials).  The item mapping of the wide kernels -- G sites x 32 / G items
 // per warp, one thread per (item, site) -- with the partial rows a thread
 // reads arriving in shared memory from the bulk-copy engine.  Each warp runs
-// a ring of kSStages stages; a stage holds kSChunk state slots of every row
+// a ring of kSSlots / CH stages; a stage holds CH state slots of every row
 // of the warp's 32 / G items (one cp.async.bulk per row and chunk, issued by
 // the item's first lane, completion counted on the stage's mbarrier), and is
-// refilled as soon as the warp has consumed it.  So up to kSStages chunks of
+// refilled as soon as the warp has consumed it.  So up to kSSlots / CH chunks of
 // rows are in flight per warp whatever the items' state counts, the
 // load/store unit reads only shared memory for them, and no register holds
 // a load in flight.  A warp takes every nw-th slab (32 / G consecutive
@@ -3027,18 +3039,20 @@ __global__ void __launch_bounds__(kWWarps * 32) k_items_w(laml_batch b, const in
 // its scalars one slab ahead.  Every thread's arithmetic is the direct wide
 // kernels', in the same order, so the results are bitwise equal.
 // ---------------------------------------------------------------------------
-constexpr int kSWarps = 4;    // warps per block
-constexpr int kSChunk = 16;   // state slots of a row per stage
-constexpr int kSStages = 4;   // stages per warp
+constexpr int kSWarps = 4;     // warps per block
+constexpr int kSSlots = 64;    // state slots of each row a warp's ring holds
+// CH state slots of a row per stage, kSSlots / CH stages per warp: the
+// autotuner's states-per-stage axis (laml_batch.wide_chunk)
 
-template <int G, int NR>
+template <int G, int NR, int CH>
 struct SGeom {
     static constexpr int P = 32 / G;                 // items per warp
-    static constexpr int row = kSChunk * G;          // floats of one row's chunk
+    static constexpr int S = kSSlots / CH;           // stages per warp
+    static constexpr int row = CH * G;               // floats of one row's chunk
     static constexpr int item = NR * row + G;        // + G floats: items start G banks apart
     static constexpr int stage = P * item;
-    static constexpr size_t warp_bytes = (size_t)kSStages * stage * sizeof(float);
-    static constexpr size_t block_bytes = kSWarps * (warp_bytes + kSStages * sizeof(uint64_t));
+    static constexpr size_t warp_bytes = (size_t)S * stage * sizeof(float);
+    static constexpr size_t block_bytes = kSWarps * (warp_bytes + S * sizeof(uint64_t));
 };
 
 // one thread's item of a slab: descriptor, site, the group's slot count and
@@ -3111,21 +3125,22 @@ __device__ __forceinline__ void s_load(const laml_batch& b, const ItemDesc& d, b
     }
 }
 
-// chunks of a slab: its staged items' largest slot count over kSChunk
+// chunks of a slab: its staged items' largest slot count over CH
+template <int CH>
 __device__ __forceinline__ int s_chunks(const SItem& t) {
     const int c = t.staged ? t.Cg : 0;
     const int m = __reduce_max_sync(kFull, c);
-    return (m + kSChunk - 1) / kSChunk;
+    return (m + CH - 1) / CH;
 }
 
 // the item's leader lane: arrive on the stage's mbarrier with the bytes of
 // chunk c of the item's rows (0 when it has none) and start their copies
-template <int G, int KIND>
+template <int G, int KIND, int CH>
 __device__ __forceinline__ void s_issue(const laml_batch& b, const SItem& t, int c, float* dst,
                                         uint64_t* bar) {
-    constexpr int R = SGeom<G, 1>::row;
-    const int j0 = c * kSChunk;
-    const int ns = t.staged ? min(kSChunk, t.Cg - j0) : 0;
+    constexpr int R = CH * G;
+    const int j0 = c * CH;
+    const int ns = t.staged ? min(CH, t.Cg - j0) : 0;
     const uint32_t bytes = ns > 0 ? (uint32_t)ns * G * 4u : 0u;
     const bool uin = KIND == 1, vin = !(t.d.flags & 1), win = !(t.d.flags & 2);
     const uint32_t tx = bytes ? (uin ? bytes : 0u) + (vin ? bytes : 0u) + (win ? bytes : 0u) : 0u;
@@ -3156,19 +3171,19 @@ __device__ __forceinline__ void s_outside_chunk(const float* su, const float* sv
         const float av = VL ? (cv.code == j ? cv.e1 : cstv) : sv[k] * cv.f;
         const float aw = WL ? (cw.code == j ? cw.e1 : cstw) : sw[k] * cw.f;
         const float qj = __ldg(qrow + j * G);
-        const float xa = o * fmaf(bw.z, aw, kw);
-        const float xb = o * fmaf(bv.z, av, kv);
-        sa += xa;
+        const float xa = mulr(o, fmaf(bw.z, aw, kw));
+        const float xb = mulr(o, fmaf(bv.z, av, kv));
+        sa = addr(sa, xa);
         da = fmaf(xa, av, da);
-        sb += xb;
+        sb = addr(sb, xb);
         db = fmaf(xb, aw, db);
         if (!VL) {
-            const float r = fmaf(pxa, qj, bv.z * xa);
+            const float r = fmaf(pxa, qj, mulr(bv.z, xa));
             __stcg(ra + j * G, r);
             ma = fmaxf(ma, r);
         }
         if (!WL) {
-            const float r = fmaf(pxb, qj, bw.z * xb);
+            const float r = fmaf(pxb, qj, mulr(bw.z, xb));
             __stcg(rb + j * G, r);
             mb = fmaxf(mb, r);
         }
@@ -3195,13 +3210,13 @@ __device__ __forceinline__ void s_inside_chunk(const float* sv, const float* sw,
     }
 }
 
-template <int G, int KIND>
+template <int G, int KIND, int CH>
 __global__ void __launch_bounds__(kSWarps * 32) k_items_ws(laml_batch b, const int32_t* desc,
                                                            int64_t n, int want_post,
                                                            int respect_status) {
     constexpr int NR = KIND == 1 ? 3 : 2;
-    using Geo = SGeom<G, NR>;
-    constexpr int P = Geo::P, R = Geo::row;
+    using Geo = SGeom<G, NR, CH>;
+    constexpr int P = Geo::P, R = Geo::row, kSStages = Geo::S;
     extern __shared__ __align__(128) unsigned char ssm[];
     const int lane32 = threadIdx.x & 31, wib = threadIdx.x >> 5;
     const int sub = lane32 / G, l = lane32 % G;
@@ -3227,7 +3242,7 @@ __global__ void __launch_bounds__(kSWarps * 32) k_items_ws(laml_batch b, const i
     }
     int64_t i2 = item_of(sc + 2 * nw);
     ItemDesc d2 = load_desc(desc, i2 < n ? i2 : 0);   // two slabs ahead
-    int nch_cur = s_chunks(cur), nch_nxt = s_chunks(nxt);
+    int nch_cur = s_chunks<CH>(cur), nch_nxt = s_chunks<CH>(nxt);
     int iw = 0, ic = 0;   // next chunk to issue: slab (0 cur, 1 nxt), chunk
     int qi = 0, qc = 0;   // chunks issued / consumed by this warp
     auto issue_more = [&]() {
@@ -3240,8 +3255,8 @@ __global__ void __launch_bounds__(kSWarps * 32) k_items_ws(laml_batch b, const i
             float* dst = ring + (qi % kSStages) * Geo::stage + sub * Geo::item;
             uint64_t* bar = bars + (qi % kSStages);
             if (leader) {
-                if (iw == 0) s_issue<G, KIND>(b, cur, ic, dst, bar);
-                else s_issue<G, KIND>(b, nxt, ic, dst, bar);
+                if (iw == 0) s_issue<G, KIND, CH>(b, cur, ic, dst, bar);
+                else s_issue<G, KIND, CH>(b, nxt, ic, dst, bar);
             }
             ++qi;
             ++ic;
@@ -3266,7 +3281,7 @@ __global__ void __launch_bounds__(kSWarps * 32) k_items_ws(laml_batch b, const i
                 return;
             }
             const float* st = ring + stg * Geo::stage + sub * Geo::item + l;
-            const int j0 = c * kSChunk;
+            const int j0 = c * CH;
             if (run && j0 < C) {
                 const float* su = st;
                 const float* sv = st + (KIND == 1 ? R : 0);
@@ -3277,8 +3292,8 @@ __global__ void __launch_bounds__(kSWarps * 32) k_items_ws(laml_batch b, const i
                 if (c == 0) {   // slots 0 and 1: the item's heads
                     if (cv.row) { cv.s0 = sv[0] * cv.f; cv.ss = sv[G] * cv.f; }
                     if (cw.row) { cw.s0 = sw[0] * cw.f; cw.ss = sw[G] * cw.f; }
-                    const float ev0 = bv.x * cv.s0 + bv.y * cv.D + bv.w * cv.ss;
-                    const float ew0 = bw.x * cw.s0 + bw.y * cw.D + bw.w * cw.ss;
+                    const float ev0 = edge0(bv, cv.s0, cv.D, cv.ss);
+                    const float ew0 = edge0(bw, cw.s0, cw.D, cw.ss);
                     if (KIND == 1) {
                         const float o0 = su[0] * cur.fo, os = su[G] * cur.fo;
                         A.x0 = o0 * ew0; A.xs = os * cw.ss; A.X = cur.Xo + cw.X;
@@ -3300,7 +3315,7 @@ __global__ void __launch_bounds__(kSWarps * 32) k_items_ws(laml_batch b, const i
                         dot = 0.f;
                     }
                 }
-                const int jlo = max(j0, 2), jhi = min(j0 + kSChunk, C);
+                const int jlo = max(j0, 2), jhi = min(j0 + CH, C);
                 if (KIND == 1) {
 #define LAML_S_OUT(VL, WL)                                                                     \
     s_outside_chunk<G, VL, WL>(su, sv, sw, j0, jlo, jhi, cur.fo, cv, cw, bv, bw, cur.s.qrow,  \
@@ -3384,7 +3399,7 @@ __global__ void __launch_bounds__(kSWarps * 32) k_items_ws(laml_batch b, const i
         cur = nxt;
         nch_cur = nch_nxt;
         s_load<G, KIND>(b, d2, i2 < n, l, rs, nxt);
-        nch_nxt = s_chunks(nxt);
+        nch_nxt = s_chunks<CH>(nxt);
         i2 = item_of(sc + 2 * nw);
         d2 = load_desc(desc, i2 < n ? i2 : 0);
         if (iw == 1) iw = 0;   // the issue position moves with the slab
@@ -3680,6 +3695,10 @@ int validate(const laml_batch* b) {
         laml::set_error("laml_batch: in_desc, out_desc and grp_desc (laml_plan_fill) are required");
         return LAML_ERR_ARG;
     }
+    if (b->wide_chunk != 0 && b->wide_chunk != 8 && b->wide_chunk != 16 && b->wide_chunk != 32) {
+        laml::set_error("laml_batch: wide_chunk must be 0, 8, 16 or 32");
+        return LAML_ERR_ARG;
+    }
     return LAML_OK;
 }
 
@@ -3738,13 +3757,13 @@ bool wide_staged() {
     return on;
 }
 
-template <int G, int KIND>
-int launch_staged_wide(const laml_batch& b, const int32_t* desc, int64_t n, int want_post,
-                       int respect_status, cudaStream_t st) {
-    using Geo = SGeom<G, KIND == 1 ? 3 : 2>;
+template <int G, int KIND, int CH>
+int launch_staged_wide_t(const laml_batch& b, const int32_t* desc, int64_t n, int want_post,
+                         int respect_status, cudaStream_t st) {
+    using Geo = SGeom<G, KIND == 1 ? 3 : 2, CH>;
     static bool attr_set = false;
     if (!attr_set) {
-        int rc = check(cudaFuncSetAttribute(k_items_ws<G, KIND>,
+        int rc = check(cudaFuncSetAttribute(k_items_ws<G, KIND, CH>,
                                             cudaFuncAttributeMaxDynamicSharedMemorySize,
                                             (int)Geo::block_bytes),
                        "staged wide kernel shared memory limit");
@@ -3754,7 +3773,7 @@ int launch_staged_wide(const laml_batch& b, const int32_t* desc, int64_t n, int 
     static int per_sm = 0;
     if (!per_sm) {
         int rc = check(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-                           &per_sm, k_items_ws<G, KIND>, kSWarps * 32, Geo::block_bytes),
+                           &per_sm, k_items_ws<G, KIND, CH>, kSWarps * 32, Geo::block_bytes),
                        "staged wide kernel occupancy");
         if (rc) return rc;
         if (per_sm < 1) per_sm = 1;
@@ -3763,9 +3782,19 @@ int launch_staged_wide(const laml_batch& b, const int32_t* desc, int64_t n, int 
     int64_t blocks = (slabs + kSWarps - 1) / kSWarps;
     const int64_t cap = (int64_t)per_sm * num_sms();
     if (blocks > cap) blocks = cap;
-    k_items_ws<G, KIND><<<(unsigned)blocks, kSWarps * 32, Geo::block_bytes, st>>>(
+    k_items_ws<G, KIND, CH><<<(unsigned)blocks, kSWarps * 32, Geo::block_bytes, st>>>(
         b, desc, n, want_post, respect_status);
     return check(cudaGetLastError(), "k_items_ws launch");
+}
+
+template <int G, int KIND>
+int launch_staged_wide(const laml_batch& b, const int32_t* desc, int64_t n, int want_post,
+                       int respect_status, cudaStream_t st) {
+    switch (b.wide_chunk) {
+        case 8: return launch_staged_wide_t<G, KIND, 8>(b, desc, n, want_post, respect_status, st);
+        case 32: return launch_staged_wide_t<G, KIND, 32>(b, desc, n, want_post, respect_status, st);
+        default: return launch_staged_wide_t<G, KIND, 16>(b, desc, n, want_post, respect_status, st);
+    }
 }
 
 template <int G>

@@ -235,6 +235,18 @@ class DeviceBatch:
         N.check(N.lib().laml_plan_descriptors(
             C.byref(b), b.in_desc, b.out_desc, b.grp_desc, self._s()))
 
+    @property
+    def wide_chunk(self) -> int:
+        """State slots per stage of the bulk-staged wide level kernels (8, 16
+        or 32; 0 = 16): a tiling choice, the results are bitwise the same."""
+        return int(self.b.wide_chunk)
+
+    @wide_chunk.setter
+    def wide_chunk(self, ch: int):
+        if ch not in (0, 8, 16, 32):
+            raise ValueError("wide_chunk must be 0, 8, 16 or 32")
+        self.b.wide_chunk = int(ch)
+
     # -- raw entry points -------------------------------------------------
     def _s(self):
         return C.c_void_p(self._stream_ptr)
@@ -292,7 +304,8 @@ class DeviceBatch:
         """A CUDA graph of ``iters`` EM iterations on this batch (replay with
         ``launch_graph``); cached per argument set."""
         tol = rel_tol if rel_tol is not None else (EM_STOP_COMPAT if self.compat else EM_STOP_EXACT)
-        key = (iters, rounds, tol, max_iters, bool(persistent), self._mflags(polish))
+        key = (iters, rounds, tol, max_iters, bool(persistent), self._mflags(polish),
+               self.wide_chunk)
         if not hasattr(self, "_graphs"):
             self._graphs = {}
         if key not in self._graphs:

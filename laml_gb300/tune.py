@@ -1,11 +1,22 @@
-"""Tile-shape autotuner: sites per warp group (G = 8, 16 or 32).
+"""Tile-shape autotuner.
 
-G sets how many sites share one interleaved state column block, hence the
-coalescing width of every load (4*G bytes per group) and the number of
-(node, group) items per warp (32/G).  Small G wastes no lanes on site
-padding; large G gives wider transactions.  ``autotune`` times a few fused
-EM iterations of a sub-batch for each G on the device and keeps the fastest;
-``pick_group_sites`` is the no-GPU fallback cost model.
+Two axes of the level kernels' tiling:
+
+* sites per group G (8, 16 or 32): how many sites share one interleaved
+  state column block, hence the width of every row access (4 G bytes per
+  slot) and the number of (node, group) items per warp (32 / G).  Small G
+  wastes no lanes on site padding; large G gives wider transactions and
+  fewer items.
+* state slots per stage of the bulk-staged wide kernels (8, 16 or 32, with 8,
+  4 or 2 stages per warp: the same shared memory): how many slots of each
+  row one bulk copy moves, i.e. the granularity of the pipeline that feeds
+  a thread's state loop.
+
+``autotune`` times fused EM iterations of a sample of the batch for every
+shape on the device and keeps the fastest (cached per workload shape);
+``pick_group_sites`` is the no-GPU cost model used when the batch is too
+small for timing to mean anything.  This replaces the reference's one dense
+layout: every site padded to the largest state count (fast_em/laml.py:205).
 """
 from __future__ import annotations
 
@@ -14,7 +25,9 @@ from typing import Dict, Optional, Sequence
 
 import numpy as np
 
-_CACHE: Dict[tuple, int] = {}
+GROUP_SITES = (8, 16, 32)
+WIDE_CHUNKS = (8, 16, 32)
+_CACHE: Dict[tuple, dict] = {}
 
 
 def _padding_cost(K: int, G: int) -> float:
@@ -35,29 +48,45 @@ def pick_group_sites(workload=None, n_sites: Optional[int] = None) -> int:
     return best
 
 
-def autotune(newicks: Sequence[str], rows, Q, leaf_order, compat=True, sample=32, iters=3,
-             device="cuda") -> int:
-    """Time ``iters`` fused EM iterations on ``sample`` trees for each G."""
+def _key(newicks, Q, compat, sample):
+    n = len(newicks)
+    avg = int(np.mean([s.count(",") + 1 for s in newicks[:min(n, 8)]]))
+    return (min(n, sample), len(Q), avg, bool(compat))
+
+
+def autotune(newicks: Sequence[str], rows, Q, leaf_order, compat=True, sample=128, iters=2,
+             device="cuda", group_sites=GROUP_SITES, wide_chunks=WIDE_CHUNKS) -> dict:
+    """Time ``iters`` EM iterations (the graph of per-level launches, as the
+    solver replays it) on the first ``sample`` trees for every (G, slots per
+    stage) and return {"group_sites", "wide_chunk", "ms": {"G/chunk": ms}}.
+    Cached per (sample size, sites, tree size, model)."""
     import torch
 
     from .problem import make_batch
-    key = (len(newicks), len(Q), compat)
+    key = _key(newicks, Q, compat, sample)
     if key in _CACHE:
         return _CACHE[key]
     nw = list(newicks[:sample])
-    best, best_t = 8, None
-    for G in (8, 16, 32):
+    times = {}
+    best, best_t = None, None
+    for G in group_sites:
         b = make_batch(nw, rows, Q, leaf_order, compat=compat, group_sites=G, device=device)
-        b.branch_terms()
-        b.inside(update_em=True)
-        b.em_iterations(1, rel_tol=-1.0)
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        b.em_iterations(iters, rel_tol=-1.0)
-        torch.cuda.synchronize()
-        t = time.perf_counter() - t0
-        if best_t is None or t < best_t:
-            best, best_t = G, t
+        for ch in wide_chunks:
+            b.wide_chunk = ch
+            b.branch_terms()
+            b.inside(update_em=True)
+            g = b.em_graph(iters, rel_tol=-1.0, max_iters=1 << 30, persistent=False)
+            b.launch_graph(g)   # warm
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            b.launch_graph(g)
+            torch.cuda.synchronize()
+            t = (time.perf_counter() - t0) / iters
+            times[f"{G}/{ch}"] = t * 1e3
+            if best_t is None or t < best_t:
+                best, best_t = (G, ch), t
         del b
-    _CACHE[key] = best
-    return best
+    out = {"group_sites": best[0], "wide_chunk": best[1], "ms": times,
+           "sample_trees": len(nw), "iters": iters}
+    _CACHE[key] = out
+    return out
