@@ -506,7 +506,10 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--seed", type=int, default=0)
-    ap.add_argument("--group-sites", type=int, default=0)
+    ap.add_argument("--group-sites", type=int, default=0,
+                    help="sites per group (0: the autotuner's choice)")
+    ap.add_argument("--wide-chunk", type=int, default=0,
+                    help="state slots per stage of the staged wide kernels (0: autotuned)")
     ap.add_argument("--e2e-steps", type=int, default=2)
     ap.add_argument("--ref-trees", type=int, default=16)
     ap.add_argument("--no-cpu", action="store_true")
@@ -560,11 +563,20 @@ def main():
     dev = torch.device("cuda", local)
     w = synth.workload_config(WORKLOAD, seed=args.seed + rank)
     w.newicks = w.newicks[:args.trees]
-    G = args.group_sites or tune.pick_group_sites(w)
+    # the tile shape: sites per group x state slots per stage, timed on a
+    # sample of the batch by the autotuner (not part of the timed region)
+    tuned = None
+    if args.group_sites and args.wide_chunk:
+        G, CH = args.group_sites, args.wide_chunk
+    else:
+        tuned = tune.autotune(w.newicks, w.rows, w.Q, w.leaf_order, compat=True, device=dev)
+        G = args.group_sites or tuned["group_sites"]
+        CH = args.wide_chunk or tuned["wide_chunk"]
     stream = torch.cuda.Stream(dev)
     with torch.cuda.stream(stream):
         b = PB.make_batch(w.newicks, w.rows, w.Q, w.leaf_order, compat=True, group_sites=G,
                           nu=0.5, phi=0.5, device=dev, stream=stream)
+        b.wide_chunk = CH
         b.branch_terms()
         b.inside(update_em=True)
     llh_start = b.work["tr_llh"].cpu().numpy().copy()
@@ -651,13 +663,14 @@ def main():
     # e2e: public API from host strings / matrix to host results
     e2e = None
     if not args.no_e2e:
-        score_candidates(w.newicks, w.rows, w.Q, w.leaf_order, group_sites=G, device=dev)
+        score_candidates(w.newicks, w.rows, w.Q, w.leaf_order, group_sites=G, wide_chunk=CH,
+                         device=dev)
         torch.cuda.synchronize(dev)
         tot_iters, t_e2e, h2d, d2h = 0, 0.0, 0, 0
         for _ in range(args.e2e_steps):
             t_a = time.perf_counter()
             res = score_candidates(w.newicks, w.rows, w.Q, w.leaf_order, group_sites=G,
-                                   device=dev)
+                                   wide_chunk=CH, device=dev)
             t_e2e += time.perf_counter() - t_a
             tot_iters += sum(r.iterations for r in res.results)
             h2d, d2h = res.h2d_bytes, res.d2h_bytes
@@ -709,7 +722,10 @@ def main():
             "config": {"workload": "512 NNI candidates of a 1000-leaf Yule tree, 40 sites, "
                                    "M_k~U{5..50}, q~Dir(0.5), nu=0.1, phi=0.15, fastEM semantics",
                        "trees_per_gpu": T, "nodes_per_gpu": nodes, "sites": K,
-                       "group_sites": G, "l2": "inputs larger than L2 (partials "
+                       "group_sites": G, "wide_chunk": CH,
+                       "tile_shape": "autotuned" if tuned else "given",
+                       "autotune_ms_per_em_iteration": tuned["ms"] if tuned else None,
+                       "l2": "inputs larger than L2 (partials "
                        f"{2 * 4 * b.sizes['part_floats'] / 1e9:.2f} GB)",
                        "parallelism": f"replicas{world}" if world > 1 else "single"},
             "node_site_updates_per_s": nsu,

@@ -27,7 +27,7 @@ extern "C" {
 #define LAML_ERR_CUDA -2       /* a CUDA runtime call failed */
 #define LAML_ERR_PARSE -3      /* malformed newick */
 #define LAML_ERR_PRIOR -4      /* an observed state has no prior (phylogeny.py:91-93) */
-#define LAML_ERR_TIMEOUT -5    /* a device-side grid barrier gave up waiting */
+#define LAML_ERR_TIMEOUT -5    /* a device-side wait (grid barrier, mbarrier) gave up */
 #define LAML_ERR_NOT_BINARY -6 /* a node with more than two children */
 #define LAML_ERR_LEAF -7       /* a leaf label missing from the leaf order */
 
@@ -298,6 +298,13 @@ typedef struct laml_batch {
      * 32 (with 8, 4 or 2 stages per warp); 0 = 16.  A tiling choice only
      * (laml_gb300/tune.py picks it): results are bitwise the same. */
     int32_t wide_chunk;
+    /* limit in ns of every device-side wait (the persistent kernel's grid
+     * barrier, the staged kernels' mbarrier phases): 0 = 2 s.  A wait that
+     * runs out sets LAML_ERR_TIMEOUT in the error word, waits (2 s at most)
+     * for its own copies in flight and returns; the context stays usable.
+     * Negative: give up at the first check that finds the wait unsatisfied
+     * (to exercise that path). */
+    int64_t wait_limit_ns;
 } laml_batch;
 
 /* A tree's partials are FP32 values with power-of-two exponents (linear)

@@ -35,7 +35,8 @@ class ScoreResult:
 
 
 def score_candidates(newicks: Sequence[str], rows: dict, Q, leaf_order: Sequence[str],
-                     compat: bool = True, group_sites: int = 8, nu: float = 0.5,
+                     compat: bool = True, group_sites: Optional[int] = None,
+                     wide_chunk: Optional[int] = None, nu: float = 0.5,
                      phi: float = 0.5, rounds: int = MSTEP_ROUNDS, max_iters: int = 100000,
                      fix_nu=None, fix_phi=None, masks=None, device="cuda", chunk: int = 4,
                      rng: Optional[random.Random] = None,
@@ -47,10 +48,24 @@ def score_candidates(newicks: Sequence[str], rows: dict, Q, leaf_order: Sequence
     independent of the others in its batch, so the parts give each tree the
     result it has in one batch (up to FP32 summation order when a level's
     width crosses the wide/narrow rule).  Default: 2 parts from 256
-    candidates on, else 1."""
+    candidates on, else 1.
+
+    ``group_sites`` / ``wide_chunk`` (the tile shape): None = picked by the
+    autotuner (``tune.autotune``, cached per workload shape) for 64 or more
+    candidates, by the cost model below that."""
     import threading
     from concurrent.futures import ThreadPoolExecutor
 
+    from . import tune
+
+    if group_sites is None or wide_chunk is None:
+        if len(newicks) >= 64 and torch.device(device).type == "cuda":
+            t = tune.autotune(newicks, rows, Q, leaf_order, compat=compat, device=device)
+            group_sites = group_sites or t["group_sites"]
+            wide_chunk = wide_chunk or t["wide_chunk"]
+        else:
+            group_sites = group_sites or tune.pick_group_sites(n_sites=len(Q))
+            wide_chunk = wide_chunk or 16
     ds = dataset_from_rows(rows, Q, leaf_order, compat, group_sites)
     rng = rng if rng is not None else random
     T = len(newicks)
@@ -80,6 +95,7 @@ def score_candidates(newicks: Sequence[str], rows: dict, Q, leaf_order: Sequence
         b = make_batch(nws, rows, Q, leaf_order, compat=compat, group_sites=group_sites, nu=nu,
                        phi=phi, d=d, mask=sub(masks), fix_nu=sub(fix_nu), fix_phi=sub(fix_phi),
                        device=device, trees=trees, dataset=ds, stream=st)
+        b.wide_chunk = wide_chunk
         return b, st
 
     res, h2d, d2h = [], 0, 0

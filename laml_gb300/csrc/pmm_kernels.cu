@@ -2504,6 +2504,13 @@ __device__ __forceinline__ unsigned ld_acquire(const uint32_t* p) {
     return v;
 }
 
+// limit of the device-side waits (grid barrier, mbarrier phases) in ns:
+// laml_batch.wait_limit_ns, 0 = 2 s; negative = give up at the first check
+// that finds the wait unsatisfied
+__device__ __forceinline__ long long wait_limit(const laml_batch& b) {
+    return b.wait_limit_ns == 0 ? 2000000000ll : b.wait_limit_ns;
+}
+
 __device__ bool grid_barrier(const laml_batch& b, unsigned& gen) {
     __syncthreads();
     __shared__ int s_ok;
@@ -2515,9 +2522,10 @@ __device__ bool grid_barrier(const laml_batch& b, unsigned& gen) {
             atomicExch(b.barrier + 1, gen + 1);
         } else {
             const unsigned long long t0 = gtimer();
+            const long long lim = wait_limit(b);
             while (ld_acquire(b.barrier + 1) <= gen) {
                 if (*(volatile int*)b.error != 0) { ok = 0; break; }
-                if (gtimer() - t0 > 2000000000ull) {   // 2 s
+                if (lim < 0 || (long long)(gtimer() - t0) > lim) {
                     atomicCAS(b.error, 0, LAML_ERR_TIMEOUT);
                     ok = 0;
                     break;
@@ -2606,16 +2614,30 @@ __device__ __forceinline__ void fence_mbar_init() {
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
 }
 
-// bounded wait for a phase of an mbarrier (2 s, then LAML_ERR_TIMEOUT)
+// bounded wait for a phase of an mbarrier (the batch's wait limit, then
+// LAML_ERR_TIMEOUT)
 __device__ __forceinline__ bool mbar_wait(const laml_batch& b, uint64_t* bar, uint32_t parity) {
     if (mbar_try_wait(bar, parity)) return true;
-    const unsigned long long t0 = gtimer();
-    for (uint32_t it = 0; it < (1u << 26); ++it) {
-        if (mbar_try_wait(bar, parity)) return true;
-        if ((it & 63) == 0 && gtimer() - t0 > 2000000000ull) break;
+    const long long lim = wait_limit(b);
+    if (lim >= 0) {
+        const unsigned long long t0 = gtimer();
+        for (uint32_t it = 0; it < (1u << 26); ++it) {
+            if (mbar_try_wait(bar, parity)) return true;
+            if ((it & 63) == 0 && (long long)(gtimer() - t0) > lim) break;
+        }
     }
     atomicCAS(b.error, 0, LAML_ERR_TIMEOUT);
     return false;
+}
+
+// after a wait gave up: wait (2 s at most, whatever the batch's limit) for a
+// phase whose bulk copies are in flight, so none lands after the block exits
+__device__ __forceinline__ void mbar_drain(uint64_t* bar, uint32_t parity) {
+    const unsigned long long t0 = gtimer();
+    for (uint32_t it = 0; it < (1u << 26); ++it) {
+        if (mbar_try_wait(bar, parity)) return;
+        if ((it & 63) == 0 && gtimer() - t0 > 2000000000ull) return;
+    }
 }
 
 struct WItem {
@@ -3011,8 +3033,8 @@ __global__ void __launch_bounds__(kWWarps * 32) k_items_w(laml_batch b, const in
         if (!witem_run<G, KIND, true>(b, t, bufs + cur * per, cmax, lane, want_post != 0,
                                       respect_status != 0, bars + cur, par)) {
             // timed out: wait (bounded) for this warp's copies still in flight
-            mbar_wait(b, bars + cur, par);
-            if (has1) mbar_wait(b, bars + (cur ^ 1), (ph >> (cur ^ 1)) & 1u);
+            mbar_drain(bars + cur, par);
+            if (has1) mbar_drain(bars + (cur ^ 1), (ph >> (cur ^ 1)) & 1u);
             return;
         }
         __syncwarp();
@@ -3275,9 +3297,10 @@ __global__ void __launch_bounds__(kSWarps * 32) k_items_ws(laml_batch b, const i
             issue_more();
             const int stg = qc % kSStages;
             if (!mbar_wait(b, bars + stg, (uint32_t)(qc / kSStages) & 1u)) {
-                // timed out: wait (bounded) for this warp's other copies, then leave
-                for (int q = qc + 1; q < qi; ++q)
-                    mbar_wait(b, bars + (q % kSStages), (uint32_t)(q / kSStages) & 1u);
+                // gave up: wait (bounded) for this warp's copies in flight,
+                // the stage waited on included, then leave
+                for (int q = qc; q < qi; ++q)
+                    mbar_drain(bars + (q % kSStages), (uint32_t)(q / kSStages) & 1u);
                 return;
             }
             const float* st = ring + stg * Geo::stage + sub * Geo::item + l;
