@@ -3062,14 +3062,15 @@ __global__ void __launch_bounds__(kWWarps * 32) k_items_w(laml_batch b, const in
 // kernels', in the same order, so the results are bitwise equal.
 // ---------------------------------------------------------------------------
 constexpr int kSWarps = 4;     // warps per block
-constexpr int kSSlots = 64;    // state slots of each row a warp's ring holds
-// CH state slots of a row per stage, kSSlots / CH stages per warp: the
-// autotuner's states-per-stage axis (laml_batch.wide_chunk)
+constexpr int kSSlots = 32;    // state slots of each row a warp's ring holds
+constexpr int kSMinBlocks = 4; // resident blocks per SM asked (<= 128 registers)
+// CH state slots of a row per stage, max(2, kSSlots / CH) stages per warp:
+// the autotuner's states-per-stage axis (laml_batch.wide_chunk)
 
 template <int G, int NR, int CH>
 struct SGeom {
     static constexpr int P = 32 / G;                 // items per warp
-    static constexpr int S = kSSlots / CH;           // stages per warp
+    static constexpr int S = kSSlots / CH > 2 ? kSSlots / CH : 2;   // stages per warp
     static constexpr int row = CH * G;               // floats of one row's chunk
     static constexpr int item = NR * row + G;        // + G floats: items start G banks apart
     static constexpr int stage = P * item;
@@ -3147,9 +3148,32 @@ __device__ __forceinline__ void s_load(const laml_batch& b, const ItemDesc& d, b
     }
 }
 
+// what an item's leader lane needs to copy the item's rows: row offsets,
+// the group's offset and slot count, whether the rows are staged at all
+struct SIss {
+    int u_prow8, v_ref, w_ref, flags, goff, Cg;
+    bool staged;
+};
+
+template <int KIND>
+__device__ __forceinline__ SIss s_iss(const laml_batch& b, const ItemDesc& d, bool valid,
+                                      bool respect_status) {
+    const bool rs = KIND == 1 || respect_status;
+    SIss t;
+    t.u_prow8 = d.u_prow8;
+    t.v_ref = d.v_ref;
+    t.w_ref = d.w_ref;
+    t.flags = d.flags;
+    t.goff = __ldg(b.grp_desc + 8 * (int64_t)d.gd);
+    t.Cg = valid ? __ldg(b.group_C + d.gd) : 0;
+    const bool active = valid && (!rs || __ldcg(b.tr_status + d.tree) == LAML_TREE_ACTIVE);
+    t.staged = active && !tree_log(b, d.tree);
+    return t;
+}
+
 // chunks of a slab: its staged items' largest slot count over CH
 template <int CH>
-__device__ __forceinline__ int s_chunks(const SItem& t) {
+__device__ __forceinline__ int s_chunks(const SIss& t) {
     const int c = t.staged ? t.Cg : 0;
     const int m = __reduce_max_sync(kFull, c);
     return (m + CH - 1) / CH;
@@ -3158,21 +3182,21 @@ __device__ __forceinline__ int s_chunks(const SItem& t) {
 // the item's leader lane: arrive on the stage's mbarrier with the bytes of
 // chunk c of the item's rows (0 when it has none) and start their copies
 template <int G, int KIND, int CH>
-__device__ __forceinline__ void s_issue(const laml_batch& b, const SItem& t, int c, float* dst,
+__device__ __forceinline__ void s_issue(const laml_batch& b, const SIss& t, int c, float* dst,
                                         uint64_t* bar) {
     constexpr int R = CH * G;
     const int j0 = c * CH;
     const int ns = t.staged ? min(CH, t.Cg - j0) : 0;
     const uint32_t bytes = ns > 0 ? (uint32_t)ns * G * 4u : 0u;
-    const bool uin = KIND == 1, vin = !(t.d.flags & 1), win = !(t.d.flags & 2);
+    const bool uin = KIND == 1, vin = !(t.flags & 1), win = !(t.flags & 2);
     const uint32_t tx = bytes ? (uin ? bytes : 0u) + (vin ? bytes : 0u) + (win ? bytes : 0u) : 0u;
     fence_proxy_async_smem();   // this warp's reads of the stage's last use come first
     mbar_arrive_tx(bar, tx);
     if (!tx) return;
-    const int64_t off = (int64_t)t.s.goff + (int64_t)j0 * G;
-    if (uin) bulk_g2s(dst, b.out_part + (int64_t)t.d.u_prow8 * 8 + off, bytes, bar);
-    if (vin) bulk_g2s(dst + (uin ? 1 : 0) * R, b.in_part + (int64_t)t.d.v_ref * 8 + off, bytes, bar);
-    if (win) bulk_g2s(dst + (uin ? 2 : 1) * R, b.in_part + (int64_t)t.d.w_ref * 8 + off, bytes, bar);
+    const int64_t off = (int64_t)t.goff + (int64_t)j0 * G;
+    if (uin) bulk_g2s(dst, b.out_part + (int64_t)t.u_prow8 * 8 + off, bytes, bar);
+    if (vin) bulk_g2s(dst + (uin ? 1 : 0) * R, b.in_part + (int64_t)t.v_ref * 8 + off, bytes, bar);
+    if (win) bulk_g2s(dst + (uin ? 2 : 1) * R, b.in_part + (int64_t)t.w_ref * 8 + off, bytes, bar);
 }
 
 template <int G, bool VL, bool WL>
@@ -3233,9 +3257,10 @@ __device__ __forceinline__ void s_inside_chunk(const float* sv, const float* sw,
 }
 
 template <int G, int KIND, int CH>
-__global__ void __launch_bounds__(kSWarps * 32) k_items_ws(laml_batch b, const int32_t* desc,
-                                                           int64_t n, int want_post,
-                                                           int respect_status) {
+__global__ void __launch_bounds__(kSWarps * 32, kSMinBlocks) k_items_ws(laml_batch b,
+                                                                        const int32_t* desc,
+                                                                        int64_t n, int want_post,
+                                                                        int respect_status) {
     constexpr int NR = KIND == 1 ? 3 : 2;
     using Geo = SGeom<G, NR, CH>;
     constexpr int P = Geo::P, R = Geo::row, kSStages = Geo::S;
@@ -3256,16 +3281,18 @@ __global__ void __launch_bounds__(kSWarps * 32) k_items_ws(laml_batch b, const i
     __syncwarp();
     const bool rs = respect_status != 0;
     auto item_of = [&](int64_t slab) { return slab * P + sub; };
-    SItem cur, nxt;
-    {
-        const int64_t i0 = item_of(sc), i1 = item_of(sc + nw);
-        s_load<G, KIND>(b, load_desc(desc, i0 < n ? i0 : 0), i0 < n, l, rs, cur);
-        s_load<G, KIND>(b, load_desc(desc, i1 < n ? i1 : 0), i1 < n, l, rs, nxt);
-    }
-    int64_t i2 = item_of(sc + 2 * nw);
-    ItemDesc d2 = load_desc(desc, i2 < n ? i2 : 0);   // two slabs ahead
-    int nch_cur = s_chunks<CH>(cur), nch_nxt = s_chunks<CH>(nxt);
-    int iw = 0, ic = 0;   // next chunk to issue: slab (0 cur, 1 nxt), chunk
+    auto desc_of = [&](int64_t slab) {
+        const int64_t i = item_of(slab);
+        return load_desc(desc, i < n ? i : 0);
+    };
+    // the current slab's descriptor and copy state; the next slab's copy
+    // state (its rows are copied while this one computes); the slab after
+    // that's descriptor (read ahead)
+    ItemDesc dc = desc_of(sc), dn = desc_of(sc + nw), dnn = desc_of(sc + 2 * nw);
+    SIss ic_ = s_iss<KIND>(b, dc, item_of(sc) < n, rs);
+    SIss in_ = s_iss<KIND>(b, dn, item_of(sc + nw) < n, rs);
+    int nch_cur = s_chunks<CH>(ic_), nch_nxt = s_chunks<CH>(in_);
+    int iw = 0, ic = 0;   // next chunk to issue: slab (0 current, 1 next), chunk
     int qi = 0, qc = 0;   // chunks issued / consumed by this warp
     auto issue_more = [&]() {
         while (qi - qc < kSStages) {
@@ -3277,14 +3304,17 @@ __global__ void __launch_bounds__(kSWarps * 32) k_items_ws(laml_batch b, const i
             float* dst = ring + (qi % kSStages) * Geo::stage + sub * Geo::item;
             uint64_t* bar = bars + (qi % kSStages);
             if (leader) {
-                if (iw == 0) s_issue<G, KIND, CH>(b, cur, ic, dst, bar);
-                else s_issue<G, KIND, CH>(b, nxt, ic, dst, bar);
+                if (iw == 0) s_issue<G, KIND, CH>(b, ic_, ic, dst, bar);
+                else s_issue<G, KIND, CH>(b, in_, ic, dst, bar);
             }
             ++qi;
             ++ic;
         }
     };
     for (;;) {
+        issue_more();   // this slab's rows (and the next's) in flight first
+        SItem cur;
+        s_load<G, KIND>(b, dc, item_of(sc) < n, l, rs, cur);
         float cv_[8] = {0, 0, 0, 0, 0, 0, 0, 0}, cw_[8] = {0, 0, 0, 0, 0, 0, 0, 0};
         const bool run = cur.live && cur.staged;
         const int C = run ? cur.s.C : 0;
@@ -3416,15 +3446,16 @@ __global__ void __launch_bounds__(kSWarps * 32) k_items_ws(laml_batch b, const i
                 inside_log_item<G>(b, dl, sl, gl);
             }
         }
-        // rotate: next slab's state (loaded a slab ago) becomes current
+        // rotate: the next slab becomes current
         sc += nw;
         if (sc >= nslab) break;
-        cur = nxt;
+        dc = dn;
+        ic_ = in_;
         nch_cur = nch_nxt;
-        s_load<G, KIND>(b, d2, i2 < n, l, rs, nxt);
-        nch_nxt = s_chunks<CH>(nxt);
-        i2 = item_of(sc + 2 * nw);
-        d2 = load_desc(desc, i2 < n ? i2 : 0);
+        dn = dnn;
+        in_ = s_iss<KIND>(b, dn, item_of(sc + nw) < n, rs);
+        nch_nxt = s_chunks<CH>(in_);
+        dnn = desc_of(sc + 2 * nw);
         if (iw == 1) iw = 0;   // the issue position moves with the slab
         else { iw = 0; ic = 0; }
     }
