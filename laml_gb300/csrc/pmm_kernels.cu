@@ -2595,6 +2595,17 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
     return ok != 0;
 }
 
+// non-blocking test of a phase (try_wait may suspend the thread for a while)
+__device__ __forceinline__ bool mbar_test_wait(uint64_t* bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile("{\n\t.reg .pred p;\n\tmbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+                 "selp.u32 %0, 1, 0, p;\n\t}"
+                 : "=r"(ok)
+                 : "r"(smem_u32(bar)), "r"(parity)
+                 : "memory");
+    return ok != 0;
+}
+
 // global -> shared bulk copy (16-byte aligned addresses, size a multiple of 16)
 __device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes,
                                          uint64_t* bar) {
@@ -2617,9 +2628,14 @@ __device__ __forceinline__ void fence_mbar_init() {
 // bounded wait for a phase of an mbarrier (the batch's wait limit, then
 // LAML_ERR_TIMEOUT)
 __device__ __forceinline__ bool mbar_wait(const laml_batch& b, uint64_t* bar, uint32_t parity) {
-    if (mbar_try_wait(bar, parity)) return true;
     const long long lim = wait_limit(b);
-    if (lim >= 0) {
+    if (lim < 0) {   // one check, without the suspension try_wait may take
+        if (mbar_test_wait(bar, parity)) return true;
+        atomicCAS(b.error, 0, LAML_ERR_TIMEOUT);
+        return false;
+    }
+    if (mbar_try_wait(bar, parity)) return true;
+    {
         const unsigned long long t0 = gtimer();
         for (uint32_t it = 0; it < (1u << 26); ++it) {
             if (mbar_try_wait(bar, parity)) return true;
