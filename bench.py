@@ -508,8 +508,9 @@ def main():
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--group-sites", type=int, default=0,
                     help="sites per group (0: the autotuner's choice)")
-    ap.add_argument("--wide-chunk", type=int, default=0,
-                    help="state slots per stage of the staged wide kernels (0: autotuned)")
+    ap.add_argument("--wide-chunk", type=int, default=-1,
+                    help="wide levels: 0 per-thread loads, 8/16 bulk-staged rows with that many "
+                         "slots per stage (-1: the autotuner's choice)")
     ap.add_argument("--e2e-steps", type=int, default=2)
     ap.add_argument("--ref-trees", type=int, default=16)
     ap.add_argument("--no-cpu", action="store_true")
@@ -566,12 +567,12 @@ def main():
     # the tile shape: sites per group x state slots per stage, timed on a
     # sample of the batch by the autotuner (not part of the timed region)
     tuned = None
-    if args.group_sites and args.wide_chunk:
+    if args.group_sites and args.wide_chunk >= 0:
         G, CH = args.group_sites, args.wide_chunk
     else:
         tuned = tune.autotune(w.newicks, w.rows, w.Q, w.leaf_order, compat=True, device=dev)
         G = args.group_sites or tuned["group_sites"]
-        CH = args.wide_chunk or tuned["wide_chunk"]
+        CH = args.wide_chunk if args.wide_chunk >= 0 else tuned["wide_chunk"]
     stream = torch.cuda.Stream(dev)
     with torch.cuda.stream(stream):
         b = PB.make_batch(w.newicks, w.rows, w.Q, w.leaf_order, compat=True, group_sites=G,
@@ -651,7 +652,7 @@ def main():
                     "of internal parents, both children per item)", n_out + 2)
     roof_in = roof(pb["inside"], ms_in / 1e3, "k_items inside levels (one launch per height)",
                    n_in + 1)
-    if T == 512 and G == 8:
+    if T == 512 and G == 8 and CH == 0:
         roof_out["traffic"] = TRAFFIC_PER_LAUNCH["outside"]
         roof_in["traffic"] = TRAFFIC_PER_LAUNCH["inside"]
     roof_it = roof(pb["em_iteration"], avg_launch_s,
@@ -723,6 +724,8 @@ def main():
                                    "M_k~U{5..50}, q~Dir(0.5), nu=0.1, phi=0.15, fastEM semantics",
                        "trees_per_gpu": T, "nodes_per_gpu": nodes, "sites": K,
                        "group_sites": G, "wide_chunk": CH,
+                       "wide_kernel": "direct per-thread loads" if CH == 0 else
+                       f"bulk-staged, {CH} slots per stage",
                        "tile_shape": "autotuned" if tuned else "given",
                        "autotune_ms_per_em_iteration": tuned["ms"] if tuned else None,
                        "l2": "inputs larger than L2 (partials "

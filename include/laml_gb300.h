@@ -294,9 +294,11 @@ typedef struct laml_batch {
      * place of its dataset's -- the totals over all ranks when the tree's
      * sites are split across ranks and cnt_part holds the reduced counts */
     const double* tr_mstats;
-    /* state slots per stage of the bulk-staged wide level kernels: 8, 16 or
-     * 32 (with 8, 4 or 2 stages per warp); 0 = 16.  A tiling choice only
-     * (laml_gb300/tune.py picks it): results are bitwise the same. */
+    /* the wide levels' kernel (more than 8192 items): 0 = per-thread row
+     * loads; 8 or 16 = rows copied into per-warp shared-memory stages by the
+     * bulk-copy engine, that many state slots per stage (4 or 2 stages).  A
+     * tiling choice only (laml_gb300/tune.py picks it): results are bitwise
+     * the same. */
     int32_t wide_chunk;
     /* limit in ns of every device-side wait (the persistent kernel's grid
      * barrier, the staged kernels' mbarrier phases): 0 = 2 s.  A wait that

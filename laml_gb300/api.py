@@ -61,11 +61,10 @@ def score_candidates(newicks: Sequence[str], rows: dict, Q, leaf_order: Sequence
     if group_sites is None or wide_chunk is None:
         if len(newicks) >= 64 and torch.device(device).type == "cuda":
             t = tune.autotune(newicks, rows, Q, leaf_order, compat=compat, device=device)
-            group_sites = group_sites or t["group_sites"]
-            wide_chunk = wide_chunk or t["wide_chunk"]
         else:
-            group_sites = group_sites or tune.pick_group_sites(n_sites=len(Q))
-            wide_chunk = wide_chunk or 16
+            t = {"group_sites": tune.pick_group_sites(n_sites=len(Q)), "wide_chunk": 0}
+        group_sites = t["group_sites"] if group_sites is None else group_sites
+        wide_chunk = t["wide_chunk"] if wide_chunk is None else wide_chunk
     ds = dataset_from_rows(rows, Q, leaf_order, compat, group_sites)
     rng = rng if rng is not None else random
     T = len(newicks)

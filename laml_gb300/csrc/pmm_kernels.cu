@@ -34,7 +34,6 @@
 #include <cfloat>
 #include <cmath>
 #include <cstdio>
-#include <cstdlib>
 #include <string>
 #include <vector>
 
@@ -3765,8 +3764,8 @@ int validate(const laml_batch* b) {
         laml::set_error("laml_batch: in_desc, out_desc and grp_desc (laml_plan_fill) are required");
         return LAML_ERR_ARG;
     }
-    if (b->wide_chunk != 0 && b->wide_chunk != 8 && b->wide_chunk != 16 && b->wide_chunk != 32) {
-        laml::set_error("laml_batch: wide_chunk must be 0, 8, 16 or 32");
+    if (b->wide_chunk != 0 && b->wide_chunk != 8 && b->wide_chunk != 16) {
+        laml::set_error("laml_batch: wide_chunk must be 0, 8 or 16");
         return LAML_ERR_ARG;
     }
     return LAML_OK;
@@ -3817,16 +3816,6 @@ int launch_staged(const laml_batch& b, const int32_t* desc, int64_t n, int want_
     return check(cudaGetLastError(), "k_items_w launch");
 }
 
-// the wide levels' kernel: bulk-staged (default) or direct per-thread loads
-// (LAML_WIDE_KERNEL=direct in the environment, read once)
-bool wide_staged() {
-    static const bool on = [] {
-        const char* e = std::getenv("LAML_WIDE_KERNEL");
-        return !(e && std::string(e) == "direct");
-    }();
-    return on;
-}
-
 template <int G, int KIND, int CH>
 int launch_staged_wide_t(const laml_batch& b, const int32_t* desc, int64_t n, int want_post,
                          int respect_status, cudaStream_t st) {
@@ -3860,19 +3849,18 @@ int launch_staged_wide_t(const laml_batch& b, const int32_t* desc, int64_t n, in
 template <int G, int KIND>
 int launch_staged_wide(const laml_batch& b, const int32_t* desc, int64_t n, int want_post,
                        int respect_status, cudaStream_t st) {
-    switch (b.wide_chunk) {
-        case 8: return launch_staged_wide_t<G, KIND, 8>(b, desc, n, want_post, respect_status, st);
-        case 32: return launch_staged_wide_t<G, KIND, 32>(b, desc, n, want_post, respect_status, st);
-        default: return launch_staged_wide_t<G, KIND, 16>(b, desc, n, want_post, respect_status, st);
-    }
+    if (b.wide_chunk == 8)
+        return launch_staged_wide_t<G, KIND, 8>(b, desc, n, want_post, respect_status, st);
+    return launch_staged_wide_t<G, KIND, 16>(b, desc, n, want_post, respect_status, st);
 }
 
 template <int G>
 int launch_items(const laml_batch& b, const int32_t* items, int64_t n, int kind, int want_post,
                  int respect_status, cudaStream_t st, const int32_t* desc = nullptr) {
     if (n <= 0) return LAML_OK;
-    // wide inside / outside levels below the roots: bulk-staged rows
-    if ((kind == 0 || kind == 1) && !narrow_level(n) && b.max_states > 0 && wide_staged()) {
+    // wide inside / outside levels below the roots: bulk-staged rows when
+    // the batch asks for them (wide_chunk), else per-thread loads
+    if ((kind == 0 || kind == 1) && !narrow_level(n) && b.max_states > 0 && b.wide_chunk > 0) {
         return kind == 0 ? launch_staged_wide<G, 0>(b, desc, n, want_post, respect_status, st)
                          : launch_staged_wide<G, 1>(b, desc, n, want_post, respect_status, st);
     }

@@ -237,14 +237,15 @@ class DeviceBatch:
 
     @property
     def wide_chunk(self) -> int:
-        """State slots per stage of the bulk-staged wide level kernels (8, 16
-        or 32; 0 = 16): a tiling choice, the results are bitwise the same."""
+        """The wide levels' kernel: 0 per-thread row loads (default), 8 or 16
+        bulk-staged rows with that many state slots per stage.  A tiling
+        choice: the results are bitwise the same."""
         return int(self.b.wide_chunk)
 
     @wide_chunk.setter
     def wide_chunk(self, ch: int):
-        if ch not in (0, 8, 16, 32):
-            raise ValueError("wide_chunk must be 0, 8, 16 or 32")
+        if ch not in (0, 8, 16):
+            raise ValueError("wide_chunk must be 0, 8 or 16")
         self.b.wide_chunk = int(ch)
 
     # -- raw entry points -------------------------------------------------

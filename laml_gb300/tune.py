@@ -7,10 +7,10 @@ Two axes of the level kernels' tiling:
   slot) and the number of (node, group) items per warp (32 / G).  Small G
   wastes no lanes on site padding; large G gives wider transactions and
   fewer items.
-* state slots per stage of the bulk-staged wide kernels (8, 16 or 32, with 8,
-  4 or 2 stages per warp: the same shared memory): how many slots of each
-  row one bulk copy moves, i.e. the granularity of the pipeline that feeds
-  a thread's state loop.
+* the wide levels' kernel: per-thread row loads (0), or rows copied into
+  per-warp shared-memory stages by the bulk-copy engine with 8 or 16 state
+  slots per stage (4 or 2 stages): how the state loops of the levels with
+  more than 8192 items are fed.
 
 ``autotune`` times fused EM iterations of a sample of the batch for every
 shape on the device and keeps the fastest (cached per workload shape);
@@ -26,7 +26,7 @@ from typing import Dict, Optional, Sequence
 import numpy as np
 
 GROUP_SITES = (8, 16, 32)
-WIDE_CHUNKS = (8, 16, 32)
+WIDE_CHUNKS = (0, 8, 16)
 _CACHE: Dict[tuple, dict] = {}
 
 
@@ -57,8 +57,8 @@ def _key(newicks, Q, compat, sample):
 def autotune(newicks: Sequence[str], rows, Q, leaf_order, compat=True, sample=128, iters=2,
              device="cuda", group_sites=GROUP_SITES, wide_chunks=WIDE_CHUNKS) -> dict:
     """Time ``iters`` EM iterations (the graph of per-level launches, as the
-    solver replays it) on the first ``sample`` trees for every (G, slots per
-    stage) and return {"group_sites", "wide_chunk", "ms": {"G/chunk": ms}}.
+    solver replays it) on the first ``sample`` trees for every (G, wide
+    kernel) and return {"group_sites", "wide_chunk", "ms": {"G/chunk": ms}}.
     Cached per (sample size, sites, tree size, model)."""
     import torch
 

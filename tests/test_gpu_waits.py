@@ -4,7 +4,8 @@ its own copies still in flight and returns, and the context stays usable.
 
 The limit set negative makes each wait give up at its first unsatisfied
 check -- a wait that runs out on purpose, with no fault, trap or hang: on the
-staged per-level kernels (mbarrier phases of the bulk copies) and on the
+staged per-level kernels (mbarrier phases of the bulk copies, narrow and
+wide levels) and on the
 persistent kernel (its grid barrier).  The next calls on the same context,
 with the limit back at its default, match the FP64 C restatement."""
 import numpy as np
@@ -29,6 +30,7 @@ def test_staged_level_waits_run_out_then_recover():
     w = _case()
     b = PB.make_batch(w.newicks, w.rows, w.Q, w.leaf_order, compat=True, nu=0.5, phi=0.5)
     assert max(np.diff(b._h_in_off)) > 8192 and min(np.diff(b._h_in_off)) <= 8192
+    b.wide_chunk = 16   # wide levels on the bulk-staged kernels too
     b.b.wait_limit_ns = -1
     b.branch_terms()
     b.inside(update_em=True)
