@@ -820,6 +820,222 @@ def ultrametric_d(S, nu, d, mask, tree: ParsedTree):
 # ----------------------------------------------------------------------------
 # EM loops
 # ----------------------------------------------------------------------------
+# ----------------------------------------------------------------------------
+# fastEM's own M-step: 100 steps of L-BFGS with a line search on
+# M_step_loss_fn in (log d, logit nu, logit phi), FP32 (fast_em/laml.py:49-110).
+# The reference runs optax (>= 0.2.4, < 1.0; not vendored): optax.lbfgs with
+# scale_init_precond=True -- the two-loop recursion over the last 10 pairs,
+# the initial inverse Hessian <s, y> / <y, y> of the newest pair -- and its
+# default zoom line search (strong Wolfe, c1 = 1e-4, c2 = 0.9, first trial
+# step 1, at most 20 evaluations), chained with
+# scale_by_backtracking_linesearch(15): an Armijo test (slope 1e-4) on the
+# step found, shrunk by 0.8 up to 15 times.  This restates those published
+# methods (Nocedal & Wright, Numerical Optimization, algorithms 3.5, 3.6 and
+# 7.4); optax's own iterates are not reproduced bit for bit (parity unpinned).
+# ----------------------------------------------------------------------------
+LBFGS_STEPS = 100          # M_STEP_DESCENT_STEPS, fast_em/laml.py:44
+LBFGS_MEMORY = 10
+WOLFE_C1, WOLFE_C2, ZOOM_EVALS = 1e-4, 0.9, 20
+BACKTRACK_STEPS, BACKTRACK_FACTOR = 15, 0.8
+
+
+def mstep_loss_grad(x, counts, leaf_resp_total, R, M, branch_mask, param_mask):
+    """M_step_loss_fn (fast_em/laml.py:62-78) and its gradient in FP32 at
+    x = (log d [N], logit nu, logit phi); the gradient is masked as
+    laml.py:88-92 masks it."""
+    f32 = np.float32
+    x = np.asarray(x, dtype=f32)
+    N = x.shape[0] - 2
+    lo = f32(math.log(CALC_EPS))
+    u = x[:N]
+    d = np.exp(np.clip(u, lo, -lo))
+    sd = (u > lo) & (u < -lo)
+    with np.errstate(over="ignore"):
+        sig = f32(1) / (f32(1) + np.exp(-x[N:]))
+    mp = np.clip(sig, f32(CALC_EPS), f32(1 - CALC_EPS))
+    sm = (sig > f32(CALC_EPS)) & (sig < f32(1 - CALC_EPS))
+    nu, phi = mp[0], mp[1]
+    e = np.asarray(counts, dtype=f32)
+    ln2 = f32(math.log(2.0))
+
+    def l1m(z):   # log(1 - e^-z), fast_em's log1mexp_pos
+        with np.errstate(divide="ignore", invalid="ignore"):
+            return np.where(z > ln2, np.log1p(-np.exp(-z)), np.log(-np.expm1(-z)))
+
+    dn = d * nu
+    c1 = -e[:, 0] * d * (f32(1) + nu)
+    c2 = e[:, 1] * (l1m(d) - d * nu)
+    c3 = e[:, 2] * l1m(dn)
+    c4 = -e[:, 3] * d * nu
+    c5 = e[:, 4] * l1m(dn)
+    R32, M32, LR = f32(R), f32(M), f32(leaf_resp_total)
+    c6 = R32 * np.log(f32(1) - phi) + (M32 - LR) * np.log(phi)
+    loss = -(np.sum(c1 + c2 + c3 + c4 + c5, dtype=f32) + c6)
+    with np.errstate(divide="ignore", over="ignore"):
+        ie = f32(1) / np.expm1(d)
+        ien = f32(1) / np.expm1(dn)
+    cs = e[:, 2] + e[:, 4]
+    dfd = -e[:, 0] * (f32(1) + nu) + e[:, 1] * (ie - nu) + cs * nu * ien - e[:, 3] * nu
+    dfn = np.sum(-(e[:, 0] + e[:, 1] + e[:, 3]) * d + cs * d * ien, dtype=f32)
+    dfp = -R32 / (f32(1) - phi) + (M32 - LR) / phi
+    g = np.empty_like(x)
+    g[:N] = np.where(sd, -dfd * d, f32(0)) * np.asarray(branch_mask, dtype=f32)
+    gm = np.array([-dfn, -dfp], dtype=f32) * mp * (f32(1) - mp)
+    g[N:] = np.where(sm, gm, f32(0)) * np.asarray(param_mask, dtype=f32)
+    return f32(loss), g
+
+
+def _cubic_step(lo, flo, dlo, hi, fhi, dhi):
+    """Minimiser of the cubic through (lo, flo, dlo), (hi, fhi, dhi) (Nocedal
+    & Wright eq. 3.59), kept inside the bracket by 10% of its width;
+    bisection where the cubic has no usable minimiser."""
+    w = abs(hi - lo)
+    if np.isfinite(fhi) and np.isfinite(dhi) and w > 0:
+        d1 = dlo + dhi - 3 * (flo - fhi) / (lo - hi)
+        rad = d1 * d1 - dlo * dhi
+        if rad >= 0:
+            d2 = math.copysign(math.sqrt(rad), hi - lo)
+            den = dhi - dlo + 2 * d2
+            if den != 0:
+                a = hi - (hi - lo) * (dhi + d2 - d1) / den
+                if min(lo, hi) + 0.1 * w <= a <= max(lo, hi) - 0.1 * w:
+                    return a
+    return 0.5 * (lo + hi)
+
+
+def _zoom_search(fg, x, f0, g0, p):
+    """A step along p meeting the strong Wolfe conditions: first trial 1,
+    doubled while the slope stays negative, then the zoom of the bracket;
+    at most ZOOM_EVALS evaluations.  Returns (step, f, g); on exhaustion the
+    best point with sufficient decrease seen, else the last trial."""
+    d0 = float(np.dot(g0, p))
+    st = {"n": 0, "best": None}
+
+    def ev(a):
+        st["n"] += 1
+        f, g = fg(x + np.float32(a) * p)
+        f = float(f)
+        if np.isfinite(f) and f <= f0 + WOLFE_C1 * a * d0 and (
+                st["best"] is None or f < st["best"][1]):
+            st["best"] = (a, f, g)
+        return f, g, float(np.dot(g, p))
+
+    def zoom(lo, flo, dlo, hi, fhi, dhi):
+        last = None
+        while st["n"] < ZOOM_EVALS:
+            a = _cubic_step(lo, flo, dlo, hi, fhi, dhi)
+            f, g, da = ev(a)
+            last = (a, f, g)
+            if not np.isfinite(f) or f > f0 + WOLFE_C1 * a * d0 or f >= flo:
+                hi, fhi, dhi = a, f, da
+            else:
+                if abs(da) <= -WOLFE_C2 * d0:
+                    return a, f, g
+                if da * (hi - lo) >= 0:
+                    hi, fhi, dhi = lo, flo, dlo
+                lo, flo, dlo = a, f, da
+        return st["best"] if st["best"] is not None else last
+
+    a_prev, f_prev, d_prev = 0.0, f0, d0
+    a = 1.0
+    while st["n"] < ZOOM_EVALS:
+        f, g, da = ev(a)
+        if not np.isfinite(f) or f > f0 + WOLFE_C1 * a * d0 or (a_prev > 0 and f >= f_prev):
+            return zoom(a_prev, f_prev, d_prev, a, f, da)
+        if abs(da) <= -WOLFE_C2 * d0:
+            return a, f, g
+        if da >= 0:
+            return zoom(a, f, da, a_prev, f_prev, d_prev)
+        a_prev, f_prev, d_prev = a, f, da
+        a = 2.0 * a
+    if st["best"] is not None:
+        return st["best"]
+    return a_prev, f_prev, fg(x + np.float32(a_prev) * p)[1]
+
+
+def lbfgs_start(d, nu, phi):
+    """The EM loop's parameter vector (fast_em/laml.py:126-139): log max(d,
+    EPS) and the logits of nu and phi clamped to [EPS, 1 - EPS], FP32."""
+    N = len(d)
+    x = np.empty(N + 2, dtype=np.float32)
+    x[:N] = np.log(np.maximum(np.asarray(d, dtype=np.float64), EPS))
+    nu = min(max(nu, EPS), 1 - EPS)
+    phi = min(max(phi, EPS), 1 - EPS)
+    x[N] = math.log(nu / (1 - nu))
+    x[N + 1] = math.log(phi / (1 - phi))
+    return x
+
+
+def lbfgs_params(x):
+    """(d, nu, phi) of a parameter vector as the E-step reads them:
+    exp(log d), sigmoid(logits), unclamped (laml.py:151-156)."""
+    x = np.asarray(x, dtype=np.float64)
+    N = len(x) - 2
+    with np.errstate(over="ignore"):
+        mp = 1.0 / (1.0 + np.exp(-x[N:]))
+    return np.exp(x[:N]), float(mp[0]), float(mp[1])
+
+
+def mstep_compat_lbfgs(counts, leaf_resp_total, R, M, x, branch_mask, fix_nu, fix_phi,
+                       steps=LBFGS_STEPS):
+    """fastEM's M-step as the reference runs it (fast_em/laml.py:84-110): 100
+    L-BFGS steps with the zoom line search and the chained backtracking
+    test, from the EM loop's parameter vector x (log d, logit nu, logit
+    phi; the loop keeps it across iterations, laml.py:190).  Returns the new
+    vector."""
+    f32 = np.float32
+    x = np.asarray(x, dtype=f32).copy()
+    pm = np.array([0.0 if fix_nu else 1.0, 0.0 if fix_phi else 1.0], dtype=f32)
+    bm = np.asarray(branch_mask, dtype=f32)
+
+    def fg(z):
+        return mstep_loss_grad(z, counts, leaf_resp_total, R, M, bm, pm)
+
+    f, g = fg(x)
+    S, Y, W = [], [], []
+    for _ in range(steps):
+        q = g.copy()
+        al = []
+        for s_, y_, w_ in zip(reversed(S), reversed(Y), reversed(W)):
+            a = w_ * f32(np.dot(s_, q))
+            q = q - a * y_
+            al.append(a)
+        gam = f32(1)
+        if S:
+            yy = f32(np.dot(Y[-1], Y[-1]))
+            if yy > 0:
+                gam = f32(np.dot(S[-1], Y[-1])) / yy
+        z = gam * q
+        for (s_, y_, w_), a in zip(zip(S, Y, W), reversed(al)):
+            z = z + s_ * (a - w_ * f32(np.dot(y_, z)))
+        p = -z
+        if not float(np.dot(g, p)) < 0:   # not a descent direction: the gradient
+            p = -g
+            S, Y, W = [], [], []
+        if not float(np.dot(g, p)) < 0:
+            break                          # stationary under the masks
+        a, fn, gn = _zoom_search(fg, x, float(f), g, p)
+        u = np.float32(a) * p
+        slope = float(np.dot(g, u))       # the chained backtracking test
+        t = 1.0
+        for _ in range(BACKTRACK_STEPS):
+            if np.isfinite(fn) and fn <= float(f) + 1e-4 * t * slope:
+                break
+            t *= BACKTRACK_FACTOR
+            fn, gn = fg(x + np.float32(t) * u)
+            fn = float(fn)
+        xn = x + np.float32(t) * u
+        s_, y_ = xn - x, gn - g
+        sy = f32(np.dot(s_, y_))
+        S.append(s_)
+        Y.append(y_)
+        W.append(f32(0) if sy == 0 else f32(1) / sy)
+        if len(S) > LBFGS_MEMORY:
+            S.pop(0), Y.pop(0), W.pop(0)
+        x, f, g = xn, f32(fn), gn
+    return x
+
+
 @dataclass
 class EMResult:
     llh: float
@@ -832,8 +1048,12 @@ class EMResult:
 
 
 def em_compat(prob: Problem, d, nu, phi, branch_mask=None, fix_nu=False, fix_phi=False,
-              max_iters=10_000, rounds=MSTEP_ROUNDS, stop=EM_STOP_COMPAT) -> EMResult:
-    """optimize_parameters_expectation_maximization (fast_em/laml.py:112-194):
+              max_iters=10_000, rounds=MSTEP_ROUNDS, stop=EM_STOP_COMPAT,
+              mstep="stationary") -> EMResult:
+    """optimize_parameters_expectation_maximization (fast_em/laml.py:112-194)
+    with ``mstep`` "stationary" (the M-step objective solved to its
+    stationary point) or "lbfgs" (the reference's 100 L-BFGS steps,
+    ``mstep_compat_lbfgs``, the parameter vector kept across iterations):
     clamp nu, phi to [EPS, 1-EPS], floor d at EPS, loop E -> M -> logL until
     the relative change is below 1e-5; on convergence return the new logL
     with the parameters *before* the last M-step (the loop breaks before
@@ -846,6 +1066,9 @@ def em_compat(prob: Problem, d, nu, phi, branch_mask=None, fix_nu=False, fix_phi
     chars = prob.enc.chars
     M = float(np.sum(chars == MISSING))
     R = float(np.sum(chars != MISSING))
+    x = lbfgs_start(d, nu, phi) if mstep == "lbfgs" else None
+    if x is not None:
+        d, nu, phi = lbfgs_params(x)
     prev, _ = log_likelihood(prob, d, nu, phi)
     trace = [prev]
     it = 0
@@ -853,8 +1076,13 @@ def em_compat(prob: Problem, d, nu, phi, branch_mask=None, fix_nu=False, fix_phi
     while it < max_iters:
         it += 1
         es = e_step(prob, d, nu, phi)
-        dn, nun, phin = mstep_compat(es.counts, float(es.leaf_resp.sum()), R, M, d, nu, phi,
-                                     mask, fix_nu, fix_phi, rounds=rounds)
+        if x is not None:
+            xn = mstep_compat_lbfgs(es.counts, float(es.leaf_resp.sum()), R, M, x, mask,
+                                    fix_nu, fix_phi)
+            dn, nun, phin = lbfgs_params(xn)
+        else:
+            dn, nun, phin = mstep_compat(es.counts, float(es.leaf_resp.sum()), R, M, d, nu,
+                                         phi, mask, fix_nu, fix_phi, rounds=rounds)
         cur, _ = log_likelihood(prob, dn, nun, phin)
         trace.append(cur)
         if abs(cur - prev) / abs(prev) < stop:
@@ -863,6 +1091,8 @@ def em_compat(prob: Problem, d, nu, phi, branch_mask=None, fix_nu=False, fix_phi
             cur = prev
             break
         d, nu, phi = dn, nun, phin
+        if x is not None:
+            x = xn
         prev = cur
     return EMResult(cur, d, nu, phi, it, trace)
 
