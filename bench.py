@@ -580,6 +580,7 @@ def main():
         b.wide_chunk = CH
         b.branch_terms()
         b.inside(update_em=True)
+    stream.synchronize()   # the read below runs on the default stream
     llh_start = b.work["tr_llh"].cpu().numpy().copy()
     T = b.T
     nodes = b.sizes["n_nodes"]
