@@ -22,10 +22,13 @@ Every likelihood, E-step and M-step runs on the GPU; there is no CPU path.
 Only binary trees are supported (a polytomy raises ValueError).  With
 ``ultra_constr=True`` every M-step solves the branch lengths under
 EM_solver's ultrametric equalities (EM_solver.py:53-89, 358-361) on the
-device; the equalities that tie the roots of several trees together are not
-implemented (``ultra_constr=True`` with more than one tree raises
-NotImplementedError).  Constraints without a solution end the EM with status
-"d_infeasible", as EM_solver.EM_optimization does (EM_solver.py:491-495).
+device.  Several trees share one nu and one phi and run one EM on their
+summed log-likelihood, as EM_solver's M-step over all of its trees does
+(EM_solver.py:307-459), with their roots at one height under
+``ultra_constr`` (EM_solver.py:81-84): the trees are joined under
+zero-length fixed branches (laml_gb300/forest.py).  Constraints without a
+solution end the EM with status "d_infeasible", as
+EM_solver.EM_optimization does (EM_solver.py:491-495).
 """
 from __future__ import annotations
 
@@ -36,6 +39,7 @@ import numpy as np
 
 from .encoding import EncodedTree, char_matrix, encode_dataset, encode_newick
 from ._native import TREE_INFEASIBLE
+from .forest import join_forest
 from .engine import MSTEP_ROUNDS, DeviceBatch
 from .fast_em.phylogeny import Phylogeny, build_phylogeny, tree_to_networkx
 
@@ -227,9 +231,6 @@ class fastEM_solver:
                  max_trials=100, random_seeds=None, ultra_constr=False):
         """EM_solver.optimize_one from ``initials`` starting points (the best
         nllh wins), seeds as ML_solver.optimize (ML_solver.py:263-282)."""
-        if ultra_constr and len(self.trees) > 1:
-            raise NotImplementedError("ultra_constr=True ties the roots of several trees "
-                                      "together (EM_solver.py:81-84); not implemented")
         if random_seeds is None:
             rseeds = [int(_random.random() * 10000) for _ in range(initials)]
         elif isinstance(random_seeds, int):
@@ -269,6 +270,8 @@ class fastEM_solver:
                 d[u] = max(2 * DMIN, self._d[i][u]) if has else x[k]
                 k += 1
             ds.append(d)
+        if len(self.trees) > 1:
+            return self._optimize_forest(ds, masks, nu, phi, fixed_phi, fixed_nu, ultra_constr)
         total, out_d, status = 0.0, [], "optimal"
         for i, t in enumerate(self.trees):
             b = DeviceBatch([self._dataset(i, False)], [t], [0], [ds[i]], [nu], [phi],
@@ -282,6 +285,29 @@ class fastEM_solver:
             out_d.append(r.branch_lengths)
             nu, phi = r.nu, r.phi
         return -total, nu, phi, out_d, status
+
+
+    def _optimize_forest(self, ds, masks, nu, phi, fixed_phi, fixed_nu, ultra_constr):
+        """EM_solver's EM over all of its trees at once (one nu, one phi, the
+        summed log-likelihood; with ultra_constr the trees' roots at one
+        height, EM_solver.py:81-84): the trees joined under zero-length
+        fixed branches (laml_gb300/forest.py), one device EM."""
+        joined, maps, joins = join_forest(self.trees)
+        rows = [self.charMtrx[c] for i in range(len(self.trees))
+                for c in self.ordered_leaf_labels[i]]
+        dset = encode_dataset(char_matrix(rows, exact=True), self.Q, compat=False,
+                              group_sites=self.G)
+        dj = np.zeros(joined.num_nodes)
+        mj = np.zeros(joined.num_nodes, bool)
+        for m, d, msk in zip(maps, ds, masks):
+            dj[m] = d
+            mj[m] = msk
+        b = DeviceBatch([dset], [joined], [0], [dj], [nu], [phi], compat=False, mask=[mj],
+                        fix_nu=fixed_nu is not None, fix_phi=fixed_phi is not None,
+                        device=self.device, ultrametric=ultra_constr)
+        r = b.run_em(max_iters=1000)[0]
+        status = "d_infeasible" if r.status == TREE_INFEASIBLE else "optimal"
+        return -r.llh, r.nu, r.phi, [r.branch_lengths[m].copy() for m in maps], status
 
 
 def _ts_postorder(t: EncodedTree):

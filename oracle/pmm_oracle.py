@@ -626,7 +626,8 @@ def mstep_compat(counts, leaf_resp_total, R, M, d, nu, phi, branch_mask, fix_nu,
 
 
 def mstep_exact(counts, post1_leaf_missing_sum, R, d, nu, phi, branch_mask, K, ncells,
-                opt_phi=True, opt_nu=True, ultra_tree: Optional[ParsedTree] = None):
+                opt_phi=True, opt_nu=True, ultra_tree: Optional[ParsedTree] = None,
+                ultra_constraints=None):
     """EM_solver.Mstep (EM_solver.py:307-459) without MOSEK: closed-form phi
     (318-326), per-branch S normalisation (339-348), d in [dmin, dmax] given
     the old nu (349-366) and nu in [0, 1] given the new d (392-407), each a
@@ -658,8 +659,9 @@ def mstep_exact(counts, post1_leaf_missing_sum, R, d, nu, phi, branch_mask, K, n
     def fp(x):
         return -a + S1 * _inv_expm1(x) + c * nu * _inv_expm1(nu * x)
 
-    if ultra_tree is not None:
-        d, ok = ultrametric_d(S, nu, d, mask, ultra_tree)
+    ultra = ultra_tree is not None or ultra_constraints is not None
+    if ultra:
+        d, ok = ultrametric_d(S, nu, d, mask, ultra_tree, ultra_constraints)
         if not ok:
             return d, nu, phi, False
     else:
@@ -681,7 +683,7 @@ def mstep_exact(counts, post1_leaf_missing_sum, R, d, nu, phi, branch_mask, K, n
         else:
             nu = float(_bisect_decreasing(np.vectorize(gp), np.array(1e-300), np.array(1.0),
                                           iters=300))
-    if ultra_tree is not None:
+    if ultra:
         return d, nu, phi_star, True
     return d, nu, phi_star
 
@@ -722,7 +724,54 @@ def ultrametric_constraints(tree: ParsedTree, mask, d):
     return M, b, np.array(free, dtype=np.int64)
 
 
-def ultrametric_d(S, nu, d, mask, tree: ParsedTree):
+def ultrametric_constraints_forest(trees: Sequence[ParsedTree], masks, ds):
+    """EM_solver.ultrametric_constr (EM_solver.py:53-89) for several trees:
+    each tree's rows, columns the optimised branches of all trees (tree by
+    tree, treeswift postorder), then one row per further tree equating its
+    root's path (its own branch included) with the first tree's
+    (EM_solver.py:81-84).  ``free`` indexes the trees' concatenated branch
+    vectors."""
+    vecs, consts, rows = [], [], {}
+    cols, off, ncol = [], 0, 0
+    per = []
+    for tr, mask, d in zip(trees, masks, ds):
+        post = treeswift_postorder_ids(tr)
+        mask = np.asarray(mask, bool)
+        free = [x for x in post if mask[x]]
+        per.append((tr, post, mask, d, free, ncol))
+        cols += [off + x for x in free]
+        ncol += len(free)
+        off += len(tr.parent)
+    roots = []
+    for tr, post, mask, d, free, c0 in per:
+        col = {x: c0 + i for i, x in enumerate(free)}
+        vec, const = {}, {}
+        for x in post:
+            ch = tr.children[x]
+            if not ch:
+                v = np.zeros(ncol)
+                c = 0.0 if mask[x] else float(d[x])
+            else:
+                a, b_ = ch[-1], ch[0]
+                m = vec[a] - vec[b_]
+                if np.any(m != 0):
+                    key, neg = tuple(m), tuple(-m)
+                    if key not in rows and neg not in rows:
+                        rows[key] = const[b_] - const[a]
+                v = vec[a].copy()
+                c = const[a] + (0.0 if mask[x] else float(d[x]))
+            if mask[x]:
+                v[col[x]] = 1.0
+            vec[x], const[x] = v, c
+        roots.append((vec[tr.root], const[tr.root]))
+    for v, c in roots[1:]:
+        rows[tuple(roots[0][0] - v)] = c - roots[0][1]
+    M = np.array([list(k) for k in rows], dtype=np.float64).reshape(len(rows), ncol)
+    b = np.array(list(rows.values()), dtype=np.float64)
+    return M, b, np.array(cols, dtype=np.int64)
+
+
+def ultrametric_d(S, nu, d, mask, tree: Optional[ParsedTree], constraints=None):
     """The branch-length part of EM_solver.Mstep with ultra_constr_cache
     (EM_solver.py:349-366): maximise over the optimised branches
     sum -a d + S1 log(1-e^{-d}) + c log(1-e^{-nu d}) with d in [dmin, dmax]
@@ -737,7 +786,8 @@ def ultrametric_d(S, nu, d, mask, tree: ParsedTree):
 
     S0, S1, S2, S3, S4 = (S[:, i] for i in range(5))
     use_s = nu > EPS_NU
-    M, rhs, free = ultrametric_constraints(tree, mask, d)
+    M, rhs, free = constraints if constraints is not None else \
+        ultrametric_constraints(tree, mask, d)
     n = len(free)
     out = np.asarray(d, np.float64).copy()
     if n == 0:
@@ -1140,6 +1190,58 @@ def em_exact(prob: Problem, d, nu, phi, branch_mask=None, fix_nu=False, fix_phi=
         pre = cur
         it += 1
     return EMResult(cur, d, nu, phi, it, trace)
+
+
+def em_exact_forest(probs: Sequence[Problem], ds, nu, phi, masks=None, fix_nu=False,
+                    fix_phi=False, max_iters=1000, stop=None, ultra=False,
+                    ncells=None) -> EMResult:
+    """EM_solver.EM_optimization with several trees (EM_solver.py:461-512):
+    every tree's E-step, one M-step over all of them (phi from all leaves,
+    every branch, one nu; EM_solver.py:307-459), the stopping rule on the
+    summed log-likelihood; with ``ultra`` the branch lengths under every
+    tree's equalities and the root rows that tie the trees together
+    (ultrametric_constraints_forest).  ``ncells``: the character matrix's
+    cells (the phi zero threshold, 1 / (sites x cells)); default the first
+    tree's leaves.  The result's ``d`` is the list of the trees' lengths."""
+    stop = CONV_EPS_EXACT if stop is None else stop
+    k = len(probs)
+    ds = [np.asarray(x, dtype=np.float64).copy() for x in ds]
+    masks = [np.ones(len(p.tree.parent), bool) if masks is None else np.asarray(masks[i], bool)
+             for i, p in enumerate(probs)]
+    K = probs[0].enc.chars.shape[1]
+    ncells = probs[0].tree.num_leaves if ncells is None else ncells
+    sizes = [len(p.tree.parent) for p in probs]
+    cuts = np.cumsum([0] + sizes)
+
+    def llh_all(ds_, nu_, phi_):
+        return sum(log_likelihood(p, d_, nu_, phi_)[0] for p, d_ in zip(probs, ds_))
+
+    pre = llh_all(ds, nu, phi)
+    trace = [pre]
+    it, cur = 1, pre
+    while it <= max_iters:
+        counts, ls, lc, R = [], 0.0, 0.0, 0.0
+        for p, d_ in zip(probs, ds):
+            es = e_step(p, d_, nu, phi)
+            (a, c), r = exact_leaf_stats(p, es)
+            counts.append(es.counts)
+            ls, lc, R = ls + a, lc + c, R + r
+        cons = (ultrametric_constraints_forest([p.tree for p in probs], masks, ds)
+                if ultra else None)
+        out = mstep_exact(np.concatenate(counts), (ls, lc), R, np.concatenate(ds), nu, phi,
+                          np.concatenate(masks), K, ncells, opt_phi=not fix_phi,
+                          opt_nu=not fix_nu, ultra_constraints=cons)
+        if ultra and not out[3]:
+            return EMResult(pre, ds, nu, phi, it, trace, "d_infeasible")
+        dcat, nu, phi = out[:3]
+        ds = [dcat[cuts[i]:cuts[i + 1]].copy() for i in range(k)]
+        cur = llh_all(ds, nu, phi)
+        trace.append(cur)
+        if abs((cur - pre) / pre) < stop:
+            break
+        pre = cur
+        it += 1
+    return EMResult(cur, ds, nu, phi, it, trace)
 
 
 def exact_initials(tree: ParsedTree, N_postorder_lengths, randseed, fixed_phi=None,
