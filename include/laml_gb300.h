@@ -307,6 +307,9 @@ typedef struct laml_batch {
      * Negative: give up at the first check that finds the wait unsatisfied
      * (to exercise that path). */
     int64_t wait_limit_ns;
+    /* LAML_MSTEP_LBFGS only, else NULL: [LAML_LBFGS_SLOTS * (n_nodes + 2 T)]
+     * FP32 vectors of the L-BFGS solve */
+    float* nd_lbfgs;
 } laml_batch;
 
 /* A tree's partials are FP32 values with power-of-two exponents (linear)
@@ -396,6 +399,16 @@ int laml_gradient(const laml_batch* b, double* grad_d, double* grad_nu_phi, void
  * fallback the solve takes when the primal-dual method has not converged in
  * 60 iterations), so that path stays checked. */
 #define LAML_MSTEP_ULTRA_PD_SHORT 8
+/* Compat model only: the M-step the reference itself runs -- 100 FP32
+ * L-BFGS steps (memory 10, zoom line search for the strong Wolfe conditions,
+ * a chained backtracking test) on the M_step_loss_fn objective over
+ * (log d, logit nu, logit phi) (fast_em/laml.py:49-110, optax.lbfgs) --
+ * instead of solving that objective to its stationary point.  Needs
+ * nd_lbfgs.  One team per tree, ~60 block synchronisations per step: meant
+ * for trees of a few thousand nodes. */
+#define LAML_MSTEP_LBFGS 16
+/* floats per node and per tree parameter of laml_batch.nd_lbfgs */
+#define LAML_LBFGS_SLOTS 25
 /* doubles per node of laml_batch.nd_uwork */
 #define LAML_UWORK_SLOTS 17
 

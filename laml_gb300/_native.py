@@ -21,6 +21,8 @@ TREE_ACTIVE, TREE_CONVERGED, TREE_NAN, TREE_MAXITER, TREE_INFEASIBLE = 0, 1, 2, 
 MODE_LINEAR, MODE_LOG = 0, 1
 MSTEP_FP64_POLISH, MSTEP_ULTRAMETRIC, MSTEP_ULTRA_BARRIER = 1, 2, 4
 MSTEP_ULTRA_PD_SHORT = 8
+MSTEP_LBFGS = 16
+LBFGS_SLOTS = 25   # LAML_LBFGS_SLOTS: floats per node and tree parameter of nd_lbfgs
 UWORK_SLOTS = 17   # LAML_UWORK_SLOTS: doubles per node of nd_uwork
 OUT_POSTERIORS, OUT_TRUE_ROOT = 1, 2
 
@@ -88,7 +90,7 @@ BATCH_FIELDS = [
     ("barrier", vp), ("error", vp), ("max_states", i32), ("max_tree_nodes", i32),
     ("tr_leaf", vp), ("nd_uorder", vp), ("nd_uwork", vp),
     ("plan_part_floats", i64), ("plan_scalar_len", i64), ("tr_mstats", vp),
-    ("wide_chunk", i32), ("wait_limit_ns", i64),
+    ("wide_chunk", i32), ("wait_limit_ns", i64), ("nd_lbfgs", vp),
 ]
 
 

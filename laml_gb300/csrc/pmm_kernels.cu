@@ -2229,6 +2229,248 @@ __device__ __noinline__ int ultra_dstep(const laml_batch& b, int p, Team& T, dou
     return kUltraOk;
 }
 
+// ---------------------------------------------------------------------------
+// fastEM's own M-step (LAML_MSTEP_LBFGS, compat model): 100 steps of
+// L-BFGS on M_step_loss_fn over x = (log d, logit nu, logit phi) in FP32, as
+// fast_em/laml.py:49-110 runs it with optax (optax.lbfgs with
+// scale_init_precond=True: the two-loop recursion over the last 10 pairs,
+// the initial inverse Hessian <s, y> / <y, y> of the newest pair; its zoom
+// line search for the strong Wolfe conditions, c1 = 1e-4, c2 = 0.9, first
+// trial 1, at most 20 evaluations; chained with a backtracking Armijo test,
+// factor 0.8, at most 15 times).  The published methods restated (Nocedal &
+// Wright, algorithms 3.5, 3.6 and 7.4), not optax's code: iterates agree
+// with the oracle's restatement to FP32 rounding, not bit for bit with optax.
+// One team per tree; the vectors live in nd_lbfgs (LAML_LBFGS_SLOTS floats
+// per node and per tree parameter), the scalars in every thread's registers.
+// ---------------------------------------------------------------------------
+namespace lbfgs {
+constexpr int kM = 10, kSteps = 100, kZoom = 20, kBack = 15;
+constexpr float kC1 = 1e-4f, kC2 = 0.9f, kBackFactor = 0.8f;
+constexpr int kX = 0, kG = 1, kP = 2, kXT = 3, kGT = 4, kS = 5, kY = 5 + kM;
+static_assert(kY + kM <= LAML_LBFGS_SLOTS, "nd_lbfgs slots");
+
+// log(1 - e^-z) for z > 0 as fast_em's log1mexp_pos
+__device__ __forceinline__ float l1m(float z) {
+    return z > 0.69314718f ? log1pf(-expf(-z)) : logf(-expm1f(-z));
+}
+}  // namespace lbfgs
+
+template <class Team>
+__device__ __noinline__ void lbfgs_mstep(const laml_batch& b, int p, Team& T, int N, int base, double Mm,
+                            double Rr, double LRd, uint8_t fix, double& nu, double& phi,
+                            float* Dd) {
+    using namespace lbfgs;
+    const int64_t stride = b.n_nodes + 2 * (int64_t)b.n_trees;
+    float* W = b.nd_lbfgs;
+    const int NP = N + 2;
+    auto at = [&](int slot, int i) -> float& {   // i < N: branch i; N: nu; N + 1: phi
+        const int64_t idx = i < N ? (int64_t)base + i : b.n_nodes + 2 * (int64_t)p + (i - N);
+        return W[(int64_t)slot * stride + idx];
+    };
+    const float lo = logf((float)kCalcEps), feps = (float)kCalcEps;
+    const float M = (float)Mm, R = (float)Rr, LR = (float)LRd;
+    const bool fnu = fix & 1, fphi = fix & 2;
+    // loss and gradient at slot Z into slot Gs; with dir >= 0 also the
+    // slope along slot dir
+    auto eval = [&](int Z, int Gs, int dir, float& f, float& slope) {
+        const float zn = at(Z, N), zp = at(Z, N + 1);
+        const float sn = 1.f / (1.f + expf(-zn)), sp = 1.f / (1.f + expf(-zp));
+        const float vn = fminf(fmaxf(sn, feps), 1.f - feps), vp = fminf(fmaxf(sp, feps), 1.f - feps);
+        const bool inn = sn > feps && sn < 1.f - feps, inp = sp > feps && sp < 1.f - feps;
+        float ls = 0.f, dfn = 0.f, dot = 0.f;
+        for (int v = T.tid(); v < N; v += T.size()) {
+            const double* c = b.nd_cnt + (int64_t)(base + v) * 6;
+            const float c0 = (float)__ldcg(c), c1 = (float)__ldcg(c + 1), c2 = (float)__ldcg(c + 2),
+                        c3 = (float)__ldcg(c + 3), c4 = (float)__ldcg(c + 4);
+            const float u = at(Z, v);
+            const float d = expf(fminf(fmaxf(u, lo), -lo));
+            const float dn = d * vn;
+            const float a1 = l1m(d), an = l1m(dn);
+            ls += -c0 * d * (1.f + vn) + c1 * (a1 - d * vn) + c2 * an - c3 * d * vn + c4 * an;
+            const float ie = 1.f / expm1f(d), ien = 1.f / expm1f(dn), cs = c2 + c4;
+            const float dfd = -c0 * (1.f + vn) + c1 * (ie - vn) + cs * vn * ien - c3 * vn;
+            dfn += -(c0 + c1 + c3) * d + cs * d * ien;
+            const bool free = u > lo && u < -lo && __ldg(b.nd_mask + base + v);
+            const float g = free ? -dfd * d : 0.f;
+            at(Gs, v) = g;
+            if (dir >= 0) dot += g * at(dir, v);
+        }
+        const float2 r = T.sum2f(ls, dfn);
+        const float dsum = dir >= 0 ? T.sum2f(dot, 0.f).x : 0.f;
+        const float c6 = R * logf(1.f - vp) + (M - LR) * logf(vp);
+        f = -(r.x + c6);
+        const float gn = (fnu || !inn) ? 0.f : -r.y * vn * (1.f - vn);
+        const float gp = (fphi || !inp) ? 0.f : -(-R / (1.f - vp) + (M - LR) / vp) * vp * (1.f - vp);
+        slope = dir >= 0 ? dsum + gn * at(dir, N) + gp * at(dir, N + 1) : 0.f;
+        T.sync();   // every thread has read the parameters' slots
+        if (T.leader()) {
+            at(Gs, N) = gn;
+            at(Gs, N + 1) = gp;
+        }
+        T.sync();
+    };
+    auto dotv = [&](int A, int B) {
+        float s = 0.f;
+        for (int i = T.tid(); i < NP; i += T.size()) s += at(A, i) * at(B, i);
+        return T.sum2f(s, 0.f).x;
+    };
+    auto axpy = [&](int Yv, float a, int Xv) {   // Y += a X
+        for (int i = T.tid(); i < NP; i += T.size()) at(Yv, i) += a * at(Xv, i);
+        T.sync();
+    };
+    auto set = [&](int Yv, float a, int Xv, float c, int Zv) {   // Y = a X + c Z
+        for (int i = T.tid(); i < NP; i += T.size())
+            at(Yv, i) = a * at(Xv, i) + (Zv >= 0 ? c * at(Zv, i) : 0.f);
+        T.sync();
+    };
+    // the EM loop's parameter vector (laml.py:126-139; kept across
+    // iterations there, recovered here from d, nu, phi in FP64)
+    for (int v = T.tid(); v < N; v += T.size()) at(kX, v) = (float)log(__ldcg(b.nd_d + base + v));
+    if (T.leader()) {
+        at(kX, N) = (float)log(nu / (1.0 - nu));
+        at(kX, N + 1) = (float)log(phi / (1.0 - phi));
+    }
+    T.sync();
+    float f, s0;
+    eval(kX, kG, -1, f, s0);
+    float rho[kM], alpha[kM];
+    int cnt = 0, head = 0;
+    float gamma = 1.f;
+    for (int step = 0; step < kSteps; ++step) {
+        // direction: two-loop recursion into kP
+        set(kP, 1.f, kG, 0.f, -1);
+        for (int h = cnt - 1; h >= 0; --h) {
+            const int q = (head + h) % kM;
+            alpha[q] = rho[q] * dotv(kS + q, kP);
+            axpy(kP, -alpha[q], kY + q);
+        }
+        if (cnt > 0) set(kP, gamma, kP, 0.f, -1);
+        for (int h = 0; h < cnt; ++h) {
+            const int q = (head + h) % kM;
+            const float beta = rho[q] * dotv(kY + q, kP);
+            axpy(kP, alpha[q] - beta, kS + q);
+        }
+        set(kP, -1.f, kP, 0.f, -1);
+        float d0 = dotv(kG, kP);
+        if (!(d0 < 0.f)) {   // not a descent direction: the gradient, memory cleared
+            set(kP, -1.f, kG, 0.f, -1);
+            cnt = 0;
+            head = 0;
+            d0 = dotv(kG, kP);
+            if (!(d0 < 0.f)) break;   // stationary under the masks
+        }
+        // zoom line search: trial a evaluated into kXT / kGT
+        int nev = 0;
+        float best_a = -1.f, best_f = 0.f;
+        auto trial = [&](float a, float& fa, float& da) {
+            set(kXT, 1.f, kX, a, kP);
+            eval(kXT, kGT, kP, fa, da);
+            ++nev;
+            if (isfinite(fa) && fa <= f + kC1 * a * d0 && (best_a < 0.f || fa < best_f)) {
+                best_a = a;
+                best_f = fa;
+            }
+        };
+        float acc_a = -1.f, acc_f = 0.f;   // accepted step; kXT / kGT hold it when set
+        bool have = false;
+        float ap = 0.f, fp = f, dp = d0, a = 1.f;
+        float lo_a = 0.f, lo_f = 0.f, lo_d = 0.f, hi_a = 0.f, hi_f = 0.f, hi_d = 0.f;
+        bool zoom = false;
+        while (nev < kZoom) {
+            float fa, da;
+            trial(a, fa, da);
+            if (!isfinite(fa) || fa > f + kC1 * a * d0 || (ap > 0.f && fa >= fp)) {
+                lo_a = ap; lo_f = fp; lo_d = dp; hi_a = a; hi_f = fa; hi_d = da;
+                zoom = true;
+                break;
+            }
+            if (fabsf(da) <= -kC2 * d0) { acc_a = a; acc_f = fa; have = true; break; }
+            if (da >= 0.f) {
+                lo_a = a; lo_f = fa; lo_d = da; hi_a = ap; hi_f = fp; hi_d = dp;
+                zoom = true;
+                break;
+            }
+            ap = a; fp = fa; dp = da;
+            a = 2.f * a;
+        }
+        while (zoom && !have && nev < kZoom) {
+            // cubic through the bracket's ends (Nocedal & Wright eq. 3.59),
+            // kept 10% inside it, else the midpoint
+            float at_ = 0.5f * (lo_a + hi_a);
+            const float w = fabsf(hi_a - lo_a);
+            if (isfinite(hi_f) && isfinite(hi_d) && w > 0.f) {
+                const float d1 = lo_d + hi_d - 3.f * (lo_f - hi_f) / (lo_a - hi_a);
+                const float rad = d1 * d1 - lo_d * hi_d;
+                if (rad >= 0.f) {
+                    const float d2 = copysignf(sqrtf(rad), hi_a - lo_a);
+                    const float den = hi_d - lo_d + 2.f * d2;
+                    if (den != 0.f) {
+                        const float c = hi_a - (hi_a - lo_a) * (hi_d + d2 - d1) / den;
+                        if (c >= fminf(lo_a, hi_a) + 0.1f * w && c <= fmaxf(lo_a, hi_a) - 0.1f * w)
+                            at_ = c;
+                    }
+                }
+            }
+            float fa, da;
+            trial(at_, fa, da);
+            if (!isfinite(fa) || fa > f + kC1 * at_ * d0 || fa >= lo_f) {
+                hi_a = at_; hi_f = fa; hi_d = da;
+            } else {
+                if (fabsf(da) <= -kC2 * d0) { acc_a = at_; acc_f = fa; have = true; break; }
+                if (da * (hi_a - lo_a) >= 0.f) { hi_a = lo_a; hi_f = lo_f; hi_d = lo_d; }
+                lo_a = at_; lo_f = fa; lo_d = da;
+            }
+        }
+        if (!have) {   // exhausted: the best sufficient-decrease point seen, else the last
+            if (best_a >= 0.f) {
+                acc_a = best_a;
+                float fa, da;
+                set(kXT, 1.f, kX, acc_a, kP);
+                eval(kXT, kGT, kP, fa, da);
+                acc_f = fa;
+            } else {
+                acc_a = a;
+                float fa, da;
+                set(kXT, 1.f, kX, acc_a, kP);
+                eval(kXT, kGT, kP, fa, da);
+                acc_f = fa;
+            }
+        }
+        // the chained backtracking test on the step found
+        const float slope = acc_a * d0;
+        float t = 1.f;
+        for (int k = 0; k < kBack; ++k) {
+            if (isfinite(acc_f) && acc_f <= f + kC1 * t * slope) break;
+            t *= kBackFactor;
+            float da;
+            set(kXT, 1.f, kX, t * acc_a, kP);
+            eval(kXT, kGT, kP, acc_f, da);
+        }
+        // memory: s = x_new - x, y = g_new - g
+        const int q = cnt < kM ? (head + cnt) % kM : head;
+        set(kS + q, 1.f, kXT, -1.f, kX);
+        set(kY + q, 1.f, kGT, -1.f, kG);
+        const float sy = dotv(kS + q, kY + q), yy = dotv(kY + q, kY + q);
+        rho[q] = sy == 0.f ? 0.f : 1.f / sy;
+        gamma = yy > 0.f ? sy / yy : 1.f;
+        if (cnt < kM) ++cnt;
+        else head = (head + 1) % kM;
+        set(kX, 1.f, kXT, 0.f, -1);
+        set(kG, 1.f, kGT, 0.f, -1);
+        f = acc_f;
+    }
+    // back to d, nu, phi as the EM loop reads them (exp, sigmoid; laml.py:151-156)
+    for (int v = T.tid(); v < N; v += T.size()) {
+        if (!__ldg(b.nd_mask + base + v)) continue;
+        const double d = exp((double)at(kX, v));
+        Dd[v] = (float)d;
+        __stcg(b.nd_d + base + v, d);
+    }
+    nu = 1.0 / (1.0 + exp(-(double)at(kX, N)));
+    phi = 1.0 / (1.0 + exp(-(double)at(kX, N + 1)));
+    T.sync();
+}
+
 template <class Team>
 __device__ void mstep_tree(const laml_batch& b, int p, int rounds, Team& T, float4* s_cnt,
                            float* s_d, int flags, double* usm = nullptr, int ucap = 0) {
@@ -2295,6 +2537,10 @@ __device__ void mstep_tree(const laml_batch& b, int p, int rounds, Team& T, floa
         b.tr_prev[2 * p] = nu;
         b.tr_prev[2 * p + 1] = phi;
     }
+    if (compat && (flags & LAML_MSTEP_LBFGS)) {   // fastEM's own M-step
+        const double Mm = b.tr_mstats ? __ldg(b.tr_mstats + 2 * p) : __ldg(b.ds_missing + ds);
+        lbfgs_mstep<Team>(b, p, T, N, base, Mm, (double)n * K - Mm, LR, fix, nu, phi, Dd);
+    } else {
     // 2. phi (fast_em/laml.py:77 stationary point; EM_solver.py:318-326)
     if (!(fix & 2)) {
         const double M = b.tr_mstats ? __ldg(b.tr_mstats + 2 * p) : __ldg(b.ds_missing + ds);
@@ -2436,6 +2682,7 @@ __device__ void mstep_tree(const laml_batch& b, int p, int rounds, Team& T, floa
         }
         T.sync();
     }
+    }   // the stationary-point M-step
     if (T.leader()) {
         b.tr_nu[p] = nu;
         b.tr_phi[p] = phi;
@@ -3773,6 +4020,10 @@ int validate(const laml_batch* b) {
 
 // an M-step flag set the batch cannot serve
 int validate_mstep_flags(const laml_batch* b, int32_t flags, const char* who) {
+    if ((flags & LAML_MSTEP_LBFGS) && b->compat && !b->nd_lbfgs) {
+        laml::set_error(std::string(who) + ": LAML_MSTEP_LBFGS needs nd_lbfgs");
+        return LAML_ERR_ARG;
+    }
     if ((flags & LAML_MSTEP_ULTRAMETRIC) && !b->compat && (!b->nd_uorder || !b->nd_uwork)) {
         laml::set_error(std::string(who) + ": LAML_MSTEP_ULTRAMETRIC needs nd_uorder and nd_uwork");
         return LAML_ERR_ARG;

@@ -109,6 +109,7 @@ class DeviceBatch:
         self.ultra_barrier = False
         # cap its primal-dual phase at 3 iterations (the barrier phase continues)
         self.ultra_pd_short = False
+        self._lbfgs = False
         self.device = torch.device(device)
         self.stream = stream
         self.trees = list(trees)
@@ -236,6 +237,24 @@ class DeviceBatch:
             C.byref(b), b.in_desc, b.out_desc, b.grp_desc, self._s()))
 
     @property
+    def lbfgs(self) -> bool:
+        """fastEM model: run the M-step the reference itself runs (100 FP32
+        L-BFGS steps, fast_em/laml.py:49-110) instead of solving its
+        objective to the stationary point; allocates its vectors on first
+        use."""
+        return self._lbfgs
+
+    @lbfgs.setter
+    def lbfgs(self, on: bool):
+        if on and not self.compat:
+            raise ValueError("the L-BFGS M-step is the fastEM (compat) model's")
+        if on and "nd_lbfgs" not in self.work:
+            n = N.LBFGS_SLOTS * (self.sizes["n_nodes"] + 2 * self.T)
+            self.work["nd_lbfgs"] = torch.zeros(n, dtype=torch.float32, device=self.device)
+            self.b.nd_lbfgs = self.work["nd_lbfgs"].data_ptr()
+        self._lbfgs = bool(on)
+
+    @property
     def wide_chunk(self) -> int:
         """The wide levels' kernel: 0 per-thread row loads (default), 8 or 16
         bulk-staged rows with that many state slots per stage.  A tiling
@@ -288,7 +307,8 @@ class DeviceBatch:
         return ((N.MSTEP_FP64_POLISH if self._polish(polish) else 0) |
                 (N.MSTEP_ULTRAMETRIC if self.ultrametric else 0) |
                 (N.MSTEP_ULTRA_BARRIER if self.ultra_barrier else 0) |
-                (N.MSTEP_ULTRA_PD_SHORT if self.ultra_pd_short else 0))
+                (N.MSTEP_ULTRA_PD_SHORT if self.ultra_pd_short else 0) |
+                (N.MSTEP_LBFGS if self._lbfgs else 0))
 
     def mstep(self, rounds=MSTEP_ROUNDS, polish=None):
         N.check(N.lib().laml_mstep(C.byref(self.b), rounds, self._mflags(polish), self._s()))

@@ -124,7 +124,14 @@ def _lca(et: EncodedTree, a: int, b: int) -> int:
 
 
 class fastEM_solver:
-    """The reference solver's interface, every computation on the GPU."""
+    """The reference solver's interface, every computation on the GPU.
+
+    ``mstep`` (class attribute) picks the fastEM M-step: "stationary" solves
+    the M_step_loss_fn objective to its stationary point; "lbfgs" runs the
+    reference's own 100 FP32 L-BFGS steps (fast_em/laml.py:84-110,
+    LAML_MSTEP_LBFGS), which may stop short of that point."""
+
+    mstep = "stationary"
 
     def __init__(self, treeList, data, prior, params={'nu': 0, 'phi': 0, 'sigma': 0},
                  group_sites: int = 8, device="cuda"):
@@ -212,6 +219,7 @@ class fastEM_solver:
                             [np.maximum(self._d[i], 1e-6)],
                             [min(max(nu, 1e-6), 1 - 1e-6)], [min(max(phi, 1e-6), 1 - 1e-6)],
                             compat=True, mask=[mask], device=self.device)
+            b.lbfgs = self.mstep == "lbfgs"
             r = b.run_em(rounds=MSTEP_ROUNDS)[0]
             self.params.nu, self.params.phi = r.nu, r.phi
             self._d[i] = r.branch_lengths
@@ -409,6 +417,7 @@ def score_candidate_batch(candidates, strategies, data, prior, params, group_sit
         phis.append(min(max(phi, 1e-6), 1 - 1e-6))
     b = DeviceBatch([ds], trees, [0] * len(trees), d, nus, phis, compat=True, mask=masks,
                     device=device)
+    b.lbfgs = fastEM_solver.mstep == "lbfgs"
     res = b.run_em(rounds=MSTEP_ROUNDS)
     out = []
     k = 0

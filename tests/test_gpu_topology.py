@@ -83,6 +83,25 @@ def test_nni_search_reaches_brute_force_optimum(start, batched):
     assert -score == pytest.approx(nllh_bf, abs=5e-5)
 
 
+@pytest.mark.parametrize("start", ["((a,c),(b,d));", "(a,b,c,d);"])
+@pytest.mark.parametrize("batched", [False, True])
+def test_nni_search_with_the_lbfgs_mstep(start, batched):
+    """The same searches with fastEM's own M-step (100 L-BFGS steps,
+    LAML_MSTEP_LBFGS) in every candidate's EM."""
+    random.seed(11)
+    nllh_bf = _brute_force()
+    fastEM_solver.mstep = "lbfgs"
+    try:
+        cls = TS.Topology_search_batched if batched else TS.Topology_search
+        s = cls([start], fastEM_solver, data={'charMtrx': MSA}, prior={'Q': Q},
+                params={'phi': 0, 'nu': 0})
+        trees, score, best_params = s.search(maxiter=200, nreps=10, verbose=False)
+    finally:
+        fastEM_solver.mstep = "stationary"
+    print("lbfgs search", start, batched, -score, nllh_bf)
+    assert -score == pytest.approx(nllh_bf, abs=5e-5)
+
+
 def test_batched_search_native_listing_equals_newick_listing():
     """The batched NNI search on a 60-leaf tree, candidates built by
     laml_nni_candidates against one newick per candidate: the same random
