@@ -660,18 +660,27 @@ __device__ __noinline__ void outside_log_lane(const laml_batch& b, const ItemDes
     int XoA, XoB;
     if (at_root) {
         const RootEdge re = root_edge_logs(b, s.tree);
-        float ta = -INFINITY, tb = -INFINITY;   // max_j log q_j + E[.]_j
+        // each child's offset: the largest class of x + the child's own
+        // inside vector -- the class that carries the site's likelihood --
+        // so every posterior below is formed from values near 0.  (The
+        // largest class of x alone can be one the child's data rule out,
+        // e.g. silenced above an observed state in the exact model, and
+        // lie a thousand nats above the likelihood after a blow-up.)
+        float ta = -INFINITY, tb = -INFINITY;   // max_j log q_j + E[sibling]_j + in_j
         for (int j = 2; j < s.C; ++j) {
             const float lq = lgz(__ldg(s.qrow + j * G));
-            ta = fmaxf(ta, lq + laddexp(ew.lst + child_val_log<G>(cw, j), kw));
-            tb = fmaxf(tb, lq + laddexp(ev.lst + child_val_log<G>(cv, j), kv));
+            const float av = child_val_log<G>(cv, j), aw = child_val_log<G>(cw, j);
+            ta = fmaxf(ta, lq + laddexp(ew.lst + aw, kw) + av);
+            tb = fmaxf(tb, lq + laddexp(ev.lst + av, kv) + aw);
         }
         auto offset = [](double a, double c, double e) {
             const double m = fmax(a, fmax(c, e));
             return m > -(double)INFINITY ? (int)floor(m / kLn2) + 1 : 0;
         };
-        XoA = offset(re.l00 + (double)E0w, re.ls + (double)cw.ss, re.lm + (double)ta);
-        XoB = offset(re.l00 + (double)E0v, re.ls + (double)cv.ss, re.lm + (double)tb);
+        XoA = offset(re.l00 + (double)E0w + (double)cv.s0, re.ls + (double)cw.ss + (double)cv.ss,
+                     re.lm + (double)ta);
+        XoB = offset(re.l00 + (double)E0v + (double)cw.s0, re.ls + (double)cv.ss + (double)cw.ss,
+                     re.lm + (double)tb);
         // x is summed in FP64: a root-edge term and its offset can each be
         // thousands while their sum is what carries the likelihood
         const double offA = XoA * kLn2, offB = XoB * kLn2;

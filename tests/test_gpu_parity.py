@@ -304,16 +304,7 @@ def _log_mode_cases():
     for compat in (True, False):
         for where, d_big in (("root", 45.0), ("root", 600.0), ("root", 5000.0),
                              ("internal", 40.0)):
-            marks = ()
-            if not compat and d_big == 5000.0:
-                # The exact model bounds d by dmax = 10 (EM_solver); an E-step
-                # at a root branch of 5000 is outside it.  Posteriors of some
-                # leaves there are off by up to 1e-3 and the source of that
-                # error is not yet found.
-                marks = pytest.mark.xfail(reason="exact model, root branch 5000 (beyond dmax "
-                                                 "= 10): leaf posteriors off by up to 1e-3, "
-                                                 "cause not yet found", strict=False)
-            out.append(pytest.param(compat, where, d_big, marks=marks))
+            out.append(pytest.param(compat, where, d_big))
     return out
 
 
