@@ -8,13 +8,22 @@ budget are free: a cohort is one DeviceBatch (any mix of tree sizes and
 site counts) on its own CUDA stream, driven in chunks of fused EM iterations
 with per-level launches, so cohorts admitted at different times run
 concurrently on the device.  Encoded inputs, partials and EM state stay on
-the GPU for the life of the cohort; a request's future resolves as soon as
-its own tree leaves the ACTIVE state (other trees of its cohort keep
-iterating), and a cohort's memory returns to the budget when all its trees
-are done.
+the GPU; a request's future resolves as soon as its own tree leaves the
+ACTIVE state.
+
+Continuous batching at iteration boundaries: when a chunk of an EM cohort
+ends with some of its trees finished, the cohort is rebuilt from its
+unfinished trees -- each carrying its EM state (branch lengths, nu, phi, the
+log-likelihood the stopping rule compares against, its iteration count) --
+joined by queued EM requests that fit the memory the finished trees leave.
+The finished trees' memory returns to the budget then, and new arrivals
+start at the next iteration boundary instead of waiting for a whole cohort.
 
 Each tree's arithmetic does not depend on what else is in its batch, so a
-request's result is bitwise the same alone or in any mix.
+request's result is the same alone or in any mix: bitwise while its levels
+fall on the same side of the narrow / wide rule (a level with more than 8192
+items of the batch runs the per-thread kernels), else to FP32 summation
+order.
 """
 from __future__ import annotations
 
@@ -104,8 +113,11 @@ class PMMServer:
         self.max_cohort = max_cohort
         self.max_em_cohort = max_em_cohort   # EM cohorts smaller: a slow tree holds its cohort
         self.max_cohorts = max_cohorts
-        # tree-EM-iterations launched (counted when each chunk is queued)
+        # tree-EM-iterations launched (counted when each chunk is queued) and
+        # those of the requests answered (counted from their results)
         self.em_tree_iterations = 0
+        self.em_tree_iterations_completed = 0
+        self.recohorts = 0
         self.G = group_sites
         self.rounds = rounds
         self.chunk = chunk
@@ -255,10 +267,13 @@ class PMMServer:
                 res = b.results()
             for i in np.flatnonzero(newly):
                 j = c.jobs[i]
+                self.em_tree_iterations_completed += int(res[i].iterations)
                 j.future.set_result(Reply(res[i], j.t_submit, j.t_admit, now))
             c.done |= newly
         if c.done.all():
             return True
+        if c.done.any():
+            c = self._recohort(c)
         with torch.cuda.stream(c.stream):
             b.em_iterations(self.chunk, rounds=self.rounds, max_iters=self.max_iters,
                             persistent=False)
@@ -266,6 +281,60 @@ class PMMServer:
             c.host_status.copy_(b.work["tr_status"], non_blocking=True)
             c.event.record(c.stream)
         return False
+
+    def _recohort(self, c: _Cohort) -> _Cohort:
+        """Rebuild an EM cohort at an iteration boundary from its unfinished
+        trees (EM state carried over) and the queued EM requests that fit the
+        memory its finished trees free; the old batch is released."""
+        b = c.batch
+        keep = [i for i in range(len(c.jobs)) if not c.done[i]]
+        with torch.cuda.stream(c.stream):
+            res = b.results()
+            prev = b.work["tr_llh_prev"].cpu().numpy()
+            iters = b.work["tr_iter"].cpu().numpy()
+        kept = [c.jobs[i] for i in keep]
+        used = sum(j.footprint for j in kept)
+        add = []
+        with self._lock:
+            rest = collections.deque()
+            while self._pending and len(kept) + len(add) < self.max_em_cohort:
+                j = self._pending.popleft()
+                if j.req.kind == "em" and self._used - c.footprint + used + j.footprint <= self.budget:
+                    add.append(j)
+                    used += j.footprint
+                else:
+                    rest.append(j)
+                    if j.req.kind == "em":
+                        break
+            rest.extend(self._pending)
+            self._pending = rest
+        now = time.perf_counter()
+        for j in add:
+            j.t_admit = now
+        jobs = kept + add
+        d = [res[i].branch_lengths for i in keep] + \
+            [np.maximum(j.tree.branch_length, EPS) for j in add]
+        nu = [res[i].nu for i in keep] + [min(max(j.req.nu, EPS), 1 - EPS) for j in add]
+        phi = [res[i].phi for i in keep] + [min(max(j.req.phi, EPS), 1 - EPS) for j in add]
+        with torch.cuda.stream(c.stream):
+            uniq, tree_ds = {}, []
+            for j in jobs:
+                tree_ds.append(uniq.setdefault(id(j.ds), (len(uniq), j.ds))[0])
+            dsets = [x for _, x in sorted(uniq.values(), key=lambda t: t[0])]
+            nb = DeviceBatch(dsets, [j.tree for j in jobs], tree_ds, d, nu, phi, compat=True,
+                             device=self.device, stream=c.stream)
+            nb.branch_terms()
+            nb.inside(update_em=True)
+            k = len(keep)
+            if k:   # the kept trees' stopping-rule state
+                nb.work["tr_llh_prev"][:k].copy_(torch.from_numpy(prev[keep]))
+                nb.work["tr_llh"][:k].copy_(torch.from_numpy(prev[keep]))
+                nb.work["tr_iter"][:k].copy_(torch.from_numpy(iters[keep]))
+        self._used += used - c.footprint
+        self.recohorts += 1
+        return _replace_cohort(self._active, c, _Cohort(
+            jobs, nb, c.stream, "em", used, c.event, np.zeros(len(jobs), bool),
+            torch.empty(len(jobs), dtype=torch.int32, pin_memory=True)))
 
     def _run(self):
         try:
@@ -304,6 +373,11 @@ class PMMServer:
                 for j in c.jobs:
                     if not j.future.done():
                         j.future.set_exception(ex)
+
+
+def _replace_cohort(active: List[_Cohort], old: _Cohort, new: _Cohort) -> _Cohort:
+    active[active.index(old)] = new
+    return new
 
 
 def run_alone(req: Request, group_sites: int = 8, rounds: int = MSTEP_ROUNDS,
