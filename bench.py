@@ -747,7 +747,8 @@ def main():
             serving["stream_seconds"] = sa.serve_seconds
             serving["value_means"] = "tree-EM-iterations of the answered requests per second"
         except Exception as ex:   # reported, never required
-            serving = {"error": str(ex)}
+            import traceback
+            serving = {"error": str(ex), "where": traceback.format_exc()[-1500:]}
 
     if rank == 0:
         line = {

@@ -274,6 +274,7 @@ class PMMServer:
             return True
         if c.done.any():
             c = self._recohort(c)
+            b = c.batch
         with torch.cuda.stream(c.stream):
             b.em_iterations(self.chunk, rounds=self.rounds, max_iters=self.max_iters,
                             persistent=False)
