@@ -262,6 +262,7 @@ def run_serving(args, emit=True):
             except cf.TimeoutError:
                 unfinished[kind] += 1
         t_end = time.perf_counter()
+        stuck = srv.snapshot() if any(unfinished.values()) else []
         launched = srv.em_tree_iterations
         completed_iters = srv.em_tree_iterations_completed
         recohorts = srv.recohorts
@@ -281,6 +282,7 @@ def run_serving(args, emit=True):
             "em_requests": n_em, "em_completed_fraction":
                 (n_em - unfinished["em"]) / n_em if n_em else None,
             "recohorts": recohorts,
+            "unfinished_em_on_device": stuck[:12],
             "n_gpus": 1, "requests": len(futs), "completed": len(replies),
             "unfinished_at_deadline": unfinished, "drain_deadline_s": args.serve_drain,
             "offered_rate_per_s": rate, "completed_per_s": len(replies) / span,

@@ -163,6 +163,25 @@ class PMMServer:
         self._wake.set()
         return fut
 
+    def snapshot(self):
+        """The EM requests on the device now: leaves, sites, EM iterations
+        done and seconds since submission (reads the iteration counters:
+        a synchronising copy per cohort)."""
+        out = []
+        now = time.perf_counter()
+        for c in list(self._active):
+            if c.kind != "em" or c.batch is None:
+                continue
+            with torch.cuda.stream(c.stream):
+                it = c.batch.work["tr_iter"].cpu().numpy()
+                llh = c.batch.work["tr_llh"].cpu().numpy()
+            for i, j in enumerate(c.jobs):
+                if not c.done[i]:
+                    out.append({"leaves": int(j.tree.num_leaves), "sites": int(j.ds.n_sites),
+                                "iterations": int(it[i]), "llh": float(llh[i]),
+                                "seconds": now - j.t_submit})
+        return out
+
     def close(self, wait: bool = True):
         """Stop the server.  wait=True: finish every submitted request first;
         wait=False: launch no further work and fail the requests not yet
@@ -377,7 +396,7 @@ class PMMServer:
 
 
 def _replace_cohort(active: List[_Cohort], old: _Cohort, new: _Cohort) -> _Cohort:
-    active[active.index(old)] = new
+    active[next(i for i, x in enumerate(active) if x is old)] = new
     return new
 
 
