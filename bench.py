@@ -313,6 +313,7 @@ def run_passes_only(args):
     w.newicks = w.newicks[:args.trees]
     b = PB.make_batch(w.newicks, w.rows, w.Q, w.leaf_order, compat=True,
                       group_sites=args.group_sites or 8, nu=0.5, phi=0.5)
+    b.wide_chunk = max(args.wide_chunk, 0)
     b.branch_terms()
     b.inside(update_em=True)
     b.outside()

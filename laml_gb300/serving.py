@@ -107,7 +107,7 @@ def footprint_bytes(tree: EncodedTree, ds: EncodedDataset) -> int:
 class PMMServer:
     def __init__(self, device="cuda", hbm_budget: int = 64 << 30, max_cohort: int = 256,
                  max_cohorts: int = 6, group_sites: int = 8, rounds: int = MSTEP_ROUNDS,
-                 chunk: int = 2, max_iters: int = 100000, max_em_cohort: int = 64):
+                 chunk: int = 2, max_iters: int = 1000, max_em_cohort: int = 64):
         self.device = torch.device(device)
         self.budget = hbm_budget
         self.max_cohort = max_cohort
@@ -121,6 +121,10 @@ class PMMServer:
         self.G = group_sites
         self.rounds = rounds
         self.chunk = chunk
+        # fastEM's loop has no cap (fast_em/laml.py:153: while True) and some
+        # problems alternate between two log-likelihoods further apart than
+        # its 1e-5 rule forever; a request stops after max_iters iterations
+        # (EM_solver's own cap, 1000) with status LAML_TREE_MAXITER
         self.max_iters = max_iters
         self._pending: collections.deque = collections.deque()
         self._lock = threading.Lock()
@@ -401,7 +405,7 @@ def _replace_cohort(active: List[_Cohort], old: _Cohort, new: _Cohort) -> _Cohor
 
 
 def run_alone(req: Request, group_sites: int = 8, rounds: int = MSTEP_ROUNDS,
-              device="cuda") -> TreeResult:
+              device="cuda", max_iters: int = 1000) -> TreeResult:
     """The same request outside the server (for mix-vs-alone checks)."""
     lo = req.leaf_order
     tree = encode_newick(req.newick, lo)
@@ -414,4 +418,4 @@ def run_alone(req: Request, group_sites: int = 8, rounds: int = MSTEP_ROUNDS,
     if req.kind == "llh":
         llh = float(b.log_likelihood()[0])
         return TreeResult(llh, req.nu, req.phi, 0, N.TREE_CONVERGED, tree.branch_length.copy())
-    return b.run_em(rounds=rounds, persistent=False)[0]
+    return b.run_em(rounds=rounds, persistent=False, max_iters=max_iters)[0]
