@@ -39,10 +39,11 @@ sys.path.insert(0, ROOT)
 
 METRIC = "EM iters/s & node-site updates/s, batched+served vs plain GPU; p50/p99 latency"
 # DRAM bytes per launch of the outside and inside passes of the 512-candidate
-# batch (G = 8): ncu dram__bytes_read.sum + dram__bytes_write.sum summed over
-# one pass of the first 128 candidates (`--passes-only --trees 128`), times 4
-# -- the full batch holds 4x the same-shaped rows -- over the pass's launches
-TRAFFIC_PER_LAUNCH = {"outside": 168.0e6, "inside": 119.6e6}
+# batch (G = 8, per-thread wide kernels): ncu dram__bytes_read.sum +
+# dram__bytes_write.sum summed over one pass of the first 128 candidates
+# (`--passes-only --trees 128 --wide-chunk 0`), times 4 -- the full batch holds
+# 4x the same-shaped rows -- over the pass's launches (outside 25, inside 24)
+TRAFFIC_PER_LAUNCH = {"outside": 170.3e6, "inside": 119.6e6}
 UNIT = "tree-EM-iters/s"
 WORKLOAD = "nni512"
 
