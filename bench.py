@@ -467,6 +467,16 @@ def run_ultra(args):
     N_ = trees[0].num_nodes
     d0 = rng.uniform(2 * 0.005, 10.0 / 2, N_)        # ML_solver.ini_all's range
     nu0, phi0 = float(rng.random() * 0.99), float(rng.random() * 0.99)
+    if args.mstep_only:   # one E-step and one ultrametric M-step: the profiled command
+        b = PB.make_batch(w.newicks, w.rows, w.Q, w.leaf_order, compat=False, nu=nu0,
+                          phi=phi0, d=[d0], clamp=False, ultrametric=True, device=dev,
+                          trees=trees)
+        b.e_step()
+        b.mstep()
+        torch.cuda.synchronize()
+        b.check_device_error()
+        print(json.dumps({"mstep_only": True, "nodes": N_}), flush=True)
+        return
     with torch.cuda.stream(stream):
         b = PB.make_batch(w.newicks, w.rows, w.Q, w.leaf_order, compat=False, nu=nu0, phi=phi0,
                           d=[d0], clamp=False, ultrametric=True, device=dev, stream=stream,
@@ -540,6 +550,9 @@ def main():
     ap.add_argument("--workload", default="nni512",
                     choices=["nni512", "fixed250", "grad4096", "large50k", "ultra250"],
                     help="nni512 (the default bench line) or one of the other configurations")
+    ap.add_argument("--mstep-only", action="store_true",
+                    help="with --workload ultra250: one E-step and one ultrametric M-step "
+                         "(profiling)")
     ap.add_argument("--passes-only", action="store_true",
                     help="one inside and one outside pass of --trees candidates (profiling)")
     ap.add_argument("--serving", action="store_true",
