@@ -127,10 +127,20 @@ def pass_bytes(b):
       per (node, group)).
     * M-step: count partials read, branch lengths read and written, branch
       terms written (16 + 16 B per node)."""
-    s = b.sizes
-    A = 4 * s["part_floats"]
     leaf_sites = sum(t.num_leaves * b.datasets[b.tree_ds[p]].n_sites_pad
                      for p, t in enumerate(b.trees))
+    return _pass_bytes(b.sizes, leaf_sites)
+
+
+def request_bytes(tree, ds):
+    """pass_bytes of a one-tree batch of a request, from the host plan."""
+    from laml_gb300.encoding import plan_batch
+    sizes, _ = plan_batch([tree], [0], [ds], host_desc=False)
+    return _pass_bytes(sizes, tree.num_leaves * ds.n_sites_pad)
+
+
+def _pass_bytes(s, leaf_sites):
+    A = 4 * s["part_floats"]
     nn = s["n_nodes"]
     inside = 2 * A + 24 * s["scalar_len"] + 2 * leaf_sites + 16 * nn
     outside = 3 * A + 28 * s["scalar_len"] + 2 * leaf_sites + 16 * nn + 4 * s["count_floats"]
@@ -236,6 +246,11 @@ def run_serving(args, emit=True):
     # each client's matrix is encoded once (as a search client scoring many
     # trees against it would), outside the timed replay
     dsets = [srv.encode_dataset(w.rows, w.Q, w.leaf_order) for w in pool]
+    # algorithmic bytes of one inside pass and one EM iteration per problem,
+    # for the capacity arithmetic of the line
+    from laml_gb300.encoding import encode_newick
+    pbytes = [request_bytes(encode_newick(w.newicks[0], w.leaf_order), ds)
+              for w, ds in zip(pool, dsets)]
     # warm the kernels and the allocator with one small request of each kind
     for kind in ("llh", "em"):
         w = pool[0]
@@ -249,17 +264,17 @@ def run_serving(args, emit=True):
             if ta > now:
                 time.sleep(ta - now)
             w = pool[k]
-            futs.append((kind, srv.submit(S.Request(w.newicks[0], w.rows, w.Q, w.leaf_order,
-                                                    kind=kind, dataset=dsets[k]))))
+            futs.append((kind, k, srv.submit(S.Request(w.newicks[0], w.rows, w.Q, w.leaf_order,
+                                                       kind=kind, dataset=dsets[k]))))
         # wait for the replies up to a drain deadline after the last arrival;
         # the offered EM load can exceed what one GPU completes (each EM
         # request is tens of iterations over up to 10,000 leaves x 300
         # sites), so requests still running then are reported, not awaited
         deadline = time.perf_counter() + args.serve_drain
         replies, unfinished = [], {"llh": 0, "em": 0}
-        for kind, f in futs:
+        for kind, k, f in futs:
             try:
-                replies.append((kind, f.result(timeout=max(0.0, deadline - time.perf_counter()))))
+                replies.append((kind, f.result(timeout=max(0.0, deadline - time.perf_counter())), k))
             except cf.TimeoutError:
                 unfinished[kind] += 1
         t_end = time.perf_counter()
@@ -268,11 +283,19 @@ def run_serving(args, emit=True):
         completed_iters = srv.em_tree_iterations_completed
         recohorts = srv.recohorts
     srv.close(wait=not any(unfinished.values()))
-    lat = np.array([r.latency for _, r in replies]) if replies else np.zeros(1)
-    lat_em = np.array([r.latency for k, r in replies if k == "em"])
-    lat_llh = np.array([r.latency for k, r in replies if k == "llh"])
-    iters = sum(r.result.iterations for _, r in replies)
+    lat = np.array([r.latency for _, r, _ in replies]) if replies else np.zeros(1)
+    lat_em = np.array([r.latency for k, r, _ in replies if k == "em"])
+    lat_llh = np.array([r.latency for k, r, _ in replies if k == "llh"])
+    iters = sum(r.result.iterations for _, r, _ in replies)
     span = t_end - t0
+    # capacity: algorithmic bytes of the answered requests (an EM request:
+    # its iterations x one EM iteration; a likelihood request: one inside
+    # pass), over the stream's length (offered) and over the time to the
+    # last answer (sustained)
+    em_req_b = [r.result.iterations * pbytes[k]["em_iteration"]
+                for kind, r, k in replies if kind == "em"]
+    llh_b = sum(pbytes[k]["inside"] for kind, _, k in replies if kind == "llh")
+    work_b = float(sum(em_req_b) + llh_b)
     # value: tree-EM-iterations of the requests answered by the end of the
     # window, per second of the window (useful work; launched iterations of
     # requests still running are reported apart)
@@ -287,6 +310,13 @@ def run_serving(args, emit=True):
             "n_gpus": 1, "requests": len(futs), "completed": len(replies),
             "unfinished_at_deadline": unfinished, "drain_deadline_s": args.serve_drain,
             "offered_rate_per_s": rate, "completed_per_s": len(replies) / span,
+            "capacity": {
+                "algorithmic_gb": work_b / 1e9,
+                "offered_gb_per_s": work_b / dur / 1e9,
+                "sustained_gb_per_s": work_b / span / 1e9,
+                "em_request_gb_median": float(np.median(em_req_b)) / 1e9 if em_req_b else None,
+                "em_request_gb_max": float(max(em_req_b)) / 1e9 if em_req_b else None,
+                "basis": "answered requests only; bench.pass_bytes per request plan"},
             "p50_latency_s": float(np.percentile(lat, 50)),
             "p99_latency_s": float(np.percentile(lat, 99)),
             "p50_latency_em_s": float(np.percentile(lat_em, 50)) if len(lat_em) else None,
@@ -760,7 +790,7 @@ def main():
                 "em_completed_fraction", "unfinished_at_deadline", "offered_rate_per_s",
                 "p50_latency_s", "p99_latency_s", "p50_latency_em_s", "p99_latency_em_s",
                 "p50_latency_llh_s", "p99_latency_llh_s", "recohorts",
-                "em_tree_iterations_launched_per_s", "drain_deadline_s")}
+                "em_tree_iterations_launched_per_s", "drain_deadline_s", "capacity")}
             serving["stream_seconds"] = sa.serve_seconds
             serving["value_means"] = "tree-EM-iterations of the answered requests per second"
         except Exception as ex:   # reported, never required
