@@ -345,6 +345,7 @@ def run_passes_only(args):
     b = PB.make_batch(w.newicks, w.rows, w.Q, w.leaf_order, compat=True,
                       group_sites=args.group_sites or 8, nu=0.5, phi=0.5)
     b.wide_chunk = max(args.wide_chunk, 0)
+    b.wide_pc = args.wide_pc > 0
     b.branch_terms()
     b.inside(update_em=True)
     b.outside()
@@ -565,6 +566,9 @@ def main():
     ap.add_argument("--wide-chunk", type=int, default=-1,
                     help="wide levels: 0 per-thread loads, 8/16 bulk-staged rows with that many "
                          "slots per stage (-1: the autotuner's choice)")
+    ap.add_argument("--wide-pc", type=int, default=-1,
+                    help="wide levels on producer/consumer warp pairs: 1 on, 0 off "
+                         "(-1: the autotuner's choice)")
     ap.add_argument("--e2e-steps", type=int, default=2)
     ap.add_argument("--ref-trees", type=int, default=16)
     ap.add_argument("--no-cpu", action="store_true")
@@ -628,17 +632,19 @@ def main():
     # the tile shape: sites per group x state slots per stage, timed on a
     # sample of the batch by the autotuner (not part of the timed region)
     tuned = None
-    if args.group_sites and args.wide_chunk >= 0:
-        G, CH = args.group_sites, args.wide_chunk
+    if args.group_sites and args.wide_chunk >= 0 and args.wide_pc >= 0:
+        G, CH, PC = args.group_sites, args.wide_chunk, args.wide_pc > 0
     else:
         tuned = tune.autotune(w.newicks, w.rows, w.Q, w.leaf_order, compat=True, device=dev)
         G = args.group_sites or tuned["group_sites"]
         CH = args.wide_chunk if args.wide_chunk >= 0 else tuned["wide_chunk"]
+        PC = args.wide_pc > 0 if args.wide_pc >= 0 else bool(tuned.get("wide_pc", False))
     stream = torch.cuda.Stream(dev)
     with torch.cuda.stream(stream):
         b = PB.make_batch(w.newicks, w.rows, w.Q, w.leaf_order, compat=True, group_sites=G,
                           nu=0.5, phi=0.5, device=dev, stream=stream)
         b.wide_chunk = CH
+        b.wide_pc = PC
         b.branch_terms()
         b.inside(update_em=True)
     stream.synchronize()   # the read below runs on the default stream
@@ -714,7 +720,7 @@ def main():
                     "of internal parents, both children per item)", n_out + 2)
     roof_in = roof(pb["inside"], ms_in / 1e3, "k_items inside levels (one launch per height)",
                    n_in + 1)
-    if T == 512 and G == 8 and CH == 0:
+    if T == 512 and G == 8 and CH == 0 and not PC:
         roof_out["traffic"] = TRAFFIC_PER_LAUNCH["outside"]
         roof_in["traffic"] = TRAFFIC_PER_LAUNCH["inside"]
     roof_it = roof(pb["em_iteration"], avg_launch_s,
@@ -727,13 +733,13 @@ def main():
     e2e = None
     if not args.no_e2e:
         score_candidates(w.newicks, w.rows, w.Q, w.leaf_order, group_sites=G, wide_chunk=CH,
-                         device=dev)
+                         wide_pc=PC, device=dev)
         torch.cuda.synchronize(dev)
         tot_iters, t_e2e, h2d, d2h = 0, 0.0, 0, 0
         for _ in range(args.e2e_steps):
             t_a = time.perf_counter()
             res = score_candidates(w.newicks, w.rows, w.Q, w.leaf_order, group_sites=G,
-                                   wide_chunk=CH, device=dev)
+                                   wide_chunk=CH, wide_pc=PC, device=dev)
             t_e2e += time.perf_counter() - t_a
             tot_iters += sum(r.iterations for r in res.results)
             h2d, d2h = res.h2d_bytes, res.d2h_bytes
@@ -806,8 +812,9 @@ def main():
             "config": {"workload": "512 NNI candidates of a 1000-leaf Yule tree, 40 sites, "
                                    "M_k~U{5..50}, q~Dir(0.5), nu=0.1, phi=0.15, fastEM semantics",
                        "trees_per_gpu": T, "nodes_per_gpu": nodes, "sites": K,
-                       "group_sites": G, "wide_chunk": CH,
-                       "wide_kernel": "direct per-thread loads" if CH == 0 else
+                       "group_sites": G, "wide_chunk": CH, "wide_pc": PC,
+                       "wide_kernel": f"producer/consumer warp pairs, {CH or 8} slots per stage"
+                       if PC else "direct per-thread loads" if CH == 0 else
                        f"bulk-staged, {CH} slots per stage",
                        "tile_shape": "autotuned" if tuned else "given",
                        "autotune_ms_per_em_iteration": tuned["ms"] if tuned else None,

@@ -310,6 +310,14 @@ typedef struct laml_batch {
     /* LAML_MSTEP_LBFGS only, else NULL: [LAML_LBFGS_SLOTS * (n_nodes + 2 T)]
      * FP32 vectors of the L-BFGS solve */
     float* nd_lbfgs;
+    /* nonzero: the wide levels run on producer/consumer warp pairs -- a
+     * producer warp copies each slab's rows (wide_chunk state slots per
+     * stage, 0 = 8) and per-site scalars into shared memory with the
+     * bulk-copy engine while its consumer warp computes the previous ones
+     * from there.  Overrides the wide_chunk kernel choice; results are
+     * bitwise the same.  The partial, scalar, code and branch-term arrays
+     * must start on 16-byte boundaries. */
+    int32_t wide_pc;
 } laml_batch;
 
 /* A tree's partials are FP32 values with power-of-two exponents (linear)

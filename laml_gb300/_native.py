@@ -90,7 +90,7 @@ BATCH_FIELDS = [
     ("barrier", vp), ("error", vp), ("max_states", i32), ("max_tree_nodes", i32),
     ("tr_leaf", vp), ("nd_uorder", vp), ("nd_uwork", vp),
     ("plan_part_floats", i64), ("plan_scalar_len", i64), ("tr_mstats", vp),
-    ("wide_chunk", i32), ("wait_limit_ns", i64), ("nd_lbfgs", vp),
+    ("wide_chunk", i32), ("wait_limit_ns", i64), ("nd_lbfgs", vp), ("wide_pc", i32),
 ]
 
 

@@ -36,7 +36,8 @@ class ScoreResult:
 
 def score_candidates(newicks: Sequence[str], rows: dict, Q, leaf_order: Sequence[str],
                      compat: bool = True, group_sites: Optional[int] = None,
-                     wide_chunk: Optional[int] = None, nu: float = 0.5,
+                     wide_chunk: Optional[int] = None, wide_pc: Optional[bool] = None,
+                     nu: float = 0.5,
                      phi: float = 0.5, rounds: int = MSTEP_ROUNDS, max_iters: int = 100000,
                      fix_nu=None, fix_phi=None, masks=None, device="cuda", chunk: int = 4,
                      rng: Optional[random.Random] = None,
@@ -50,21 +51,24 @@ def score_candidates(newicks: Sequence[str], rows: dict, Q, leaf_order: Sequence
     width crosses the wide/narrow rule).  Default: 2 parts from 256
     candidates on, else 1.
 
-    ``group_sites`` / ``wide_chunk`` (the tile shape): None = picked by the
-    autotuner (``tune.autotune``, cached per workload shape) for 64 or more
-    candidates, by the cost model below that."""
+    ``group_sites`` / ``wide_chunk`` / ``wide_pc`` (the tile shape and the
+    wide levels' kernel): None = picked by the autotuner (``tune.autotune``,
+    cached per workload shape) for 64 or more candidates, by the cost model
+    below that."""
     import threading
     from concurrent.futures import ThreadPoolExecutor
 
     from . import tune
 
-    if group_sites is None or wide_chunk is None:
+    if group_sites is None or wide_chunk is None or wide_pc is None:
         if len(newicks) >= 64 and torch.device(device).type == "cuda":
             t = tune.autotune(newicks, rows, Q, leaf_order, compat=compat, device=device)
         else:
-            t = {"group_sites": tune.pick_group_sites(n_sites=len(Q)), "wide_chunk": 0}
+            t = {"group_sites": tune.pick_group_sites(n_sites=len(Q)), "wide_chunk": 0,
+                 "wide_pc": False}
         group_sites = t["group_sites"] if group_sites is None else group_sites
         wide_chunk = t["wide_chunk"] if wide_chunk is None else wide_chunk
+        wide_pc = bool(t.get("wide_pc", False)) if wide_pc is None else wide_pc
     ds = dataset_from_rows(rows, Q, leaf_order, compat, group_sites)
     rng = rng if rng is not None else random
     T = len(newicks)
@@ -95,6 +99,7 @@ def score_candidates(newicks: Sequence[str], rows: dict, Q, leaf_order: Sequence
                        phi=phi, d=d, mask=sub(masks), fix_nu=sub(fix_nu), fix_phi=sub(fix_phi),
                        device=device, trees=trees, dataset=ds, stream=st)
         b.wide_chunk = wide_chunk
+        b.wide_pc = wide_pc
         return b, st
 
     res, h2d, d2h = [], 0, 0

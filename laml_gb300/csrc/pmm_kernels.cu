@@ -3733,6 +3733,516 @@ __global__ void __launch_bounds__(kSWarps * 32, kSMinBlocks) k_items_ws(laml_bat
 }
 
 // ---------------------------------------------------------------------------
+// Wide levels on producer/consumer warp pairs.  The per-thread kernels wait
+// on chains of dependent loads (descriptor -> group -> rows and scalars ->
+// state loop) with every byte in flight held in registers; at the 80
+// registers the outside item needs, 24 warps per SM keep DRAM about a third
+// busy.  Here a producer warp reads each slab's descriptors (32 / G items)
+// and has the bulk-copy engine move everything its consumer warp will read
+// into shared memory: the per-site scalars and branch terms into a slab
+// header (two per pair, so one fills while the other is read) and the rows,
+// CH state slots at a time, into a ring of S stages.  The consumer then
+// waits on mbarriers only, and the bytes in flight sit in shared memory.
+// Every thread's arithmetic is the per-thread kernels' (the same chunk loops
+// and child_finish), so the results are bitwise equal.
+//
+// Header of one item (ints; every bulk destination on a 16-byte boundary):
+//   [0, 12) descriptor, [12, 20) group descriptor, [20, 24) status, mode,
+//   the group's slot count, valid | staged << 1; [24, 28) leaf terms e1,
+//   ephi, es; [32, 36) and [36, 40) branch terms of v and w; from 40 twelve
+//   G-int slots: parent's out_h, out_x; v's in_h (its codes when a leaf),
+//   in_x, in_dot; w's likewise; root_lr, root_x; site_C, site_sumq.
+// ---------------------------------------------------------------------------
+constexpr int kPcPairs = 4;     // producer/consumer warp pairs per block
+constexpr int kPcMinBlocks = 2; // resident blocks per SM asked (<= 128 registers)
+
+template <int G, int NR, int CH>
+struct PGeom {
+    static constexpr int P = 32 / G;                 // items per slab
+    static constexpr int S = CH <= 8 ? 4 : 3;        // stages per pair
+    static constexpr int row = CH * G;               // floats of one row's chunk
+    static constexpr int item = NR * row + G;        // + G floats: items start G banks apart
+    static constexpr int stage = P * item;
+    static constexpr int HI = 40 + 12 * G;           // header ints per item
+    static constexpr int hdr = P * HI;
+    static constexpr size_t pair_floats = (size_t)S * stage + 2 * hdr;
+    static constexpr int nbar = 2 * S + 4;           // full[S], empty[S], hfull[2], hempty[2]
+    static constexpr size_t block_bytes =
+        kPcPairs * (pair_floats * sizeof(float) + nbar * sizeof(uint64_t));
+};
+
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+    asm volatile("{\n\t.reg .b64 st;\n\tmbarrier.arrive.shared::cta.b64 st, [%0];\n\t}"
+                 ::"r"(smem_u32(bar))
+                 : "memory");
+}
+
+// a phase wait that lets the hardware suspend the warp until the phase
+// completes (up to kPcSuspendNs per try) instead of spinning on it; bounded
+// by the batch's wait limit like mbar_wait
+constexpr uint32_t kPcSuspendNs = 20000;
+
+__device__ __forceinline__ bool mbar_try_wait_hint(uint64_t* bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile("{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\t"
+                 "selp.u32 %0, 1, 0, p;\n\t}"
+                 : "=r"(ok)
+                 : "r"(smem_u32(bar)), "r"(parity), "r"(kPcSuspendNs)
+                 : "memory");
+    return ok != 0;
+}
+
+__device__ __forceinline__ bool pc_wait(const laml_batch& b, uint64_t* bar, uint32_t parity) {
+    const long long lim = wait_limit(b);
+    if (lim < 0) {   // one check, without suspending
+        if (mbar_test_wait(bar, parity)) return true;
+        atomicCAS(b.error, 0, LAML_ERR_TIMEOUT);
+        return false;
+    }
+    if (mbar_try_wait_hint(bar, parity)) return true;
+    const unsigned long long t0 = gtimer();
+    for (uint32_t it = 0; it < (1u << 26); ++it) {
+        if (mbar_try_wait_hint(bar, parity)) return true;
+        if ((long long)(gtimer() - t0) > lim) break;
+    }
+    atomicCAS(b.error, 0, LAML_ERR_TIMEOUT);
+    return false;
+}
+
+__device__ __forceinline__ bool aligned16(const void* p) {
+    return ((uintptr_t)p & 15u) == 0;
+}
+
+// the producer's view of one item of a slab: its descriptor, group, tree
+// state and leaf terms (read one slab ahead of its copies)
+struct PItem {
+    ItemDesc d;
+    int4 G1, G2;
+    int Cg, status, mode, tsite;
+    float e1, ephi, es;
+    bool valid, staged;
+};
+
+template <int KIND>
+__device__ __forceinline__ void pc_fetch(const laml_batch& b, const int32_t* desc, int64_t n,
+                                         bool rs, int64_t it, PItem& t) {
+    t.valid = it < n;
+    t.d = load_desc(desc, t.valid ? it : 0);
+    const int4* gp = reinterpret_cast<const int4*>(b.grp_desc) + 2 * t.d.gd;
+    t.G1 = __ldg(gp);
+    t.G2 = __ldg(gp + 1);
+    t.Cg = __ldg(b.group_C + t.d.gd);
+    t.status = __ldcg(b.tr_status + t.d.tree);
+    t.mode = __ldcg(b.tr_mode + t.d.tree);
+    t.tsite = KIND == 1 ? __ldg(b.tr_site_base + t.d.tree) : 0;
+    const Leaf L = leaf_params(b, t.d.tree);
+    t.e1 = L.e1;
+    t.ephi = L.ephi;
+    t.es = L.es;
+    const bool active = t.valid && (!(KIND == 1 || rs) || t.status == LAML_TREE_ACTIVE);
+    t.staged = active && t.mode != LAML_MODE_LOG;
+}
+
+// copy k of an item's header (0 <= k < 14): source and bytes (0: none)
+template <int G, int KIND>
+__device__ __forceinline__ uint32_t pc_hdr_src(const laml_batch& b, const PItem& t, int k,
+                                               const void*& src, int& dst_int) {
+    const ItemDesc& d = t.d;
+    const int tsite = t.tsite, sb = t.G1.y, code_base = t.G2.x, kpad = t.G2.y;
+    const int sg = d.g * G;
+    const bool vl = d.flags & 1, wl = d.flags & 2;
+    src = nullptr;
+    dst_int = 0;
+    if (!t.staged) return 0u;
+    const uint32_t s4 = G * 4u;
+    switch (k) {
+        case 0: if (KIND != 1) return 0u; src = b.out_h + (int64_t)d.u_srow + sg; dst_int = 40; return s4;
+        case 1: if (KIND != 1) return 0u; src = b.out_x + (int64_t)d.u_srow + sg; dst_int = 40 + G; return s4;
+        case 2:
+            dst_int = 40 + 2 * G;
+            if (vl) { src = b.codes + code_base + (int64_t)d.v_ref * kpad + sg; return G * 2u; }
+            src = b.in_h + (int64_t)d.v_srow + sg; return s4;
+        case 3: if (vl) return 0u; src = b.in_x + (int64_t)d.v_srow + sg; dst_int = 40 + 3 * G; return s4;
+        case 4: if (vl) return 0u; src = b.in_dot + (int64_t)d.v_srow + sg; dst_int = 40 + 4 * G; return s4;
+        case 5:
+            dst_int = 40 + 5 * G;
+            if (wl) { src = b.codes + code_base + (int64_t)d.w_ref * kpad + sg; return G * 2u; }
+            src = b.in_h + (int64_t)d.w_srow + sg; return s4;
+        case 6: if (wl) return 0u; src = b.in_x + (int64_t)d.w_srow + sg; dst_int = 40 + 6 * G; return s4;
+        case 7: if (wl) return 0u; src = b.in_dot + (int64_t)d.w_srow + sg; dst_int = 40 + 7 * G; return s4;
+        case 8: if (KIND != 1) return 0u; src = b.root_lr + (int64_t)tsite + sg; dst_int = 40 + 8 * G; return s4;
+        case 9: if (KIND != 1) return 0u; src = b.root_x + (int64_t)tsite + sg; dst_int = 40 + 9 * G; return s4;
+        case 10: src = b.site_C + sb; dst_int = 40 + 10 * G; return s4;
+        case 11: src = b.site_sumq + sb; dst_int = 40 + 11 * G; return s4;
+        case 12: src = b.nd_bt + 4 * (int64_t)d.v; dst_int = 32; return 16u;
+        default: src = b.nd_bt + 4 * (int64_t)d.w; dst_int = 36; return 16u;
+    }
+}
+
+// the slab's largest staged slot count over CH (every lane of the warp)
+template <int CH>
+__device__ __forceinline__ int pc_chunks(bool staged, int Cg) {
+    const int m = __reduce_max_sync(kFull, staged ? Cg : 0);
+    return (m + CH - 1) / CH;
+}
+
+// producer warp of a pair: headers and row chunks of the pair's slabs
+template <int G, int KIND, int CH>
+__device__ void pc_produce(const laml_batch& b, const int32_t* desc, int64_t n, bool rs,
+                           int64_t pid, int64_t npairs, float* ring, int* hdr, uint64_t* bars) {
+    using Geo = PGeom<G, KIND == 1 ? 3 : 2, CH>;
+    constexpr int P = Geo::P, S = Geo::S, R = Geo::row;
+    uint64_t* full = bars;
+    uint64_t* empty = bars + S;
+    uint64_t* hfull = bars + 2 * S;
+    uint64_t* hempty = bars + 2 * S + 2;
+    const int lane32 = threadIdx.x & 31, sub = lane32 / G, l = lane32 % G;
+    const int64_t nslab = (n + P - 1) / P;
+    int64_t q = 0, kh = 0;   // stages issued, headers issued
+    PItem t, tn;
+    if (pid < nslab) pc_fetch<KIND>(b, desc, n, rs, pid * P + sub, t);
+    for (int64_t slab = pid; slab < nslab; slab += npairs) {
+        // the next slab's items load while this one's copies go out
+        if (slab + npairs < nslab) pc_fetch<KIND>(b, desc, n, rs, (slab + npairs) * P + sub, tn);
+        // header kh & 1 of the pair: wait until its consumer has read it
+        const int h = (int)(kh & 1);
+        if (!pc_wait(b, hempty + h, (uint32_t)((kh >> 1) & 1) ^ 1u)) break;
+        int* H = hdr + h * Geo::hdr + sub * Geo::HI;
+        const ItemDesc& d = t.d;
+        if (l == 0) reinterpret_cast<int4*>(H)[0] = make_int4(d.u, d.v, d.w, d.tree | (d.flags << 24));
+        if (l == 1) reinterpret_cast<int4*>(H)[1] = make_int4(d.g, d.gd, d.u_srow, d.u_prow8);
+        if (l == 2) reinterpret_cast<int4*>(H)[2] = make_int4(d.v_ref, d.w_ref, d.v_srow, d.w_srow);
+        if (l == 3) reinterpret_cast<int4*>(H)[3] = t.G1;
+        if (l == 4) reinterpret_cast<int4*>(H)[4] = t.G2;
+        if (l == 5) reinterpret_cast<int4*>(H)[5] =
+            make_int4(t.status, t.mode, t.Cg, (t.valid ? 1 : 0) | (t.staged ? 2 : 0));
+        if (l == 6) reinterpret_cast<float4*>(H)[6] = make_float4(t.e1, t.ephi, t.es, 0.f);
+        // the header's copies: lane l issues copies l and l + G (G = 8)
+        constexpr int NC = (14 + G - 1) / G;
+        const void* hs[NC];
+        int hd[NC];
+        uint32_t hb[NC], mine = 0;
+#pragma unroll
+        for (int r = 0; r < NC; ++r) {
+            const int c = r * G + l;
+            hb[r] = c < 14 ? pc_hdr_src<G, KIND>(b, t, c, hs[r], hd[r]) : 0u;
+            if (hb[r] && !aligned16(hs[r])) {
+                atomicCAS(b.error, 0, LAML_ERR_ARG);
+                hb[r] = 0u;
+            }
+            mine += hb[r];
+        }
+        const uint32_t tot = __reduce_add_sync(kFull, mine);
+        __syncwarp();
+        if (lane32 == 0) mbar_arrive_tx(hfull + h, tot);
+        __syncwarp();
+#pragma unroll
+        for (int r = 0; r < NC; ++r)
+            if (hb[r]) bulk_g2s(H + hd[r], hs[r], hb[r], hfull + h);
+        ++kh;
+        // the rows, CH slots per stage: lane l < NR of each item copies row
+        // l -- the parent's outside row (outside only), then the internal
+        // children's inside rows
+        const float* rsrc = nullptr;
+        if (t.staged) {
+            const int64_t off = t.G1.x;
+            if (KIND == 1) {
+                if (l == 0) rsrc = b.out_part + (int64_t)d.u_prow8 * 8 + off;
+                if (l == 1 && !(d.flags & 1)) rsrc = b.in_part + (int64_t)d.v_ref * 8 + off;
+                if (l == 2 && !(d.flags & 2)) rsrc = b.in_part + (int64_t)d.w_ref * 8 + off;
+            } else {
+                if (l == 0 && !(d.flags & 1)) rsrc = b.in_part + (int64_t)d.v_ref * 8 + off;
+                if (l == 1 && !(d.flags & 2)) rsrc = b.in_part + (int64_t)d.w_ref * 8 + off;
+            }
+        }
+        float* rdst = ring + sub * Geo::item + l * R;
+        const int nch = pc_chunks<CH>(t.staged, t.Cg);
+        bool ok = true;
+        for (int c = 0; c < nch; ++c) {
+            const int st = (int)(q % S);
+            if (!pc_wait(b, empty + st, (uint32_t)((q / S) & 1) ^ 1u)) { ok = false; break; }
+            const int j0 = c * CH;
+            const int ns = rsrc ? min(CH, t.Cg - j0) : 0;
+            const uint32_t by = ns > 0 ? (uint32_t)ns * G * 4u : 0u;
+            const uint32_t stot = __reduce_add_sync(kFull, by);
+            __syncwarp();
+            if (lane32 == 0) mbar_arrive_tx(full + st, stot);
+            __syncwarp();
+            if (by) bulk_g2s(rdst + st * Geo::stage, rsrc + (int64_t)j0 * G, by, full + st);
+            ++q;
+        }
+        if (!ok) break;
+        t = tn;
+    }
+    // every copy this warp started lands before the block may exit: the
+    // last header of each buffer and the last S stages (bounded waits)
+    if (lane32 == 0) {
+        for (int64_t kk = (kh > 2 ? kh - 2 : 0); kk < kh; ++kk)
+            mbar_drain(hfull + (kk & 1), (uint32_t)((kk >> 1) & 1));
+        for (int64_t qq = (q > S ? q - S : 0); qq < q; ++qq)
+            mbar_drain(full + (qq % S), (uint32_t)((qq / S) & 1));
+    }
+    __syncwarp();
+}
+
+// consumer warp of a pair
+template <int G, int KIND, int CH>
+__device__ void pc_consume(const laml_batch& b, const int32_t* desc, int64_t n, bool rs,
+                           bool want_post, int64_t pid, int64_t npairs, const float* ring,
+                           const int* hdr, uint64_t* bars) {
+    using Geo = PGeom<G, KIND == 1 ? 3 : 2, CH>;
+    constexpr int P = Geo::P, S = Geo::S, R = Geo::row;
+    uint64_t* full = bars;
+    uint64_t* empty = bars + S;
+    uint64_t* hfull = bars + 2 * S;
+    uint64_t* hempty = bars + 2 * S + 2;
+    const int lane32 = threadIdx.x & 31, sub = lane32 / G, l = lane32 % G;
+    const bool leader = l == 0;
+    const int64_t nslab = (n + P - 1) / P;
+    int64_t q = 0, k = 0;
+    for (int64_t slab = pid; slab < nslab; slab += npairs, ++k) {
+        const int h = (int)(k & 1);
+        if (!pc_wait(b, hfull + h, (uint32_t)((k >> 1) & 1))) return;
+        const int* H = hdr + h * Geo::hdr + sub * Geo::HI;
+        SItem cur;
+        {
+            const int4 A = reinterpret_cast<const int4*>(H)[0];
+            const int4 B = reinterpret_cast<const int4*>(H)[1];
+            const int4 C = reinterpret_cast<const int4*>(H)[2];
+            ItemDesc& d = cur.d;
+            d.u = A.x; d.v = A.y; d.w = A.z;
+            d.tree = A.w & 0xffffff;
+            d.flags = (int)((unsigned)A.w >> 24);
+            d.g = B.x; d.gd = B.y; d.u_srow = B.z; d.u_prow8 = B.w;
+            d.v_ref = C.x; d.w_ref = C.y; d.v_srow = C.z; d.w_srow = C.w;
+        }
+        const int4 G1 = reinterpret_cast<const int4*>(H)[3];
+        const int4 G2 = reinterpret_cast<const int4*>(H)[4];
+        const int4 X = reinterpret_cast<const int4*>(H)[5];
+        cur.valid = X.w & 1;
+        cur.staged = (X.w & 2) != 0;
+        cur.Cg = X.z;
+        cur.logm = cur.valid && X.y == LAML_MODE_LOG;
+        const bool act_ok = !(KIND == 1 || rs) || X.x == LAML_TREE_ACTIVE;
+        if (cur.staged) {
+            SiteCtx& s = cur.s;
+            s.tree = cur.d.tree;
+            s.site = cur.d.g * G + l;
+            cur.live = s.site < G2.z;
+            s.goff = G1.x;
+            s.ds = G1.w;
+            s.C = H[40 + 10 * G + l];
+            s.sumq = __int_as_float(H[40 + 11 * G + l]);
+            s.qrow = b.q + G1.z + l;
+            cur.gc.code_base = G2.x;
+            cur.gc.kpad = G2.y;
+            const float4 Lf = reinterpret_cast<const float4*>(H)[6];
+            Leaf L;
+            L.e1 = Lf.x; L.ephi = Lf.y; L.es = Lf.z;
+            auto child = [&](bool leaf, int base) {
+                Child c;
+                c.e1 = L.e1;
+                c.ephi = L.ephi;
+                if (leaf) {
+                    const int code = reinterpret_cast<const int16_t*>(H + base)[l];
+                    c.row = nullptr;
+                    c.f = 1.f;
+                    c.X = 0;
+                    c.code = code;
+                    c.s0 = code == 0 ? L.e1 : (code == -1 ? L.ephi : 0.f);
+                    c.ss = code < 0 ? 1.f : L.es;
+                    c.D = code >= 2 ? __ldg(s.qrow + code * G) * L.e1
+                                    : (code == -1 ? L.ephi * s.sumq : 0.f);
+                } else {
+                    c.f = pow2i(-H[base + l]);
+                    c.X = H[base + G + l];
+                    c.D = __int_as_float(H[base + 2 * G + l]);
+                    c.row = b.in_part;   // marks an internal child; its slots come from the stages
+                    c.code = 0;
+                    c.s0 = c.ss = 0.f;
+                }
+                return c;
+            };
+            if (cur.live) {
+                cur.cv = child(cur.d.flags & 1, 40 + 2 * G);
+                cur.cw = child(cur.d.flags & 2, 40 + 5 * G);
+                cur.bv = reinterpret_cast<const float4*>(H)[8];
+                cur.bw = reinterpret_cast<const float4*>(H)[9];
+                if (KIND == 1) {
+                    cur.fo = pow2i(-H[40 + l]);
+                    cur.Xo = H[40 + G + l];
+                    cur.lroot = __int_as_float(H[40 + 8 * G + l]);
+                    cur.xroot = H[40 + 9 * G + l];
+                }
+            }
+        } else {
+            cur.live = cur.valid && act_ok && site_ctx_d<G>(b, cur.d, l, KIND == 1 || rs, cur.s, cur.gc);
+        }
+        // the header is read: hand it back (generic reads before the next
+        // bulk writes into it)
+        fence_proxy_async_smem();
+        __syncwarp();
+        if (lane32 == 0) mbar_arrive(hempty + h);
+        float cv_[8] = {0, 0, 0, 0, 0, 0, 0, 0}, cw_[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+        const bool run = cur.live && cur.staged;
+        const int C = run ? cur.s.C : 0;
+        ChildOut A, B;
+        float pxa = 0.f, pxb = 0.f;
+        float* row = nullptr;
+        float dot = 0.f, mx = 0.f, s0 = 0.f, ss = 0.f;
+        const int nch = pc_chunks<CH>(cur.staged, cur.Cg);
+        for (int c = 0; c < nch; ++c, ++q) {
+            const int stg = (int)(q % S);
+            if (!pc_wait(b, full + stg, (uint32_t)((q / S) & 1))) return;
+            const float* st = ring + stg * Geo::stage + sub * Geo::item + l;
+            const int j0 = c * CH;
+            if (run && j0 < C) {
+                const float* su = st;
+                const float* sv = st + (KIND == 1 ? R : 0);
+                const float* sw = st + (KIND == 1 ? 2 : 1) * R;
+                Child& cv = cur.cv;
+                Child& cw = cur.cw;
+                const float4 bv = cur.bv, bw = cur.bw;
+                if (c == 0) {   // slots 0 and 1: the item's heads
+                    if (cv.row) { cv.s0 = sv[0] * cv.f; cv.ss = sv[G] * cv.f; }
+                    if (cw.row) { cw.s0 = sw[0] * cw.f; cw.ss = sw[G] * cw.f; }
+                    const float ev0 = edge0(bv, cv.s0, cv.D, cv.ss);
+                    const float ew0 = edge0(bw, cw.s0, cw.D, cw.ss);
+                    if (KIND == 1) {
+                        const float o0 = su[0] * cur.fo, os = su[G] * cur.fo;
+                        A.x0 = o0 * ew0; A.xs = os * cw.ss; A.X = cur.Xo + cw.X;
+                        B.x0 = o0 * ev0; B.xs = os * cv.ss; B.X = cur.Xo + cv.X;
+                        A.sumx = A.dot = A.mx = 0.f;
+                        B.sumx = B.dot = B.mx = 0.f;
+                        const int64_t ro = (int64_t)cur.s.goff + l;
+                        A.orow = cv.row ? b.out_part + (int64_t)cur.d.v_ref * 8 + ro : nullptr;
+                        B.orow = cw.row ? b.out_part + (int64_t)cur.d.w_ref * 8 + ro : nullptr;
+                        pxa = bv.y * A.x0;
+                        pxb = bw.y * B.x0;
+                    } else {
+                        row = b.in_part + (int64_t)cur.d.u_prow8 * 8 + cur.s.goff + l;
+                        s0 = ev0 * ew0;
+                        ss = cv.ss * cw.ss;
+                        __stcg(row, s0);
+                        __stcg(row + G, ss);
+                        mx = fmaxf(s0, ss);
+                        dot = 0.f;
+                    }
+                }
+                const int jlo = max(j0, 2), jhi = min(j0 + CH, C);
+                if (KIND == 1) {
+#define LAML_P_OUT(VL, WL)                                                                     \
+    s_outside_chunk<G, VL, WL>(su, sv, sw, j0, jlo, jhi, cur.fo, cv, cw, bv, bw, cur.s.qrow,  \
+                               pxa, pxb, A.orow, B.orow, A.sumx, A.dot, A.mx, B.sumx, B.dot,  \
+                               B.mx)
+                    switch ((cv.row ? 0 : 1) | (cw.row ? 0 : 2)) {
+                        case 0: LAML_P_OUT(false, false); break;
+                        case 1: LAML_P_OUT(true, false); break;
+                        case 2: LAML_P_OUT(false, true); break;
+                        default: LAML_P_OUT(true, true); break;
+                    }
+#undef LAML_P_OUT
+                } else {
+#define LAML_P_IN(VL, WL) \
+    s_inside_chunk<G, VL, WL>(sv, sw, j0, jlo, jhi, cv, cw, bv, bw, cur.s.qrow, row, dot, mx)
+                    switch ((cv.row ? 0 : 1) | (cw.row ? 0 : 2)) {
+                        case 0: LAML_P_IN(false, false); break;
+                        case 1: LAML_P_IN(true, false); break;
+                        case 2: LAML_P_IN(false, true); break;
+                        default: LAML_P_IN(true, true); break;
+                    }
+#undef LAML_P_IN
+                }
+            }
+            // the stage is read: hand it back to the producer
+            fence_proxy_async_smem();
+            __syncwarp();
+            if (lane32 == 0) mbar_arrive(empty + stg);
+        }
+        // finish the slab's items
+        if (KIND == 1) {
+            if (run) {
+                child_finish<G>(b, cur.s, cur.d.v, cur.cv, cur.bv, A, want_post, cur.lroot,
+                                cur.xroot, cv_);
+                child_finish<G>(b, cur.s, cur.d.w, cur.cw, cur.bw, B, want_post, cur.lroot,
+                                cur.xroot, cw_);
+            } else if (cur.live && cur.logm) {
+                float tv[8], tw[8];
+                const ItemDesc dl = cur.d;
+                const SiteCtx sl = cur.s;
+                const GroupCtx gl = cur.gc;
+                outside_log_lane<G>(b, dl, sl, gl, want_post, tv, tw);
+#pragma unroll
+                for (int kk = 0; kk < 8; ++kk) {
+                    cv_[kk] = tv[kk];
+                    cw_[kk] = tw[kk];
+                }
+            }
+#pragma unroll
+            for (int off = G / 2; off > 0; off >>= 1) {
+#pragma unroll
+                for (int kk = 0; kk < 8; ++kk) {
+                    cv_[kk] += __shfl_xor_sync(kFull, cv_[kk], off);
+                    cw_[kk] += __shfl_xor_sync(kFull, cw_[kk], off);
+                }
+            }
+            if (cur.valid && leader && X.x == LAML_TREE_ACTIVE) {
+                write_counts<G>(b, cur.d.tree, cur.d.v, cur.d.g, cv_);
+                write_counts<G>(b, cur.d.tree, cur.d.w, cur.d.g, cw_);
+            }
+        } else {
+            if (run) {
+                const int hh = scale_exp(mx);
+                const float f = pow2i(-hh);
+                const int Xs = cur.cv.X + cur.cw.X + hh;
+                const int64_t sr = (int64_t)cur.d.u_srow + cur.s.site;
+                __stcg(b.in_h + sr, hh);
+                __stcg(b.in_x + sr, Xs);
+                __stcg(b.in_dot + sr, dot * f);
+                if (cur.d.flags & 4)
+                    root_site_llh(b, cur.s.tree, cur.s.site, root_edge_logs(b, cur.s.tree),
+                                  s0 * f, dot * f, ss * f, Xs);
+            } else if (cur.live && cur.logm) {
+                const ItemDesc dl = cur.d;
+                const SiteCtx sl = cur.s;
+                const GroupCtx gl = cur.gc;
+                inside_log_item<G>(b, dl, sl, gl);
+            }
+        }
+    }
+}
+
+template <int G, int KIND, int CH>
+__global__ void __launch_bounds__(kPcPairs * 64, kPcMinBlocks) k_items_pc(laml_batch b,
+                                                                          const int32_t* desc,
+                                                                          int64_t n,
+                                                                          int want_post,
+                                                                          int respect_status) {
+    using Geo = PGeom<G, KIND == 1 ? 3 : 2, CH>;
+    extern __shared__ __align__(128) unsigned char psm[];
+    const int wib = threadIdx.x >> 5;
+    const int pair = wib % kPcPairs;
+    const bool producer = wib >= kPcPairs;
+    float* base = reinterpret_cast<float*>(psm) + (size_t)pair * Geo::pair_floats;
+    float* ring = base;
+    int* hdr = reinterpret_cast<int*>(base + (size_t)Geo::S * Geo::stage);
+    uint64_t* bars = reinterpret_cast<uint64_t*>(psm + kPcPairs * Geo::pair_floats * sizeof(float)) +
+                     pair * Geo::nbar;
+    if ((threadIdx.x & 31) == 0 && !producer) {
+        for (int k = 0; k < Geo::nbar; ++k) mbar_init(bars + k, 1);
+        fence_mbar_init();
+    }
+    __syncthreads();
+    const int64_t pid = (int64_t)blockIdx.x * kPcPairs + pair;
+    const int64_t npairs = (int64_t)gridDim.x * kPcPairs;
+    if (producer)
+        pc_produce<G, KIND, CH>(b, desc, n, respect_status != 0, pid, npairs, ring, hdr, bars);
+    else
+        pc_consume<G, KIND, CH>(b, desc, n, respect_status != 0, want_post != 0, pid, npairs,
+                                ring, hdr, bars);
+}
+
+// ---------------------------------------------------------------------------
 // kernels
 // ---------------------------------------------------------------------------
 template <int G, int KIND, bool AS = false>
@@ -4024,6 +4534,17 @@ int validate(const laml_batch* b) {
         laml::set_error("laml_batch: wide_chunk must be 0, 8 or 16");
         return LAML_ERR_ARG;
     }
+    if (b->wide_pc) {   // the bulk copies' sources start on 16-byte boundaries
+        const void* arr[] = {b->in_part, b->out_part, b->in_h, b->in_x, b->in_dot, b->out_h,
+                             b->out_x, b->root_lr, b->root_x, b->site_C, b->site_sumq,
+                             b->codes, b->nd_bt};
+        for (const void* p : arr)
+            if (((uintptr_t)p & 15u) != 0) {
+                laml::set_error("laml_batch: wide_pc needs 16-byte aligned partial, scalar, "
+                                "code and branch-term arrays");
+                return LAML_ERR_ARG;
+            }
+    }
     return LAML_OK;
 }
 
@@ -4114,10 +4635,54 @@ int launch_staged_wide(const laml_batch& b, const int32_t* desc, int64_t n, int 
     return launch_staged_wide_t<G, KIND, 16>(b, desc, n, want_post, respect_status, st);
 }
 
+template <int G, int KIND, int CH>
+int launch_pc_wide_t(const laml_batch& b, const int32_t* desc, int64_t n, int want_post,
+                     int respect_status, cudaStream_t st) {
+    using Geo = PGeom<G, KIND == 1 ? 3 : 2, CH>;
+    static bool attr_set = false;
+    if (!attr_set) {
+        int rc = check(cudaFuncSetAttribute(k_items_pc<G, KIND, CH>,
+                                            cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                            (int)Geo::block_bytes),
+                       "producer/consumer kernel shared memory limit");
+        if (rc) return rc;
+        attr_set = true;
+    }
+    static int per_sm = 0;
+    if (!per_sm) {
+        int rc = check(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+                           &per_sm, k_items_pc<G, KIND, CH>, kPcPairs * 64, Geo::block_bytes),
+                       "producer/consumer kernel occupancy");
+        if (rc) return rc;
+        if (per_sm < 1) per_sm = 1;
+    }
+    const int64_t slabs = (n + Geo::P - 1) / Geo::P;
+    int64_t blocks = (slabs + kPcPairs - 1) / kPcPairs;
+    const int64_t cap = (int64_t)per_sm * num_sms();
+    if (blocks > cap) blocks = cap;
+    k_items_pc<G, KIND, CH><<<(unsigned)blocks, kPcPairs * 64, Geo::block_bytes, st>>>(
+        b, desc, n, want_post, respect_status);
+    return check(cudaGetLastError(), "k_items_pc launch");
+}
+
+template <int G, int KIND>
+int launch_pc_wide(const laml_batch& b, const int32_t* desc, int64_t n, int want_post,
+                   int respect_status, cudaStream_t st) {
+    if (b.wide_chunk == 16)
+        return launch_pc_wide_t<G, KIND, 16>(b, desc, n, want_post, respect_status, st);
+    return launch_pc_wide_t<G, KIND, 8>(b, desc, n, want_post, respect_status, st);
+}
+
 template <int G>
 int launch_items(const laml_batch& b, const int32_t* items, int64_t n, int kind, int want_post,
                  int respect_status, cudaStream_t st, const int32_t* desc = nullptr) {
     if (n <= 0) return LAML_OK;
+    // wide inside / outside levels below the roots on producer/consumer
+    // warp pairs when the batch asks for them (wide_pc)
+    if ((kind == 0 || kind == 1) && !narrow_level(n) && b.wide_pc) {
+        return kind == 0 ? launch_pc_wide<G, 0>(b, desc, n, want_post, respect_status, st)
+                         : launch_pc_wide<G, 1>(b, desc, n, want_post, respect_status, st);
+    }
     // wide inside / outside levels below the roots: bulk-staged rows when
     // the batch asks for them (wide_chunk), else per-thread loads
     if ((kind == 0 || kind == 1) && !narrow_level(n) && b.max_states > 0 && b.wide_chunk > 0) {

@@ -267,6 +267,18 @@ class DeviceBatch:
             raise ValueError("wide_chunk must be 0, 8 or 16")
         self.b.wide_chunk = int(ch)
 
+    @property
+    def wide_pc(self) -> bool:
+        """Run the wide levels on producer/consumer warp pairs (a producer
+        warp bulk-copies rows and per-site scalars into shared memory for its
+        consumer warp; ``wide_chunk`` state slots per stage, 0 = 8).  A tiling
+        choice: the results are bitwise the same."""
+        return bool(self.b.wide_pc)
+
+    @wide_pc.setter
+    def wide_pc(self, on: bool):
+        self.b.wide_pc = 1 if on else 0
+
     # -- raw entry points -------------------------------------------------
     def _s(self):
         return C.c_void_p(self._stream_ptr)
@@ -326,7 +338,7 @@ class DeviceBatch:
         ``launch_graph``); cached per argument set."""
         tol = rel_tol if rel_tol is not None else (EM_STOP_COMPAT if self.compat else EM_STOP_EXACT)
         key = (iters, rounds, tol, max_iters, bool(persistent), self._mflags(polish),
-               self.wide_chunk)
+               self.wide_chunk, self.wide_pc)
         if not hasattr(self, "_graphs"):
             self._graphs = {}
         if key not in self._graphs:

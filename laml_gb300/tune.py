@@ -7,10 +7,12 @@ Two axes of the level kernels' tiling:
   slot) and the number of (node, group) items per warp (32 / G).  Small G
   wastes no lanes on site padding; large G gives wider transactions and
   fewer items.
-* the wide levels' kernel: per-thread row loads (0), or rows copied into
+* the wide levels' kernel: per-thread row loads (0); rows copied into
   per-warp shared-memory stages by the bulk-copy engine with 8 or 16 state
-  slots per stage (4 or 2 stages): how the state loops of the levels with
-  more than 8192 items are fed.
+  slots per stage (4 or 2 stages), each warp issuing its own copies; or
+  producer/consumer warp pairs, a producer warp copying rows (8 or 16
+  slots per stage) and per-site scalars for its consumer warp: how the
+  state loops of the levels with more than 8192 items are fed.
 
 ``autotune`` times fused EM iterations of a sample of the batch for every
 shape on the device and keeps the fastest (cached per workload shape);
@@ -26,7 +28,8 @@ from typing import Dict, Optional, Sequence
 import numpy as np
 
 GROUP_SITES = (8, 16, 32)
-WIDE_CHUNKS = (0, 8, 16)
+# (state slots per stage, producer/consumer pairs)
+WIDE_KERNELS = ((0, False), (8, False), (16, False), (8, True), (16, True))
 _CACHE: Dict[tuple, dict] = {}
 
 
@@ -55,11 +58,12 @@ def _key(newicks, Q, compat, sample):
 
 
 def autotune(newicks: Sequence[str], rows, Q, leaf_order, compat=True, sample=128, iters=2,
-             device="cuda", group_sites=GROUP_SITES, wide_chunks=WIDE_CHUNKS) -> dict:
+             device="cuda", group_sites=GROUP_SITES, wide_kernels=WIDE_KERNELS) -> dict:
     """Time ``iters`` EM iterations (the graph of per-level launches, as the
     solver replays it) on the first ``sample`` trees for every (G, wide
-    kernel) and return {"group_sites", "wide_chunk", "ms": {"G/chunk": ms}}.
-    Cached per (sample size, sites, tree size, model)."""
+    kernel) and return {"group_sites", "wide_chunk", "wide_pc", "ms":
+    {"G/chunk" or "G/pc chunk": ms}}.  Cached per (sample size, sites, tree
+    size, model)."""
     import torch
 
     from .problem import make_batch
@@ -71,8 +75,9 @@ def autotune(newicks: Sequence[str], rows, Q, leaf_order, compat=True, sample=12
     best, best_t = None, None
     for G in group_sites:
         b = make_batch(nw, rows, Q, leaf_order, compat=compat, group_sites=G, device=device)
-        for ch in wide_chunks:
+        for ch, pc in wide_kernels:
             b.wide_chunk = ch
+            b.wide_pc = pc
             b.branch_terms()
             b.inside(update_em=True)
             g = b.em_graph(iters, rel_tol=-1.0, max_iters=1 << 30, persistent=False)
@@ -82,11 +87,11 @@ def autotune(newicks: Sequence[str], rows, Q, leaf_order, compat=True, sample=12
             b.launch_graph(g)
             torch.cuda.synchronize()
             t = (time.perf_counter() - t0) / iters
-            times[f"{G}/{ch}"] = t * 1e3
+            times[f"{G}/pc {ch}" if pc else f"{G}/{ch}"] = t * 1e3
             if best_t is None or t < best_t:
-                best, best_t = (G, ch), t
+                best, best_t = (G, ch, pc), t
         del b
-    out = {"group_sites": best[0], "wide_chunk": best[1], "ms": times,
+    out = {"group_sites": best[0], "wide_chunk": best[1], "wide_pc": best[2], "ms": times,
            "sample_trees": len(nw), "iters": iters}
     _CACHE[key] = out
     return out

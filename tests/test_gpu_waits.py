@@ -5,7 +5,7 @@ its own copies still in flight and returns, and the context stays usable.
 The limit set negative makes each wait give up at its first unsatisfied
 check -- a wait that runs out on purpose, with no fault, trap or hang: on the
 staged per-level kernels (mbarrier phases of the bulk copies, narrow and
-wide levels) and on the
+wide levels), on the producer/consumer pairs of the wide levels and on the
 persistent kernel (its grid barrier).  The next calls on the same context,
 with the limit back at its default, match the FP64 C restatement."""
 import numpy as np
@@ -31,6 +31,25 @@ def test_staged_level_waits_run_out_then_recover():
     b = PB.make_batch(w.newicks, w.rows, w.Q, w.leaf_order, compat=True, nu=0.5, phi=0.5)
     assert max(np.diff(b._h_in_off)) > 8192 and min(np.diff(b._h_in_off)) <= 8192
     b.wide_chunk = 16   # wide levels on the bulk-staged kernels too
+    b.b.wait_limit_ns = -1
+    b.branch_terms()
+    b.inside(update_em=True)
+    b.outside()
+    torch.cuda.synchronize()
+    assert int(b.work["error"].item()) == ERR_TIMEOUT
+    b.work["error"].zero_()
+    b.b.wait_limit_ns = 0
+    llh = b.log_likelihood()
+    b.check_device_error()
+    ref = cpu_port.loglik(w.newicks, w.rows, w.Q, w.leaf_order, 0.5, 0.5)
+    np.testing.assert_allclose(llh, ref, rtol=1e-6)
+
+
+def test_pc_level_waits_run_out_then_recover():
+    w = _case()
+    b = PB.make_batch(w.newicks, w.rows, w.Q, w.leaf_order, compat=True, nu=0.5, phi=0.5)
+    assert max(np.diff(b._h_in_off)) > 8192
+    b.wide_pc = True   # wide levels on producer/consumer warp pairs
     b.b.wait_limit_ns = -1
     b.branch_terms()
     b.inside(update_em=True)
