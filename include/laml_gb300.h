@@ -312,11 +312,11 @@ typedef struct laml_batch {
     float* nd_lbfgs;
     /* nonzero: the wide levels run on producer/consumer warp pairs -- a
      * producer warp copies each slab's rows (wide_chunk state slots per
-     * stage, 0 = 8) and per-site scalars into shared memory with the
-     * bulk-copy engine while its consumer warp computes the previous ones
-     * from there.  Overrides the wide_chunk kernel choice; results are
-     * bitwise the same.  The partial, scalar, code and branch-term arrays
-     * must start on 16-byte boundaries. */
+     * stage, 0 = 8) into shared memory with the bulk-copy engine, and
+     * stores the per-site scalars there, while its consumer warp computes
+     * the previous slabs from there.  Overrides the wide_chunk kernel choice; results are
+     * bitwise the same.  in_part and out_part must start on 16-byte
+     * boundaries. */
     int32_t wide_pc;
 } laml_batch;
 

@@ -3470,7 +3470,39 @@ __device__ __forceinline__ void s_issue(const laml_batch& b, const SIss& t, int 
     if (win) bulk_g2s(dst + (uin ? 2 : 1) * R, b.in_part + (int64_t)t.w_ref * 8 + off, bytes, bar);
 }
 
+// one state slot of a staged outside chunk (k: the slot's offset in the stage)
 template <int G, bool VL, bool WL>
+__device__ __forceinline__ void s_outside_slot(const float* su, const float* sv, const float* sw,
+                                               int k, int j, float fo, const Child& cv,
+                                               const Child& cw, float bvz, float bwz, float kv,
+                                               float kw, float cstv, float cstw, float qj,
+                                               float pxa, float pxb, float* __restrict__ ra,
+                                               float* __restrict__ rb, float& sa, float& da,
+                                               float& ma, float& sb, float& db, float& mb) {
+    const float o = su[k] * fo;
+    const float av = VL ? (cv.code == j ? cv.e1 : cstv) : sv[k] * cv.f;
+    const float aw = WL ? (cw.code == j ? cw.e1 : cstw) : sw[k] * cw.f;
+    const float xa = mulr(o, fmaf(bwz, aw, kw));
+    const float xb = mulr(o, fmaf(bvz, av, kv));
+    sa = addr(sa, xa);
+    da = fmaf(xa, av, da);
+    sb = addr(sb, xb);
+    db = fmaf(xb, aw, db);
+    if (!VL) {
+        const float r = fmaf(pxa, qj, mulr(bvz, xa));
+        __stcg(ra, r);
+        ma = fmaxf(ma, r);
+    }
+    if (!WL) {
+        const float r = fmaf(pxb, qj, mulr(bwz, xb));
+        __stcg(rb, r);
+        mb = fmaxf(mb, r);
+    }
+}
+
+// slots jlo .. jhi - 1 of a staged chunk starting at slot j0; a full chunk
+// (jlo = j0, jhi = j0 + CH) runs unrolled at fixed offsets
+template <int G, int CH, bool VL, bool WL>
 __device__ __forceinline__ void s_outside_chunk(const float* su, const float* sv, const float* sw,
                                                 int j0, int jlo, int jhi, float fo,
                                                 const Child& cv, const Child& cw,
@@ -3481,33 +3513,41 @@ __device__ __forceinline__ void s_outside_chunk(const float* su, const float* sv
                                                 float& ma, float& sb, float& db, float& mb) {
     const float cstv = cv.code == -1 ? cv.ephi : 0.f, cstw = cw.code == -1 ? cw.ephi : 0.f;
     const float kv = bv.w * cv.ss, kw = bw.w * cw.ss;
-#pragma unroll 4
-    for (int j = jlo; j < jhi; ++j) {
-        const int k = (j - j0) * G;
-        const float o = su[k] * fo;
-        const float av = VL ? (cv.code == j ? cv.e1 : cstv) : sv[k] * cv.f;
-        const float aw = WL ? (cw.code == j ? cw.e1 : cstw) : sw[k] * cw.f;
-        const float qj = __ldg(qrow + j * G);
-        const float xa = mulr(o, fmaf(bw.z, aw, kw));
-        const float xb = mulr(o, fmaf(bv.z, av, kv));
-        sa = addr(sa, xa);
-        da = fmaf(xa, av, da);
-        sb = addr(sb, xb);
-        db = fmaf(xb, aw, db);
-        if (!VL) {
-            const float r = fmaf(pxa, qj, mulr(bv.z, xa));
-            __stcg(ra + j * G, r);
-            ma = fmaxf(ma, r);
-        }
-        if (!WL) {
-            const float r = fmaf(pxb, qj, mulr(bw.z, xb));
-            __stcg(rb + j * G, r);
-            mb = fmaxf(mb, r);
-        }
+    if (jlo == j0 && jhi == j0 + CH) {
+        const float* q0 = qrow + j0 * G;
+        float* a0 = VL ? nullptr : ra + j0 * G;
+        float* b0 = WL ? nullptr : rb + j0 * G;
+#pragma unroll
+        for (int k = 0; k < CH; ++k)
+            s_outside_slot<G, VL, WL>(su, sv, sw, k * G, j0 + k, fo, cv, cw, bv.z, bw.z, kv, kw,
+                                      cstv, cstw, __ldg(q0 + k * G), pxa, pxb,
+                                      VL ? nullptr : a0 + k * G, WL ? nullptr : b0 + k * G,
+                                      sa, da, ma, sb, db, mb);
+        return;
     }
+#pragma unroll 4
+    for (int j = jlo; j < jhi; ++j)
+        s_outside_slot<G, VL, WL>(su, sv, sw, (j - j0) * G, j, fo, cv, cw, bv.z, bw.z, kv, kw,
+                                  cstv, cstw, __ldg(qrow + j * G), pxa, pxb,
+                                  VL ? nullptr : ra + j * G, WL ? nullptr : rb + j * G, sa, da,
+                                  ma, sb, db, mb);
 }
 
 template <int G, bool VL, bool WL>
+__device__ __forceinline__ void s_inside_slot(const float* sv, const float* sw, int k, int j,
+                                              const Child& cv, const Child& cw, float bvz,
+                                              float bwz, float kv, float kw, float cstv,
+                                              float cstw, float qj, float* __restrict__ r,
+                                              float& dot, float& mx) {
+    const float av = VL ? (cv.code == j ? cv.e1 : cstv) : sv[k] * cv.f;
+    const float aw = WL ? (cw.code == j ? cw.e1 : cstw) : sw[k] * cw.f;
+    const float x = fmaf(bvz, av, kv) * fmaf(bwz, aw, kw);
+    __stcg(r, x);
+    dot = fmaf(qj, x, dot);
+    mx = fmaxf(mx, x);
+}
+
+template <int G, int CH, bool VL, bool WL>
 __device__ __forceinline__ void s_inside_chunk(const float* sv, const float* sw, int j0, int jlo,
                                                int jhi, const Child& cv, const Child& cw,
                                                const float4& bv, const float4& bw,
@@ -3515,16 +3555,19 @@ __device__ __forceinline__ void s_inside_chunk(const float* sv, const float* sw,
                                                float* __restrict__ row, float& dot, float& mx) {
     const float cstv = cv.code == -1 ? cv.ephi : 0.f, cstw = cw.code == -1 ? cw.ephi : 0.f;
     const float kv = bv.w * cv.ss, kw = bw.w * cw.ss;
-#pragma unroll 4
-    for (int j = jlo; j < jhi; ++j) {
-        const int k = (j - j0) * G;
-        const float av = VL ? (cv.code == j ? cv.e1 : cstv) : sv[k] * cv.f;
-        const float aw = WL ? (cw.code == j ? cw.e1 : cstw) : sw[k] * cw.f;
-        const float x = fmaf(bv.z, av, kv) * fmaf(bw.z, aw, kw);
-        __stcg(row + j * G, x);
-        dot = fmaf(__ldg(qrow + j * G), x, dot);
-        mx = fmaxf(mx, x);
+    if (jlo == j0 && jhi == j0 + CH) {
+        const float* q0 = qrow + j0 * G;
+        float* r0 = row + j0 * G;
+#pragma unroll
+        for (int k = 0; k < CH; ++k)
+            s_inside_slot<G, VL, WL>(sv, sw, k * G, j0 + k, cv, cw, bv.z, bw.z, kv, kw, cstv,
+                                     cstw, __ldg(q0 + k * G), r0 + k * G, dot, mx);
+        return;
     }
+#pragma unroll 4
+    for (int j = jlo; j < jhi; ++j)
+        s_inside_slot<G, VL, WL>(sv, sw, (j - j0) * G, j, cv, cw, bv.z, bw.z, kv, kw, cstv, cstw,
+                                 __ldg(qrow + j * G), row + j * G, dot, mx);
 }
 
 template <int G, int KIND, int CH>
@@ -3642,7 +3685,7 @@ __global__ void __launch_bounds__(kSWarps * 32, kSMinBlocks) k_items_ws(laml_bat
                 const int jlo = max(j0, 2), jhi = min(j0 + CH, C);
                 if (KIND == 1) {
 #define LAML_S_OUT(VL, WL)                                                                     \
-    s_outside_chunk<G, VL, WL>(su, sv, sw, j0, jlo, jhi, cur.fo, cv, cw, bv, bw, cur.s.qrow,  \
+    s_outside_chunk<G, CH, VL, WL>(su, sv, sw, j0, jlo, jhi, cur.fo, cv, cw, bv, bw, cur.s.qrow,  \
                                pxa, pxb, A.orow, B.orow, A.sumx, A.dot, A.mx, B.sumx, B.dot,  \
                                B.mx)
                     switch ((cv.row ? 0 : 1) | (cw.row ? 0 : 2)) {
@@ -3654,7 +3697,7 @@ __global__ void __launch_bounds__(kSWarps * 32, kSMinBlocks) k_items_ws(laml_bat
 #undef LAML_S_OUT
                 } else {
 #define LAML_S_IN(VL, WL) \
-    s_inside_chunk<G, VL, WL>(sv, sw, j0, jlo, jhi, cv, cw, bv, bw, cur.s.qrow, row, dot, mx)
+    s_inside_chunk<G, CH, VL, WL>(sv, sw, j0, jlo, jhi, cv, cw, bv, bw, cur.s.qrow, row, dot, mx)
                     switch ((cv.row ? 0 : 1) | (cw.row ? 0 : 2)) {
                         case 0: LAML_S_IN(false, false); break;
                         case 1: LAML_S_IN(true, false); break;
@@ -3738,15 +3781,18 @@ __global__ void __launch_bounds__(kSWarps * 32, kSMinBlocks) k_items_ws(laml_bat
 // state loop) with every byte in flight held in registers; at the 80
 // registers the outside item needs, 24 warps per SM keep DRAM about a third
 // busy.  Here a producer warp reads each slab's descriptors (32 / G items)
-// and has the bulk-copy engine move everything its consumer warp will read
-// into shared memory: the per-site scalars and branch terms into a slab
-// header (two per pair, so one fills while the other is read) and the rows,
-// CH state slots at a time, into a ring of S stages.  The consumer then
-// waits on mbarriers only, and the bytes in flight sit in shared memory.
+// and per-site scalars one slab ahead and stores them into a slab header
+// (two per pair, so one fills while the other is read), and has the
+// bulk-copy engine move the slab's rows, CH state slots at a time, into a
+// ring of S stages.  The consumer then waits on mbarriers only, and the row
+// bytes in flight sit in shared memory.  (Bulk copies issued from several
+// lanes of one instruction go out one lane at a time, so the per-site
+// scalars, 32 bytes per array and item, are moved by plain loads instead.)
 // Every thread's arithmetic is the per-thread kernels' (the same chunk loops
 // and child_finish), so the results are bitwise equal.
 //
-// Header of one item (ints; every bulk destination on a 16-byte boundary):
+// Header of one item (ints; written by the producer's plain stores, released
+// to the consumer by the header's mbarrier):
 //   [0, 12) descriptor, [12, 20) group descriptor, [20, 24) status, mode,
 //   the group's slot count, valid | staged << 1; [24, 28) leaf terms e1,
 //   ephi, es; [32, 36) and [36, 40) branch terms of v and w; from 40 twelve
@@ -3777,10 +3823,11 @@ __device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
                  : "memory");
 }
 
-// a phase wait that lets the hardware suspend the warp until the phase
-// completes (up to kPcSuspendNs per try) instead of spinning on it; bounded
-// by the batch's wait limit like mbar_wait
+// a phase wait that sleeps between tries (32 ns doubling to kPcSleepNs), so
+// that a warp waiting on its partner leaves the issue slots to the warps
+// with work; bounded by the batch's wait limit like mbar_wait
 constexpr uint32_t kPcSuspendNs = 20000;
+constexpr unsigned kPcSleepNs = 512;
 
 __device__ __forceinline__ bool mbar_try_wait_hint(uint64_t* bar, uint32_t parity) {
     uint32_t ok;
@@ -3801,7 +3848,10 @@ __device__ __forceinline__ bool pc_wait(const laml_batch& b, uint64_t* bar, uint
     }
     if (mbar_try_wait_hint(bar, parity)) return true;
     const unsigned long long t0 = gtimer();
+    unsigned ns = 32;
     for (uint32_t it = 0; it < (1u << 26); ++it) {
+        __nanosleep(ns);
+        if (ns < kPcSleepNs) ns <<= 1;
         if (mbar_try_wait_hint(bar, parity)) return true;
         if ((long long)(gtimer() - t0) > lim) break;
     }
@@ -3809,18 +3859,17 @@ __device__ __forceinline__ bool pc_wait(const laml_batch& b, uint64_t* bar, uint
     return false;
 }
 
-__device__ __forceinline__ bool aligned16(const void* p) {
-    return ((uintptr_t)p & 15u) == 0;
-}
-
 // the producer's view of one item of a slab: its descriptor, group, tree
-// state and leaf terms (read one slab ahead of its copies)
+// state and leaf terms (read one slab ahead), then this lane's site's
+// scalars and the branch terms (read while the slab before is issued)
 struct PItem {
     ItemDesc d;
     int4 G1, G2;
     int Cg, status, mode, tsite;
     float e1, ephi, es;
     bool valid, staged;
+    int sc[12];      // the header's per-site slots at this lane's site
+    float4 bt;       // lane 0: v's branch terms, lane 1: w's
 };
 
 template <int KIND>
@@ -3843,40 +3892,38 @@ __device__ __forceinline__ void pc_fetch(const laml_batch& b, const int32_t* des
     t.staged = active && t.mode != LAML_MODE_LOG;
 }
 
-// copy k of an item's header (0 <= k < 14): source and bytes (0: none)
+// slot k of the header at lane l's site: parent's out_h, out_x; v's in_h
+// (its code when a leaf), in_x, in_dot; w's likewise; root_lr, root_x;
+// site_C, site_sumq
 template <int G, int KIND>
-__device__ __forceinline__ uint32_t pc_hdr_src(const laml_batch& b, const PItem& t, int k,
-                                               const void*& src, int& dst_int) {
+__device__ __forceinline__ void pc_scalars(const laml_batch& b, int l, PItem& t) {
+    if (!t.staged) return;
     const ItemDesc& d = t.d;
-    const int tsite = t.tsite, sb = t.G1.y, code_base = t.G2.x, kpad = t.G2.y;
-    const int sg = d.g * G;
+    const int s = d.g * G + l;
     const bool vl = d.flags & 1, wl = d.flags & 2;
-    src = nullptr;
-    dst_int = 0;
-    if (!t.staged) return 0u;
-    const uint32_t s4 = G * 4u;
-    switch (k) {
-        case 0: if (KIND != 1) return 0u; src = b.out_h + (int64_t)d.u_srow + sg; dst_int = 40; return s4;
-        case 1: if (KIND != 1) return 0u; src = b.out_x + (int64_t)d.u_srow + sg; dst_int = 40 + G; return s4;
-        case 2:
-            dst_int = 40 + 2 * G;
-            if (vl) { src = b.codes + code_base + (int64_t)d.v_ref * kpad + sg; return G * 2u; }
-            src = b.in_h + (int64_t)d.v_srow + sg; return s4;
-        case 3: if (vl) return 0u; src = b.in_x + (int64_t)d.v_srow + sg; dst_int = 40 + 3 * G; return s4;
-        case 4: if (vl) return 0u; src = b.in_dot + (int64_t)d.v_srow + sg; dst_int = 40 + 4 * G; return s4;
-        case 5:
-            dst_int = 40 + 5 * G;
-            if (wl) { src = b.codes + code_base + (int64_t)d.w_ref * kpad + sg; return G * 2u; }
-            src = b.in_h + (int64_t)d.w_srow + sg; return s4;
-        case 6: if (wl) return 0u; src = b.in_x + (int64_t)d.w_srow + sg; dst_int = 40 + 6 * G; return s4;
-        case 7: if (wl) return 0u; src = b.in_dot + (int64_t)d.w_srow + sg; dst_int = 40 + 7 * G; return s4;
-        case 8: if (KIND != 1) return 0u; src = b.root_lr + (int64_t)tsite + sg; dst_int = 40 + 8 * G; return s4;
-        case 9: if (KIND != 1) return 0u; src = b.root_x + (int64_t)tsite + sg; dst_int = 40 + 9 * G; return s4;
-        case 10: src = b.site_C + sb; dst_int = 40 + 10 * G; return s4;
-        case 11: src = b.site_sumq + sb; dst_int = 40 + 11 * G; return s4;
-        case 12: src = b.nd_bt + 4 * (int64_t)d.v; dst_int = 32; return 16u;
-        default: src = b.nd_bt + 4 * (int64_t)d.w; dst_int = 36; return 16u;
+    if (KIND == 1) {
+        t.sc[0] = __ldcg(b.out_h + (int64_t)d.u_srow + s);
+        t.sc[1] = __ldcg(b.out_x + (int64_t)d.u_srow + s);
+        t.sc[8] = __float_as_int(__ldcg(b.root_lr + (int64_t)t.tsite + s));
+        t.sc[9] = __ldcg(b.root_x + (int64_t)t.tsite + s);
     }
+    if (vl) {
+        t.sc[2] = __ldg(b.codes + t.G2.x + (int64_t)d.v_ref * t.G2.y + s);
+    } else {
+        t.sc[2] = __ldcg(b.in_h + (int64_t)d.v_srow + s);
+        t.sc[3] = __ldcg(b.in_x + (int64_t)d.v_srow + s);
+        t.sc[4] = __float_as_int(__ldcg(b.in_dot + (int64_t)d.v_srow + s));
+    }
+    if (wl) {
+        t.sc[5] = __ldg(b.codes + t.G2.x + (int64_t)d.w_ref * t.G2.y + s);
+    } else {
+        t.sc[5] = __ldcg(b.in_h + (int64_t)d.w_srow + s);
+        t.sc[6] = __ldcg(b.in_x + (int64_t)d.w_srow + s);
+        t.sc[7] = __float_as_int(__ldcg(b.in_dot + (int64_t)d.w_srow + s));
+    }
+    t.sc[10] = __ldg(b.site_C + t.G1.y + l);
+    t.sc[11] = __float_as_int(__ldg(b.site_sumq + t.G1.y + l));
+    if (l < 2) t.bt = load_bt(b, l == 0 ? d.v : d.w);
 }
 
 // the slab's largest staged slot count over CH (every lane of the warp)
@@ -3886,7 +3933,8 @@ __device__ __forceinline__ int pc_chunks(bool staged, int Cg) {
     return (m + CH - 1) / CH;
 }
 
-// producer warp of a pair: headers and row chunks of the pair's slabs
+// producer warp of a pair: headers (plain stores) and row chunks (bulk
+// copies) of the pair's slabs
 template <int G, int KIND, int CH>
 __device__ void pc_produce(const laml_batch& b, const int32_t* desc, int64_t n, bool rs,
                            int64_t pid, int64_t npairs, float* ring, int* hdr, uint64_t* bars) {
@@ -3898,12 +3946,16 @@ __device__ void pc_produce(const laml_batch& b, const int32_t* desc, int64_t n, 
     uint64_t* hempty = bars + 2 * S + 2;
     const int lane32 = threadIdx.x & 31, sub = lane32 / G, l = lane32 % G;
     const int64_t nslab = (n + P - 1) / P;
-    int64_t q = 0, kh = 0;   // stages issued, headers issued
+    int64_t q = 0, kh = 0;   // stages issued, headers written
     PItem t, tn;
-    if (pid < nslab) pc_fetch<KIND>(b, desc, n, rs, pid * P + sub, t);
+    if (pid < nslab) {
+        pc_fetch<KIND>(b, desc, n, rs, pid * P + sub, t);
+        pc_scalars<G, KIND>(b, l, t);
+    }
     for (int64_t slab = pid; slab < nslab; slab += npairs) {
-        // the next slab's items load while this one's copies go out
-        if (slab + npairs < nslab) pc_fetch<KIND>(b, desc, n, rs, (slab + npairs) * P + sub, tn);
+        const bool more = slab + npairs < nslab;
+        // the next slab's items load while this one goes out
+        if (more) pc_fetch<KIND>(b, desc, n, rs, (slab + npairs) * P + sub, tn);
         // header kh & 1 of the pair: wait until its consumer has read it
         const int h = (int)(kh & 1);
         if (!pc_wait(b, hempty + h, (uint32_t)((kh >> 1) & 1) ^ 1u)) break;
@@ -3917,28 +3969,20 @@ __device__ void pc_produce(const laml_batch& b, const int32_t* desc, int64_t n, 
         if (l == 5) reinterpret_cast<int4*>(H)[5] =
             make_int4(t.status, t.mode, t.Cg, (t.valid ? 1 : 0) | (t.staged ? 2 : 0));
         if (l == 6) reinterpret_cast<float4*>(H)[6] = make_float4(t.e1, t.ephi, t.es, 0.f);
-        // the header's copies: lane l issues copies l and l + G (G = 8)
-        constexpr int NC = (14 + G - 1) / G;
-        const void* hs[NC];
-        int hd[NC];
-        uint32_t hb[NC], mine = 0;
+        if (t.staged) {
+            if (l < 2) reinterpret_cast<float4*>(H)[8 + l] = t.bt;
 #pragma unroll
-        for (int r = 0; r < NC; ++r) {
-            const int c = r * G + l;
-            hb[r] = c < 14 ? pc_hdr_src<G, KIND>(b, t, c, hs[r], hd[r]) : 0u;
-            if (hb[r] && !aligned16(hs[r])) {
-                atomicCAS(b.error, 0, LAML_ERR_ARG);
-                hb[r] = 0u;
+            for (int k = 0; k < 12; ++k) {
+                if (k == 2 && (d.flags & 1))
+                    reinterpret_cast<int16_t*>(H + 40 + 2 * G)[l] = (int16_t)t.sc[2];
+                else if (k == 5 && (d.flags & 2))
+                    reinterpret_cast<int16_t*>(H + 40 + 5 * G)[l] = (int16_t)t.sc[5];
+                else
+                    H[40 + k * G + l] = t.sc[k];
             }
-            mine += hb[r];
         }
-        const uint32_t tot = __reduce_add_sync(kFull, mine);
         __syncwarp();
-        if (lane32 == 0) mbar_arrive_tx(hfull + h, tot);
-        __syncwarp();
-#pragma unroll
-        for (int r = 0; r < NC; ++r)
-            if (hb[r]) bulk_g2s(H + hd[r], hs[r], hb[r], hfull + h);
+        if (lane32 == 0) mbar_arrive(hfull + h);   // releases the header's stores
         ++kh;
         // the rows, CH slots per stage: lane l < NR of each item copies row
         // l -- the parent's outside row (outside only), then the internal
@@ -3972,16 +4016,16 @@ __device__ void pc_produce(const laml_batch& b, const int32_t* desc, int64_t n, 
             ++q;
         }
         if (!ok) break;
-        t = tn;
+        if (more) {
+            t = tn;
+            pc_scalars<G, KIND>(b, l, t);
+        }
     }
     // every copy this warp started lands before the block may exit: the
-    // last header of each buffer and the last S stages (bounded waits)
-    if (lane32 == 0) {
-        for (int64_t kk = (kh > 2 ? kh - 2 : 0); kk < kh; ++kk)
-            mbar_drain(hfull + (kk & 1), (uint32_t)((kk >> 1) & 1));
+    // last S stages (bounded waits)
+    if (lane32 == 0)
         for (int64_t qq = (q > S ? q - S : 0); qq < q; ++qq)
             mbar_drain(full + (qq % S), (uint32_t)((qq / S) & 1));
-    }
     __syncwarp();
 }
 
@@ -4132,7 +4176,7 @@ __device__ void pc_consume(const laml_batch& b, const int32_t* desc, int64_t n, 
                 const int jlo = max(j0, 2), jhi = min(j0 + CH, C);
                 if (KIND == 1) {
 #define LAML_P_OUT(VL, WL)                                                                     \
-    s_outside_chunk<G, VL, WL>(su, sv, sw, j0, jlo, jhi, cur.fo, cv, cw, bv, bw, cur.s.qrow,  \
+    s_outside_chunk<G, CH, VL, WL>(su, sv, sw, j0, jlo, jhi, cur.fo, cv, cw, bv, bw, cur.s.qrow,  \
                                pxa, pxb, A.orow, B.orow, A.sumx, A.dot, A.mx, B.sumx, B.dot,  \
                                B.mx)
                     switch ((cv.row ? 0 : 1) | (cw.row ? 0 : 2)) {
@@ -4144,7 +4188,7 @@ __device__ void pc_consume(const laml_batch& b, const int32_t* desc, int64_t n, 
 #undef LAML_P_OUT
                 } else {
 #define LAML_P_IN(VL, WL) \
-    s_inside_chunk<G, VL, WL>(sv, sw, j0, jlo, jhi, cv, cw, bv, bw, cur.s.qrow, row, dot, mx)
+    s_inside_chunk<G, CH, VL, WL>(sv, sw, j0, jlo, jhi, cv, cw, bv, bw, cur.s.qrow, row, dot, mx)
                     switch ((cv.row ? 0 : 1) | (cw.row ? 0 : 2)) {
                         case 0: LAML_P_IN(false, false); break;
                         case 1: LAML_P_IN(true, false); break;
@@ -4534,16 +4578,10 @@ int validate(const laml_batch* b) {
         laml::set_error("laml_batch: wide_chunk must be 0, 8 or 16");
         return LAML_ERR_ARG;
     }
-    if (b->wide_pc) {   // the bulk copies' sources start on 16-byte boundaries
-        const void* arr[] = {b->in_part, b->out_part, b->in_h, b->in_x, b->in_dot, b->out_h,
-                             b->out_x, b->root_lr, b->root_x, b->site_C, b->site_sumq,
-                             b->codes, b->nd_bt};
-        for (const void* p : arr)
-            if (((uintptr_t)p & 15u) != 0) {
-                laml::set_error("laml_batch: wide_pc needs 16-byte aligned partial, scalar, "
-                                "code and branch-term arrays");
-                return LAML_ERR_ARG;
-            }
+    if (b->wide_pc && ((((uintptr_t)b->in_part) | ((uintptr_t)b->out_part)) & 15u) != 0) {
+        // the bulk copies of rows start on 16-byte boundaries
+        laml::set_error("laml_batch: wide_pc needs 16-byte aligned in_part and out_part");
+        return LAML_ERR_ARG;
     }
     return LAML_OK;
 }
