@@ -728,6 +728,18 @@ def main():
                     "persistent": "k_em_persistent",
                     "levels": "k_items per level, k_mstep"}[args.path], 1)
     llh_now = b.work["tr_llh"].cpu().numpy()
+    with torch.cuda.stream(stream):
+        # the other EM-iteration drivers on the same batch (after the timed
+        # region): one cooperative persistent launch, or the per-level
+        # launches without the graph
+        ms_paths = {}
+        for p_ in ("persistent", "levels"):
+            if p_ != args.path:
+                ms_paths[p_] = pass_ms(lambda p_=p_: b.em_iterations(
+                    1, rel_tol=-1.0, max_iters=1 << 30, persistent=p_ == "persistent"), reps=3)
+        if args.path != "graph":
+            g2 = b.em_graph(1, rel_tol=-1.0, max_iters=1 << 30, persistent=False)
+            ms_paths["graph"] = pass_ms(lambda: b.launch_graph(g2), reps=3)
 
     # e2e: public API from host strings / matrix to host results
     e2e = None
@@ -833,6 +845,7 @@ def main():
             "gpu_launches": args.steps * (1 if args.path == "persistent" else
                                           b.sizes["n_in_levels"] + b.sizes["n_out_levels"] + 4),
             "path": args.path,
+            "ms_per_em_iteration_other_paths": ms_paths,
             "wall_s_timed": t1 - t0,
             "llh_mean": float(np.mean(llh_now)),
             "parity": parity,

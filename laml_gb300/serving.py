@@ -72,7 +72,9 @@ class Reply:
         return self.t_done - self.t_submit
 
 
-@dataclass
+# the server's own records compare by identity: their fields hold arrays,
+# and a list of them is searched with == (list.remove, in)
+@dataclass(eq=False)
 class _Job:
     req: Request
     tree: EncodedTree
@@ -83,7 +85,7 @@ class _Job:
     t_admit: float = 0.0
 
 
-@dataclass
+@dataclass(eq=False)
 class _Cohort:
     jobs: List[_Job]
     batch: DeviceBatch
