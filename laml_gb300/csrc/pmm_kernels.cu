@@ -62,6 +62,10 @@ constexpr unsigned kFull = 0xffffffffu;
 #define LAML_CHUNK 4
 #endif
 constexpr int kChunk = LAML_CHUNK;   // states loaded ahead per step of a state loop
+#ifndef LAML_OCHUNK
+#define LAML_OCHUNK LAML_CHUNK
+#endif
+constexpr int kOChunk = LAML_OCHUNK;   // the same for the outside items' state loop
 #ifndef LAML_MINB
 #define LAML_MINB 4
 #endif
@@ -69,10 +73,10 @@ constexpr int kChunk = LAML_CHUNK;   // states loaded ahead per step of a state 
 #define LAML_MINB_IN 8   // resident blocks per SM asked of the other item kernels (64 registers)
 #endif
 #ifndef LAML_MINB_OUT
-#define LAML_MINB_OUT 6   // resident blocks per SM asked of the outside kernel (85 registers)
+#define LAML_MINB_OUT 8   // resident blocks per SM asked of the outside kernel (64 registers)
 #endif
 constexpr int kMstepStage = 2048;    // branches of a tree staged in shared memory by the M-step
-constexpr int kOStash = 24;          // words per thread the outside item parks in shared memory
+constexpr int kOStash = 34;          // words per thread the outside item parks in shared memory
 
 // ---------------------------------------------------------------------------
 // small helpers
@@ -931,17 +935,17 @@ __device__ __forceinline__ void outside_states(const float* __restrict__ urow, f
         }
     };
     int j = 2;
-    for (; j + kChunk <= C; j += kChunk) {
-        float ou[kChunk], av[kChunk], aw[kChunk], qv[kChunk];
+    for (; j + kOChunk <= C; j += kOChunk) {
+        float ou[kOChunk], av[kOChunk], aw[kOChunk], qv[kOChunk];
 #pragma unroll
-        for (int k = 0; k < kChunk; ++k) {
+        for (int k = 0; k < kOChunk; ++k) {
             ou[k] = __ldcg(urow + (j + k) * G) * fo;
             av[k] = slot_val<G, VL>(rv, cv.f, cv.code, cv.e1, cstv, j + k);
             aw[k] = slot_val<G, WL>(rw, cw.f, cw.code, cw.e1, cstw, j + k);
             qv[k] = __ldg(qrow + (j + k) * G);
         }
 #pragma unroll
-        for (int k = 0; k < kChunk; ++k) step(ou[k], av[k], aw[k], qv[k], j + k);
+        for (int k = 0; k < kOChunk; ++k) step(ou[k], av[k], aw[k], qv[k], j + k);
     }
     for (; j < C; ++j)
         step(__ldcg(urow + j * G) * fo, slot_val<G, VL>(rv, cv.f, cv.code, cv.e1, cstv, j),
@@ -1111,6 +1115,17 @@ __device__ void outside_item_d(const laml_batch& b, const ItemDesc& d, int lane,
     SiteCtx s;
     GroupCtx gc;
     const bool live = act && site_ctx_d<G>(b, d, lane, true, s, gc);
+    // the descriptor and site fields the item needs after its state loop
+    // wait in this thread's shared-memory column (AS), not in registers
+    constexpr int S_ = kItemsBlock;
+    float* sq_ = AS ? sm + threadIdx.x : nullptr;
+    if constexpr (AS) {
+        sq_[24 * S_] = __int_as_float(d.v); sq_[25 * S_] = __int_as_float(d.w);
+        sq_[26 * S_] = __int_as_float(d.tree); sq_[27 * S_] = __int_as_float(d.g);
+        sq_[28 * S_] = __int_as_float(d.flags); sq_[29 * S_] = __int_as_float(d.v_ref);
+        sq_[30 * S_] = __int_as_float(d.w_ref); sq_[31 * S_] = __int_as_float(s.site);
+        sq_[32 * S_] = __int_as_float(s.ds); sq_[33 * S_] = __int_as_float(s.goff);
+    }
     if (live && lane == 0) {   // the parent's outside row and the children's rows into L2
         const uint32_t bytes = (uint32_t)s.C * G * sizeof(float);
         prefetch_l2(b.out_part + (int64_t)d.u_prow8 * 8 + s.goff, bytes);
@@ -1148,7 +1163,6 @@ __device__ void outside_item_d(const laml_batch& b, const ItemDesc& d, int lane,
         B.sumx = B.dot = B.mx = 0.f;
         A.orow = cv.row ? b.out_part + (int64_t)d.v_ref * 8 + s.goff + lane : nullptr;
         B.orow = cw.row ? b.out_part + (int64_t)d.w_ref * 8 + s.goff + lane : nullptr;
-        const int64_t t = __ldg(b.tr_site_base + s.tree) + s.site;
         if constexpr (AS) {
             // what child_finish needs after the state loop waits in this
             // thread's shared-memory column, read back through volatile loads,
@@ -1172,24 +1186,35 @@ __device__ void outside_item_d(const laml_batch& b, const ItemDesc& d, int lane,
                 default: outside_states<G, true, true>(urow, fo, cv, cw, bv, bw, s.qrow, s.C, A, B); break;
             }
             const volatile float* vp = sp;
+            const int dflags = __float_as_int(vp[28 * S]);
             Child cv2, cw2;   // child_finish reads row only as "leaf or not"
             cv2.s0 = vp[0 * S]; cv2.ss = vp[1 * S]; cv2.D = vp[2 * S];
             cv2.X = __float_as_int(vp[3 * S]); cv2.code = __float_as_int(vp[4 * S]);
-            cv2.row = (d.flags & 1) ? nullptr : b.in_part;
+            cv2.row = (dflags & 1) ? nullptr : b.in_part;
             cw2.s0 = vp[5 * S]; cw2.ss = vp[6 * S]; cw2.D = vp[7 * S];
             cw2.X = __float_as_int(vp[8 * S]); cw2.code = __float_as_int(vp[9 * S]);
-            cw2.row = (d.flags & 2) ? nullptr : b.in_part;
+            cw2.row = (dflags & 2) ? nullptr : b.in_part;
             const float4 bv2 = make_float4(vp[10 * S], vp[11 * S], vp[22 * S], vp[12 * S]);
             const float4 bw2 = make_float4(vp[13 * S], vp[14 * S], vp[23 * S], vp[15 * S]);
             A.x0 = vp[16 * S]; A.xs = vp[17 * S]; A.X = __float_as_int(vp[18 * S]);
             B.x0 = vp[19 * S]; B.xs = vp[20 * S]; B.X = __float_as_int(vp[21 * S]);
-            A.orow = (d.flags & 1) ? nullptr : b.out_part + (int64_t)d.v_ref * 8 + s.goff + lane;
-            B.orow = (d.flags & 2) ? nullptr : b.out_part + (int64_t)d.w_ref * 8 + s.goff + lane;
+            const int dv = __float_as_int(vp[24 * S]), dw = __float_as_int(vp[25 * S]);
+            SiteCtx s2;   // child_finish reads the site, its tree and dataset
+            s2.tree = __float_as_int(vp[26 * S]);
+            s2.site = __float_as_int(vp[31 * S]);
+            s2.ds = __float_as_int(vp[32 * S]);
+            const int64_t ro = (int64_t)__float_as_int(vp[33 * S]) + lane;   // group offset + lane
+            A.orow = (dflags & 1) ? nullptr
+                                  : b.out_part + (int64_t)__float_as_int(vp[29 * S]) * 8 + ro;
+            B.orow = (dflags & 2) ? nullptr
+                                  : b.out_part + (int64_t)__float_as_int(vp[30 * S]) * 8 + ro;
+            const int64_t t = __ldg(b.tr_site_base + s2.tree) + s2.site;
             const float lroot = __ldcg(b.root_lr + t);
             const int xroot = __ldcg(b.root_x + t);
-            child_finish<G>(b, s, d.v, cv2, bv2, A, want_post, lroot, xroot, cv_);
-            child_finish<G>(b, s, d.w, cw2, bw2, B, want_post, lroot, xroot, cw_);
+            child_finish<G>(b, s2, dv, cv2, bv2, A, want_post, lroot, xroot, cv_);
+            child_finish<G>(b, s2, dw, cw2, bw2, B, want_post, lroot, xroot, cw_);
         } else {
+            const int64_t t = __ldg(b.tr_site_base + s.tree) + s.site;
             switch ((cv.row ? 0 : 1) | (cw.row ? 0 : 2)) {   // warp-uniform: items are sorted by it
                 case 0: outside_states<G, false, false>(urow, fo, cv, cw, bv, bw, s.qrow, s.C, A, B); break;
                 case 1: outside_states<G, true, false>(urow, fo, cv, cw, bv, bw, s.qrow, s.C, A, B); break;
@@ -1210,7 +1235,14 @@ __device__ void outside_item_d(const laml_batch& b, const ItemDesc& d, int lane,
             cw_[k] += __shfl_xor_sync(kFull, cw_[k], off);
         }
     }
-    if (act && lane == 0 && __ldcg(b.tr_status + d.tree) == LAML_TREE_ACTIVE) {
+    if constexpr (AS) {
+        const volatile float* vq = sq_;
+        const int tr = __float_as_int(vq[26 * S_]), g = __float_as_int(vq[27 * S_]);
+        if (act && lane == 0 && __ldcg(b.tr_status + tr) == LAML_TREE_ACTIVE) {
+            write_counts<G>(b, tr, __float_as_int(vq[24 * S_]), g, cv_);
+            write_counts<G>(b, tr, __float_as_int(vq[25 * S_]), g, cw_);
+        }
+    } else if (act && lane == 0 && __ldcg(b.tr_status + d.tree) == LAML_TREE_ACTIVE) {
         write_counts<G>(b, d.tree, d.v, d.g, cv_);
         write_counts<G>(b, d.tree, d.w, d.g, cw_);
     }
@@ -4308,10 +4340,12 @@ __device__ __forceinline__ void for_items(const laml_batch& b, const int32_t* it
     }
     constexpr int IPW = 32 / G;
     const int lane32 = threadIdx.x & 31, lane = lane32 % G, sub = lane32 / G;
-    const int64_t nw = (n + IPW - 1) / IPW;
-    for (int64_t wi = gwarp; wi < nw; wi += nwarps) {
-        const int64_t it = wi * IPW + sub;
-        const bool act = it < n;
+    // a level's items are int32-indexed (the plan's level offsets are int32)
+    const int n32 = (int)n;
+    const int nw = (n32 + IPW - 1) / IPW;
+    for (int wi = gwarp; wi < nw; wi += nwarps) {
+        const int it = wi * IPW + sub;
+        const bool act = it < n32;
         if constexpr (KIND <= 1 || KIND == 5) {   // descriptor-driven inside / outside
             const ItemDesc d = load_desc(desc, act ? it : 0);
             if constexpr (KIND == 0) {
