@@ -43,7 +43,7 @@ METRIC = "EM iters/s & node-site updates/s, batched+served vs plain GPU; p50/p99
 # dram__bytes_write.sum summed over one pass of the first 128 candidates
 # (`--passes-only --trees 128 --wide-chunk 0`), times 4 -- the full batch holds
 # 4x the same-shaped rows -- over the pass's launches (outside 25, inside 24)
-TRAFFIC_PER_LAUNCH = {"outside": 170.3e6, "inside": 119.6e6}
+TRAFFIC_PER_LAUNCH = {"outside": 175.9e6, "inside": 119.6e6}
 UNIT = "tree-EM-iters/s"
 WORKLOAD = "nni512"
 
@@ -569,6 +569,8 @@ def main():
     ap.add_argument("--wide-pc", type=int, default=-1,
                     help="wide levels on producer/consumer warp pairs: 1 on, 0 off "
                          "(-1: the autotuner's choice)")
+    ap.add_argument("--no-other-paths", action="store_true",
+                    help="skip timing the other EM-iteration drivers after the timed region")
     ap.add_argument("--e2e-steps", type=int, default=2)
     ap.add_argument("--ref-trees", type=int, default=16)
     ap.add_argument("--no-cpu", action="store_true")
@@ -733,11 +735,11 @@ def main():
         # region): one cooperative persistent launch, or the per-level
         # launches without the graph
         ms_paths = {}
-        for p_ in ("persistent", "levels"):
+        for p_ in (() if args.no_other_paths else ("persistent", "levels")):
             if p_ != args.path:
                 ms_paths[p_] = pass_ms(lambda p_=p_: b.em_iterations(
                     1, rel_tol=-1.0, max_iters=1 << 30, persistent=p_ == "persistent"), reps=3)
-        if args.path != "graph":
+        if args.path != "graph" and not args.no_other_paths:
             g2 = b.em_graph(1, rel_tol=-1.0, max_iters=1 << 30, persistent=False)
             ms_paths["graph"] = pass_ms(lambda: b.launch_graph(g2), reps=3)
 
