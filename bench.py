@@ -457,6 +457,15 @@ def run_workload(args):
                      "grad_nu": float(nu.grad[0].item()), "grad_phi": float(phi.grad[0].item())})
     else:   # large50k: EM to convergence
         with torch.cuda.stream(stream):
+            # untimed warm-up: the EM graph run_em replays (instantiated and
+            # cached here) and a first launch of the M-step and likelihood
+            # kernels; the parameters are restored before the timed run
+            b.em_graph(8, rel_tol=1e-8, max_iters=2000, persistent=False)
+            d0 = b.v["nd_d"].clone()
+            b.log_likelihood()
+            b.mstep()
+            b.set_params(d=d0, nu=[nu0], phi=[phi0])
+            stream.synchronize()
             t0 = time.perf_counter()
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             e0.record(stream)

@@ -72,9 +72,13 @@ constexpr int kOChunk = LAML_OCHUNK;   // the same for the outside items' state 
 #ifndef LAML_MINB_IN
 #define LAML_MINB_IN 8   // resident blocks per SM asked of the other item kernels (64 registers)
 #endif
-#ifndef LAML_MINB_OUT
-#define LAML_MINB_OUT 8   // resident blocks per SM asked of the outside kernel (64 registers)
-#endif
+// resident blocks per SM asked of the wide outside kernel: 8 (64 registers)
+// for batches of up to kOutBlocksStates states per site, 6 (80 registers)
+// above -- longer state loops reload more of what 64 registers spill and
+// leave less L1 beside 8 blocks' stashes (measured: 512 candidates of 40
+// sites and 7-52 states, outside pass 1.85 ms at 8 blocks, 1.98 at 6; one
+// 50,000-leaf tree of 300 sites and 22-102 states, 2.81 ms at 8, 2.27 at 6)
+constexpr int kOutBlocksStates = 64;
 constexpr int kMstepStage = 2048;    // branches of a tree staged in shared memory by the M-step
 constexpr int kOStash = 34;          // words per thread the outside item parks in shared memory
 
@@ -4367,8 +4371,8 @@ __device__ __forceinline__ void for_items(const laml_batch& b, const int32_t* it
     }
 }
 
-template <int G, int KIND>
-__global__ void __launch_bounds__(kItemsBlock, KIND == 1 ? LAML_MINB_OUT : LAML_MINB_IN) k_items(laml_batch b, const int32_t* items, int64_t n,
+template <int G, int KIND, int MB = KIND == 1 ? 8 : LAML_MINB_IN>
+__global__ void __launch_bounds__(kItemsBlock, MB) k_items(laml_batch b, const int32_t* items, int64_t n,
                                                    int want_post, int respect_status,
                                                    const int32_t* desc) {
     const int gwarp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -4777,7 +4781,12 @@ int launch_items(const laml_batch& b, const int32_t* items, int64_t n, int kind,
     const size_t sm1 = sizeof(float) * as_words<1>() * kItemsBlock;
     switch (kind) {
         case 0: k_items<G, 0><<<(unsigned)blocks, kItemsBlock, sm0, st>>>(b, items, n, want_post, respect_status, desc); break;
-        case 1: k_items<G, 1><<<(unsigned)blocks, kItemsBlock, sm1, st>>>(b, items, n, want_post, respect_status, desc); break;
+        case 1:
+            if (b.max_states > 0 && b.max_states <= kOutBlocksStates)
+                k_items<G, 1, 8><<<(unsigned)blocks, kItemsBlock, sm1, st>>>(b, items, n, want_post, respect_status, desc);
+            else
+                k_items<G, 1, 6><<<(unsigned)blocks, kItemsBlock, sm1, st>>>(b, items, n, want_post, respect_status, desc);
+            break;
         case 2: k_items<G, 2><<<(unsigned)blocks, kItemsBlock, 0, st>>>(b, items, n, want_post, respect_status, desc); break;
         case 3: k_items<G, 3><<<(unsigned)blocks, kItemsBlock, 0, st>>>(b, items, n, want_post, respect_status, desc); break;
         case 5: k_items<G, 5><<<(unsigned)blocks, kItemsBlock, 0, st>>>(b, items, n, want_post, respect_status, desc); break;
