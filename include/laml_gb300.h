@@ -190,6 +190,14 @@ typedef struct laml_plan_output {
     /* per global group, 8 int32: {group_off, first site (global), q offset,
      * dataset}, {code offset, sites_pad, real sites, 0} */
     int32_t* grp_desc;
+    /* optional, instead of in_items / out_items (left NULL) when every
+     * dataset of the batch has the same group count NG: the internal nodes
+     * in the schedule's order, [internal nodes] each.  Item k of a level
+     * with item offset o and c nodes is node lnodes[o / NG + (k - o) % c]
+     * of group (k - o) / c -- laml_plan_descriptors expands them on the
+     * device (4 bytes a node to copy instead of 8 a (node, group) item). */
+    int32_t* in_lnodes;
+    int32_t* out_lnodes;
 } laml_plan_output;
 
 int laml_plan_measure(const laml_plan_input* in, laml_plan_sizes* sizes);
@@ -318,6 +326,10 @@ typedef struct laml_batch {
      * bitwise the same.  in_part and out_part must start on 16-byte
      * boundaries. */
     int32_t wide_pc;
+    /* laml_plan_output's in_lnodes / out_lnodes on the device, read by
+     * laml_plan_descriptors when in_items / out_items are NULL (every
+     * dataset with the same group count) */
+    const int32_t *in_lnodes, *out_lnodes;
 } laml_batch;
 
 /* A tree's partials are FP32 values with power-of-two exponents (linear)
@@ -342,7 +354,8 @@ typedef struct laml_batch {
 int laml_supported_group_sites(void);
 
 /* Builds in_desc / out_desc / grp_desc (laml_plan_output's layout, byte for
- * byte) on the device from the batch's node arrays, items and dataset
+ * byte) on the device from the batch's node arrays, items (or level node
+ * lists, in_lnodes / out_lnodes, when the items are NULL) and dataset
  * tables, so a caller uploads the node arrays only (the descriptors are 48
  * bytes per item, most of a batch's host->device bytes otherwise).  Outputs
  * are device buffers of 12 * n_in_items, 12 * n_out_items and

@@ -57,7 +57,7 @@ PLAN_OUT_FIELDS = ["tr_node_base", "tr_root", "tr_quirk", "tr_site_base", "tr_cn
                    "tr_post_base", "nd_tree", "nd_c0", "nd_c1", "nd_parent", "nd_sib",
                    "nd_leafrow", "nd_prow", "nd_srow", "in_level_off", "in_items",
                    "out_level_off", "out_items", "root_items", "in_desc", "out_desc",
-                   "grp_desc"]
+                   "grp_desc", "in_lnodes", "out_lnodes"]
 
 
 class PlanOutput(C.Structure):
@@ -91,6 +91,7 @@ BATCH_FIELDS = [
     ("tr_leaf", vp), ("nd_uorder", vp), ("nd_uwork", vp),
     ("plan_part_floats", i64), ("plan_scalar_len", i64), ("tr_mstats", vp),
     ("wide_chunk", i32), ("wait_limit_ns", i64), ("nd_lbfgs", vp), ("wide_pc", i32),
+    ("in_lnodes", vp), ("out_lnodes", vp),
 ]
 
 

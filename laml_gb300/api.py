@@ -43,9 +43,11 @@ def score_candidates(newicks: Sequence[str], rows: dict, Q, leaf_order: Sequence
                      rng: Optional[random.Random] = None,
                      pipeline: Optional[int] = None) -> ScoreResult:
     """``pipeline`` parts: the candidates are cut into that many contiguous
-    parts, each its own device batch on its own stream; a worker thread
-    parses, plans and uploads part k+1 while part k iterates, so the host
-    work of all parts but the first overlaps the device.  Each tree's EM is
+    parts of growing size (part k holds a share k + 1), each its own device
+    batch on its own stream; a worker thread parses, plans and uploads part
+    k+1 while part k iterates, so the host work of all parts but the first
+    -- the smallest -- overlaps the device, and the matrix is encoded on a
+    second thread while the first part's newicks are parsed.  Each tree's EM is
     independent of the others in its batch, so the parts give each tree the
     result it has in one batch (up to FP32 summation order when a level's
     width crosses the wide/narrow rule).  Default: 2 parts from 256
@@ -69,12 +71,17 @@ def score_candidates(newicks: Sequence[str], rows: dict, Q, leaf_order: Sequence
         group_sites = t["group_sites"] if group_sites is None else group_sites
         wide_chunk = t["wide_chunk"] if wide_chunk is None else wide_chunk
         wide_pc = bool(t.get("wide_pc", False)) if wide_pc is None else wide_pc
-    ds = dataset_from_rows(rows, Q, leaf_order, compat, group_sites)
     rng = rng if rng is not None else random
     T = len(newicks)
     parts = pipeline if pipeline is not None else (2 if T >= 256 else 1)
     parts = max(1, min(int(parts), T))
-    bounds = [T * k // parts for k in range(parts + 1)]
+    # part k holds a share k + 1 of the candidates: the first part's host
+    # work, the only host work not hidden behind a part's EM, is the smallest
+    wsum = parts * (parts + 1) // 2
+    bounds = [T * (k * (k + 1) // 2) // wsum for k in range(parts + 1)]
+    ds_pool = ThreadPoolExecutor(1)
+    # the matrix encodes while the first part's newicks are parsed
+    ds_fut = ds_pool.submit(dataset_from_rows, rows, Q, leaf_order, compat, group_sites)
     dev = torch.device(device)
     if dev.type == "cuda" and dev.index is None:   # the worker thread needs the index
         dev = torch.device("cuda", torch.cuda.current_device())
@@ -91,6 +98,7 @@ def score_candidates(newicks: Sequence[str], rows: dict, Q, leaf_order: Sequence
                 for i in np.flatnonzero(~t.has_length):
                     x[i] = rng.uniform(0.01, 0.5)
             d.append(x)
+        ds = ds_fut.result()
         sub = lambda a: None if a is None else (a[lo:hi] if not np.isscalar(a) else a)  # noqa: E731
         if dev.type == "cuda" and threading.current_thread() is not threading.main_thread():
             torch.cuda.set_device(dev)
@@ -105,6 +113,7 @@ def score_candidates(newicks: Sequence[str], rows: dict, Q, leaf_order: Sequence
     res, h2d, d2h = [], 0, 0
     if parts == 1:
         b, _ = prep(0)
+        ds_pool.shutdown()
         res = b.run_em(rounds=rounds, max_iters=max_iters, chunk=chunk)
         return ScoreResult(res, b.h2d_bytes, b.last_d2h_bytes)
     with ThreadPoolExecutor(1) as ex:
@@ -118,4 +127,5 @@ def score_candidates(newicks: Sequence[str], rows: dict, Q, leaf_order: Sequence
             h2d += b.h2d_bytes
             d2h += b.last_d2h_bytes
             del b
+    ds_pool.shutdown()
     return ScoreResult(res, h2d, d2h)

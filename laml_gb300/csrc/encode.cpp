@@ -978,8 +978,22 @@ extern "C" int laml_plan_fill(const laml_plan_input* in, laml_plan_output* o) {
     // items, group-major within a level (groups are sorted by state count)
     bool uniform = true;
     for (int p = 0; p < T; ++p) uniform = uniform && in->ds_groups[in->tree_dataset[p]] == maxNG;
-    auto emit = [&](int side, int first, int last, int32_t* off, int32_t* items) {
+    const bool want_items = o->in_items && o->out_items;
+    if (!want_items && !(uniform && o->in_lnodes && o->out_lnodes)) {
+        set_error("plan: in_items/out_items are required unless every dataset has the same "
+                  "group count and in_lnodes/out_lnodes are given");
+        return LAML_ERR_ARG;
+    }
+    if ((o->in_desc || o->out_desc) && !want_items) {
+        set_error("plan: host descriptors need in_items/out_items");
+        return LAML_ERR_ARG;
+    }
+    auto emit = [&](int side, int first, int last, int32_t* off, int32_t* items,
+                    int32_t* lout) {
         const int32_t* nodes = lnodes[side].data();
+        if (lout)   // the level node lists, first..last (level 0 is empty)
+            std::memcpy(lout, nodes + lstart[side][first],
+                        sizeof(int32_t) * (size_t)(lstart[side][last + 1] - lstart[side][first]));
         if (uniform) {
             // every tree has maxNG groups: item k of level l is node
             // a_l + (k - off_l) % cnt_l of group (k - off_l) / cnt_l; one
@@ -992,6 +1006,7 @@ extern "C" int laml_plan_fill(const laml_plan_input* in, laml_plan_output* o) {
                 off[l - first] = (int32_t)o64[l - first];
             }
             off[nl] = (int32_t)o64[nl];
+            if (!items) return;
             parallel_for(o64[nl], [&](int64_t k0, int64_t k1) {
                 int li = (int)(std::upper_bound(o64.begin(), o64.end(), k0) - o64.begin()) - 1;
                 for (int64_t k = k0; k < k1; ++k) {
@@ -1024,8 +1039,8 @@ extern "C" int laml_plan_fill(const laml_plan_input* in, laml_plan_output* o) {
         }
         off[last - first + 1] = (int32_t)k;
     };
-    emit(0, 1, H, o->in_level_off, o->in_items);
-    emit(1, 1, D, o->out_level_off, o->out_items);
+    emit(0, 1, H, o->in_level_off, o->in_items, o->in_lnodes);
+    emit(1, 1, D, o->out_level_off, o->out_items, o->out_lnodes);
     int64_t k = 0;
     for (int g = 0; g < maxNG; ++g)
         for (int p = 0; p < T; ++p) {

@@ -4497,11 +4497,9 @@ __global__ void k_branch_terms(laml_batch b) {
 
 // Item descriptors from the node arrays already on the device: the same 12
 // int32 per item that laml_plan_fill writes on the host, three 16-byte stores.
-__global__ void k_item_desc(laml_batch b, const int32_t* __restrict__ items, int64_t n,
-                            int32_t* __restrict__ desc) {
-    for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n;
-         k += (int64_t)gridDim.x * blockDim.x) {
-        const int u = items[2 * k], g = items[2 * k + 1];
+__device__ __forceinline__ void item_desc(const laml_batch& b, int u, int g, int64_t k,
+                                          int32_t* __restrict__ desc) {
+    {
         const int tree = b.nd_tree[u];
         const int d = b.tr_ds[tree];
         const int v = b.nd_c0[u], w = b.nd_c1[u];
@@ -4514,6 +4512,36 @@ __global__ void k_item_desc(laml_batch b, const int32_t* __restrict__ items, int
         e[1] = make_int4(g, b.ds_group_base[d] + g, (int32_t)b.nd_srow[u],
                          (int32_t)(b.nd_prow[u] / 8));
         e[2] = make_int4(rv, rw, (int32_t)b.nd_srow[v], (int32_t)b.nd_srow[w]);
+    }
+}
+
+__global__ void k_item_desc(laml_batch b, const int32_t* __restrict__ items, int64_t n,
+                            int32_t* __restrict__ desc) {
+    for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n;
+         k += (int64_t)gridDim.x * blockDim.x)
+        item_desc(b, items[2 * k], items[2 * k + 1], k, desc);
+}
+
+// The same descriptors from the level node lists (every dataset with NG
+// groups): item k of level l, with item offset o_l and c_l = (o_{l+1} - o_l)
+// / NG nodes, is node lnodes[o_l / NG + (k - o_l) % c_l] of group
+// (k - o_l) / c_l -- the plan's group-major order within a level.
+__global__ void k_item_desc_nodes(laml_batch b, const int32_t* __restrict__ lnodes,
+                                  const int32_t* __restrict__ level_off, int n_levels, int64_t n,
+                                  int32_t* __restrict__ desc) {
+    const int NG = b.ds_groups[0];
+    for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n;
+         k += (int64_t)gridDim.x * blockDim.x) {
+        int lo = 0, hi = n_levels;   // the level: level_off[lo] <= k < level_off[lo + 1]
+        while (hi - lo > 1) {
+            const int mid = (lo + hi) >> 1;
+            if (level_off[mid] <= k) lo = mid; else hi = mid;
+        }
+        const int64_t o = level_off[lo];
+        const int64_t c = (level_off[lo + 1] - o) / NG;
+        const int64_t r = k - o;
+        const int64_t g = r / c;
+        item_desc(b, lnodes[o / NG + (r - g * c)], (int)g, k, desc);
     }
 }
 
@@ -4971,10 +4999,24 @@ extern "C" int laml_plan_descriptors(const laml_batch* b, int32_t* in_desc, int3
     cudaStream_t st = (cudaStream_t)stream;
     const int64_t cap = (int64_t)num_sms() * 8;
     auto blocks = [&](int64_t n) { return (unsigned)std::max<int64_t>(1, std::min(cap, (n + kBlock - 1) / kBlock)); };
-    if (b->n_in_items > 0)
-        k_item_desc<<<blocks(b->n_in_items), kBlock, 0, st>>>(*b, b->in_items, b->n_in_items, in_desc);
-    if (b->n_out_items > 0)
-        k_item_desc<<<blocks(b->n_out_items), kBlock, 0, st>>>(*b, b->out_items, b->n_out_items, out_desc);
+    if ((!b->in_items && !b->in_lnodes) || (!b->out_items && !b->out_lnodes)) {
+        laml::set_error("laml_plan_descriptors: the batch needs items or level node lists");
+        return LAML_ERR_ARG;
+    }
+    if (b->n_in_items > 0) {
+        if (b->in_items)
+            k_item_desc<<<blocks(b->n_in_items), kBlock, 0, st>>>(*b, b->in_items, b->n_in_items, in_desc);
+        else
+            k_item_desc_nodes<<<blocks(b->n_in_items), kBlock, 0, st>>>(
+                *b, b->in_lnodes, b->in_level_off, b->n_in_levels, b->n_in_items, in_desc);
+    }
+    if (b->n_out_items > 0) {
+        if (b->out_items)
+            k_item_desc<<<blocks(b->n_out_items), kBlock, 0, st>>>(*b, b->out_items, b->n_out_items, out_desc);
+        else
+            k_item_desc_nodes<<<blocks(b->n_out_items), kBlock, 0, st>>>(
+                *b, b->out_lnodes, b->out_level_off, b->n_out_levels, b->n_out_items, out_desc);
+    }
     k_group_desc<<<b->n_datasets, 128, 0, st>>>(*b, grp_desc);
     return check(cudaGetLastError(), "laml_plan_descriptors");
 }

@@ -225,11 +225,15 @@ def nni_candidates(tree: EncodedTree, moves) -> List[EncodedTree]:
 
 
 def plan_batch(trees: Sequence[EncodedTree], tree_ds: Sequence[int],
-               datasets: Sequence[EncodedDataset], host_desc: bool = True):
+               datasets: Sequence[EncodedDataset], host_desc: bool = True,
+               items: bool = True):
     """Level schedule + buffer offsets of a batch (laml_plan_*).  Returns
     (sizes: dict, arrays: dict of numpy arrays).  With ``host_desc`` False
     the item and group descriptors are left out (laml_plan_descriptors
-    builds them on the device)."""
+    builds them on the device).  With ``items`` False (device descriptors,
+    every dataset with the same group count) the (node, group) item lists
+    are replaced by the level node lists ``in_lnodes`` / ``out_lnodes``,
+    which laml_plan_descriptors expands on the device."""
     L = N.lib()
     T = len(trees)
     tn = np.asarray([t.num_nodes for t in trees], np.int32)
@@ -261,11 +265,18 @@ def plan_batch(trees: Sequence[EncodedTree], tree_ds: Sequence[int],
         "nd_sib": np.empty(nn, np.int32), "nd_leafrow": np.empty(nn, np.int32),
         "nd_prow": np.empty(nn, np.int64), "nd_srow": np.empty(nn, np.int64),
         "in_level_off": np.empty(sz.n_in_levels + 1, np.int32),
-        "in_items": np.empty(2 * max(1, sz.n_in_items), np.int32),
         "out_level_off": np.empty(sz.n_out_levels + 1, np.int32),
-        "out_items": np.empty(2 * max(1, sz.n_out_items), np.int32),
         "root_items": np.empty(2 * max(1, sz.n_root_items), np.int32),
     }
+    if not items and (host_desc or len({d.n_groups for d in datasets}) != 1):
+        items = True   # host descriptors, or datasets of different group counts
+    if items:
+        arr["in_items"] = np.empty(2 * max(1, sz.n_in_items), np.int32)
+        arr["out_items"] = np.empty(2 * max(1, sz.n_out_items), np.int32)
+    else:
+        n_int = int(np.sum(tn) - np.sum(tl))
+        arr["in_lnodes"] = np.empty(max(1, n_int), np.int32)
+        arr["out_lnodes"] = np.empty(max(1, n_int), np.int32)
     if host_desc:
         arr["in_desc"] = np.empty(12 * max(1, sz.n_in_items), np.int32)
         arr["out_desc"] = np.empty(12 * max(1, sz.n_out_items), np.int32)

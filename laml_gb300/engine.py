@@ -115,7 +115,7 @@ class DeviceBatch:
         self.trees = list(trees)
         self.tree_ds = np.asarray(tree_ds, np.int32)
         self.datasets = list(datasets)
-        sizes, plan = plan_batch(trees, tree_ds, datasets, host_desc=False)
+        sizes, plan = plan_batch(trees, tree_ds, datasets, host_desc=False, items=False)
         self.sizes = sizes
         self._node_base = plan["tr_node_base"].astype(np.int64)
         self.last_d2h_bytes = 0
@@ -168,9 +168,10 @@ class DeviceBatch:
             pk.add("nd_uorder", ultra_schedule(trees, self._node_base))
         for k in ("tr_node_base", "tr_root", "tr_quirk", "tr_site_base", "tr_cnt_base",
                   "tr_post_base", "nd_tree", "nd_c0", "nd_c1", "nd_parent", "nd_sib",
-                  "nd_leafrow", "nd_prow", "nd_srow", "in_level_off", "in_items",
-                  "out_level_off", "out_items", "root_items"):
-            pk.add(k, plan[k])
+                  "nd_leafrow", "nd_prow", "nd_srow", "in_level_off", "out_level_off",
+                  "root_items", "in_items", "out_items", "in_lnodes", "out_lnodes"):
+            if k in plan:   # items, or the level node lists the device expands
+                pk.add(k, plan[k])
         self._h2d_bytes = pk.size
         ctx = torch.cuda.stream(stream) if stream is not None else _nullctx()
         with ctx:
@@ -437,7 +438,18 @@ class DeviceBatch:
         dev = torch.cat([w["tr_llh"].view(-1), v["tr_nu"].view(-1), v["tr_phi"].view(-1),
                          w["tr_prev"].view(-1), v["nd_d"].view(-1), w["nd_d_prev"].view(-1),
                          w["tr_iter"].to(torch.float64), w["tr_status"].to(torch.float64)])
-        host = dev.cpu().numpy()
+        nbytes = dev.numel() * 8
+        stage = getattr(self, "_pinned", None)
+        if stage is not None and stage.is_pinned() and stage.numel() >= nbytes:
+            # the upload's pinned staging buffer (idle since the upload) takes
+            # the copy: a DMA into page-locked memory, no fresh pageable
+            # allocation to fault in; every tree's lengths are copied out of it
+            hv = stage[:nbytes].view(torch.float64)
+            hv.copy_(dev, non_blocking=True)
+            torch.cuda.current_stream(self.device).synchronize()
+            host = hv.numpy()
+        else:
+            host = dev.cpu().numpy()
         self.last_d2h_bytes = host.nbytes
         o = 0
         llh = host[o:o + T]; o += T

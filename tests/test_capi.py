@@ -146,6 +146,30 @@ def test_plan_levels():
                     assert lvl[c] < lvl[u]
 
 
+def test_level_node_lists_give_the_items():
+    """plan_batch(items=False): item k of a level with item offset o and c
+    nodes is node lnodes[o / NG + (k - o) % c] of group (k - o) // c -- the
+    rule laml_plan_descriptors applies on the device."""
+    rng = np.random.default_rng(7)
+    trees = [E.encode_newick(synth.yule_tree(n, rng).newick()) for n in (9, 40, 3, 17)]
+    mat = np.zeros((40, 21), np.int32)
+    ds = E.encode_dataset(mat, [{1: 1.0}] * 21, compat=True, group_sites=8)
+    sizes, ref = E.plan_batch(trees, [0] * 4, [ds], host_desc=False)
+    s2, ln = E.plan_batch(trees, [0] * 4, [ds], host_desc=False, items=False)
+    assert "in_items" not in ln and s2 == sizes
+    NG = ds.n_groups
+    for side, nl in (("in", sizes["n_in_levels"]), ("out", sizes["n_out_levels"])):
+        off = ln[f"{side}_level_off"]
+        np.testing.assert_array_equal(off, ref[f"{side}_level_off"])
+        items = ref[f"{side}_items"][:2 * sizes[f"n_{side}_items"]].reshape(-1, 2)
+        nodes = ln[f"{side}_lnodes"]
+        for l in range(nl):
+            o, c = off[l], (off[l + 1] - off[l]) // NG
+            for k in range(off[l], off[l + 1]):
+                r = k - o
+                assert (nodes[o // NG + r % c], r // c) == tuple(items[k])
+
+
 def test_item_descriptors_match_plan():
     rng = np.random.default_rng(9)
     trees = [E.encode_newick(synth.yule_tree(n, rng).newick()) for n in (9, 31, 4)]

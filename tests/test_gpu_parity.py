@@ -299,6 +299,24 @@ def test_device_descriptors_equal_host_plan():
         np.testing.assert_array_equal(b.work[k][:n].cpu().numpy(), plan[k][:n], err_msg=k)
 
 
+def test_device_descriptors_from_level_node_lists():
+    """One group count across the batch: the engine uploads the level node
+    lists instead of the (node, group) items and the device expands them
+    into laml_plan_fill's descriptor bytes."""
+    from laml_gb300.encoding import plan_batch
+    from laml_gb300.engine import DeviceBatch
+    w = synth.pmm_workload(60, 29, 3, 12, 0.5, 0.1, 0.15, seed=23, n_trees=5)
+    ds = PB.dataset_from_rows(w.rows, w.Q, w.leaf_order, True, 8)
+    trees = PB.encode_trees(w.newicks, w.leaf_order)
+    b = DeviceBatch([ds], trees, [0] * 5, [t.branch_length for t in trees], 0.3, 0.2)
+    torch.cuda.synchronize()
+    assert "in_lnodes" in b.v and "in_items" not in b.v
+    sizes, plan = plan_batch(trees, [0] * 5, [ds])
+    for k, n in (("in_desc", 12 * sizes["n_in_items"]), ("out_desc", 12 * sizes["n_out_items"]),
+                 ("grp_desc", 8 * sizes["n_groups_total"])):
+        np.testing.assert_array_equal(b.work[k][:n].cpu().numpy(), plan[k][:n], err_msg=k)
+
+
 def _log_mode_cases():
     out = []
     for compat in (True, False):
