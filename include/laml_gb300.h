@@ -487,6 +487,19 @@ int laml_inside_noalloc(const laml_batch* b, int64_t part_floats, int64_t scalar
  * reference's host EM loop (fast_em/laml.py:153-192). */
 int laml_em_graph_create(const laml_batch* b, int32_t iters, int32_t rounds, double rel_tol,
                          int32_t max_iters, int32_t flags, int32_t persistent, void** graph);
+/* The EM loop itself as one CUDA graph: a conditional WHILE node repeats
+ * `chunk` fused EM iterations (laml_em_graph_create's body) while some tree
+ * is LAML_TREE_ACTIVE, no error is recorded and fewer than max_chunks
+ * chunks ran in this launch -- the convergence test runs on the device
+ * after every chunk, so one laml_graph_launch runs EM to convergence with no
+ * host round trip (fast_em/laml.py:141-194's loop; the reference syncs the
+ * host every iteration).  `counter` is one device int32, zero when the graph
+ * is created, that the graph counts its chunks in (and leaves at zero after
+ * every launch); it must outlive the graph and not be shared by two graphs
+ * launched concurrently.  Destroy with laml_graph_destroy. */
+int laml_em_graph_loop_create(const laml_batch* b, int32_t chunk, int32_t rounds,
+                              double rel_tol, int32_t max_iters, int32_t flags,
+                              int32_t max_chunks, int32_t* counter, void** graph);
 int laml_graph_launch(void* graph, void* stream);
 void laml_graph_destroy(void* graph);
 

@@ -124,6 +124,7 @@ EXPORTS = {
     "laml_em_run_levels": (i32, [P(Batch), i32, i32, f64, i32, i32, vp]),
     "laml_inside_noalloc": (i32, [P(Batch), i64, i64, vp]),
     "laml_em_graph_create": (i32, [P(Batch), i32, i32, f64, i32, i32, i32, P(vp)]),
+    "laml_em_graph_loop_create": (i32, [P(Batch), i32, i32, f64, i32, i32, i32, vp, P(vp)]),
     "laml_graph_launch": (i32, [vp, vp]),
     "laml_graph_destroy": (None, [vp]),
     "laml_last_error": (C.c_char_p, []),

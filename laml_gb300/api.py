@@ -12,6 +12,7 @@ log-likelihood.
 from __future__ import annotations
 
 import random
+import threading
 from dataclasses import dataclass
 from typing import List, Optional, Sequence
 
@@ -32,6 +33,22 @@ class ScoreResult:
     @property
     def scores(self):
         return [r.llh for r in self.results]
+
+
+_STREAMS: dict = {}
+_STREAMS_LOCK = threading.Lock()
+
+
+def _part_stream(dev, k):
+    """The stream of pipeline part k on a device, the same across calls: the
+    caching allocator keeps freed device blocks per stream, so a part that
+    reuses its stream reuses the previous call's buffers instead of
+    allocating afresh."""
+    with _STREAMS_LOCK:
+        key = (str(dev), k)
+        if key not in _STREAMS:
+            _STREAMS[key] = torch.cuda.Stream(dev)
+        return _STREAMS[key]
 
 
 def score_candidates(newicks: Sequence[str], rows: dict, Q, leaf_order: Sequence[str],
@@ -102,7 +119,7 @@ def score_candidates(newicks: Sequence[str], rows: dict, Q, leaf_order: Sequence
         sub = lambda a: None if a is None else (a[lo:hi] if not np.isscalar(a) else a)  # noqa: E731
         if dev.type == "cuda" and threading.current_thread() is not threading.main_thread():
             torch.cuda.set_device(dev)
-        st = torch.cuda.Stream(dev) if (parts > 1 and dev.type == "cuda") else None
+        st = _part_stream(dev, k) if (parts > 1 and dev.type == "cuda") else None
         b = make_batch(nws, rows, Q, leaf_order, compat=compat, group_sites=group_sites, nu=nu,
                        phi=phi, d=d, mask=sub(masks), fix_nu=sub(fix_nu), fix_phi=sub(fix_phi),
                        device=device, trees=trees, dataset=ds, stream=st)

@@ -4950,6 +4950,27 @@ struct GraphHolder {
     cudaGraphExec_t exec = nullptr;
 };
 
+// The condition of a looping EM graph, run after every chunk: another chunk
+// while some tree is still ACTIVE, no error is recorded and fewer than
+// max_chunks chunks ran in this launch.  The counter returns to 0 when the
+// loop ends, so every launch starts from 0; max_chunks bounds the loop
+// whatever the trees' state.
+__global__ void k_em_loop_cond(laml_batch b, cudaGraphConditionalHandle h, int32_t* counter,
+                               int max_chunks) {
+    __shared__ int any;
+    if (threadIdx.x == 0) any = 0;
+    __syncthreads();
+    for (int t = threadIdx.x; t < b.n_trees; t += blockDim.x)
+        if (__ldcg(b.tr_status + t) == LAML_TREE_ACTIVE) any = 1;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        const int c = *counter + 1;
+        const bool more = any && c < max_chunks && __ldcg(b.error) == 0;
+        *counter = more ? c : 0;
+        cudaGraphSetConditional(h, more ? 1u : 0u);
+    }
+}
+
 #define DISPATCH_G(b, call)                                   \
     switch ((b).group_sites) {                                \
         case 8: { constexpr int GG = 8; return call; }        \
@@ -5103,6 +5124,68 @@ extern "C" int laml_em_graph_create(const laml_batch* b, int32_t iters, int32_t 
         delete g;
         return rc;
     }
+    *graph = g;
+    return LAML_OK;
+}
+
+extern "C" int laml_em_graph_loop_create(const laml_batch* b, int32_t chunk, int32_t rounds,
+                                         double rel_tol, int32_t max_iters, int32_t flags,
+                                         int32_t max_chunks, int32_t* counter, void** graph) {
+    int rc = validate(b);
+    if (!rc) rc = validate_mstep_flags(b, flags, "laml_em_graph_loop_create");
+    if (rc) return rc;
+    if (!graph || !counter || chunk <= 0 || max_chunks <= 0) {
+        laml::set_error("laml_em_graph_loop_create: bad argument");
+        return LAML_ERR_ARG;
+    }
+    if (!b->h_in_level_off || !b->h_out_level_off) {
+        laml::set_error("laml_em_graph_loop_create: per-level capture needs the host level offsets");
+        return LAML_ERR_ARG;
+    }
+    GraphHolder* g = new GraphHolder();
+    auto fail = [&](int code) {
+        if (g->exec) cudaGraphExecDestroy(g->exec);
+        if (g->graph) cudaGraphDestroy(g->graph);
+        delete g;
+        return code;
+    };
+    if ((rc = check(cudaGraphCreate(&g->graph, 0), "graph create"))) return fail(rc);
+    cudaGraphConditionalHandle h;
+    if ((rc = check(cudaGraphConditionalHandleCreate(&h, g->graph, 1, cudaGraphCondAssignDefault),
+                    "conditional handle")))
+        return fail(rc);
+    cudaGraphNodeParams cp = {};
+    cp.type = cudaGraphNodeTypeConditional;
+    cp.conditional.handle = h;
+    cp.conditional.type = cudaGraphCondTypeWhile;
+    cp.conditional.size = 1;
+    cudaGraphNode_t node;
+    if ((rc = check(cudaGraphAddNode(&node, g->graph, nullptr, nullptr, 0, &cp),
+                    "conditional node")))
+        return fail(rc);
+    cudaGraph_t body = cp.conditional.phGraph_out[0];
+    cudaStream_t st;
+    if ((rc = check(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking), "stream")))
+        return fail(rc);
+    rc = check(cudaStreamBeginCaptureToGraph(st, body, nullptr, nullptr, 0,
+                                             cudaStreamCaptureModeThreadLocal),
+               "begin capture");
+    if (!rc) {
+        auto run = [&]() -> int {
+            DISPATCH_G(*b, (em_levels_t<GG>(*b, chunk, rounds, rel_tol, max_iters, flags, st)));
+        };
+        int brc = run();
+        if (!brc) {
+            k_em_loop_cond<<<1, 256, 0, st>>>(*b, h, counter, max_chunks);
+            brc = check(cudaGetLastError(), "k_em_loop_cond");
+        }
+        cudaGraph_t out = nullptr;
+        int erc = check(cudaStreamEndCapture(st, &out), "end capture");
+        rc = brc ? brc : erc;
+    }
+    cudaStreamDestroy(st);
+    if (!rc) rc = check(cudaGraphInstantiate(&g->exec, g->graph, 0), "graph instantiate");
+    if (rc) return fail(rc);
     *graph = g;
     return LAML_OK;
 }

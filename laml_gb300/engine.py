@@ -350,6 +350,28 @@ class DeviceBatch:
             self._graphs[key] = h
         return self._graphs[key]
 
+    def em_graph_loop(self, chunk=4, rounds=MSTEP_ROUNDS, rel_tol=None, max_iters=100000,
+                      polish=None):
+        """A CUDA graph that runs EM to convergence in one launch: a device-side
+        WHILE loop over ``chunk``-iteration bodies that stops when no tree is
+        ACTIVE (laml_em_graph_loop_create); cached per argument set."""
+        tol = rel_tol if rel_tol is not None else (EM_STOP_COMPAT if self.compat else EM_STOP_EXACT)
+        max_chunks = (max_iters + chunk - 1) // chunk + 1
+        key = ("loop", chunk, rounds, tol, max_iters, self._mflags(polish), self.wide_chunk,
+               self.wide_pc)
+        if not hasattr(self, "_graphs"):
+            self._graphs = {}
+        if key not in self._graphs:
+            h = C.c_void_p()
+            # the graph's chunk counter: one device int per graph, zero between launches
+            cnt = torch.zeros(1, dtype=torch.int32, device=self.device)
+            self.work[f"loop_counter_{len(self._graphs)}"] = cnt
+            N.check(N.lib().laml_em_graph_loop_create(
+                C.byref(self.b), chunk, rounds, tol, max_iters, key[5], max_chunks,
+                C.c_void_p(cnt.data_ptr()), C.byref(h)))
+            self._graphs[key] = h
+        return self._graphs[key]
+
     def launch_graph(self, g):
         N.check(N.lib().laml_graph_launch(g, self._s()))
 
@@ -402,25 +424,30 @@ class DeviceBatch:
                persistent=None, polish=None, path=None):
         """EM to convergence for every tree: inside at the start parameters,
         then chunks of ``chunk`` fused iterations until no tree is ACTIVE.
-        ``path``: "graph" (a CUDA graph of the per-level launches, replayed
-        per chunk; the default), "levels" (the same launches issued directly)
-        or "persistent" (one cooperative kernel per chunk); ``persistent``
-        True / False is shorthand for "persistent" / "levels"."""
+        ``path``: "graph" (one launch of a CUDA graph whose device-side WHILE
+        node repeats ``chunk`` iterations of per-level launches until no tree
+        is ACTIVE; the default), "levels" (the same launches issued directly,
+        the host testing convergence after every chunk) or "persistent" (one
+        cooperative kernel per chunk); ``persistent`` True / False is
+        shorthand for "persistent" / "levels"."""
         if path is None:
             path = "graph" if persistent is None else ("persistent" if persistent else "levels")
         if path not in ("graph", "levels", "persistent"):
             raise ValueError(f"unknown EM path {path!r}")
         self.branch_terms()
         self.inside(update_em=True)
-        g = (self.em_graph(chunk, rounds=rounds, rel_tol=rel_tol, max_iters=max_iters,
-                           persistent=False, polish=polish) if path == "graph" else None)
+        if path == "graph":
+            # the whole loop on the device: one launch, one host check (the
+            # graph's own chunk cap is past every tree's iteration cap)
+            g = self.em_graph_loop(chunk, rounds=rounds, rel_tol=rel_tol, max_iters=max_iters,
+                                   polish=polish)
+            self.launch_graph(g)
+            self.check_device_error()
+            return self.results()
         done = 0
         while True:
-            if g is not None:
-                self.launch_graph(g)
-            else:
-                self.em_iterations(chunk, rounds=rounds, rel_tol=rel_tol, max_iters=max_iters,
-                                   persistent=path == "persistent", polish=polish)
+            self.em_iterations(chunk, rounds=rounds, rel_tol=rel_tol, max_iters=max_iters,
+                               persistent=path == "persistent", polish=polish)
             done += chunk
             st = self.work["tr_status"]
             if not bool((st == N.TREE_ACTIVE).any()):
