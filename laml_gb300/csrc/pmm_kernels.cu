@@ -384,6 +384,54 @@ __device__ __forceinline__ void write_counts(const laml_batch& b, int tree, int 
     __stcg(dst + 1, make_float4(c[4], c[5], c[6], c[7]));
 }
 
+// The two children's 8 count sums over an item's G lanes, reduce-scattered:
+// each round a lane keeps half of the values it holds, adds its partner's
+// copy of that half and hands over the other half, so after log2(G) rounds
+// lane l holds the totals of 16/G of the 16 values and stores them itself.
+// Every total comes from the same pairs in the same order as a full
+// butterfly (x_l + x_{l^off}, commutative), so the bits are those of an
+// all-reduce, with 14 exchanges instead of 48 for G = 8.
+template <int G>
+__device__ __forceinline__ void scatter_counts(const laml_batch& b, int tree, int v, int w, int g,
+                                               int lane, bool act, const float* cv,
+                                               const float* cw) {
+    float x[16];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+        x[k] = cv[k];
+        x[8 + k] = cw[k];
+    }
+    int base = 0;
+#pragma unroll
+    for (int off = G / 2, n = 16; off > 0; off >>= 1) {
+        if (n > 1) {
+            const bool up = (lane & off) != 0;
+#pragma unroll
+            for (int i = 0; i < 8; ++i) {
+                if (i < n / 2) {
+                    const float keep = up ? x[i + n / 2] : x[i];
+                    const float give = up ? x[i] : x[i + n / 2];
+                    x[i] = keep + __shfl_xor_sync(kFull, give, off);
+                }
+            }
+            base += up ? n / 2 : 0;
+            n /= 2;
+        } else {   // G = 32: the last round adds the one value both lanes hold
+            x[0] += __shfl_xor_sync(kFull, x[0], off);
+        }
+    }
+    if (!act || __ldcg(b.tr_status + tree) != LAML_TREE_ACTIVE) return;
+    constexpr int PER = G >= 16 ? 1 : 16 / G;   // totals a lane stores
+    if (G == 32 && (lane & 1)) return;          // lanes 2m, 2m + 1 hold the same total
+    const int ds = __ldg(b.tr_ds + tree);
+    const int NG = __ldg(b.ds_groups + ds);
+    const int node = base < 8 ? v : w;
+    float* dst = b.cnt_part + __ldg(b.tr_cnt_base + tree) +
+                 ((int64_t)(node - __ldg(b.tr_node_base + tree)) * NG + g) * 8 + (base & 7);
+    if (PER == 2) __stcg(reinterpret_cast<float2*>(dst), make_float2(x[0], x[1]));
+    else __stcg(dst, x[0]);
+}
+
 // ---------------------------------------------------------------------------
 // Descriptor-driven items: every address an item needs comes from its 48-byte
 // descriptor and the per-group table, so the loads of an item form a chain of
@@ -880,27 +928,33 @@ __device__ __forceinline__ void inside_states(const Child& cv, const Child& cw, 
     const float* __restrict__ rw = cw.row;
     const float cstv = cv.code == -1 ? cv.ephi : 0.f, cstw = cw.code == -1 ? cw.ephi : 0.f;
     const float kv = bv.w * cv.ss, kw = bw.w * cw.ss;
+    // a leaf's factor b.z a_j + k takes two values (a_j = e1 at the leaf's
+    // state, the constant elsewhere): formed once, selected per state
+    const float fev = fmaf(bv.z, cv.e1, kv), fcv = fmaf(bv.z, cstv, kv);
+    const float few = fmaf(bw.z, cw.e1, kw), fcw = fmaf(bw.z, cstw, kw);
+    auto fac_v = [&](int jj, float a) { return VL ? (cv.code == jj ? fev : fcv) : fmaf(bv.z, a, kv); };
+    auto fac_w = [&](int jj, float a) { return WL ? (cw.code == jj ? few : fcw) : fmaf(bw.z, a, kw); };
     int j = 2;
     for (; j + kChunk <= C; j += kChunk) {
         float av[kChunk], aw[kChunk], qv[kChunk];
 #pragma unroll
         for (int k = 0; k < kChunk; ++k) {
-            av[k] = slot_val<G, VL>(rv, cv.f, cv.code, cv.e1, cstv, j + k);
-            aw[k] = slot_val<G, WL>(rw, cw.f, cw.code, cw.e1, cstw, j + k);
+            av[k] = VL ? 0.f : slot_val<G, VL>(rv, cv.f, cv.code, cv.e1, cstv, j + k);
+            aw[k] = WL ? 0.f : slot_val<G, WL>(rw, cw.f, cw.code, cw.e1, cstw, j + k);
             qv[k] = __ldg(qrow + (j + k) * G);
         }
 #pragma unroll
         for (int k = 0; k < kChunk; ++k) {
-            const float x = fmaf(bv.z, av[k], kv) * fmaf(bw.z, aw[k], kw);
+            const float x = fac_v(j + k, av[k]) * fac_w(j + k, aw[k]);
             __stcg(row + (j + k) * G, x);
             dot = fmaf(qv[k], x, dot);
             mx = fmaxf(mx, x);
         }
     }
     for (; j < C; ++j) {
-        const float av = slot_val<G, VL>(rv, cv.f, cv.code, cv.e1, cstv, j);
-        const float aw = slot_val<G, WL>(rw, cw.f, cw.code, cw.e1, cstw, j);
-        const float x = fmaf(bv.z, av, kv) * fmaf(bw.z, aw, kw);
+        const float av = VL ? 0.f : slot_val<G, VL>(rv, cv.f, cv.code, cv.e1, cstv, j);
+        const float aw = WL ? 0.f : slot_val<G, WL>(rw, cw.f, cw.code, cw.e1, cstw, j);
+        const float x = fac_v(j, av) * fac_w(j, aw);
         __stcg(row + j * G, x);
         dot = fmaf(__ldg(qrow + j * G), x, dot);
         mx = fmaxf(mx, x);
@@ -1018,6 +1072,8 @@ __device__ __forceinline__ void inside_states_as(const Child& cv, const Child& c
     const bool live[NR] = {!VL, !WL};
     const float cstv = cv.code == -1 ? cv.ephi : 0.f, cstw = cw.code == -1 ? cw.ephi : 0.f;
     const float kv = bv.w * cv.ss, kw = bw.w * cw.ss;
+    const float fev = fmaf(bv.z, cv.e1, kv), fcv = fmaf(bv.z, cstv, kv);   // a leaf's two factors
+    const float few = fmaf(bw.z, cw.e1, kw), fcw = fmaf(bw.z, cstw, kw);
     const int nch = (C - 2 + kAsChunk - 1) / kAsChunk;
 #pragma unroll
     for (int c = 0; c < kAsStages - 1; ++c) {
@@ -1032,9 +1088,11 @@ __device__ __forceinline__ void inside_states_as(const Child& cv, const Child& c
         for (int k = 0; k < kAsChunk; ++k) {
             const int j = j0 + k;
             if (j < C) {
-                const float av = VL ? (cv.code == j ? cv.e1 : cstv) : st[(k * NR) * S] * cv.f;
-                const float aw = WL ? (cw.code == j ? cw.e1 : cstw) : st[(k * NR + 1) * S] * cw.f;
-                const float x = fmaf(bv.z, av, kv) * fmaf(bw.z, aw, kw);
+                const float fv = VL ? (cv.code == j ? fev : fcv)
+                                    : fmaf(bv.z, st[(k * NR) * S] * cv.f, kv);
+                const float fw = WL ? (cw.code == j ? few : fcw)
+                                    : fmaf(bw.z, st[(k * NR + 1) * S] * cw.f, kw);
+                const float x = fv * fw;
                 __stcg(row + j * G, x);
                 dot = fmaf(__ldg(qrow + j * G), x, dot);
                 mx = fmaxf(mx, x);
@@ -1231,24 +1289,13 @@ __device__ void outside_item_d(const laml_batch& b, const ItemDesc& d, int lane,
             child_finish<G>(b, s, d.w, cw, bw, B, want_post, lroot, xroot, cw_);
         }
     }
-#pragma unroll
-    for (int off = G / 2; off > 0; off >>= 1) {
-#pragma unroll
-        for (int k = 0; k < 8; ++k) {
-            cv_[k] += __shfl_xor_sync(kFull, cv_[k], off);
-            cw_[k] += __shfl_xor_sync(kFull, cw_[k], off);
-        }
-    }
     if constexpr (AS) {
         const volatile float* vq = sq_;
         const int tr = __float_as_int(vq[26 * S_]), g = __float_as_int(vq[27 * S_]);
-        if (act && lane == 0 && __ldcg(b.tr_status + tr) == LAML_TREE_ACTIVE) {
-            write_counts<G>(b, tr, __float_as_int(vq[24 * S_]), g, cv_);
-            write_counts<G>(b, tr, __float_as_int(vq[25 * S_]), g, cw_);
-        }
-    } else if (act && lane == 0 && __ldcg(b.tr_status + d.tree) == LAML_TREE_ACTIVE) {
-        write_counts<G>(b, d.tree, d.v, d.g, cv_);
-        write_counts<G>(b, d.tree, d.w, d.g, cw_);
+        scatter_counts<G>(b, tr, __float_as_int(vq[24 * S_]), __float_as_int(vq[25 * S_]), g,
+                          lane, act, cv_, cw_);
+    } else {
+        scatter_counts<G>(b, d.tree, d.v, d.w, d.g, lane, act, cv_, cw_);
     }
 }
 
