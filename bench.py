@@ -242,7 +242,7 @@ def run_serving(args, emit=True):
         if t > dur:
             break
         arrivals.append((t, int(rng.integers(len(pool))), "llh" if rng.random() < 0.5 else "em"))
-    srv = S.PMMServer(hbm_budget=args.serve_budget << 30)
+    srv = S.PMMServer(hbm_budget=args.serve_budget << 30, graphs=not args.serve_no_graphs)
     # each client's matrix is encoded once (as a search client scoring many
     # trees against it would), outside the timed replay
     dsets = [srv.encode_dataset(w.rows, w.Q, w.leaf_order) for w in pool]
@@ -606,6 +606,8 @@ def main():
     ap.add_argument("--serve-seconds", type=float, default=5.0)
     ap.add_argument("--serve-pool", type=int, default=16)
     ap.add_argument("--serve-budget", type=int, default=64, help="HBM budget in GiB")
+    ap.add_argument("--serve-no-graphs", action="store_true",
+                    help="serving: EM chunks as per-level launches instead of graph replays")
     ap.add_argument("--no-serving", action="store_true",
                     help="leave the short serving stream out of the default line")
     ap.add_argument("--bench-serve-seconds", type=float, default=2.0,
