@@ -242,7 +242,8 @@ def run_serving(args, emit=True):
         if t > dur:
             break
         arrivals.append((t, int(rng.integers(len(pool))), "llh" if rng.random() < 0.5 else "em"))
-    srv = S.PMMServer(hbm_budget=args.serve_budget << 30, graphs=not args.serve_no_graphs)
+    srv = S.PMMServer(hbm_budget=args.serve_budget << 30, graphs=not args.serve_no_graphs,
+                      chunk=args.serve_chunk, max_em_cohort=args.serve_em_cohort)
     # each client's matrix is encoded once (as a search client scoring many
     # trees against it would), outside the timed replay
     dsets = [srv.encode_dataset(w.rows, w.Q, w.leaf_order) for w in pool]
@@ -326,7 +327,9 @@ def run_serving(args, emit=True):
             "higher_is_better": True, "dtype": "f32", "data": "synthetic",
             "config": {"workload": "Poisson requests, leaves log-U(200,10000), sites U(30,300), "
                                    "M_k U{5..100}, nu U(0,0.2), phi U(0,0.3); half llh, half EM",
-                       "pool": len(pool), "seconds": dur, "hbm_budget_gb": args.serve_budget},
+                       "pool": len(pool), "seconds": dur, "hbm_budget_gb": args.serve_budget,
+                       "chunk": args.serve_chunk, "max_em_cohort": args.serve_em_cohort,
+                       "graphs": not args.serve_no_graphs},
             "clocks": clk.summary()}
     if emit:
         print(json.dumps(line), flush=True)
@@ -606,6 +609,10 @@ def main():
     ap.add_argument("--serve-seconds", type=float, default=5.0)
     ap.add_argument("--serve-pool", type=int, default=16)
     ap.add_argument("--serve-budget", type=int, default=64, help="HBM budget in GiB")
+    ap.add_argument("--serve-chunk", type=int, default=4,
+                    help="serving: EM iterations between cohort rebuilds")
+    ap.add_argument("--serve-em-cohort", type=int, default=128,
+                    help="serving: most EM requests in one cohort")
     ap.add_argument("--serve-no-graphs", action="store_true",
                     help="serving: EM chunks as per-level launches instead of graph replays")
     ap.add_argument("--no-serving", action="store_true",

@@ -109,7 +109,7 @@ def footprint_bytes(tree: EncodedTree, ds: EncodedDataset) -> int:
 class PMMServer:
     def __init__(self, device="cuda", hbm_budget: int = 64 << 30, max_cohort: int = 256,
                  max_cohorts: int = 6, group_sites: int = 8, rounds: int = MSTEP_ROUNDS,
-                 chunk: int = 2, max_iters: int = 1000, max_em_cohort: int = 64,
+                 chunk: int = 4, max_iters: int = 1000, max_em_cohort: int = 128,
                  graphs: bool = True):
         self.device = torch.device(device)
         self.budget = hbm_budget
