@@ -64,7 +64,10 @@ def score_candidates(newicks: Sequence[str], rows: dict, Q, leaf_order: Sequence
     batch on its own stream; a worker thread parses, plans and uploads part
     k+1 while part k iterates, so the host work of all parts but the first
     -- the smallest -- overlaps the device, and the matrix is encoded on a
-    second thread while the first part's newicks are parsed.  Each tree's EM is
+    second thread while the first part's newicks are parsed.  Each part's EM
+    (one launch of its EM loop graph) goes to the device as soon as the part
+    is built and runs beside the parts queued before it; the results are
+    collected at the end.  Each tree's EM is
     independent of the others in its batch, so the parts give each tree the
     result it has in one batch (up to FP32 summation order when a level's
     width crosses the wide/narrow rule).  Default: 2 parts from 256
@@ -135,14 +138,21 @@ def score_candidates(newicks: Sequence[str], rows: dict, Q, leaf_order: Sequence
         return ScoreResult(res, b.h2d_bytes, b.last_d2h_bytes)
     with ThreadPoolExecutor(1) as ex:
         fut = ex.submit(prep, 0)
+        queued = []
         for k in range(parts):
             b, st = fut.result()
             if k + 1 < parts:
                 fut = ex.submit(prep, k + 1)
+            # each part's EM goes to the device as soon as the part is built,
+            # on its own stream, and runs beside the parts queued before it
             with torch.cuda.stream(st):
-                res += b.run_em(rounds=rounds, max_iters=max_iters, chunk=chunk)
+                b.run_em_start(rounds=rounds, max_iters=max_iters, chunk=chunk)
+            queued.append((b, st))
+        for b, st in queued:
+            with torch.cuda.stream(st):
+                res += b.run_em_finish()
             h2d += b.h2d_bytes
             d2h += b.last_d2h_bytes
-            del b
+        del queued
     ds_pool.shutdown()
     return ScoreResult(res, h2d, d2h)

@@ -434,16 +434,12 @@ class DeviceBatch:
             path = "graph" if persistent is None else ("persistent" if persistent else "levels")
         if path not in ("graph", "levels", "persistent"):
             raise ValueError(f"unknown EM path {path!r}")
+        if path == "graph":
+            self.run_em_start(rounds=rounds, rel_tol=rel_tol, max_iters=max_iters, chunk=chunk,
+                              polish=polish)
+            return self.run_em_finish()
         self.branch_terms()
         self.inside(update_em=True)
-        if path == "graph":
-            # the whole loop on the device: one launch, one host check (the
-            # graph's own chunk cap is past every tree's iteration cap)
-            g = self.em_graph_loop(chunk, rounds=rounds, rel_tol=rel_tol, max_iters=max_iters,
-                                   polish=polish)
-            self.launch_graph(g)
-            self.check_device_error()
-            return self.results()
         done = 0
         while True:
             self.em_iterations(chunk, rounds=rounds, rel_tol=rel_tol, max_iters=max_iters,
@@ -456,6 +452,23 @@ class DeviceBatch:
                 break
         if path == "persistent":
             self.check_device_error()
+        return self.results()
+
+    def run_em_start(self, rounds=MSTEP_ROUNDS, rel_tol=None, max_iters=100000, chunk=4,
+                     polish=None):
+        """Queue EM to convergence on the batch's stream without waiting: the
+        start-parameter inside pass, then one launch of the EM loop graph (the
+        whole loop runs on the device; its chunk cap is past every tree's
+        iteration cap).  ``run_em_finish`` waits and returns the results."""
+        self.branch_terms()
+        self.inside(update_em=True)
+        g = self.em_graph_loop(chunk, rounds=rounds, rel_tol=rel_tol, max_iters=max_iters,
+                               polish=polish)
+        self.launch_graph(g)
+
+    def run_em_finish(self) -> List[TreeResult]:
+        """Wait for ``run_em_start``'s work and return the per-tree results."""
+        self.check_device_error()
         return self.results()
 
     def results(self) -> List[TreeResult]:
