@@ -35,6 +35,14 @@ class ScoreResult:
         return [r.llh for r in self.results]
 
 
+def part_bounds(T: int, parts: int) -> List[int]:
+    """Bounds of the pipeline parts of T candidates: part k holds a share
+    k + 1, so the first part's host work -- the only host work not hidden
+    behind a part's EM -- is the smallest."""
+    wsum = parts * (parts + 1) // 2
+    return [T * (k * (k + 1) // 2) // wsum for k in range(parts + 1)]
+
+
 _STREAMS: dict = {}
 _STREAMS_LOCK = threading.Lock()
 
@@ -95,10 +103,7 @@ def score_candidates(newicks: Sequence[str], rows: dict, Q, leaf_order: Sequence
     T = len(newicks)
     parts = pipeline if pipeline is not None else (2 if T >= 256 else 1)
     parts = max(1, min(int(parts), T))
-    # part k holds a share k + 1 of the candidates: the first part's host
-    # work, the only host work not hidden behind a part's EM, is the smallest
-    wsum = parts * (parts + 1) // 2
-    bounds = [T * (k * (k + 1) // 2) // wsum for k in range(parts + 1)]
+    bounds = part_bounds(T, parts)
     ds_pool = ThreadPoolExecutor(1)
     # the matrix encodes while the first part's newicks are parsed
     ds_fut = ds_pool.submit(dataset_from_rows, rows, Q, leaf_order, compat, group_sites)
